@@ -1,0 +1,170 @@
+/*
+ * qfvm_gb300 — GB300 (sm_103a) statevector engine, C ABI.
+ *
+ * This header is the drop-in boundary for pyquafu's statevector hot path.  The
+ * reference binds its C++ engine to Python through the pybind11 module `qfvm`
+ * (src/qfvm/qfvm.cpp:263-288); the entry points below carry the same
+ * operations over plain pointers and sizes, so any FFI (ctypes, cffi, a
+ * pybind11 shim) can bind them.  All functions return a qfvm_status; on
+ * failure qfvm_last_error() holds a message for the calling thread.  Nothing
+ * here exits the process or traps the device.
+ *
+ * Conventions (identical to the reference):
+ *   - amplitude index bit q is qubit q (little-endian), statevector.hpp:1388-1401;
+ *   - host states are interleaved complex128 (re, im) arrays of 2^n entries;
+ *   - a gate's qubits list holds its controls first, then its targets
+ *     (ControlledGate.pos = ctrls + targs); matrix row/column bit j refers to
+ *     target j (statevector.hpp:954-963).
+ */
+#ifndef QFVM_GB300_H
+#define QFVM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QFVM_ABI_VERSION 1
+#define QFVM_MAX_OP_QUBITS 16
+#define QFVM_MAX_QUBITS 34
+
+/* Status codes. */
+typedef enum {
+    QFVM_OK = 0,
+    QFVM_ERR_INVALID = 1,     /* bad argument (qubit index, size, matrix shape ...) */
+    QFVM_ERR_CUDA = 2,        /* a CUDA call failed */
+    QFVM_ERR_NOMEM = 3,       /* device allocation failed */
+    QFVM_ERR_UNSUPPORTED = 4, /* valid input the engine does not handle */
+    QFVM_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
+    QFVM_ERR_NODEVICE = 6     /* no CUDA device */
+} qfvm_status;
+
+/* Operation kinds.  1..17 are the named gates of the reference's OPMAP table
+ * (src/qfvm/qasm.hpp:43-46, dispatched in simulator.hpp:30-113); everything
+ * else is a matrix gate (simulator.hpp:12-28). */
+enum {
+    QFVM_OP_X = 1, QFVM_OP_Y, QFVM_OP_Z, QFVM_OP_H, QFVM_OP_S, QFVM_OP_SDG, QFVM_OP_T,
+    QFVM_OP_TDG, QFVM_OP_P, QFVM_OP_RX, QFVM_OP_RY, QFVM_OP_RZ, QFVM_OP_CX, QFVM_OP_CZ,
+    QFVM_OP_CP, QFVM_OP_CCX, QFVM_OP_RZZ,
+    QFVM_OP_MATRIX = 32,  /* targ matrix in the pool: mat_dim x mat_dim, row-major complex128 */
+    QFVM_OP_MEASURE = 40, /* not accepted by the gate entry points */
+    QFVM_OP_RESET = 41
+};
+
+/* Precision of a device state. */
+enum {
+    QFVM_C128 = 0, /* complex128 storage, IEEE FP64 arithmetic */
+    QFVM_C64 = 1,  /* complex64 storage, FP32 arithmetic, FP64 reductions */
+    QFVM_C128_DS = 2 /* complex128 storage, double-single (FP32 pair) arithmetic */
+};
+
+/* One gate of a packed circuit (128 bytes). */
+typedef struct qfvm_op {
+    int32_t kind;      /* QFVM_OP_* */
+    int32_t ncontrols; /* leading entries of qubits[] that are controls */
+    int32_t nqubits;   /* controls + targets */
+    int32_t mat_dim;   /* QFVM_OP_MATRIX: 2^targets; else 0 */
+    int32_t qubits[QFVM_MAX_OP_QUBITS];
+    int32_t slot;      /* parameter slot for batched/adjoint runs, -1 if none */
+    int32_t reserved;
+    double params[4];  /* gate angles (params[0] is the rotation angle) */
+    int64_t mat_offset; /* complex index of the matrix in the pool, -1 if none */
+} qfvm_op;
+
+/* ------------------------------------------------------------------ */
+/* Library state                                                       */
+/* ------------------------------------------------------------------ */
+
+/* Message for the last failed call on this thread ("" if none). */
+const char* qfvm_last_error(void);
+int32_t qfvm_abi_version(void);
+/* Number of kernel launches issued by this library since load (all threads). */
+uint64_t qfvm_launch_count(void);
+
+/* ------------------------------------------------------------------ */
+/* Reference-shaped entry points (host buffers), src/qfvm/qfvm.cpp      */
+/* ------------------------------------------------------------------ */
+
+/* simulate_circuit (qfvm.cpp:68-134, final-measure branch :90-103).
+ * Runs the gates of a circuit on the GPU.  `state` holds 2^n complex128
+ * amplitudes: if `state_given` is nonzero it is the input state (the
+ * reference adopts a non-empty inputstate in place, qfvm.cpp:86-89),
+ * otherwise the run starts from |0..0>.  On return `state` holds the final
+ * state.  If shots > 0, `uniforms[shots]` (host draws in [0,1)) select one
+ * basis index per shot by the sequential FP64 CDF scan of
+ * measure_samples (statevector.hpp:1387-1397), written to out_indices; an
+ * index of 2^n means the uniform was not below the total probability. */
+int qfvm_simulate_circuit(int32_t num_qubits, const qfvm_op* ops, int64_t n_ops, const double* matpool,
+                          int64_t matpool_len, double* state, int32_t state_given, const double* uniforms,
+                          int64_t shots, uint64_t* out_indices);
+
+/* applyop_statevec (qfvm.cpp:36-50): one gate applied in place to a host state
+ * of state_len amplitudes (a power of two). */
+int qfvm_applyop_statevec(const qfvm_op* op, const double* matpool, int64_t matpool_len, double* state,
+                          uint64_t state_len);
+
+/* sampling_statevec (qfvm.cpp:52-66): one basis index per host uniform. */
+int qfvm_sampling_statevec(const double* state, uint64_t state_len, const double* uniforms, int64_t shots,
+                           uint64_t* out_indices);
+
+/* expect_statevec (qfvm.cpp:246-261, statevector.hpp:1250-1305): unweighted
+ * <P_k> for Pauli strings given as flip mask (X and Y), Z mask (Z and Y) and
+ * the number of Y factors. */
+int qfvm_expect_statevec(const double* state, uint64_t state_len, const uint64_t* x_masks,
+                         const uint64_t* z_masks, const int32_t* y_counts, int64_t n_terms, double* out);
+
+/* ------------------------------------------------------------------ */
+/* Device-resident statevector (engine-owned HBM buffer)               */
+/* ------------------------------------------------------------------ */
+
+typedef struct qfvm_sv qfvm_sv;
+
+int qfvm_sv_create(int32_t num_qubits, int32_t precision, qfvm_sv** out);
+int qfvm_sv_destroy(qfvm_sv* sv);
+int qfvm_sv_set_zero(qfvm_sv* sv);                                     /* |0..0> */
+int qfvm_sv_upload(qfvm_sv* sv, const double* host_c128, uint64_t n_amps);   /* host complex128 -> device */
+int qfvm_sv_download(qfvm_sv* sv, double* host_c128, uint64_t n_amps); /* device -> host complex128 */
+int qfvm_sv_apply(qfvm_sv* sv, const qfvm_op* ops, int64_t n_ops, const double* matpool, int64_t matpool_len);
+int qfvm_sv_expect(qfvm_sv* sv, const uint64_t* x_masks, const uint64_t* z_masks, const int32_t* y_counts,
+                   int64_t n_terms, double* out);
+int qfvm_sv_sample(qfvm_sv* sv, const double* uniforms, int64_t shots, uint64_t* out_indices);
+int qfvm_sv_norm2(qfvm_sv* sv, double* out);                           /* FP64 sum |a|^2 */
+/* Raw device pointer and byte size of the state (for host-side interop). */
+int qfvm_sv_device_ptr(qfvm_sv* sv, void** dev_ptr, uint64_t* nbytes);
+/* Stream the engine issues this state's work on (cudaStream_t as void*). */
+int qfvm_sv_stream(qfvm_sv* sv, void** stream);
+
+/* ------------------------------------------------------------------ */
+/* Compiled circuits: plan once, run many times on device states        */
+/* ------------------------------------------------------------------ */
+
+typedef struct qfvm_plan qfvm_plan;
+
+/* Classify and fuse a gate list for states of `num_qubits` at `precision`.
+ * tile_qubits / reg_qubits select the fused-pass shape (0 = engine default). */
+int qfvm_plan_create(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int64_t n_ops,
+                     const double* matpool, int64_t matpool_len, int32_t tile_qubits, int32_t reg_qubits,
+                     qfvm_plan** out);
+int qfvm_plan_destroy(qfvm_plan* plan);
+/* Plan statistics: fused passes, register rounds, gates, algorithmic bytes of
+ * one run (2 * bytes per amplitude * 2^n per pass) and gate-equivalent bytes. */
+int qfvm_plan_stats(const qfvm_plan* plan, int64_t* passes, int64_t* rounds, int64_t* gates,
+                    double* pass_bytes, double* gate_bytes);
+int qfvm_plan_run(qfvm_plan* plan, qfvm_sv* sv);
+
+/* Host-only planning (no device needed): build the fused schedule and copy
+ * its records out, for inspection and for testing the fuser.  Records are the
+ * engine's internal layouts: 48-byte pass, 52-byte step and 48-byte op
+ * records; counts[] receives passes, steps, ops, coefficients. */
+int qfvm_plan_host_build(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int64_t n_ops,
+                         const double* matpool, int64_t matpool_len, int32_t tile_qubits, int32_t reg_qubits,
+                         qfvm_plan** out);
+int qfvm_plan_host_counts(const qfvm_plan* plan, int64_t counts[4], int32_t shape[3]);
+int qfvm_plan_host_copy(const qfvm_plan* plan, void* passes, void* steps, void* kops, double* coef);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QFVM_GB300_H */

@@ -1,0 +1,623 @@
+// C ABI of the GB300 statevector engine (declared in include/qfvm_gb300.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+#include "kernels.h"
+#include "qfvm_gb300.h"
+
+using namespace qsv;
+
+namespace {
+
+thread_local std::string g_err;
+std::atomic<uint64_t> g_launches{0};
+std::mutex g_boundary_mu;  // serialises the host-buffer entry points (shared cached state)
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define QSV_CUDA(call, what)                                                                        \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) {                                                                   \
+            return fail(e_ == cudaErrorMemoryAllocation ? QFVM_ERR_NOMEM : QFVM_ERR_CUDA,           \
+                        std::string(what) + ": " + cudaGetErrorString(e_));                        \
+        }                                                                                          \
+    } while (0)
+
+#define QSV_TRY(expr)          \
+    do {                       \
+        int rc_ = (expr);      \
+        if (rc_ != QFVM_OK) return rc_; \
+    } while (0)
+
+int check_device() {
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) return fail(QFVM_ERR_NODEVICE, "no CUDA device available");
+    return QFVM_OK;
+}
+
+// Growable device scratch buffer.
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes) {
+        if (bytes <= cap) return QFVM_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(bytes, 256);
+        QSV_CUDA(cudaMalloc(&p, want), "scratch allocation");
+        cap = want;
+        return QFVM_OK;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <class T>
+    T* as() {
+        return static_cast<T*>(p);
+    }
+};
+
+}  // namespace
+
+struct qfvm_sv {
+    int n = 0, precision = QFVM_C128;
+    uint64_t N = 0;
+    void* d = nullptr;
+    cudaStream_t stream = nullptr;
+    DevBuf red, masks, sample_blk, sample_shots, staging;
+};
+
+struct qfvm_plan {
+    HostPlan hp;
+    void* dbuf = nullptr;
+    PassDesc* dpass = nullptr;
+    StepDesc* dsteps = nullptr;
+    KOp* dops = nullptr;
+    void* dcoef = nullptr;
+};
+
+namespace {
+
+int store_precision(int precision) { return precision == QFVM_C64 ? QFVM_C64 : QFVM_C128; }
+
+size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+
+int upload_plan(qfvm_plan* p) {
+    const HostPlan& hp = p->hp;
+    const bool f32 = hp.precision == QFVM_C64;
+    const size_t b_pass = align256(hp.passes.size() * sizeof(PassDesc));
+    const size_t b_steps = align256(std::max<size_t>(hp.steps.size(), 1) * sizeof(StepDesc));
+    const size_t b_ops = align256(std::max<size_t>(hp.ops.size(), 1) * sizeof(KOp));
+    const size_t b_coef = align256(std::max<size_t>(hp.coef.size(), 1) * (f32 ? sizeof(float) : sizeof(double)));
+    const size_t total = b_pass + b_steps + b_ops + b_coef;
+    std::vector<unsigned char> host(total, 0);
+    std::memcpy(host.data(), hp.passes.data(), hp.passes.size() * sizeof(PassDesc));
+    if (!hp.steps.empty()) std::memcpy(host.data() + b_pass, hp.steps.data(), hp.steps.size() * sizeof(StepDesc));
+    if (!hp.ops.empty()) std::memcpy(host.data() + b_pass + b_steps, hp.ops.data(), hp.ops.size() * sizeof(KOp));
+    unsigned char* cdst = host.data() + b_pass + b_steps + b_ops;
+    if (f32) {
+        float* f = reinterpret_cast<float*>(cdst);
+        for (size_t i = 0; i < hp.coef.size(); ++i) f[i] = static_cast<float>(hp.coef[i]);
+    } else if (!hp.coef.empty()) {
+        std::memcpy(cdst, hp.coef.data(), hp.coef.size() * sizeof(double));
+    }
+    QSV_CUDA(cudaMalloc(&p->dbuf, total), "plan allocation");
+    QSV_CUDA(cudaMemcpy(p->dbuf, host.data(), total, cudaMemcpyHostToDevice), "plan upload");
+    unsigned char* b = static_cast<unsigned char*>(p->dbuf);
+    p->dpass = reinterpret_cast<PassDesc*>(b);
+    p->dsteps = reinterpret_cast<StepDesc*>(b + b_pass);
+    p->dops = reinterpret_cast<KOp*>(b + b_pass + b_steps);
+    p->dcoef = b + b_pass + b_steps + b_ops;
+    return QFVM_OK;
+}
+
+int make_plan(int n, int precision, const qfvm_op* ops, int64_t n_ops, const double* matpool, int64_t matpool_len,
+              int T, int R, qfvm_plan** out) {
+    if (n < 1 || n > QFVM_MAX_QUBITS) return fail(QFVM_ERR_INVALID, "qubit count out of range");
+    if (n_ops < 0 || (n_ops > 0 && ops == nullptr)) return fail(QFVM_ERR_INVALID, "bad op list");
+    std::vector<GOp> gops;
+    std::string err;
+    if (!classify(n, ops, n_ops, matpool, matpool_len, &gops, &err)) return fail(QFVM_ERR_INVALID, err);
+    const int sp = store_precision(precision);
+    if (T > 0 || R > 0) {
+        int dT, dR;
+        default_shape(n, sp, &dT, &dR);
+        const int tt = T > 0 ? T : dT, rr = R > 0 ? R : dR;
+        if (!pass_shape_supported(sp, tt, rr)) return fail(QFVM_ERR_INVALID, "tile shape not compiled in");
+    }
+    qfvm_plan* p = new qfvm_plan();
+    if (!build_plan(n, sp, gops, T, R, &p->hp, &err)) {
+        delete p;
+        return fail(QFVM_ERR_INVALID, err);
+    }
+    int rc = upload_plan(p);
+    if (rc != QFVM_OK) {
+        if (p->dbuf) cudaFree(p->dbuf);
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return QFVM_OK;
+}
+
+void free_plan(qfvm_plan* p) {
+    if (!p) return;
+    if (p->dbuf) cudaFree(p->dbuf);
+    delete p;
+}
+
+int run_plan(qfvm_plan* p, qfvm_sv* sv) {
+    const HostPlan& hp = p->hp;
+    if (hp.n != sv->n || hp.precision != sv->precision) return fail(QFVM_ERR_INVALID, "plan/state mismatch");
+    for (size_t i = 0; i < hp.passes.size(); ++i) {
+        const PassDesc& pd = hp.passes[i];
+        cudaError_t e = cudaSuccess;
+        if (pd.type == PASS_TILE) {
+            e = launch_tile_pass(sv->precision, hp.T, hp.R, sv->d, p->dpass + i, p->dsteps, p->dops, p->dcoef, hp.n,
+                                 pd.H, sv->stream);
+        } else if (pd.type == PASS_SMALL) {
+            e = launch_small(sv->precision, sv->d, 0, 1, hp.n, p->dops + pd.op_begin, pd.op_count, p->dcoef,
+                             sv->stream);
+        } else {
+            e = launch_globalop(sv->precision, sv->d, hp.n, p->dops + pd.op_begin, p->dcoef, sv->stream);
+        }
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        if (e != cudaSuccess) return fail(QFVM_ERR_CUDA, std::string("pass launch: ") + cudaGetErrorString(e));
+    }
+    return QFVM_OK;
+}
+
+int sv_create(int n, int precision, qfvm_sv** out) {
+    QSV_TRY(check_device());
+    if (n < 1 || n > QFVM_MAX_QUBITS) return fail(QFVM_ERR_INVALID, "qubit count out of range");
+    if (precision != QFVM_C128 && precision != QFVM_C64 && precision != QFVM_C128_DS)
+        return fail(QFVM_ERR_INVALID, "unknown precision");
+    qfvm_sv* sv = new qfvm_sv();
+    sv->n = n;
+    sv->precision = store_precision(precision);
+    sv->N = 1ULL << n;
+    cudaError_t e = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete sv;
+        return fail(QFVM_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e));
+    }
+    e = cudaMalloc(&sv->d, sv->N * amp_bytes(sv->precision));
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(sv->stream);
+        delete sv;
+        return fail(e == cudaErrorMemoryAllocation ? QFVM_ERR_NOMEM : QFVM_ERR_CUDA,
+                    std::string("state allocation: ") + cudaGetErrorString(e));
+    }
+    *out = sv;
+    return QFVM_OK;
+}
+
+void sv_free(qfvm_sv* sv) {
+    if (!sv) return;
+    if (sv->stream) cudaStreamSynchronize(sv->stream);
+    if (sv->d) cudaFree(sv->d);
+    sv->red.release();
+    sv->masks.release();
+    sv->sample_blk.release();
+    sv->sample_shots.release();
+    sv->staging.release();
+    if (sv->stream) cudaStreamDestroy(sv->stream);
+    delete sv;
+}
+
+int sv_set_zero(qfvm_sv* sv) {
+    cudaError_t e = launch_set_basis(sv->precision, sv->d, sv->N, 0, sv->stream);
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    QSV_CUDA(e, "set_zero");
+    return QFVM_OK;
+}
+
+constexpr uint64_t STAGE_AMPS = 1ULL << 24;
+
+int sv_upload(qfvm_sv* sv, const double* host, uint64_t n_amps) {
+    if (n_amps != sv->N) return fail(QFVM_ERR_INVALID, "state length does not match the device state");
+    if (!host) return fail(QFVM_ERR_INVALID, "null host buffer");
+    if (sv->precision == QFVM_C128) {
+        QSV_CUDA(cudaMemcpyAsync(sv->d, host, sv->N * 16, cudaMemcpyHostToDevice, sv->stream), "upload");
+        QSV_CUDA(cudaStreamSynchronize(sv->stream), "upload sync");
+        return QFVM_OK;
+    }
+    const uint64_t chunk = std::min<uint64_t>(STAGE_AMPS, sv->N);
+    QSV_TRY(sv->staging.ensure(chunk * 16));
+    for (uint64_t off = 0; off < sv->N; off += chunk) {
+        const uint64_t m = std::min(chunk, sv->N - off);
+        QSV_CUDA(cudaMemcpyAsync(sv->staging.p, host + 2 * off, m * 16, cudaMemcpyHostToDevice, sv->stream),
+                 "upload");
+        QSV_CUDA(launch_convert(true, sv->staging.p, static_cast<float2*>(sv->d) + off, m, sv->stream), "convert");
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        QSV_CUDA(cudaStreamSynchronize(sv->stream), "upload sync");
+    }
+    return QFVM_OK;
+}
+
+int sv_download(qfvm_sv* sv, double* host, uint64_t n_amps) {
+    if (n_amps != sv->N) return fail(QFVM_ERR_INVALID, "state length does not match the device state");
+    if (!host) return fail(QFVM_ERR_INVALID, "null host buffer");
+    if (sv->precision == QFVM_C128) {
+        QSV_CUDA(cudaMemcpyAsync(host, sv->d, sv->N * 16, cudaMemcpyDeviceToHost, sv->stream), "download");
+        QSV_CUDA(cudaStreamSynchronize(sv->stream), "download sync");
+        return QFVM_OK;
+    }
+    const uint64_t chunk = std::min<uint64_t>(STAGE_AMPS, sv->N);
+    QSV_TRY(sv->staging.ensure(chunk * 16));
+    for (uint64_t off = 0; off < sv->N; off += chunk) {
+        const uint64_t m = std::min(chunk, sv->N - off);
+        QSV_CUDA(launch_convert(false, static_cast<float2*>(sv->d) + off, sv->staging.p, m, sv->stream), "convert");
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        QSV_CUDA(cudaMemcpyAsync(host + 2 * off, sv->staging.p, m * 16, cudaMemcpyDeviceToHost, sv->stream),
+                 "download");
+        QSV_CUDA(cudaStreamSynchronize(sv->stream), "download sync");
+    }
+    return QFVM_OK;
+}
+
+int sv_expect(qfvm_sv* sv, const uint64_t* xm, const uint64_t* zm, const int32_t* ny, int64_t nterms, double* out) {
+    if (nterms < 0) return fail(QFVM_ERR_INVALID, "negative term count");
+    if (nterms == 0) return QFVM_OK;
+    if (!xm || !zm || !ny || !out) return fail(QFVM_ERR_INVALID, "null term buffer");
+    const uint64_t lim = sv->n >= 64 ? ~0ULL : ((1ULL << sv->n) - 1);
+    for (int64_t t = 0; t < nterms; ++t)
+        if ((xm[t] | zm[t]) & ~lim) return fail(QFVM_ERR_INVALID, "Pauli term acts outside the state");
+    // group terms by flip mask, in first-seen order
+    std::vector<uint64_t> keys;
+    std::vector<std::vector<int64_t>> groups;
+    for (int64_t t = 0; t < nterms; ++t) {
+        auto it = std::find(keys.begin(), keys.end(), xm[t]);
+        if (it == keys.end()) {
+            keys.push_back(xm[t]);
+            groups.push_back({t});
+        } else {
+            groups[it - keys.begin()].push_back(t);
+        }
+    }
+    // launch batches of up to EXPECT_BATCH terms
+    std::vector<uint64_t> hz;
+    std::vector<int32_t> hy;
+    std::vector<std::pair<int64_t, int>> where;  // (term, batch slot)
+    struct Batch {
+        uint64_t x;
+        size_t first;
+        int count;
+    };
+    std::vector<Batch> batches;
+    for (size_t g = 0; g < groups.size(); ++g) {
+        for (size_t s = 0; s < groups[g].size(); s += EXPECT_BATCH) {
+            Batch b{keys[g], hz.size(), 0};
+            for (size_t k = s; k < groups[g].size() && k < s + EXPECT_BATCH; ++k) {
+                hz.push_back(zm[groups[g][k]]);
+                hy.push_back(ny[groups[g][k]]);
+                ++b.count;
+            }
+            batches.push_back(b);
+        }
+    }
+    // order of terms as laid out in hz
+    std::vector<int64_t> order;
+    for (auto& g : groups)
+        for (int64_t t : g) order.push_back(t);
+    const size_t nt = hz.size();
+    QSV_TRY(sv->masks.ensure(align256(nt * 8) + align256(nt * 4) + align256(nt * 8)));
+    uint64_t* dz = sv->masks.as<uint64_t>();
+    int32_t* dy = reinterpret_cast<int32_t*>(reinterpret_cast<char*>(sv->masks.p) + align256(nt * 8));
+    double* dout = reinterpret_cast<double*>(reinterpret_cast<char*>(sv->masks.p) + align256(nt * 8) + align256(nt * 4));
+    QSV_TRY(sv->red.ensure(static_cast<size_t>(REDUCE_BLOCKS) * EXPECT_BATCH * sizeof(double)));
+    QSV_CUDA(cudaMemcpyAsync(dz, hz.data(), nt * 8, cudaMemcpyHostToDevice, sv->stream), "term upload");
+    QSV_CUDA(cudaMemcpyAsync(dy, hy.data(), nt * 4, cudaMemcpyHostToDevice, sv->stream), "term upload");
+    const int nblocks = static_cast<int>(std::min<uint64_t>(REDUCE_BLOCKS, std::max<uint64_t>(1, sv->N / 2048)));
+    for (const Batch& b : batches) {
+        cudaError_t e;
+        if (b.x == 0) {
+            e = launch_expect_z(sv->precision, sv->d, sv->N, dz + b.first, b.count, sv->red.as<double>(), nblocks,
+                                sv->stream);
+        } else {
+            const int flip_q = 63 - __builtin_clzll(b.x);
+            e = launch_expect_x(sv->precision, sv->d, sv->N, b.x, flip_q, dz + b.first, dy + b.first, b.count,
+                                sv->red.as<double>(), nblocks, sv->stream);
+        }
+        QSV_CUDA(e, "expectation");
+        QSV_CUDA(launch_reduce_partials(sv->red.as<double>(), nblocks, b.count, dout + b.first, sv->stream),
+                 "expectation reduce");
+        g_launches.fetch_add(2, std::memory_order_relaxed);
+    }
+    std::vector<double> res(nt);
+    QSV_CUDA(cudaMemcpyAsync(res.data(), dout, nt * 8, cudaMemcpyDeviceToHost, sv->stream), "result download");
+    QSV_CUDA(cudaStreamSynchronize(sv->stream), "expectation sync");
+    for (size_t i = 0; i < nt; ++i) out[order[i]] = res[i];
+    return QFVM_OK;
+}
+
+int sv_sample(qfvm_sv* sv, const double* uni, int64_t shots, uint64_t* out) {
+    if (shots < 0) return fail(QFVM_ERR_INVALID, "negative shot count");
+    if (shots == 0) return QFVM_OK;
+    if (!uni || !out) return fail(QFVM_ERR_INVALID, "null sample buffer");
+    const uint64_t bs = std::min<uint64_t>(4096, sv->N);
+    const uint64_t nb = sv->N / bs;
+    QSV_TRY(sv->sample_blk.ensure(align256(nb * 8) + align256((nb + 1) * 8)));
+    double* dbsum = sv->sample_blk.as<double>();
+    double* dpre = reinterpret_cast<double*>(reinterpret_cast<char*>(sv->sample_blk.p) + align256(nb * 8));
+    const size_t s = static_cast<size_t>(shots);
+    QSV_TRY(sv->sample_shots.ensure(align256(s * 8) * 3 + align256(s)));
+    char* sb = static_cast<char*>(sv->sample_shots.p);
+    double* duni = reinterpret_cast<double*>(sb);
+    uint64_t* didx = reinterpret_cast<uint64_t*>(sb + align256(s * 8));
+    int64_t* dord = reinterpret_cast<int64_t*>(sb + 2 * align256(s * 8));
+    uint8_t* dunsure = reinterpret_cast<uint8_t*>(sb + 3 * align256(s * 8));
+    QSV_CUDA(cudaMemcpyAsync(duni, uni, s * 8, cudaMemcpyHostToDevice, sv->stream), "uniform upload");
+    QSV_CUDA(launch_sample(sv->precision, sv->d, sv->N, bs, dbsum, dpre, duni, shots, didx, dunsure, sv->stream),
+             "sampling");
+    g_launches.fetch_add(3, std::memory_order_relaxed);
+    std::vector<uint8_t> unsure(s);
+    QSV_CUDA(cudaMemcpyAsync(out, didx, s * 8, cudaMemcpyDeviceToHost, sv->stream), "sample download");
+    QSV_CUDA(cudaMemcpyAsync(unsure.data(), dunsure, s, cudaMemcpyDeviceToHost, sv->stream), "sample download");
+    QSV_CUDA(cudaStreamSynchronize(sv->stream), "sampling sync");
+    std::vector<int64_t> ord;
+    for (size_t i = 0; i < s; ++i)
+        if (unsure[i]) ord.push_back(static_cast<int64_t>(i));
+    if (!ord.empty()) {
+        std::stable_sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return uni[a] < uni[b]; });
+        QSV_CUDA(cudaMemcpyAsync(dord, ord.data(), ord.size() * 8, cudaMemcpyHostToDevice, sv->stream),
+                 "order upload");
+        QSV_CUDA(launch_sample_exact(sv->precision, sv->d, sv->N, duni, dord, static_cast<int64_t>(ord.size()), didx,
+                                     sv->stream),
+                 "exact sampling");
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        QSV_CUDA(cudaMemcpyAsync(out, didx, s * 8, cudaMemcpyDeviceToHost, sv->stream), "sample download");
+        QSV_CUDA(cudaStreamSynchronize(sv->stream), "sampling sync");
+    }
+    return QFVM_OK;
+}
+
+// Process-wide cached state for the host-buffer entry points (one per
+// storage precision), so repeated calls do not re-allocate HBM.
+qfvm_sv* g_cached[2] = {nullptr, nullptr};
+
+int cached_state(int n, int precision, qfvm_sv** out) {
+    const int k = store_precision(precision) == QFVM_C64 ? 1 : 0;
+    if (g_cached[k] && g_cached[k]->n == n) {
+        *out = g_cached[k];
+        return QFVM_OK;
+    }
+    if (g_cached[k]) {
+        sv_free(g_cached[k]);
+        g_cached[k] = nullptr;
+    }
+    QSV_TRY(sv_create(n, precision, &g_cached[k]));
+    *out = g_cached[k];
+    return QFVM_OK;
+}
+
+int log2_len(uint64_t len, int* n) {
+    if (len < 2 || (len & (len - 1)) != 0) return fail(QFVM_ERR_INVALID, "state length must be a power of two >= 2");
+    int k = 0;
+    while ((1ULL << k) < len) ++k;
+    if (k > QFVM_MAX_QUBITS) return fail(QFVM_ERR_INVALID, "state too large");
+    *n = k;
+    return QFVM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* qfvm_last_error(void) { return g_err.c_str(); }
+int32_t qfvm_abi_version(void) { return QFVM_ABI_VERSION; }
+uint64_t qfvm_launch_count(void) { return g_launches.load(); }
+
+int qfvm_sv_create(int32_t num_qubits, int32_t precision, qfvm_sv** out) {
+    if (!out) return fail(QFVM_ERR_INVALID, "null output");
+    return sv_create(num_qubits, precision, out);
+}
+int qfvm_sv_destroy(qfvm_sv* sv) {
+    sv_free(sv);
+    return QFVM_OK;
+}
+int qfvm_sv_set_zero(qfvm_sv* sv) {
+    if (!sv) return fail(QFVM_ERR_INVALID, "null state");
+    QSV_TRY(sv_set_zero(sv));
+    QSV_CUDA(cudaStreamSynchronize(sv->stream), "set_zero sync");
+    return QFVM_OK;
+}
+int qfvm_sv_upload(qfvm_sv* sv, const double* host, uint64_t n_amps) {
+    if (!sv) return fail(QFVM_ERR_INVALID, "null state");
+    return sv_upload(sv, host, n_amps);
+}
+int qfvm_sv_download(qfvm_sv* sv, double* host, uint64_t n_amps) {
+    if (!sv) return fail(QFVM_ERR_INVALID, "null state");
+    return sv_download(sv, host, n_amps);
+}
+int qfvm_sv_apply(qfvm_sv* sv, const qfvm_op* ops, int64_t n_ops, const double* matpool, int64_t matpool_len) {
+    if (!sv) return fail(QFVM_ERR_INVALID, "null state");
+    qfvm_plan* p = nullptr;
+    QSV_TRY(make_plan(sv->n, sv->precision, ops, n_ops, matpool, matpool_len, 0, 0, &p));
+    int rc = run_plan(p, sv);
+    cudaError_t e = cudaStreamSynchronize(sv->stream);
+    free_plan(p);
+    if (rc != QFVM_OK) return rc;
+    QSV_CUDA(e, "apply sync");
+    return QFVM_OK;
+}
+int qfvm_sv_expect(qfvm_sv* sv, const uint64_t* x_masks, const uint64_t* z_masks, const int32_t* y_counts,
+                   int64_t n_terms, double* out) {
+    if (!sv) return fail(QFVM_ERR_INVALID, "null state");
+    return sv_expect(sv, x_masks, z_masks, y_counts, n_terms, out);
+}
+int qfvm_sv_sample(qfvm_sv* sv, const double* uniforms, int64_t shots, uint64_t* out_indices) {
+    if (!sv) return fail(QFVM_ERR_INVALID, "null state");
+    return sv_sample(sv, uniforms, shots, out_indices);
+}
+int qfvm_sv_norm2(qfvm_sv* sv, double* out) {
+    if (!sv || !out) return fail(QFVM_ERR_INVALID, "null argument");
+    uint64_t x = 0, z = 0;
+    int32_t y = 0;
+    return sv_expect(sv, &x, &z, &y, 1, out);
+}
+int qfvm_sv_device_ptr(qfvm_sv* sv, void** dev_ptr, uint64_t* nbytes) {
+    if (!sv) return fail(QFVM_ERR_INVALID, "null state");
+    if (dev_ptr) *dev_ptr = sv->d;
+    if (nbytes) *nbytes = sv->N * amp_bytes(sv->precision);
+    return QFVM_OK;
+}
+int qfvm_sv_stream(qfvm_sv* sv, void** stream) {
+    if (!sv || !stream) return fail(QFVM_ERR_INVALID, "null argument");
+    *stream = sv->stream;
+    return QFVM_OK;
+}
+
+int qfvm_plan_create(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int64_t n_ops, const double* matpool,
+                     int64_t matpool_len, int32_t tile_qubits, int32_t reg_qubits, qfvm_plan** out) {
+    if (!out) return fail(QFVM_ERR_INVALID, "null output");
+    QSV_TRY(check_device());
+    return make_plan(num_qubits, precision, ops, n_ops, matpool, matpool_len, tile_qubits, reg_qubits, out);
+}
+int qfvm_plan_destroy(qfvm_plan* plan) {
+    free_plan(plan);
+    return QFVM_OK;
+}
+int qfvm_plan_stats(const qfvm_plan* plan, int64_t* passes, int64_t* rounds, int64_t* gates, double* pass_bytes,
+                    double* gate_bytes) {
+    if (!plan) return fail(QFVM_ERR_INVALID, "null plan");
+    const PlanStats& s = plan->hp.stats;
+    if (passes) *passes = s.passes;
+    if (rounds) *rounds = s.rounds;
+    if (gates) *gates = s.gates;
+    if (pass_bytes) *pass_bytes = s.pass_bytes;
+    if (gate_bytes) *gate_bytes = s.gate_bytes;
+    return QFVM_OK;
+}
+int qfvm_plan_run(qfvm_plan* plan, qfvm_sv* sv) {
+    if (!plan || !sv) return fail(QFVM_ERR_INVALID, "null argument");
+    if (!plan->dbuf) return fail(QFVM_ERR_INVALID, "host-only plan cannot run");
+    return run_plan(plan, sv);
+}
+
+int qfvm_plan_host_build(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int64_t n_ops,
+                         const double* matpool, int64_t matpool_len, int32_t tile_qubits, int32_t reg_qubits,
+                         qfvm_plan** out) {
+    if (!out) return fail(QFVM_ERR_INVALID, "null output");
+    if (num_qubits < 1 || num_qubits > QFVM_MAX_QUBITS) return fail(QFVM_ERR_INVALID, "qubit count out of range");
+    if (n_ops < 0 || (n_ops > 0 && ops == nullptr)) return fail(QFVM_ERR_INVALID, "bad op list");
+    std::vector<GOp> gops;
+    std::string err;
+    if (!classify(num_qubits, ops, n_ops, matpool, matpool_len, &gops, &err)) return fail(QFVM_ERR_INVALID, err);
+    if (tile_qubits > 0 || reg_qubits > 0) {
+        int dT, dR;
+        default_shape(num_qubits, store_precision(precision), &dT, &dR);
+        const int tt = tile_qubits > 0 ? tile_qubits : dT, rr = reg_qubits > 0 ? reg_qubits : dR;
+        if (!pass_shape_supported(store_precision(precision), tt, rr))
+            return fail(QFVM_ERR_INVALID, "tile shape not compiled in");
+    }
+    qfvm_plan* p = new qfvm_plan();
+    if (!build_plan(num_qubits, store_precision(precision), gops, tile_qubits, reg_qubits, &p->hp, &err)) {
+        delete p;
+        return fail(QFVM_ERR_INVALID, err);
+    }
+    *out = p;
+    return QFVM_OK;
+}
+
+int qfvm_plan_host_counts(const qfvm_plan* plan, int64_t counts[4], int32_t shape[3]) {
+    if (!plan || !counts || !shape) return fail(QFVM_ERR_INVALID, "null argument");
+    counts[0] = static_cast<int64_t>(plan->hp.passes.size());
+    counts[1] = static_cast<int64_t>(plan->hp.steps.size());
+    counts[2] = static_cast<int64_t>(plan->hp.ops.size());
+    counts[3] = static_cast<int64_t>(plan->hp.coef.size());
+    shape[0] = plan->hp.T;
+    shape[1] = plan->hp.R;
+    shape[2] = plan->hp.L;
+    return QFVM_OK;
+}
+
+int qfvm_plan_host_copy(const qfvm_plan* plan, void* passes, void* steps, void* kops, double* coef) {
+    if (!plan) return fail(QFVM_ERR_INVALID, "null plan");
+    const HostPlan& hp = plan->hp;
+    if (passes) std::memcpy(passes, hp.passes.data(), hp.passes.size() * sizeof(PassDesc));
+    if (steps) std::memcpy(steps, hp.steps.data(), hp.steps.size() * sizeof(StepDesc));
+    if (kops) std::memcpy(kops, hp.ops.data(), hp.ops.size() * sizeof(KOp));
+    if (coef) std::memcpy(coef, hp.coef.data(), hp.coef.size() * sizeof(double));
+    return QFVM_OK;
+}
+
+int qfvm_simulate_circuit(int32_t num_qubits, const qfvm_op* ops, int64_t n_ops, const double* matpool,
+                          int64_t matpool_len, double* state, int32_t state_given, const double* uniforms,
+                          int64_t shots, uint64_t* out_indices) {
+    std::lock_guard<std::mutex> lk(g_boundary_mu);
+    if (!state) return fail(QFVM_ERR_INVALID, "null state buffer");
+    QSV_TRY(check_device());
+    qfvm_plan* p = nullptr;
+    QSV_TRY(make_plan(num_qubits, QFVM_C128, ops, n_ops, matpool, matpool_len, 0, 0, &p));
+    qfvm_sv* sv = nullptr;
+    int rc = cached_state(num_qubits, QFVM_C128, &sv);
+    if (rc == QFVM_OK) rc = state_given ? sv_upload(sv, state, sv->N) : sv_set_zero(sv);
+    if (rc == QFVM_OK) rc = run_plan(p, sv);
+    if (rc == QFVM_OK && shots > 0) rc = sv_sample(sv, uniforms, shots, out_indices);
+    if (rc == QFVM_OK) rc = sv_download(sv, state, sv->N);
+    free_plan(p);
+    return rc;
+}
+
+int qfvm_applyop_statevec(const qfvm_op* op, const double* matpool, int64_t matpool_len, double* state,
+                          uint64_t state_len) {
+    std::lock_guard<std::mutex> lk(g_boundary_mu);
+    if (!op || !state) return fail(QFVM_ERR_INVALID, "null argument");
+    int n = 0;
+    QSV_TRY(log2_len(state_len, &n));
+    QSV_TRY(check_device());
+    qfvm_plan* p = nullptr;
+    QSV_TRY(make_plan(n, QFVM_C128, op, 1, matpool, matpool_len, 0, 0, &p));
+    qfvm_sv* sv = nullptr;
+    int rc = cached_state(n, QFVM_C128, &sv);
+    if (rc == QFVM_OK) rc = sv_upload(sv, state, sv->N);
+    if (rc == QFVM_OK) rc = run_plan(p, sv);
+    if (rc == QFVM_OK) rc = sv_download(sv, state, sv->N);
+    free_plan(p);
+    return rc;
+}
+
+int qfvm_sampling_statevec(const double* state, uint64_t state_len, const double* uniforms, int64_t shots,
+                           uint64_t* out_indices) {
+    std::lock_guard<std::mutex> lk(g_boundary_mu);
+    if (!state) return fail(QFVM_ERR_INVALID, "null state buffer");
+    int n = 0;
+    QSV_TRY(log2_len(state_len, &n));
+    QSV_TRY(check_device());
+    qfvm_sv* sv = nullptr;
+    QSV_TRY(cached_state(n, QFVM_C128, &sv));
+    QSV_TRY(sv_upload(sv, state, sv->N));
+    return sv_sample(sv, uniforms, shots, out_indices);
+}
+
+int qfvm_expect_statevec(const double* state, uint64_t state_len, const uint64_t* x_masks, const uint64_t* z_masks,
+                         const int32_t* y_counts, int64_t n_terms, double* out) {
+    std::lock_guard<std::mutex> lk(g_boundary_mu);
+    if (!state) return fail(QFVM_ERR_INVALID, "null state buffer");
+    int n = 0;
+    QSV_TRY(log2_len(state_len, &n));
+    QSV_TRY(check_device());
+    qfvm_sv* sv = nullptr;
+    QSV_TRY(cached_state(n, QFVM_C128, &sv));
+    QSV_TRY(sv_upload(sv, state, sv->N));
+    return sv_expect(sv, x_masks, z_masks, y_counts, n_terms, out);
+}
+
+}  // extern "C"

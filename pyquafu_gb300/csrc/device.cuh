@@ -1,0 +1,464 @@
+// Device-side building blocks of the statevector kernels (templates shared by
+// the per-precision translation units).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <type_traits>
+
+#include "engine.h"
+#include "policy.cuh"
+
+namespace qsv {
+
+// ---------------------------------------------------------------------------
+// shared-memory swizzle: XOR-fold the higher index bits onto the bits that
+// select the 16-byte (or 8-byte) slot inside a 128-byte wavefront.  Bit p of
+// the element index lands on slot bit (p mod GB), so any GB lane bits with
+// distinct residues mod GB hit distinct bank groups.
+// ---------------------------------------------------------------------------
+template <int GB>
+__device__ __forceinline__ uint32_t swz(uint32_t s) {
+    constexpr uint32_t M = (1u << GB) - 1;
+    uint32_t x = s;
+#pragma unroll
+    for (int k = 1; k * GB < 32; ++k) x ^= (s >> (k * GB)) & M;
+    return x;
+}
+
+__device__ __forceinline__ uint64_t insert0(uint64_t j, int p) {
+    return ((j >> p) << (p + 1)) | (j & ((1ULL << p) - 1));
+}
+
+template <int N, class F>
+__device__ __forceinline__ void with_bit(int b, F&& f) {
+    switch (b) {
+        case 0: f(std::integral_constant<int, 0>()); break;
+        case 1: if constexpr (N > 1) f(std::integral_constant<int, 1>()); break;
+        case 2: if constexpr (N > 2) f(std::integral_constant<int, 2>()); break;
+        case 3: if constexpr (N > 3) f(std::integral_constant<int, 3>()); break;
+        case 4: if constexpr (N > 4) f(std::integral_constant<int, 4>()); break;
+        case 5: if constexpr (N > 5) f(std::integral_constant<int, 5>()); break;
+        default: break;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Register-round operations: a thread holds 2^R amplitudes that differ in the
+// R register bits; target bits are compile-time after the with_bit dispatch.
+// ---------------------------------------------------------------------------
+template <class P, int R, int TB, bool CTRL, class F>
+__device__ __forceinline__ void reg_pairs(typename P::A (&a)[1 << R], uint32_t creg, F&& f) {
+#pragma unroll
+    for (int j = 0; j < (1 << R); ++j) {
+        if (j & (1 << TB)) continue;
+        if (!CTRL || ((static_cast<uint32_t>(j) & creg) == creg)) f(a[j], a[j | (1 << TB)]);
+    }
+}
+
+template <class P, int R, bool CTRL>
+__device__ __forceinline__ void reg_op1(typename P::A (&a)[1 << R], const KOp& op, const typename P::C* coef) {
+    using C = typename P::C;
+    const uint32_t creg = op.creg;
+    switch (op.kind) {
+        case K_X:
+            with_bit<R>(op.t0, [&](auto tb) {
+                constexpr int TB = decltype(tb)::value;
+                reg_pairs<P, R, TB, CTRL>(a, creg, [](typename P::A& x, typename P::A& y) {
+                    typename P::A t = x;
+                    x = y;
+                    y = t;
+                });
+            });
+            break;
+        case K_Y:
+            with_bit<R>(op.t0, [&](auto tb) {
+                constexpr int TB = decltype(tb)::value;
+                reg_pairs<P, R, TB, CTRL>(a, creg, [](typename P::A& x, typename P::A& y) { pair_y<P>(x, y); });
+            });
+            break;
+        case K_REAL: {
+            const C m0 = P::coef(coef, op.coef), m1 = P::coef(coef, op.coef + 1);
+            const C m2 = P::coef(coef, op.coef + 2), m3 = P::coef(coef, op.coef + 3);
+            with_bit<R>(op.t0, [&](auto tb) {
+                constexpr int TB = decltype(tb)::value;
+                reg_pairs<P, R, TB, CTRL>(
+                    a, creg, [&](typename P::A& x, typename P::A& y) { pair_real<P>(x, y, m0, m1, m2, m3); });
+            });
+            break;
+        }
+        case K_RX: {
+            const C c = P::coef(coef, op.coef), s = P::coef(coef, op.coef + 1);
+            const C ns = P::cneg(s);
+            with_bit<R>(op.t0, [&](auto tb) {
+                constexpr int TB = decltype(tb)::value;
+                reg_pairs<P, R, TB, CTRL>(a, creg,
+                                          [&](typename P::A& x, typename P::A& y) { pair_rx<P>(x, y, c, s, ns); });
+            });
+            break;
+        }
+        case K_DENSE: {
+            C m[8], nmi[4];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) m[i] = P::coef(coef, op.coef + i);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) nmi[i] = P::cneg(m[2 * i + 1]);
+            with_bit<R>(op.t0, [&](auto tb) {
+                constexpr int TB = decltype(tb)::value;
+                reg_pairs<P, R, TB, CTRL>(a, creg,
+                                          [&](typename P::A& x, typename P::A& y) { pair_dense<P>(x, y, m, nmi); });
+            });
+            break;
+        }
+        default: break;
+    }
+}
+
+template <class P, int R, int B0, int B1, bool CTRL, class F>
+__device__ __forceinline__ void reg_quads(typename P::A (&a)[1 << R], uint32_t creg, F&& f) {
+#pragma unroll
+    for (int j = 0; j < (1 << R); ++j) {
+        if (j & ((1 << B0) | (1 << B1))) continue;
+        if (!CTRL || ((static_cast<uint32_t>(j) & creg) == creg))
+            f(a[j], a[j | (1 << B0)], a[j | (1 << B1)], a[j | (1 << B0) | (1 << B1)]);
+    }
+}
+
+template <class P, int R, bool CTRL>
+__device__ __forceinline__ void reg_swap(typename P::A (&a)[1 << R], const KOp& op) {
+    const uint32_t creg = op.creg;
+    with_bit<R>(op.t0, [&](auto b0) {
+        constexpr int B0 = decltype(b0)::value;
+        with_bit<R>(op.t1, [&](auto b1) {
+            constexpr int B1 = decltype(b1)::value;
+            if constexpr (B0 < B1) {
+                reg_quads<P, R, B0, B1, CTRL>(
+                    a, creg, [](typename P::A&, typename P::A& v1, typename P::A& v2, typename P::A&) {
+                        typename P::A t = v1;
+                        v1 = v2;
+                        v2 = t;
+                    });
+            }
+        });
+    });
+}
+
+template <class P, int R>
+__device__ __forceinline__ void reg_diag(typename P::A (&a)[1 << R], const KOp& op, uint64_t gthr,
+                                         const typename P::C* coef) {
+    using C = typename P::C;
+    const uint32_t creg = op.creg, preg = op.preg;
+    const int pt = __popcll(gthr & op.pthr) & 1;
+    if (op.flags & F_D1_SPEC) {
+        const int sp = op.special;
+#pragma unroll
+        for (int j = 0; j < (1 << R); ++j) {
+            if ((static_cast<uint32_t>(j) & creg) != creg) continue;
+            if ((pt ^ (__popc(static_cast<uint32_t>(j) & preg) & 1)) == 0) continue;
+            amp_special<P>(a[j], sp);
+        }
+        return;
+    }
+    const C d0r = P::coef(coef, op.coef), d0i = P::coef(coef, op.coef + 1);
+    const C d1r = P::coef(coef, op.coef + 2), d1i = P::coef(coef, op.coef + 3);
+    const C nd0i = P::cneg(d0i), nd1i = P::cneg(d1i);
+    const bool d0one = (op.flags & F_D0_ONE) != 0;
+#pragma unroll
+    for (int j = 0; j < (1 << R); ++j) {
+        if ((static_cast<uint32_t>(j) & creg) != creg) continue;
+        const int par = pt ^ (__popc(static_cast<uint32_t>(j) & preg) & 1);
+        if (par) {
+            amp_phase<P>(a[j], d1r, d1i, nd1i);
+        } else if (!d0one) {
+            amp_phase<P>(a[j], d0r, d0i, nd0i);
+        }
+    }
+}
+
+template <class P, int R>
+__device__ __forceinline__ void reg_apply(typename P::A (&a)[1 << R], const KOp& op, uint64_t gthr,
+                                          const typename P::C* coef) {
+    if ((gthr & op.cthr) != op.cthr) return;  // a control outside the registers is 0
+    switch (op.kind) {
+        case K_DIAG: reg_diag<P, R>(a, op, gthr, coef); break;
+        case K_SWAP:
+            if (op.creg) reg_swap<P, R, true>(a, op);
+            else reg_swap<P, R, false>(a, op);
+            break;
+        default:
+            if (op.creg) reg_op1<P, R, true>(a, op, coef);
+            else reg_op1<P, R, false>(a, op, coef);
+            break;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Whole-state pass: the state (<= 2^13 complex128 / 2^14 complex64) lives in
+// shared memory of one CTA per state; every gate is one sweep over it.
+// blockIdx.x selects a state of a batch (stride `stride` elements).
+// ---------------------------------------------------------------------------
+template <class P>
+__device__ __forceinline__ void small_apply(typename P::S* sm, int n, const KOp& op, const typename P::C* coef) {
+    constexpr int GB = P::GBITS;
+    using A = typename P::A;
+    using C = typename P::C;
+    const uint32_t N = 1u << n;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t cm = static_cast<uint32_t>(op.cthr);
+    switch (op.kind) {
+        case K_DIAG: {
+            const uint32_t pm = static_cast<uint32_t>(op.pthr);
+            const C d0r = P::coef(coef, op.coef), d0i = P::coef(coef, op.coef + 1);
+            const C d1r = P::coef(coef, op.coef + 2), d1i = P::coef(coef, op.coef + 3);
+            for (uint32_t i = tid; i < N; i += nt) {
+                if ((i & cm) != cm) continue;
+                const int par = __popc(i & pm) & 1;
+                if (!par && (op.flags & F_D0_ONE)) continue;
+                const uint32_t ad = swz<GB>(i);
+                A v = P::s2a(sm[ad]);
+                if (op.flags & F_D1_SPEC) amp_special<P>(v, op.special);
+                else if (par) amp_phase<P>(v, d1r, d1i, P::cneg(d1i));
+                else amp_phase<P>(v, d0r, d0i, P::cneg(d0i));
+                sm[ad] = P::a2s(v);
+            }
+            break;
+        }
+        case K_SWAP:
+        case K_DENSE2: {
+            const int t0 = op.t0, t1 = op.t1;
+            const int lo = t0 < t1 ? t0 : t1, hi = t0 < t1 ? t1 : t0;
+            for (uint32_t qd = tid; qd < (N >> 2); qd += nt) {
+                const uint32_t i = static_cast<uint32_t>(insert0(insert0(qd, lo), hi));
+                if ((i & cm) != cm) continue;
+                const uint32_t a0 = swz<GB>(i), a1 = swz<GB>(i | (1u << t0)), a2 = swz<GB>(i | (1u << t1)),
+                               a3 = swz<GB>(i | (1u << t0) | (1u << t1));
+                A v0 = P::s2a(sm[a0]), v1 = P::s2a(sm[a1]), v2 = P::s2a(sm[a2]), v3 = P::s2a(sm[a3]);
+                if (op.kind == K_SWAP) {
+                    A t = v1;
+                    v1 = v2;
+                    v2 = t;
+                } else {
+                    quad_dense<P>(v0, v1, v2, v3, coef, op.coef);
+                }
+                sm[a0] = P::a2s(v0);
+                sm[a1] = P::a2s(v1);
+                sm[a2] = P::a2s(v2);
+                sm[a3] = P::a2s(v3);
+            }
+            break;
+        }
+        case K_DENSEK: {
+            const int k = op.k;
+            const uint32_t dim = 1u << k;
+            uint8_t srt[MAXK];
+            for (int j = 0; j < k; ++j) srt[j] = op.tk[j];
+            for (int x = 1; x < k; ++x)
+                for (int y = x; y > 0 && srt[y - 1] > srt[y]; --y) {
+                    uint8_t t = srt[y];
+                    srt[y] = srt[y - 1];
+                    srt[y - 1] = t;
+                }
+            for (uint32_t g = tid; g < (N >> k); g += nt) {
+                uint32_t i = g;
+                for (int j = 0; j < k; ++j) i = static_cast<uint32_t>(insert0(i, srt[j]));
+                if ((i & cm) != cm) continue;
+                A in[1 << MAXK];
+                for (uint32_t m = 0; m < dim; ++m) {
+                    uint32_t idx = i;
+                    for (int j = 0; j < k; ++j)
+                        if ((m >> j) & 1) idx |= 1u << op.tk[j];
+                    in[m] = P::s2a(sm[swz<GB>(idx)]);
+                }
+                for (uint32_t r = 0; r < dim; ++r) {
+                    typename P::R xr = P::mul(P::coef(coef, op.coef + 2 * (r * dim)), in[0].x);
+                    typename P::R xi = P::mul(P::coef(coef, op.coef + 2 * (r * dim)), in[0].y);
+                    xr = P::madd(P::cneg(P::coef(coef, op.coef + 2 * (r * dim) + 1)), in[0].y, xr);
+                    xi = P::madd(P::coef(coef, op.coef + 2 * (r * dim) + 1), in[0].x, xi);
+                    for (uint32_t c = 1; c < dim; ++c) {
+                        const C mr = P::coef(coef, op.coef + 2 * (r * dim + c));
+                        const C mi = P::coef(coef, op.coef + 2 * (r * dim + c) + 1);
+                        xr = P::madd(mr, in[c].x, xr);
+                        xr = P::madd(P::cneg(mi), in[c].y, xr);
+                        xi = P::madd(mr, in[c].y, xi);
+                        xi = P::madd(mi, in[c].x, xi);
+                    }
+                    uint32_t idx = i;
+                    for (int j = 0; j < k; ++j)
+                        if ((r >> j) & 1) idx |= 1u << op.tk[j];
+                    A o;
+                    o.x = xr;
+                    o.y = xi;
+                    sm[swz<GB>(idx)] = P::a2s(o);
+                }
+            }
+            break;
+        }
+        default: {
+            const int t = op.t0;
+            C m[8], nmi[4];
+            if (op.kind == K_REAL) {
+                for (int x = 0; x < 4; ++x) m[x] = P::coef(coef, op.coef + x);
+            } else if (op.kind == K_RX) {
+                m[0] = P::coef(coef, op.coef);
+                m[1] = P::coef(coef, op.coef + 1);
+                m[2] = P::cneg(m[1]);
+            } else if (op.kind == K_DENSE) {
+                for (int x = 0; x < 8; ++x) m[x] = P::coef(coef, op.coef + x);
+                for (int x = 0; x < 4; ++x) nmi[x] = P::cneg(m[2 * x + 1]);
+            }
+            for (uint32_t pr = tid; pr < (N >> 1); pr += nt) {
+                const uint32_t i0 = static_cast<uint32_t>(insert0(pr, t));
+                if ((i0 & cm) != cm) continue;
+                const uint32_t a0 = swz<GB>(i0), a1 = swz<GB>(i0 | (1u << t));
+                A x = P::s2a(sm[a0]), y = P::s2a(sm[a1]);
+                switch (op.kind) {
+                    case K_X: {
+                        A tt = x;
+                        x = y;
+                        y = tt;
+                        break;
+                    }
+                    case K_Y: pair_y<P>(x, y); break;
+                    case K_REAL: pair_real<P>(x, y, m[0], m[1], m[2], m[3]); break;
+                    case K_RX: pair_rx<P>(x, y, m[0], m[1], m[2]); break;
+                    case K_DENSE: pair_dense<P>(x, y, m, nmi); break;
+                    default: break;
+                }
+                sm[a0] = P::a2s(x);
+                sm[a1] = P::a2s(y);
+            }
+            break;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused tile pass.  One CTA per tile of 2^T amplitudes: tile-local bit k is
+// global qubit tq[k]; the low L qubits are contiguous so every global access
+// is a run of 2^L amplitudes.  The tile is staged in shared memory, then each
+// register round loads 2^R amplitudes per thread, applies its gates in
+// registers and writes them back.
+// ---------------------------------------------------------------------------
+// Shared-memory step of a tile pass (kept out of line so its registers do not
+// weigh on the register rounds).
+template <class P>
+__device__ __noinline__ void tile_smem_op(typename P::S* sm, int T, uint64_t base, KOp o,
+                                          const typename P::C* coef) {
+    if ((base & o.cthr) == o.cthr) {
+        o.cthr = o.creg;  // tile-local control mask
+        small_apply<P>(sm, T, o, coef);
+    }
+}
+
+template <int T, int R, int SB>
+struct PassOcc {
+    // CTAs per SM the register budget is sized for
+    static constexpr int value = 1;
+};
+
+template <class P, int T, int R>
+__global__ void __launch_bounds__(1 << (T - R), PassOcc<T, R, P::SBYTES>::value) k_pass(typename P::G* __restrict__ state,
+                                                       const PassDesc* __restrict__ pdp,
+                                                       const StepDesc* __restrict__ steps,
+                                                       const KOp* __restrict__ ops,
+                                                       const typename P::C* __restrict__ coef) {
+    constexpr int NT = 1 << (T - R);
+    constexpr int NA = 1 << R;
+    constexpr int GB = P::GBITS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    typename P::S* sm = reinterpret_cast<typename P::S*>(smem_raw);
+    uint64_t* choff = reinterpret_cast<uint64_t*>(smem_raw + (sizeof(typename P::S) << T));
+
+    const int tid = threadIdx.x;
+    const int L = pdp->L;
+    const int H = pdp->H;
+    uint64_t base = static_cast<uint64_t>(blockIdx.x) << L;
+    for (int k = 0; k < H; ++k) base = insert0(base, pdp->tq[L + k]);
+
+    for (int c = tid; c < (1 << H); c += NT) {
+        uint64_t off = 0;
+        for (int k = 0; k < H; ++k)
+            if ((c >> k) & 1) off |= 1ULL << pdp->tq[L + k];
+        choff[c] = off;
+    }
+    __syncthreads();
+
+    const uint32_t lmask = (1u << L) - 1;
+    constexpr int PER = (1 << T) / NT;  // elements per thread (>= 2^R)
+    constexpr int BATCH = PER < 8 ? PER : 8;
+#pragma unroll 1
+    for (int it = 0; it < PER; it += BATCH) {
+        typename P::G v[BATCH];
+#pragma unroll
+        for (int u = 0; u < BATCH; ++u) {
+            const uint32_t s = static_cast<uint32_t>((it + u) * NT + tid);
+            v[u] = __ldcs(state + (base | choff[s >> L] | (s & lmask)));
+        }
+#pragma unroll
+        for (int u = 0; u < BATCH; ++u) {
+            const uint32_t s = static_cast<uint32_t>((it + u) * NT + tid);
+            sm[swz<GB>(s)] = P::g2s(v[u]);
+        }
+    }
+    __syncthreads();
+
+    const int nsteps = pdp->step_count;
+    const StepDesc* sd = steps + pdp->step_begin;
+    for (int si = 0; si < nsteps; ++si, ++sd) {
+        if (sd->type == STEP_SMEM) {
+            // dense multi-target gate applied in shared memory over the tile
+            for (int oi = 0; oi < sd->op_count; ++oi) {
+                tile_smem_op<P>(sm, T, base, ops[sd->op_begin + oi], coef);
+                __syncthreads();
+            }
+            continue;
+        }
+        uint32_t sb = 0;
+        uint64_t gthr = base;
+#pragma unroll
+        for (int k = 0; k < T - R; ++k) {
+            if ((tid >> k) & 1) {
+                sb |= 1u << sd->tpos[k];
+                gthr |= 1ULL << sd->tglob[k];
+            }
+        }
+        const uint32_t psb = swz<GB>(sb);
+        uint32_t rsw[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) rsw[k] = swz<GB>(1u << sd->rpos[k]);
+        typename P::A a[NA];
+#pragma unroll
+        for (int j = 0; j < NA; ++j) {
+            uint32_t ad = psb;
+#pragma unroll
+            for (int k = 0; k < R; ++k)
+                if ((j >> k) & 1) ad ^= rsw[k];
+            a[j] = P::s2a(sm[ad]);
+        }
+        const KOp* op = ops + sd->op_begin;
+        const int nop = sd->op_count;
+        for (int oi = 0; oi < nop; ++oi) {
+            const KOp o = op[oi];
+            reg_apply<P, R>(a, o, gthr, coef);
+        }
+        uint32_t psb2 = psb;
+        asm volatile("" : "+r"(psb2));  // recompute the addresses instead of keeping 2^R of them live
+#pragma unroll
+        for (int j = 0; j < NA; ++j) {
+            uint32_t ad = psb2;
+#pragma unroll
+            for (int k = 0; k < R; ++k)
+                if ((j >> k) & 1) ad ^= rsw[k];
+            sm[ad] = P::a2s(a[j]);
+        }
+        __syncthreads();
+    }
+
+#pragma unroll 8
+    for (int it = 0; it < PER; ++it) {
+        const uint32_t s = static_cast<uint32_t>(it * NT + tid);
+        __stcs(state + (base | choff[s >> L] | (s & lmask)), P::s2g(sm[swz<GB>(s)]));
+    }
+}
+
+}  // namespace qsv

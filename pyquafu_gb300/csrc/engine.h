@@ -1,0 +1,124 @@
+// Internal declarations of the GB300 statevector engine (host planner + kernels).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "qfvm_gb300.h"
+
+namespace qsv {
+
+// ---------------------------------------------------------------------------
+// Classified gates ("gops"): every circuit gate becomes one of these kinds,
+// expressed on global qubit indices.  Coefficients are FP64, computed on the
+// host exactly as the reference builds its matrices (statevector.hpp:340-437).
+// ---------------------------------------------------------------------------
+enum GKind : uint8_t {
+    K_DENSE = 1,  // 2x2 complex on t0 (8 coefs: m00 re,im, m01, m10, m11)
+    K_REAL = 2,   // 2x2 real on t0 (4 coefs)
+    K_RX = 3,     // [[c, -i s], [-i s, c]] on t0 (coefs c, s)
+    K_DIAG = 4,   // amp *= d[parity(idx & pmask)] (coefs d0 re,im, d1 re,im)
+    K_X = 5,      // swap the t0 pair
+    K_Y = 6,      // [[0,-i],[i,0]] on t0
+    K_SWAP = 7,   // exchange qubits t0 and t1
+    K_DENSE2 = 8, // 4x4 complex on (t0 = bit 0, t1 = bit 1), 32 coefs
+    K_DENSEK = 9  // 2^k x 2^k complex on tk[0..k-1] (bit j = tk[j]), 2*4^k coefs
+};
+
+// DIAG flags
+enum : uint8_t {
+    F_D0_ONE = 1,  // d0 == 1 exactly: parity-0 amplitudes are untouched
+    F_D1_SPEC = 2  // d1 is exactly -1, i or -i (see SP_*), applied without arithmetic
+};
+enum : uint8_t { SP_NEG1 = 1, SP_I = 2, SP_NEGI = 3 };
+
+constexpr int MAXK = 6;  // largest dense target count handled by the global-op kernel
+
+struct GOp {
+    GKind kind;
+    uint8_t flags = 0, special = 0;
+    int t0 = -1, t1 = -1;
+    int k = 0;
+    int tk[MAXK] = {0};
+    uint64_t cmask = 0;  // control qubits (all must be 1)
+    uint64_t pmask = 0;  // DIAG parity qubits
+    std::vector<double> coef;
+    int src = -1;   // index of the circuit op it came from
+    int slot = -1;  // parameter slot (batched / adjoint runs)
+};
+
+// ---------------------------------------------------------------------------
+// Device-side plan records (POD, uploaded once per plan)
+// ---------------------------------------------------------------------------
+// One operation as executed by a kernel.  For register rounds the target
+// fields are register-bit indices and creg/preg are masks over register-index
+// bits; cthr/pthr are masks over global index bits evaluated against the
+// thread's base index.  For whole-state kernels all masks are global.
+struct KOp {
+    uint8_t kind, flags, special, k;
+    uint8_t t0, t1, pad0, pad1;
+    uint32_t creg, preg;
+    uint64_t cthr, pthr;
+    uint32_t coef;  // offset into the coefficient pool (in reals)
+    uint8_t tk[MAXK];
+    uint8_t pad2[2];
+};
+static_assert(sizeof(KOp) == 48, "KOp layout");
+
+constexpr int MAX_TILE = 14;
+
+// A fused pass over the state: tiles of T qubits, the low L of which are the
+// contiguous qubits 0..L-1; tq[] lists the tile's global qubits ascending.
+struct PassDesc {
+    int32_t type;  // PASS_*
+    int32_t T, L, H;
+    int32_t step_begin, step_count;
+    int32_t op_begin, op_count;  // PASS_SMALL / PASS_GLOBALOP: ops applied
+    uint8_t tq[16];
+};
+enum : int32_t { PASS_TILE = 0, PASS_SMALL = 1, PASS_GLOBALOP = 2 };
+static_assert(sizeof(PassDesc) == 48, "PassDesc layout");
+
+// One register round inside a tile pass: register bit k holds tile-local
+// position rpos[k]; thread-index bit k selects tile-local position tpos[k].
+struct StepDesc {
+    int32_t type;  // STEP_*
+    int32_t op_begin, op_count;
+    uint8_t rpos[8];
+    uint8_t tpos[16];
+    uint8_t tglob[16];  // global qubit of thread bit k (= tq[tpos[k]])
+};
+enum : int32_t { STEP_ROUND = 0, STEP_SMEM = 1 };
+static_assert(sizeof(StepDesc) == 52, "StepDesc layout");
+
+struct PlanStats {
+    int64_t passes = 0, rounds = 0, gates = 0;
+    double pass_bytes = 0, gate_bytes = 0;
+};
+
+// Host-side plan (built by plan.cpp, executed by kernels.cu).
+struct HostPlan {
+    int n = 0, precision = QFVM_C128, T = 0, R = 0, L = 0;
+    std::vector<PassDesc> passes;
+    std::vector<StepDesc> steps;
+    std::vector<KOp> ops;
+    std::vector<double> coef;  // FP64 coefficient pool
+    PlanStats stats;
+};
+
+int amp_bytes(int precision);
+int small_max_qubits(int precision);
+void default_shape(int n, int precision, int* T, int* R);
+
+// plan.cpp
+// Classify circuit ops into gops; returns a message on invalid input.
+bool classify(int n, const qfvm_op* ops, int64_t n_ops, const double* matpool, int64_t matpool_len,
+              std::vector<GOp>* out, std::string* err);
+bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R, HostPlan* plan,
+                std::string* err);
+// Gate-equivalent bytes of one gop: 2 * bytes per amplitude * amplitudes it
+// must touch.
+double gop_bytes(const GOp& g, int n, int precision);
+
+}  // namespace qsv

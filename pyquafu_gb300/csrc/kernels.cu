@@ -1,0 +1,487 @@
+// GB300 statevector kernels: whole-state passes, the generic k-target gate,
+// FP64 reductions (Pauli expectation, norms) and the sampling pipeline (block
+// sums, block prefix, per-shot locate, exact fallback).  The fused tile-pass
+// kernel is instantiated per precision in pass_c128.cu / pass_c64.cu.
+#include "device.cuh"
+#include "kernels.h"
+
+namespace qsv {
+
+template <class P>
+__global__ void __launch_bounds__(512) k_small(typename P::G* __restrict__ state, uint64_t stride, int n,
+                                               const KOp* __restrict__ ops, int nops,
+                                               const typename P::C* __restrict__ coef) {
+    constexpr int GB = P::GBITS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    typename P::S* sm = reinterpret_cast<typename P::S*>(smem_raw);
+    typename P::G* st = state + stride * blockIdx.x;
+    const uint32_t N = 1u << n;
+    for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) sm[swz<GB>(i)] = P::g2s(st[i]);
+    __syncthreads();
+    for (int oi = 0; oi < nops; ++oi) {
+        const KOp o = ops[oi];
+        small_apply<P>(sm, n, o, coef);
+        __syncthreads();
+    }
+    for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) st[i] = P::s2g(sm[swz<GB>(i)]);
+}
+
+// ---------------------------------------------------------------------------
+// Dense gate on k targets straight on global memory (large states; rare).
+// ---------------------------------------------------------------------------
+template <class P>
+__global__ void __launch_bounds__(256) k_globalop(typename P::G* __restrict__ state, int n,
+                                                  const KOp* __restrict__ opp, const typename P::C* __restrict__ coef) {
+    using A = typename P::A;
+    using C = typename P::C;
+    const KOp op = *opp;
+    const int k = op.k;
+    const uint32_t dim = 1u << k;
+    uint8_t srt[MAXK];
+    for (int j = 0; j < k; ++j) srt[j] = op.tk[j];
+    for (int x = 1; x < k; ++x)
+        for (int y = x; y > 0 && srt[y - 1] > srt[y]; --y) {
+            uint8_t t = srt[y];
+            srt[y] = srt[y - 1];
+            srt[y - 1] = t;
+        }
+    const uint64_t groups = 1ULL << (n - k);
+    for (uint64_t g = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; g < groups;
+         g += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        uint64_t i = g;
+        for (int j = 0; j < k; ++j) i = insert0(i, srt[j]);
+        if ((i & op.cthr) != op.cthr) continue;
+        A in[1 << MAXK];
+        for (uint32_t m = 0; m < dim; ++m) {
+            uint64_t idx = i;
+            for (int j = 0; j < k; ++j)
+                if ((m >> j) & 1) idx |= 1ULL << op.tk[j];
+            in[m] = P::g2s(state[idx]);
+        }
+        for (uint32_t r = 0; r < dim; ++r) {
+            typename P::R xr = P::mul(P::coef(coef, op.coef + 2 * (r * dim)), in[0].x);
+            typename P::R xi = P::mul(P::coef(coef, op.coef + 2 * (r * dim)), in[0].y);
+            xr = P::madd(P::cneg(P::coef(coef, op.coef + 2 * (r * dim) + 1)), in[0].y, xr);
+            xi = P::madd(P::coef(coef, op.coef + 2 * (r * dim) + 1), in[0].x, xi);
+            for (uint32_t c = 1; c < dim; ++c) {
+                const C mr = P::coef(coef, op.coef + 2 * (r * dim + c));
+                const C mi = P::coef(coef, op.coef + 2 * (r * dim + c) + 1);
+                xr = P::madd(mr, in[c].x, xr);
+                xr = P::madd(P::cneg(mi), in[c].y, xr);
+                xi = P::madd(mr, in[c].y, xi);
+                xi = P::madd(mi, in[c].x, xi);
+            }
+            uint64_t idx = i;
+            for (int j = 0; j < k; ++j)
+                if ((r >> j) & 1) idx |= 1ULL << op.tk[j];
+            A o;
+            o.x = xr;
+            o.y = xi;
+            state[idx] = P::s2g(o);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Utility kernels
+// ---------------------------------------------------------------------------
+template <class P>
+__global__ void k_set_basis(typename P::G* state, uint64_t N, uint64_t index) {
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < N;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        state[i] = P::make_g(i == index ? 1.0 : 0.0, 0.0);
+}
+
+__global__ void k_c128_to_c64(const double2* __restrict__ in, float2* __restrict__ out, uint64_t n) {
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const double2 v = in[i];
+        out[i] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+    }
+}
+
+__global__ void k_c64_to_c128(const float2* __restrict__ in, double2* __restrict__ out, uint64_t n) {
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const float2 v = in[i];
+        out[i] = make_double2(static_cast<double>(v.x), static_cast<double>(v.y));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 reductions
+// ---------------------------------------------------------------------------
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double* red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < NT / 32; ++i) s += red[i];
+    }
+    return s;  // valid in thread 0
+}
+
+// Z-only Pauli terms: sum_j |a_j|^2 (-1)^popcount(j & z_t)  (statevector.hpp:1281-1290)
+template <class P>
+__global__ void __launch_bounds__(256) k_expect_z(const typename P::G* __restrict__ state, uint64_t N,
+                                                  const uint64_t* __restrict__ zm, int nterms,
+                                                  double* __restrict__ partial) {
+    __shared__ double red[8];
+    double acc[EXPECT_BATCH];
+#pragma unroll
+    for (int t = 0; t < EXPECT_BATCH; ++t) acc[t] = 0.0;
+    uint64_t zl[EXPECT_BATCH];
+#pragma unroll
+    for (int t = 0; t < EXPECT_BATCH; ++t) zl[t] = t < nterms ? zm[t] : 0;
+    for (uint64_t j = blockIdx.x * 256ULL + threadIdx.x; j < N; j += gridDim.x * 256ULL) {
+        const typename P::G g = state[j];
+        const double re = P::gre(g), im = P::gim(g);
+        const double p = __fma_rn(re, re, __dmul_rn(im, im));
+#pragma unroll
+        for (int t = 0; t < EXPECT_BATCH; ++t)
+            if (t < nterms) acc[t] += (__popcll(j & zl[t]) & 1) ? -p : p;
+    }
+    for (int t = 0; t < nterms; ++t) {
+        const double s = block_sum<256>(acc[t], red);
+        if (threadIdx.x == 0) partial[static_cast<size_t>(blockIdx.x) * EXPECT_BATCH + t] = s;
+    }
+}
+
+// Terms sharing one flip mask x: sum over pairs (i0, i0^x) of
+// 2 Re(a_i0 conj(a_i1) phase) (statevector.hpp:1291-1304)
+template <class P>
+__global__ void __launch_bounds__(256) k_expect_x(const typename P::G* __restrict__ state, uint64_t N, uint64_t xmask,
+                                                  int flip_q, const uint64_t* __restrict__ zm,
+                                                  const int32_t* __restrict__ ny, int nterms,
+                                                  double* __restrict__ partial) {
+    __shared__ double red[8];
+    double acc[EXPECT_BATCH];
+    uint64_t zl[EXPECT_BATCH];
+    int yl[EXPECT_BATCH];
+#pragma unroll
+    for (int t = 0; t < EXPECT_BATCH; ++t) {
+        acc[t] = 0.0;
+        zl[t] = t < nterms ? zm[t] : 0;
+        yl[t] = t < nterms ? ny[t] : 0;
+    }
+    const uint64_t half = N >> 1;
+    for (uint64_t j = blockIdx.x * 256ULL + threadIdx.x; j < half; j += gridDim.x * 256ULL) {
+        const uint64_t i0 = insert0(j, flip_q), i1 = i0 ^ xmask;
+        const typename P::G a = state[i0], b = state[i1];
+        const double ar = P::gre(a), ai = P::gim(a), br = P::gre(b), bi = P::gim(b);
+        // v = a * conj(b)
+        const double vr = __fma_rn(ar, br, __dmul_rn(ai, bi));
+        const double vi = __fma_rn(ai, br, -__dmul_rn(ar, bi));
+#pragma unroll
+        for (int t = 0; t < EXPECT_BATCH; ++t) {
+            if (t < nterms) {
+                const int ph = ((__popcll(i0 & zl[t]) & 1) * 2 + yl[t]) & 3;
+                const double c = (ph == 0) ? vr : (ph == 1) ? -vi : (ph == 2) ? -vr : vi;
+                acc[t] += 2.0 * c;
+            }
+        }
+    }
+    for (int t = 0; t < nterms; ++t) {
+        const double s = block_sum<256>(acc[t], red);
+        if (threadIdx.x == 0) partial[static_cast<size_t>(blockIdx.x) * EXPECT_BATCH + t] = s;
+    }
+}
+
+__global__ void k_reduce_partials(const double* __restrict__ partial, int nblocks, int nterms,
+                                  double* __restrict__ out) {
+    __shared__ double red[8];
+    for (int t = 0; t < nterms; ++t) {
+        double s = 0.0;
+        for (int b = threadIdx.x; b < nblocks; b += 256) s += partial[static_cast<size_t>(b) * EXPECT_BATCH + t];
+        s = block_sum<256>(s, red);
+        if (threadIdx.x == 0) out[t] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Sampling.  q_i = fl(fl(re^2) + fl(im^2)) exactly as the sequential scan of
+// measure_samples (statevector.hpp:1392-1396) forms it.
+// ---------------------------------------------------------------------------
+template <class P>
+__device__ __forceinline__ double prob_of(const typename P::G g) {
+    const double re = P::gre(g), im = P::gim(g);
+    return __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+}
+
+template <class P>
+__global__ void __launch_bounds__(256) k_block_sums(const typename P::G* __restrict__ state, uint64_t bs,
+                                                    double* __restrict__ bsum) {
+    __shared__ double red[8];
+    const uint64_t b0 = static_cast<uint64_t>(blockIdx.x) * bs;
+    double s = 0.0;
+    for (uint64_t i = threadIdx.x; i < bs; i += 256) s += prob_of<P>(state[b0 + i]);
+    s = block_sum<256>(s, red);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = s;
+}
+
+// Exclusive prefix over nb block sums (one CTA of 1024 threads); pre[nb] = total.
+__global__ void __launch_bounds__(1024) k_scan_blocks(const double* __restrict__ bsum, uint64_t nb,
+                                                      double* __restrict__ pre) {
+    __shared__ double wsum[32];
+    __shared__ double carry_s;
+    if (threadIdx.x == 0) carry_s = 0.0;
+    __syncthreads();
+    const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (uint64_t base = 0; base < nb; base += 1024) {
+        const uint64_t i = base + threadIdx.x;
+        const double v = i < nb ? bsum[i] : 0.0;
+        double x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double y = __shfl_up_sync(0xffffffffu, x, o);
+            if (l >= o) x += y;
+        }
+        if (l == 31) wsum[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            double z = wsum[l];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const double y = __shfl_up_sync(0xffffffffu, z, o);
+                if (l >= o) z += y;
+            }
+            wsum[l] = z;
+        }
+        __syncthreads();
+        const double carry = carry_s;
+        const double incl = x + (w > 0 ? wsum[w - 1] : 0.0) + carry;
+        if (i < nb) pre[i] = incl - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry_s = incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) pre[nb] = carry_s;
+}
+
+// One warp per shot: find the block whose prefix range holds r, scan it with
+// per-lane sequential sums, and certify the answer against the error bound
+// of both summation orders; uncertain shots are resolved by k_sample_exact.
+template <class P>
+__global__ void __launch_bounds__(256) k_sample_locate(const typename P::G* __restrict__ state, uint64_t N,
+                                                       uint64_t bs, uint64_t nb, const double* __restrict__ pre,
+                                                       const double* __restrict__ uni, int64_t shots,
+                                                       uint64_t* __restrict__ out, uint8_t* __restrict__ unsure) {
+    const int lane = threadIdx.x & 31;
+    const int64_t s = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (s >= shots) return;
+    const double r = uni[s];
+    const double total = pre[nb];
+    const double u = 1.1102230246251565e-16;  // 2^-53
+    const double scale = (total > 1.0 ? total : 1.0) * 1.01 * u;
+    const double gerr = (2.0 * static_cast<double>(bs) + static_cast<double>(nb) + 8.0) * scale;
+    if (r >= total) {
+        // the reference loop ends with sample = N
+        const double d = static_cast<double>(N + 1) * scale + gerr;
+        if (lane == 0) {
+            out[s] = N;
+            unsure[s] = (r < total + d) ? 1 : 0;
+        }
+        return;
+    }
+    // largest b with pre[b] <= r
+    uint64_t lo = 0, hi = nb - 1;
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi + 1) >> 1;
+        if (pre[mid] <= r) lo = mid;
+        else hi = mid - 1;
+    }
+    const uint64_t b = lo;
+    const uint64_t per = (bs + 31) / 32;
+    const uint64_t i0 = b * bs + lane * per;
+    const uint64_t i1 = (i0 + per < (b + 1) * bs) ? i0 + per : (b + 1) * bs;
+    double ls = 0.0;
+    for (uint64_t i = i0; i < i1; ++i) ls += prob_of<P>(state[i]);
+    double incl = ls;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const double start = pre[b] + (incl - ls);
+    // find the first index k in this lane's range with r < running sum
+    double run = start, prev = start;
+    uint64_t found = ~0ULL;
+    for (uint64_t i = i0; i < i1; ++i) {
+        prev = run;
+        run += prob_of<P>(state[i]);
+        if (r < run) {
+            found = i;
+            break;
+        }
+    }
+    const unsigned ball = __ballot_sync(0xffffffffu, found != ~0ULL);
+    if (ball == 0) {
+        if (lane == 0) {
+            out[s] = N;
+            unsure[s] = 1;
+        }
+        return;
+    }
+    const int first = __ffs(ball) - 1;
+    if (lane == first) {
+        const double d = static_cast<double>(found + 2) * scale * (run > 1.0 ? run : 1.0) + gerr;
+        out[s] = found;
+        unsure[s] = (r < run - d && r >= prev + d) ? 0 : 1;
+    }
+}
+
+// Exact sequential scan (one thread) for the shots flagged as uncertain;
+// `ord` lists them by increasing uniform.  The loop is bounded by N.
+template <class P>
+__global__ void k_sample_exact(const typename P::G* __restrict__ state, uint64_t N, const double* __restrict__ uni,
+                               const int64_t* __restrict__ ord, int64_t m, uint64_t* __restrict__ out) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    double p = 0.0;
+    int64_t k = 0;
+    for (uint64_t i = 0; i < N && k < m; ++i) {
+        p = __dadd_rn(p, prob_of<P>(state[i]));
+        while (k < m && uni[ord[k]] < p) {
+            out[ord[k]] = i;
+            ++k;
+        }
+    }
+    for (; k < m; ++k) out[ord[k]] = N;
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------
+bool pass_shape_supported(int precision, int T, int R) {
+    return precision == QFVM_C64 ? pass_shape_c64(T, R) : pass_shape_c128(T, R);
+}
+
+cudaError_t launch_tile_pass(int precision, int T, int R, void* state, const PassDesc* dpass,
+                             const StepDesc* dsteps, const KOp* dops, const void* dcoef, int n, int H,
+                             cudaStream_t st) {
+    if (precision == QFVM_C64) return launch_pass_c64(T, R, state, dpass, dsteps, dops, dcoef, n, H, st);
+    return launch_pass_c128(T, R, state, dpass, dsteps, dops, dcoef, n, H, st);
+}
+
+cudaError_t launch_small(int precision, void* state, uint64_t stride, int batch, int n, const KOp* dops, int nops,
+                         const void* dcoef, cudaStream_t st) {
+    const int threads = n >= 10 ? 512 : 256;
+    if (precision == QFVM_C64) {
+        const size_t smem = sizeof(float2) << n;
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(k_small<P32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 static_cast<int>(smem));
+            if (e != cudaSuccess) return e;
+        }
+        k_small<P32><<<batch, threads, smem, st>>>(static_cast<float2*>(state), stride, n, dops, nops,
+                                                  static_cast<const float*>(dcoef));
+    } else {
+        const size_t smem = sizeof(double2) << n;
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(k_small<P64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 static_cast<int>(smem));
+            if (e != cudaSuccess) return e;
+        }
+        k_small<P64><<<batch, threads, smem, st>>>(static_cast<double2*>(state), stride, n, dops, nops,
+                                                  static_cast<const double*>(dcoef));
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_globalop(int precision, void* state, int n, const KOp* dop, const void* dcoef,
+                            cudaStream_t st) {
+    const uint64_t groups = 1ULL << (n - 1);
+    const unsigned blocks = static_cast<unsigned>(groups / 256 < 152 * 16 ? (groups + 255) / 256 : 152 * 16);
+    if (precision == QFVM_C64)
+        k_globalop<P32><<<blocks, 256, 0, st>>>(static_cast<float2*>(state), n, dop, static_cast<const float*>(dcoef));
+    else
+        k_globalop<P64><<<blocks, 256, 0, st>>>(static_cast<double2*>(state), n, dop,
+                                               static_cast<const double*>(dcoef));
+    return cudaGetLastError();
+}
+
+static unsigned grid_for(uint64_t work, unsigned per_block, unsigned cap) {
+    uint64_t b = (work + per_block - 1) / per_block;
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return static_cast<unsigned>(b);
+}
+
+cudaError_t launch_set_basis(int precision, void* state, uint64_t N, uint64_t index, cudaStream_t st) {
+    const unsigned g = grid_for(N, 256, 152 * 32);
+    if (precision == QFVM_C64) k_set_basis<P32><<<g, 256, 0, st>>>(static_cast<float2*>(state), N, index);
+    else k_set_basis<P64><<<g, 256, 0, st>>>(static_cast<double2*>(state), N, index);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_convert(bool to64, const void* in, void* out, uint64_t n, cudaStream_t st) {
+    const unsigned g = grid_for(n, 256, 152 * 32);
+    if (to64) k_c128_to_c64<<<g, 256, 0, st>>>(static_cast<const double2*>(in), static_cast<float2*>(out), n);
+    else k_c64_to_c128<<<g, 256, 0, st>>>(static_cast<const float2*>(in), static_cast<double2*>(out), n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_expect_z(int precision, const void* state, uint64_t N, const uint64_t* dzm, int nterms,
+                            double* dpartial, int nblocks, cudaStream_t st) {
+    if (precision == QFVM_C64)
+        k_expect_z<P32><<<nblocks, 256, 0, st>>>(static_cast<const float2*>(state), N, dzm, nterms, dpartial);
+    else
+        k_expect_z<P64><<<nblocks, 256, 0, st>>>(static_cast<const double2*>(state), N, dzm, nterms, dpartial);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_expect_x(int precision, const void* state, uint64_t N, uint64_t xmask, int flip_q,
+                            const uint64_t* dzm, const int32_t* dny, int nterms, double* dpartial, int nblocks,
+                            cudaStream_t st) {
+    if (precision == QFVM_C64)
+        k_expect_x<P32><<<nblocks, 256, 0, st>>>(static_cast<const float2*>(state), N, xmask, flip_q, dzm, dny,
+                                                 nterms, dpartial);
+    else
+        k_expect_x<P64><<<nblocks, 256, 0, st>>>(static_cast<const double2*>(state), N, xmask, flip_q, dzm, dny,
+                                                 nterms, dpartial);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_partials(const double* dpartial, int nblocks, int nterms, double* dout, cudaStream_t st) {
+    k_reduce_partials<<<1, 256, 0, st>>>(dpartial, nblocks, nterms, dout);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sample(int precision, const void* state, uint64_t N, uint64_t bs, double* dbsum, double* dpre,
+                          const double* duni, int64_t shots, uint64_t* dout, uint8_t* dunsure, cudaStream_t st) {
+    const uint64_t nb = N / bs;
+    if (precision == QFVM_C64)
+        k_block_sums<P32><<<static_cast<unsigned>(nb), 256, 0, st>>>(static_cast<const float2*>(state), bs, dbsum);
+    else
+        k_block_sums<P64><<<static_cast<unsigned>(nb), 256, 0, st>>>(static_cast<const double2*>(state), bs, dbsum);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_scan_blocks<<<1, 1024, 0, st>>>(dbsum, nb, dpre);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (shots > 0) {
+        const unsigned blocks = static_cast<unsigned>((shots * 32 + 255) / 256);
+        if (precision == QFVM_C64)
+            k_sample_locate<P32><<<blocks, 256, 0, st>>>(static_cast<const float2*>(state), N, bs, nb, dpre, duni,
+                                                         shots, dout, dunsure);
+        else
+            k_sample_locate<P64><<<blocks, 256, 0, st>>>(static_cast<const double2*>(state), N, bs, nb, dpre, duni,
+                                                         shots, dout, dunsure);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sample_exact(int precision, const void* state, uint64_t N, const double* duni,
+                                const int64_t* dord, int64_t m, uint64_t* dout, cudaStream_t st) {
+    if (precision == QFVM_C64)
+        k_sample_exact<P32><<<1, 32, 0, st>>>(static_cast<const float2*>(state), N, duni, dord, m, dout);
+    else
+        k_sample_exact<P64><<<1, 32, 0, st>>>(static_cast<const double2*>(state), N, duni, dord, m, dout);
+    return cudaGetLastError();
+}
+
+}  // namespace qsv

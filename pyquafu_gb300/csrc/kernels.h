@@ -1,0 +1,41 @@
+// Host-side launchers of the statevector kernels (kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "engine.h"
+
+namespace qsv {
+
+constexpr int EXPECT_BATCH = 8;   // Pauli terms reduced per kernel launch
+constexpr int REDUCE_BLOCKS = 152 * 4;
+
+bool pass_shape_supported(int precision, int T, int R);
+bool pass_shape_c128(int T, int R);
+bool pass_shape_c64(int T, int R);
+cudaError_t launch_pass_c128(int T, int R, void* state, const PassDesc* dpass, const StepDesc* dsteps,
+                             const KOp* dops, const void* dcoef, int n, int H, cudaStream_t st);
+cudaError_t launch_pass_c64(int T, int R, void* state, const PassDesc* dpass, const StepDesc* dsteps,
+                            const KOp* dops, const void* dcoef, int n, int H, cudaStream_t st);
+
+cudaError_t launch_tile_pass(int precision, int T, int R, void* state, const PassDesc* dpass,
+                             const StepDesc* dsteps, const KOp* dops, const void* dcoef, int n, int H,
+                             cudaStream_t st);
+cudaError_t launch_small(int precision, void* state, uint64_t stride, int batch, int n, const KOp* dops, int nops,
+                         const void* dcoef, cudaStream_t st);
+cudaError_t launch_globalop(int precision, void* state, int n, const KOp* dop, const void* dcoef,
+                            cudaStream_t st);
+cudaError_t launch_set_basis(int precision, void* state, uint64_t N, uint64_t index, cudaStream_t st);
+cudaError_t launch_convert(bool to64, const void* in, void* out, uint64_t n, cudaStream_t st);
+cudaError_t launch_expect_z(int precision, const void* state, uint64_t N, const uint64_t* dzm, int nterms,
+                            double* dpartial, int nblocks, cudaStream_t st);
+cudaError_t launch_expect_x(int precision, const void* state, uint64_t N, uint64_t xmask, int flip_q,
+                            const uint64_t* dzm, const int32_t* dny, int nterms, double* dpartial, int nblocks,
+                            cudaStream_t st);
+cudaError_t launch_reduce_partials(const double* dpartial, int nblocks, int nterms, double* dout, cudaStream_t st);
+cudaError_t launch_sample(int precision, const void* state, uint64_t N, uint64_t bs, double* dbsum, double* dpre,
+                          const double* duni, int64_t shots, uint64_t* dout, uint8_t* dunsure, cudaStream_t st);
+cudaError_t launch_sample_exact(int precision, const void* state, uint64_t N, const double* duni,
+                                const int64_t* dord, int64_t m, uint64_t* dout, cudaStream_t st);
+
+}  // namespace qsv

@@ -1,0 +1,651 @@
+// Host planner: classify circuit gates and fuse them into tile passes.
+//
+// Classification follows the reference's dispatch (src/qfvm/simulator.hpp:
+// 12-113) and matrix construction (src/qfvm/statevector.hpp:340-437); the
+// fuser is this engine's own: gates are grouped into passes over tiles of T
+// qubits (the low L qubits are always in the tile so that HBM accesses are
+// contiguous runs), and inside a pass into register rounds of R qubits.
+// Diagonal gates and controls need no tile membership: they are evaluated
+// from each amplitude's global index, so only the targets of non-diagonal
+// gates constrain the schedule.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <set>
+
+#include "engine.h"
+
+namespace qsv {
+
+int amp_bytes(int precision) { return precision == QFVM_C64 ? 8 : 16; }
+
+// Largest state handled by the whole-state (single CTA, shared memory) kernel.
+int small_max_qubits(int precision) { return precision == QFVM_C64 ? 14 : 13; }
+
+void default_shape(int n, int precision, int* T, int* R) {
+    if (precision == QFVM_C64) {
+        *T = 13;
+        *R = 5;
+    } else {
+        *T = 12;
+        *R = 4;
+    }
+    (void)n;
+}
+
+namespace {
+
+using cd = std::complex<double>;
+
+void set_diag(GOp& g, cd d0, cd d1) {
+    g.kind = K_DIAG;
+    g.coef = {d0.real(), d0.imag(), d1.real(), d1.imag()};
+    if (d0 == cd(1.0, 0.0)) {
+        g.flags |= F_D0_ONE;
+        if (d1 == cd(-1.0, 0.0)) {
+            g.flags |= F_D1_SPEC;
+            g.special = SP_NEG1;
+        } else if (d1 == cd(0.0, 1.0)) {
+            g.flags |= F_D1_SPEC;
+            g.special = SP_I;
+        } else if (d1 == cd(0.0, -1.0)) {
+            g.flags |= F_D1_SPEC;
+            g.special = SP_NEGI;
+        }
+    }
+}
+
+bool is_zero(cd z) { return z.real() == 0.0 && z.imag() == 0.0; }
+
+}  // namespace
+
+bool classify(int n, const qfvm_op* ops, int64_t n_ops, const double* matpool, int64_t matpool_len,
+              std::vector<GOp>* out, std::string* err) {
+    out->clear();
+    out->reserve(static_cast<size_t>(n_ops));
+    const double PI_ = 3.14159265358979323846;
+    for (int64_t i = 0; i < n_ops; ++i) {
+        const qfvm_op& o = ops[i];
+        const int nq = o.nqubits;
+        if (nq < 1 || nq > QFVM_MAX_OP_QUBITS) {
+            *err = "op " + std::to_string(i) + ": bad qubit count " + std::to_string(nq);
+            return false;
+        }
+        uint64_t seen = 0;
+        for (int j = 0; j < nq; ++j) {
+            int q = o.qubits[j];
+            if (q < 0 || q >= n) {
+                *err = "op " + std::to_string(i) + ": qubit " + std::to_string(q) + " outside a " +
+                       std::to_string(n) + "-qubit state";
+                return false;
+            }
+            if (seen & (1ULL << q)) {
+                *err = "op " + std::to_string(i) + ": repeated qubit " + std::to_string(q);
+                return false;
+            }
+            seen |= 1ULL << q;
+        }
+        for (int j = 0; j < 4; ++j) {
+            if (!std::isfinite(o.params[j])) {
+                *err = "op " + std::to_string(i) + ": non-finite parameter";
+                return false;
+            }
+        }
+        GOp g;
+        g.src = static_cast<int>(i);
+        g.slot = o.slot;
+        const int* q = o.qubits;
+        auto need = [&](int k) {
+            if (nq < k) {
+                *err = "op " + std::to_string(i) + ": gate kind " + std::to_string(o.kind) + " needs " +
+                       std::to_string(k) + " qubits";
+                return false;
+            }
+            return true;
+        };
+        const double th = o.params[0];
+        switch (o.kind) {
+            case QFVM_OP_X:
+                g.kind = K_X;
+                g.t0 = q[0];
+                break;
+            case QFVM_OP_Y:
+                g.kind = K_Y;
+                g.t0 = q[0];
+                break;
+            case QFVM_OP_Z:
+                g.pmask = 1ULL << q[0];
+                set_diag(g, 1.0, -1.0);
+                break;
+            case QFVM_OP_H: {
+                const double s = 1. / std::sqrt(2.);
+                g.kind = K_REAL;
+                g.t0 = q[0];
+                g.coef = {s, s, s, -s};
+                break;
+            }
+            case QFVM_OP_S:
+                g.pmask = 1ULL << q[0];
+                set_diag(g, 1.0, cd(0, 1));
+                break;
+            case QFVM_OP_SDG:
+                g.pmask = 1ULL << q[0];
+                set_diag(g, 1.0, cd(0, -1));
+                break;
+            case QFVM_OP_T:
+            case QFVM_OP_TDG: {
+                const double a = (o.kind == QFVM_OP_T ? 1.0 : -1.0) * PI_ / 4.;
+                g.pmask = 1ULL << q[0];
+                set_diag(g, 1.0, cd(std::cos(a), std::sin(a)));
+                break;
+            }
+            case QFVM_OP_P:
+                g.pmask = 1ULL << q[0];
+                set_diag(g, 1.0, cd(std::cos(th), std::sin(th)));
+                break;
+            case QFVM_OP_RX:
+                g.kind = K_RX;
+                g.t0 = q[0];
+                g.coef = {std::cos(th / 2), std::sin(th / 2)};
+                break;
+            case QFVM_OP_RY: {
+                const double c = std::cos(th / 2), s = std::sin(th / 2);
+                g.kind = K_REAL;
+                g.t0 = q[0];
+                g.coef = {c, -s, s, c};
+                break;
+            }
+            case QFVM_OP_RZ: {
+                const double h = th / 2.;
+                g.pmask = 1ULL << q[0];
+                set_diag(g, cd(std::cos(-h), std::sin(-h)), cd(std::cos(h), std::sin(h)));
+                break;
+            }
+            case QFVM_OP_CX:
+                if (!need(2)) return false;
+                g.kind = K_X;
+                g.cmask = 1ULL << q[0];
+                g.t0 = q[1];
+                break;
+            case QFVM_OP_CZ:
+                if (!need(2)) return false;
+                g.cmask = 1ULL << q[0];
+                g.pmask = 1ULL << q[1];
+                set_diag(g, 1.0, -1.0);
+                break;
+            case QFVM_OP_CP:
+                if (!need(2)) return false;
+                g.cmask = 1ULL << q[0];
+                g.pmask = 1ULL << q[1];
+                set_diag(g, 1.0, cd(std::cos(th), std::sin(th)));
+                break;
+            case QFVM_OP_CCX:
+                if (!need(3)) return false;
+                g.kind = K_X;
+                g.cmask = (1ULL << q[0]) | (1ULL << q[1]);
+                g.t0 = q[2];
+                break;
+            case QFVM_OP_RZZ: {
+                // simulator.hpp:90-94 applies cx . rz . cx: a phase by the parity of the two qubits.
+                if (!need(2)) return false;
+                const double h = th / 2.;
+                g.pmask = (1ULL << q[0]) | (1ULL << q[1]);
+                set_diag(g, cd(std::cos(-h), std::sin(-h)), cd(std::cos(h), std::sin(h)));
+                break;
+            }
+            case QFVM_OP_MATRIX: {
+                const int nc = o.ncontrols;
+                const int k = nq - nc;
+                if (nc < 0 || k < 1) {
+                    *err = "op " + std::to_string(i) + ": matrix gate without a target";
+                    return false;
+                }
+                if (k > MAXK) {
+                    *err = "op " + std::to_string(i) + ": " + std::to_string(k) + "-target matrix gates are not supported";
+                    return false;
+                }
+                const int64_t dim = 1LL << k;
+                if (o.mat_dim != dim || o.mat_offset < 0 || o.mat_offset + dim * dim > matpool_len) {
+                    *err = "op " + std::to_string(i) + ": matrix does not match its target count";
+                    return false;
+                }
+                const cd* m = reinterpret_cast<const cd*>(matpool) + o.mat_offset;
+                for (int j = 0; j < nc; ++j) g.cmask |= 1ULL << q[j];
+                for (int64_t j = 0; j < dim * dim; ++j) {
+                    if (!std::isfinite(m[j].real()) || !std::isfinite(m[j].imag())) {
+                        *err = "op " + std::to_string(i) + ": non-finite matrix entry";
+                        return false;
+                    }
+                }
+                if (k == 1) {
+                    const int t = q[nc];
+                    g.t0 = t;
+                    if (is_zero(m[1]) && is_zero(m[2])) {
+                        g.pmask = 1ULL << t;
+                        set_diag(g, m[0], m[3]);
+                    } else if (is_zero(m[0]) && is_zero(m[3]) && m[1] == cd(1, 0) && m[2] == cd(1, 0)) {
+                        g.kind = K_X;
+                    } else if (m[0].imag() == 0 && m[1].imag() == 0 && m[2].imag() == 0 && m[3].imag() == 0) {
+                        g.kind = K_REAL;
+                        g.coef = {m[0].real(), m[1].real(), m[2].real(), m[3].real()};
+                    } else {
+                        g.kind = K_DENSE;
+                        g.coef.resize(8);
+                        for (int j = 0; j < 4; ++j) {
+                            g.coef[2 * j] = m[j].real();
+                            g.coef[2 * j + 1] = m[j].imag();
+                        }
+                    }
+                } else if (k == 2) {
+                    g.t0 = q[nc];
+                    g.t1 = q[nc + 1];
+                    bool swap = true;
+                    for (int r = 0; r < 4 && swap; ++r)
+                        for (int c = 0; c < 4; ++c) {
+                            int want = (r == 0 && c == 0) || (r == 3 && c == 3) || (r == 1 && c == 2) ||
+                                       (r == 2 && c == 1);
+                            if (m[r * 4 + c] != cd(want ? 1.0 : 0.0, 0.0)) {
+                                swap = false;
+                                break;
+                            }
+                        }
+                    if (swap) {
+                        g.kind = K_SWAP;
+                    } else {
+                        g.kind = K_DENSE2;
+                        g.coef.resize(32);
+                        for (int j = 0; j < 16; ++j) {
+                            g.coef[2 * j] = m[j].real();
+                            g.coef[2 * j + 1] = m[j].imag();
+                        }
+                    }
+                } else {
+                    g.kind = K_DENSEK;
+                    g.k = k;
+                    for (int j = 0; j < k; ++j) g.tk[j] = q[nc + j];
+                    g.coef.resize(static_cast<size_t>(2 * dim * dim));
+                    for (int64_t j = 0; j < dim * dim; ++j) {
+                        g.coef[2 * j] = m[j].real();
+                        g.coef[2 * j + 1] = m[j].imag();
+                    }
+                }
+                break;
+            }
+            default:
+                *err = "op " + std::to_string(i) + ": kind " + std::to_string(o.kind) +
+                       " is not a gate this entry point applies";
+                return false;
+        }
+        if (g.kind == K_X || g.kind == K_Y || g.kind == K_REAL || g.kind == K_RX || g.kind == K_DENSE) {
+            if (g.cmask & (1ULL << g.t0)) {
+                *err = "op " + std::to_string(i) + ": target is also a control";
+                return false;
+            }
+        }
+        out->push_back(std::move(g));
+    }
+    return true;
+}
+
+double gop_bytes(const GOp& g, int n, int precision) {
+    const double N = std::ldexp(1.0, n);
+    const int nc = __builtin_popcountll(g.cmask);
+    double amps = N / std::ldexp(1.0, nc);
+    switch (g.kind) {
+        case K_DIAG:
+            if (g.flags & F_D0_ONE) amps *= 0.5;
+            break;
+        case K_SWAP:
+            amps *= 0.5;
+            break;
+        default:
+            break;
+    }
+    return 2.0 * amp_bytes(precision) * amps;
+}
+
+namespace {
+
+// Qubit actions for commutation: two gates commute if on every shared qubit
+// both act diagonally (controls, phases) or both act as X (targets of X/CX).
+enum Act : uint8_t { A_Z = 1, A_X = 2, A_G = 4 };
+
+void gop_actions(const GOp& g, std::vector<std::pair<int, uint8_t>>* acts) {
+    acts->clear();
+    for (int q = 0; q < 64; ++q) {
+        if (g.cmask & (1ULL << q)) acts->push_back({q, A_Z});
+        if (g.pmask & (1ULL << q)) acts->push_back({q, A_Z});
+    }
+    switch (g.kind) {
+        case K_X: acts->push_back({g.t0, A_X}); break;
+        case K_DIAG: break;
+        case K_SWAP:
+        case K_DENSE2:
+            acts->push_back({g.t0, A_G});
+            acts->push_back({g.t1, A_G});
+            break;
+        case K_DENSEK:
+            for (int j = 0; j < g.k; ++j) acts->push_back({g.tk[j], A_G});
+            break;
+        default: acts->push_back({g.t0, A_G}); break;
+    }
+}
+
+bool act_conflict(uint8_t blocked, uint8_t a) {
+    if (!blocked) return false;
+    if (a == A_Z) return (blocked & (A_X | A_G)) != 0;
+    if (a == A_X) return (blocked & (A_Z | A_G)) != 0;
+    return true;
+}
+
+void gop_targets(const GOp& g, std::vector<int>* t) {
+    t->clear();
+    switch (g.kind) {
+        case K_DIAG: break;
+        case K_SWAP:
+        case K_DENSE2:
+            t->push_back(g.t0);
+            t->push_back(g.t1);
+            break;
+        case K_DENSEK:
+            for (int j = 0; j < g.k; ++j) t->push_back(g.tk[j]);
+            break;
+        default: t->push_back(g.t0); break;
+    }
+}
+
+// Copy a gop's coefficients into the pool and return the offset.
+uint32_t push_coef(HostPlan* p, const GOp& g) {
+    uint32_t off = static_cast<uint32_t>(p->coef.size());
+    p->coef.insert(p->coef.end(), g.coef.begin(), g.coef.end());
+    return off;
+}
+
+// Whole-state op record: all masks over global index bits.
+KOp global_kop(HostPlan* p, const GOp& g) {
+    KOp k;
+    std::memset(&k, 0, sizeof(k));
+    k.kind = g.kind;
+    k.flags = g.flags;
+    k.special = g.special;
+    k.t0 = static_cast<uint8_t>(g.t0 < 0 ? 0 : g.t0);
+    k.t1 = static_cast<uint8_t>(g.t1 < 0 ? 0 : g.t1);
+    k.k = static_cast<uint8_t>(g.k);
+    for (int j = 0; j < g.k; ++j) k.tk[j] = static_cast<uint8_t>(g.tk[j]);
+    k.cthr = g.cmask;
+    k.pthr = g.pmask;
+    k.coef = push_coef(p, g);
+    return k;
+}
+
+// Thread-bit order for a register round: the first lanes get positions whose
+// residues modulo `gbits` are all distinct, which makes the shared-memory
+// swizzle of the kernels map each wavefront to distinct bank groups.
+void order_thread_bits(std::vector<int>& free_pos, int gbits) {
+    std::vector<int> head, rest;
+    std::vector<bool> used(free_pos.size(), false);
+    for (int r = 0; r < gbits; ++r) {
+        for (size_t i = 0; i < free_pos.size(); ++i) {
+            if (!used[i] && free_pos[i] % gbits == r) {
+                head.push_back(free_pos[i]);
+                used[i] = true;
+                break;
+            }
+        }
+    }
+    for (size_t i = 0; i < free_pos.size(); ++i)
+        if (!used[i]) rest.push_back(free_pos[i]);
+    free_pos = head;
+    free_pos.insert(free_pos.end(), rest.begin(), rest.end());
+}
+
+}  // namespace
+
+bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R, HostPlan* plan,
+                std::string* err) {
+    *plan = HostPlan();
+    plan->n = n;
+    plan->precision = precision;
+    if (n < 1 || n > QFVM_MAX_QUBITS) {
+        *err = "qubit count " + std::to_string(n) + " outside 1.." + std::to_string(QFVM_MAX_QUBITS);
+        return false;
+    }
+    int dT, dR;
+    default_shape(n, precision, &dT, &dR);
+    if (T <= 0) T = dT;
+    if (R <= 0) R = dR;
+    if (T < 6 || T > MAX_TILE || R < 2 || R > 6 || R >= T) {
+        *err = "invalid tile shape";
+        return false;
+    }
+    const double Sb = amp_bytes(precision);
+    const double N = std::ldexp(1.0, n);
+    PlanStats& st = plan->stats;
+    st.gates = static_cast<int64_t>(gops.size());
+    for (const auto& g : gops) st.gate_bytes += gop_bytes(g, n, precision);
+
+    // Small states: one whole-state pass with every gate in order.
+    if (n < T) {
+        if (n > small_max_qubits(precision)) {
+            *err = "state too large for the whole-state kernel";
+            return false;
+        }
+        PassDesc pd;
+        std::memset(&pd, 0, sizeof(pd));
+        pd.type = PASS_SMALL;
+        pd.T = n;
+        pd.op_begin = 0;
+        for (const auto& g : gops) plan->ops.push_back(global_kop(plan, g));
+        pd.op_count = static_cast<int32_t>(plan->ops.size());
+        plan->passes.push_back(pd);
+        st.passes = 1;
+        st.rounds = 0;
+        st.pass_bytes = 2.0 * Sb * N;
+        plan->T = n;
+        plan->R = 0;
+        plan->L = n;
+        return true;
+    }
+
+    const int L = std::min(5, T - 1);
+    const int H = T - L;
+    plan->T = T;
+    plan->R = R;
+    plan->L = L;
+    const int gbits = (precision == QFVM_C64) ? 4 : 3;
+
+    std::vector<int> pending(gops.size());
+    for (size_t i = 0; i < gops.size(); ++i) pending[i] = static_cast<int>(i);
+    std::vector<std::pair<int, uint8_t>> acts;
+    std::vector<int> targ;
+
+    while (!pending.empty()) {
+        // ---- choose the tile's high qubits and the gates of this pass ----
+        uint8_t blocked[64] = {0};
+        std::vector<int> high;  // global qubits >= L in the tile
+        std::vector<int> sched, rest;
+        for (int gi : pending) {
+            const GOp& g = gops[gi];
+            gop_actions(g, &acts);
+            bool conflict = false;
+            for (auto& a : acts) conflict |= act_conflict(blocked[a.first], a.second);
+            bool ok = !conflict && g.kind != K_DENSEK;
+            if (ok) {
+                gop_targets(g, &targ);
+                std::vector<int> add;
+                for (int t : targ)
+                    if (t >= L && std::find(high.begin(), high.end(), t) == high.end() &&
+                        std::find(add.begin(), add.end(), t) == add.end())
+                        add.push_back(t);
+                if (static_cast<int>(high.size() + add.size()) <= H) {
+                    high.insert(high.end(), add.begin(), add.end());
+                } else {
+                    ok = false;
+                }
+            }
+            if (ok) {
+                sched.push_back(gi);
+            } else {
+                for (auto& a : acts) blocked[a.first] |= a.second;
+                rest.push_back(gi);
+            }
+        }
+        if (sched.empty()) {
+            // The first pending gate cannot join a tile pass (a dense gate on
+            // more than two targets): apply it on its own.
+            const int gi = pending.front();
+            PassDesc pd;
+            std::memset(&pd, 0, sizeof(pd));
+            pd.type = PASS_GLOBALOP;
+            pd.op_begin = static_cast<int32_t>(plan->ops.size());
+            pd.op_count = 1;
+            plan->ops.push_back(global_kop(plan, gops[gi]));
+            plan->passes.push_back(pd);
+            st.passes += 1;
+            st.pass_bytes += 2.0 * Sb * N;
+            pending.erase(pending.begin());
+            continue;
+        }
+        // fill the tile to exactly T qubits
+        for (int q = L; q < n && static_cast<int>(high.size()) < H; ++q)
+            if (std::find(high.begin(), high.end(), q) == high.end()) high.push_back(q);
+        std::sort(high.begin(), high.end());
+        PassDesc pd;
+        std::memset(&pd, 0, sizeof(pd));
+        pd.type = PASS_TILE;
+        pd.T = T;
+        pd.L = L;
+        pd.H = H;
+        int local_of[64];
+        for (int q = 0; q < 64; ++q) local_of[q] = -1;
+        for (int k = 0; k < L; ++k) {
+            pd.tq[k] = static_cast<uint8_t>(k);
+            local_of[k] = k;
+        }
+        for (int k = 0; k < H; ++k) {
+            pd.tq[L + k] = static_cast<uint8_t>(high[k]);
+            local_of[high[k]] = L + k;
+        }
+        pd.step_begin = static_cast<int32_t>(plan->steps.size());
+
+        // ---- split the pass's gates into register rounds ----
+        // Two-target dense gates run as shared-memory steps of the tile (in
+        // order); everything else runs in register rounds.
+        std::vector<int> todo = sched;
+        while (!todo.empty()) {
+            if (gops[todo.front()].kind == K_DENSE2) {
+                const GOp& g = gops[todo.front()];
+                StepDesc sd;
+                std::memset(&sd, 0, sizeof(sd));
+                sd.type = STEP_SMEM;
+                sd.op_begin = static_cast<int32_t>(plan->ops.size());
+                sd.op_count = 1;
+                KOp ko;
+                std::memset(&ko, 0, sizeof(ko));
+                ko.kind = g.kind;
+                ko.t0 = static_cast<uint8_t>(local_of[g.t0]);
+                ko.t1 = static_cast<uint8_t>(local_of[g.t1]);
+                for (int q = 0; q < n; ++q) {
+                    const uint64_t b = 1ULL << q;
+                    if (g.cmask & b) {
+                        if (local_of[q] >= 0) ko.creg |= 1u << local_of[q];
+                        else ko.cthr |= b;
+                    }
+                }
+                ko.coef = push_coef(plan, g);
+                plan->ops.push_back(ko);
+                plan->steps.push_back(sd);
+                st.rounds += 1;
+                todo.erase(todo.begin());
+                continue;
+            }
+            uint8_t rblocked[64] = {0};
+            std::vector<int> regs;  // tile-local positions
+            std::vector<int> round_ops, left;
+            for (int gi : todo) {
+                const GOp& g = gops[gi];
+                gop_actions(g, &acts);
+                bool conflict = false;
+                for (auto& a : acts) conflict |= act_conflict(rblocked[a.first], a.second);
+                bool ok = !conflict && g.kind != K_DENSE2;
+                if (ok) {
+                    gop_targets(g, &targ);
+                    std::vector<int> add;
+                    for (int t : targ) {
+                        int lp = local_of[t];
+                        if (std::find(regs.begin(), regs.end(), lp) == regs.end() &&
+                            std::find(add.begin(), add.end(), lp) == add.end())
+                            add.push_back(lp);
+                    }
+                    if (static_cast<int>(regs.size() + add.size()) <= R)
+                        regs.insert(regs.end(), add.begin(), add.end());
+                    else
+                        ok = false;
+                }
+                if (ok) {
+                    round_ops.push_back(gi);
+                } else {
+                    for (auto& a : acts) rblocked[a.first] |= a.second;
+                    left.push_back(gi);
+                }
+            }
+            // pad the register set with the lowest unused positions
+            for (int p = 0; p < T && static_cast<int>(regs.size()) < R; ++p)
+                if (std::find(regs.begin(), regs.end(), p) == regs.end()) regs.push_back(p);
+            StepDesc sd;
+            std::memset(&sd, 0, sizeof(sd));
+            sd.type = STEP_ROUND;
+            for (int k = 0; k < R; ++k) sd.rpos[k] = static_cast<uint8_t>(regs[k]);
+            std::vector<int> freep;
+            for (int p = 0; p < T; ++p)
+                if (std::find(regs.begin(), regs.end(), p) == regs.end()) freep.push_back(p);
+            order_thread_bits(freep, gbits);
+            for (size_t k = 0; k < freep.size(); ++k) {
+                sd.tpos[k] = static_cast<uint8_t>(freep[k]);
+                sd.tglob[k] = pd.tq[freep[k]];
+            }
+            int reg_of_local[MAX_TILE];
+            for (int p = 0; p < MAX_TILE; ++p) reg_of_local[p] = -1;
+            for (int k = 0; k < R; ++k) reg_of_local[regs[k]] = k;
+            sd.op_begin = static_cast<int32_t>(plan->ops.size());
+            for (int gi : round_ops) {
+                const GOp& g = gops[gi];
+                KOp ko;
+                std::memset(&ko, 0, sizeof(ko));
+                ko.kind = g.kind;
+                ko.flags = g.flags;
+                ko.special = g.special;
+                if (g.t0 >= 0) ko.t0 = static_cast<uint8_t>(reg_of_local[local_of[g.t0]]);
+                if (g.t1 >= 0) ko.t1 = static_cast<uint8_t>(reg_of_local[local_of[g.t1]]);
+                for (int q = 0; q < n; ++q) {
+                    const uint64_t b = 1ULL << q;
+                    const int lp = local_of[q];
+                    const int rb = (lp >= 0) ? reg_of_local[lp] : -1;
+                    if (g.cmask & b) {
+                        if (rb >= 0) ko.creg |= 1u << rb;
+                        else ko.cthr |= b;
+                    }
+                    if (g.pmask & b) {
+                        if (rb >= 0) ko.preg |= 1u << rb;
+                        else ko.pthr |= b;
+                    }
+                }
+                ko.coef = push_coef(plan, g);
+                plan->ops.push_back(ko);
+            }
+            sd.op_count = static_cast<int32_t>(round_ops.size());
+            plan->steps.push_back(sd);
+            st.rounds += 1;
+            todo = left;
+        }
+        pd.step_count = static_cast<int32_t>(plan->steps.size()) - pd.step_begin;
+        plan->passes.push_back(pd);
+        st.passes += 1;
+        st.pass_bytes += 2.0 * Sb * N;
+        pending = rest;
+    }
+    return true;
+}
+
+}  // namespace qsv

@@ -1,0 +1,179 @@
+// Arithmetic policies of the statevector kernels.
+//
+//   P64 : complex128 storage, IEEE FP64 arithmetic
+//   P32 : complex64 storage, FP32 arithmetic
+//
+// A policy defines the global/shared/register element types and the handful
+// of real-number primitives the gate math is written in (mul, madd, add, neg),
+// so one kernel template serves every precision.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace qsv {
+
+struct P64 {
+    using R = double;   // real scalar in registers
+    using C = double;   // coefficient
+    using A = double2;  // complex amplitude in registers
+    using S = double2;  // shared-memory element
+    using G = double2;  // global-memory element
+    static constexpr int SBYTES = 16;
+    static constexpr int GBITS = 3;  // log2(elements per 128-byte wavefront)
+    __device__ static __forceinline__ A s2a(S s) { return s; }
+    __device__ static __forceinline__ S a2s(A a) { return a; }
+    __device__ static __forceinline__ S g2s(G g) { return g; }
+    __device__ static __forceinline__ G s2g(S s) { return s; }
+    __device__ static __forceinline__ R mul(C c, R x) { return __dmul_rn(c, x); }
+    __device__ static __forceinline__ R madd(C c, R x, R acc) { return __fma_rn(c, x, acc); }
+    __device__ static __forceinline__ R add(R x, R y) { return __dadd_rn(x, y); }
+    __device__ static __forceinline__ R neg(R x) {
+        // sign flip on the high word: no FP64 instruction
+        return __hiloint2double(__double2hiint(x) ^ 0x80000000, __double2loint(x));
+    }
+    __device__ static __forceinline__ C cneg(C c) { return -c; }
+    __device__ static __forceinline__ C coef(const C* pool, uint32_t i) { return __ldg(pool + i); }
+    __device__ static __forceinline__ double to_d_re(A a) { return a.x; }
+    __device__ static __forceinline__ double to_d_im(A a) { return a.y; }
+    __device__ static __forceinline__ G make_g(double re, double im) { return make_double2(re, im); }
+    __device__ static __forceinline__ double gre(G g) { return g.x; }
+    __device__ static __forceinline__ double gim(G g) { return g.y; }
+};
+
+struct P32 {
+    using R = float;
+    using C = float;
+    using A = float2;
+    using S = float2;
+    using G = float2;
+    static constexpr int SBYTES = 8;
+    static constexpr int GBITS = 4;
+    __device__ static __forceinline__ A s2a(S s) { return s; }
+    __device__ static __forceinline__ S a2s(A a) { return a; }
+    __device__ static __forceinline__ S g2s(G g) { return g; }
+    __device__ static __forceinline__ G s2g(S s) { return s; }
+    __device__ static __forceinline__ R mul(C c, R x) { return __fmul_rn(c, x); }
+    __device__ static __forceinline__ R madd(C c, R x, R acc) { return __fmaf_rn(c, x, acc); }
+    __device__ static __forceinline__ R add(R x, R y) { return __fadd_rn(x, y); }
+    __device__ static __forceinline__ R neg(R x) { return __int_as_float(__float_as_int(x) ^ 0x80000000); }
+    __device__ static __forceinline__ C cneg(C c) { return -c; }
+    __device__ static __forceinline__ C coef(const C* pool, uint32_t i) { return __ldg(pool + i); }
+    __device__ static __forceinline__ G make_g(double re, double im) {
+        return make_float2(static_cast<float>(re), static_cast<float>(im));
+    }
+    __device__ static __forceinline__ double gre(G g) { return static_cast<double>(g.x); }
+    __device__ static __forceinline__ double gim(G g) { return static_cast<double>(g.y); }
+};
+
+// ------------------------------------------------------------------------
+// Gate math on amplitude pairs, written once over the policy primitives.
+// ------------------------------------------------------------------------
+
+// [[m0, m1], [m2, m3]] real
+template <class P>
+__device__ __forceinline__ void pair_real(typename P::A& a, typename P::A& b, typename P::C m0, typename P::C m1,
+                                          typename P::C m2, typename P::C m3) {
+    typename P::A na, nb;
+    na.x = P::madd(m1, b.x, P::mul(m0, a.x));
+    na.y = P::madd(m1, b.y, P::mul(m0, a.y));
+    nb.x = P::madd(m3, b.x, P::mul(m2, a.x));
+    nb.y = P::madd(m3, b.y, P::mul(m2, a.y));
+    a = na;
+    b = nb;
+}
+
+// [[c, -i s], [-i s, c]]; ns = -s
+template <class P>
+__device__ __forceinline__ void pair_rx(typename P::A& a, typename P::A& b, typename P::C c, typename P::C s,
+                                        typename P::C ns) {
+    typename P::A na, nb;
+    na.x = P::madd(s, b.y, P::mul(c, a.x));
+    na.y = P::madd(ns, b.x, P::mul(c, a.y));
+    nb.x = P::madd(s, a.y, P::mul(c, b.x));
+    nb.y = P::madd(ns, a.x, P::mul(c, b.y));
+    a = na;
+    b = nb;
+}
+
+// general 2x2 complex; m[8] = m00 re, im, m01 re, im, m10 re, im, m11 re, im;
+// nm[k] = -m[k] for the imaginary parts
+template <class P>
+__device__ __forceinline__ void pair_dense(typename P::A& a, typename P::A& b, const typename P::C* m,
+                                           const typename P::C* nmi) {
+    typename P::A na, nb;
+    na.x = P::madd(nmi[1], b.y, P::madd(m[2], b.x, P::madd(nmi[0], a.y, P::mul(m[0], a.x))));
+    na.y = P::madd(m[3], b.x, P::madd(m[2], b.y, P::madd(m[1], a.x, P::mul(m[0], a.y))));
+    nb.x = P::madd(nmi[3], b.y, P::madd(m[6], b.x, P::madd(nmi[2], a.y, P::mul(m[4], a.x))));
+    nb.y = P::madd(m[7], b.x, P::madd(m[6], b.y, P::madd(m[5], a.x, P::mul(m[4], a.y))));
+    a = na;
+    b = nb;
+}
+
+// a *= (dr + i di); ndi = -di
+template <class P>
+__device__ __forceinline__ void amp_phase(typename P::A& a, typename P::C dr, typename P::C di, typename P::C ndi) {
+    typename P::A na;
+    na.x = P::madd(ndi, a.y, P::mul(dr, a.x));
+    na.y = P::madd(di, a.x, P::mul(dr, a.y));
+    a = na;
+}
+
+template <class P>
+__device__ __forceinline__ void amp_special(typename P::A& a, int sp) {
+    typename P::A na;
+    if (sp == 1) {  // * -1
+        na.x = P::neg(a.x);
+        na.y = P::neg(a.y);
+    } else if (sp == 2) {  // * i
+        na.x = P::neg(a.y);
+        na.y = a.x;
+    } else {  // * -i
+        na.x = a.y;
+        na.y = P::neg(a.x);
+    }
+    a = na;
+}
+
+// Y = [[0, -i], [i, 0]]
+template <class P>
+__device__ __forceinline__ void pair_y(typename P::A& a, typename P::A& b) {
+    typename P::A na, nb;
+    na.x = b.y;
+    na.y = P::neg(b.x);
+    nb.x = P::neg(a.y);
+    nb.y = a.x;
+    a = na;
+    b = nb;
+}
+
+// 4x4 complex on (v0, v1, v2, v3) = amplitudes with (t1 t0) = 00, 01, 10, 11
+template <class P>
+__device__ __forceinline__ void quad_dense(typename P::A& v0, typename P::A& v1, typename P::A& v2,
+                                           typename P::A& v3, const typename P::C* pool, uint32_t off) {
+    typename P::A in[4] = {v0, v1, v2, v3};
+    typename P::A out[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        typename P::R xr = P::mul(P::coef(pool, off + 8 * r), in[0].x);
+        typename P::R xi = P::mul(P::coef(pool, off + 8 * r), in[0].y);
+        xr = P::madd(P::cneg(P::coef(pool, off + 8 * r + 1)), in[0].y, xr);
+        xi = P::madd(P::coef(pool, off + 8 * r + 1), in[0].x, xi);
+#pragma unroll
+        for (int c = 1; c < 4; ++c) {
+            const typename P::C mr = P::coef(pool, off + 8 * r + 2 * c);
+            const typename P::C mi = P::coef(pool, off + 8 * r + 2 * c + 1);
+            xr = P::madd(mr, in[c].x, xr);
+            xr = P::madd(P::cneg(mi), in[c].y, xr);
+            xi = P::madd(mr, in[c].y, xi);
+            xi = P::madd(mi, in[c].x, xi);
+        }
+        out[r].x = xr;
+        out[r].y = xi;
+    }
+    v0 = out[0];
+    v1 = out[1];
+    v2 = out[2];
+    v3 = out[3];
+}
+
+}  // namespace qsv

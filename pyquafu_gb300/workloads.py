@@ -1,0 +1,135 @@
+"""Seeded synthetic circuits for the benchmark configurations.
+
+Random layered circuits (the statevector sweeps):
+  each layer applies one gate from {h, x, s, t, rx, ry, rz} to every qubit
+  (angles uniform in [0, 2*pi)), then cx on a random perfect matching of the
+  qubits; with ``extras`` about 5% of the layers also get cz, swap and rzz
+  (uniform angle) on random pairs and ccx on a random triple.
+
+Hardware-efficient ansatz (the gradient workloads):
+  ``layers`` x (ry on every qubit, rz on every qubit) followed by a cx ladder
+  0->1->...->n-1, optionally preceded by an ry angle-encoding layer.
+
+Circuits are returned as ``pyquafu_gb300.ir.Op`` lists (the engine's packed
+input), and ``as_protocol`` wraps them in objects with the attributes the
+reference's circuit reader uses (.instructions, .num, .cbits_num; ops with
+.name, .pos, ._paras, .ctrls, .matrix), so the drop-in ``qfvm`` module can be
+exercised without pyquafu installed.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from . import ir
+
+SWAP = np.array([[1, 0, 0, 0], [0, 0, 1, 0], [0, 1, 0, 0], [0, 0, 0, 1]], dtype=np.complex128)
+ONE_QUBIT = ("h", "x", "s", "t", "rx", "ry", "rz")
+
+
+def named(name: str, qubits, params=(), ncontrols=0) -> ir.Op:
+    return ir.Op(name, ir.NAMED_KIND[name], qubits, ncontrols, params)
+
+
+def matrix_gate(name: str, qubits, matrix, ncontrols=0) -> ir.Op:
+    return ir.Op(name, ir.OP_MATRIX, qubits, ncontrols, (), matrix=np.asarray(matrix, dtype=np.complex128))
+
+
+def random_layers(n: int, depth: int, seed: int = 0, extras: bool = False, extra_rate: float = 0.05) -> list:
+    rng = np.random.default_rng(seed)
+    ops = []
+    for _ in range(depth):
+        for q in range(n):
+            g = ONE_QUBIT[int(rng.integers(len(ONE_QUBIT)))]
+            if g in ("rx", "ry", "rz"):
+                ops.append(named(g, (q,), (float(rng.uniform(0.0, 2 * np.pi)),)))
+            else:
+                ops.append(named(g, (q,)))
+        perm = rng.permutation(n)
+        for i in range(0, n - 1, 2):
+            ops.append(named("cx", (int(perm[i]), int(perm[i + 1])), ncontrols=1))
+        if extras and n >= 3 and rng.random() < extra_rate:
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            ops.append(named("cz", (a, b), ncontrols=1))
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            ops.append(matrix_gate("swap", (a, b), SWAP))
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            ops.append(named("rzz", (a, b), (float(rng.uniform(0.0, 2 * np.pi)),)))
+            a, b, c = (int(x) for x in rng.choice(n, 3, replace=False))
+            ops.append(named("ccx", (a, b, c), ncontrols=2))
+    return ops
+
+
+def hea(n: int, layers: int, seed: int = 0, encode: np.ndarray | None = None):
+    """Hardware-efficient ansatz.  Returns (ops, params); every ry/rz of the
+    ansatz carries a parameter slot (0..2*n*layers-1); encoding gates carry
+    slots after those."""
+    rng = np.random.default_rng(seed)
+    nparam = 2 * n * layers
+    params = rng.uniform(0.0, 2 * np.pi, nparam)
+    ops = []
+    if encode is not None:
+        for q in range(n):
+            ops.append(ir.Op("ry", ir.OP_RY, (q,), 0, (float(encode[q]),), slot=nparam + q))
+    k = 0
+    for _ in range(layers):
+        for q in range(n):
+            ops.append(ir.Op("ry", ir.OP_RY, (q,), 0, (float(params[k]),), slot=k))
+            k += 1
+        for q in range(n):
+            ops.append(ir.Op("rz", ir.OP_RZ, (q,), 0, (float(params[k]),), slot=k))
+            k += 1
+        for q in range(n - 1):
+            ops.append(named("cx", (q, q + 1), ncontrols=1))
+    return ops, params
+
+
+def zz_x_hamiltonian(n: int, seed: int = 0):
+    """sum_i a_i Z_i Z_{i+1} + sum_i b_i X_i with a, b ~ N(0, 1): list of
+    (coeff, paulistr, pos)."""
+    rng = np.random.default_rng(seed)
+    a = rng.normal(size=n - 1)
+    b = rng.normal(size=n)
+    terms = [(float(a[i]), "ZZ", [i, i + 1]) for i in range(n - 1)]
+    terms += [(float(b[i]), "X", [i]) for i in range(n)]
+    return terms
+
+
+# ------------------------- circuit-protocol wrappers -------------------------
+
+
+class _ProtoGate:
+    def __init__(self, op: ir.Op):
+        self.name = op.name.upper()
+        self.pos = list(op.qubits)
+        self._paras = list(op.params)
+        self.paras = list(op.params)
+        if op.ncontrols:
+            self.ctrls = list(op.qubits[: op.ncontrols])
+        if op.matrix is not None:
+            self.matrix = op.matrix
+
+
+class _ProtoMeasure:
+    name = "measure"
+
+    def __init__(self, qbits, cbits):
+        self.qbits = list(qbits)
+        self.cbits = list(cbits)
+
+
+class ProtoCircuit:
+    """Minimal object with the circuit protocol the qfvm reader consumes."""
+
+    def __init__(self, num: int, ops, measures=None, cbits_num=None):
+        self.num = num
+        self.cbits_num = num if cbits_num is None else cbits_num
+        self.instructions = [_ProtoGate(o) for o in ops]
+        if measures:
+            q, c = zip(*measures)
+            self.instructions.append(_ProtoMeasure(q, c))
+        self.measures = dict(measures or [])
+
+
+def as_protocol(num: int, ops, measures=None) -> ProtoCircuit:
+    return ProtoCircuit(num, ops, measures)

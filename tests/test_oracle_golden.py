@@ -1,0 +1,95 @@
+"""The CPU oracle (oracle/qsv_oracle.c) against golden outputs of the
+reference's own qfvm module (tests/golden/make_golden.py)."""
+
+import numpy as np
+import pytest
+
+import helpers
+import oracle
+
+
+def test_circuits_match_reference(golden):
+    meta, states = golden
+    for case in meta["cases"]:
+        ops = [helpers.op_from_json(d) for d in case["ops"]]
+        psi_in = states.get(f"{case['tag']}__in")
+        got = oracle.simulate(case["n"], [o for o in ops if o.is_gate], psi_in)
+        ref = states[f"{case['tag']}__out"]
+        err = np.abs(got - ref).max()
+        assert err < 1e-13, (case["tag"], err)
+
+
+def test_expectations_match_reference(golden):
+    meta, states = golden
+    from types import SimpleNamespace
+
+    for case in meta["cases"]:
+        if "paulis" not in case:
+            continue
+        psi = states[f"{case['tag']}__out"]
+        paulis = [SimpleNamespace(paulistr=p, pos=pos) for p, pos in case["paulis"]]
+        got = oracle.expect_statevec(psi, paulis)
+        np.testing.assert_allclose(got, case["expect"], atol=1e-13, rtol=0)
+
+
+def test_single_gates_match_reference(golden):
+    meta, states = golden
+    for i, case in enumerate(meta["apply"]):
+        op = helpers.op_from_json(case["op"])
+        psi = states[f"apply_{i}__in"].copy()
+        oracle.apply_op(psi, op)
+        err = np.abs(psi - states[f"apply_{i}__out"]).max()
+        assert err < 1e-14, (case["tag"], err)
+
+
+def _assemble(assembly, gate_grads):
+    return [sum(c * gate_grads[i] for i, c in row) for row in assembly]
+
+
+def test_gradients_match_reference(golden):
+    meta, _ = golden
+    for case in meta["gradients"]:
+        ops = [helpers.op_from_json(d) for d in case["ops"]]
+        slots = [o.slot for o in ops]
+        terms = [(c, p, pos) for c, p, pos in case["terms"]]
+        nslot = max(slots) + 1
+        adj = oracle.grad_adjoint(case["n"], ops, slots, terms)
+        ps = oracle.grad_param_shift(case["n"], ops, slots, terms)
+        e = oracle.energy(case["n"], ops, terms)
+        assert abs(e - case["energy"]) < 1e-12
+        gate_adj = np.zeros(nslot)
+        gate_adj[: len(adj)] = adj
+        np.testing.assert_allclose(_assemble(case["assembly"], gate_adj), case["adjoint"], atol=1e-11)
+        gate_ps = np.zeros(nslot)
+        gate_ps[: len(ps)] = ps
+        np.testing.assert_allclose(_assemble(case["assembly"], gate_ps), case["param_shift"], atol=1e-11)
+
+
+def test_sampling_format_basis_states(golden):
+    meta, _ = golden
+    for case in meta["sampling"]:
+        psi = np.zeros(1 << case["n"], dtype=np.complex128)
+        psi[case["index"]] = 1.0
+        meas = [tuple(m) for m in case["measures"]]
+        u = np.linspace(0.01, 0.99, case["shots"])
+        assert oracle.measure_counts(psi, meas, u) == case["counts"]
+
+
+def test_sampling_scan_semantics():
+    rng = np.random.default_rng(3)
+    psi = rng.normal(size=64) + 1j * rng.normal(size=64)
+    psi /= np.linalg.norm(psi)
+    cdf = oracle.sequential_cdf(psi)
+    u = np.concatenate([rng.random(200), cdf[:10], [0.0, np.nextafter(cdf[-1], 2.0), 1.0]])
+    idx = oracle.sample_indices(psi, u)
+    expect = [int(np.searchsorted(cdf, r, side="right")) for r in u]  # first k with r < cdf[k]
+    assert [int(i) for i in idx] == expect
+    assert int(idx[-1]) == psi.size  # r >= total -> index 2^n (loop end)
+
+
+def test_known_answers_bell():
+    # tests/quafu/simulator/basis_test.py: Bell state probabilities
+    from pyquafu_gb300 import workloads
+
+    psi = oracle.simulate(2, [workloads.named("h", (0,)), workloads.named("cx", (0, 1), ncontrols=1)])
+    np.testing.assert_allclose(np.abs(psi) ** 2, [0.5, 0, 0, 0.5], atol=1e-15)

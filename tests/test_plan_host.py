@@ -1,0 +1,70 @@
+"""The fuser (host planner) checked on CPU: host-built plans are executed by
+a numpy interpreter (tests/helpers.py) and compared with the oracle."""
+
+import numpy as np
+import pytest
+
+import helpers
+import oracle
+from pyquafu_gb300 import workloads
+
+
+SHAPES_C128 = [(11, 4), (12, 4), (12, 5), (13, 5)]
+SHAPES_C64 = [(12, 5), (13, 5), (13, 6), (14, 6)]
+
+
+@pytest.mark.parametrize("T,R", SHAPES_C128)
+def test_random_layers_plans(T, R):
+    for n in (T, T + 1, T + 3):
+        ops = workloads.random_layers(n, 5, seed=100 + n, extras=True, extra_rate=0.6)
+        plan = helpers.host_plan(n, ops, 0, T, R)
+        got = helpers.interpret(plan, oracle.zero_state(n))
+        ref = oracle.simulate(n, ops)
+        assert np.abs(got - ref).max() < 1e-13
+        # every gate applied exactly once
+        applied = sum(int(s["op_count"]) for s in plan["steps"])
+        applied += sum(int(p["op_count"]) for p in plan["passes"] if p["type"] != 0)
+        assert applied == len(ops)
+
+
+@pytest.mark.parametrize("T,R", SHAPES_C64)
+def test_c64_shapes_plans(T, R):
+    n = T + 2
+    ops = workloads.random_layers(n, 4, seed=7, extras=True, extra_rate=0.5)
+    plan = helpers.host_plan(n, ops, 1, T, R)
+    got = helpers.interpret(plan, oracle.zero_state(n))
+    assert np.abs(got - oracle.simulate(n, ops)).max() < 1e-13
+
+
+def test_all_gate_kinds_in_tile_passes(golden):
+    meta, states = golden
+    case = [c for c in meta["cases"] if c["tag"] == "allgates_n12"][0]
+    ops = [helpers.op_from_json(d) for d in case["ops"]]
+    plan = helpers.host_plan(12, ops, 0, 11, 4)
+    kinds = {int(o["kind"]) for o in plan["ops"]}
+    assert helpers.K_DENSE2 in kinds and helpers.K_SWAP in kinds and helpers.K_DIAG in kinds
+    got = helpers.interpret(plan, oracle.zero_state(12))
+    assert np.abs(got - states["allgates_n12__out"]).max() < 1e-13
+
+
+def test_dense_k_gate_becomes_global_pass():
+    rng = np.random.default_rng(0)
+    m = np.linalg.qr(rng.normal(size=(8, 8)) + 1j * rng.normal(size=(8, 8)))[0]
+    ops = [workloads.named("h", (q,)) for q in range(13)]
+    ops.append(workloads.matrix_gate("u3q", (12, 1, 7), m))
+    ops += [workloads.named("rx", (q,), (0.3 * q,)) for q in range(13)]
+    plan = helpers.host_plan(13, ops, 0, 12, 4)
+    assert 2 in [int(p["type"]) for p in plan["passes"]]
+    got = helpers.interpret(plan, oracle.zero_state(13))
+    assert np.abs(got - oracle.simulate(13, ops)).max() < 1e-13
+
+
+def test_invalid_ops_rejected():
+    from pyquafu_gb300 import _native as nat
+
+    with pytest.raises(nat.QfvmError):
+        helpers.host_plan(4, [workloads.named("h", (4,))])
+    with pytest.raises(nat.QfvmError):
+        helpers.host_plan(4, [workloads.named("cx", (2, 2), ncontrols=1)])
+    with pytest.raises(nat.QfvmError):
+        helpers.host_plan(4, [workloads.named("h", (0,))], 0, 9, 4)  # shape not compiled in
