@@ -1,0 +1,400 @@
+"""Benchmark: statevector gate sweeps of a 30-qubit complex128 random circuit.
+
+Workload (seeded, synthetic): 30 qubits, complex128 (16 GiB state), 40 random
+layers (one of h/x/s/t/rx/ry/rz per qubit, angles U[0, 2pi), then cx on a
+random perfect matching), plus cz/swap/rzz on random pairs and ccx on a
+random triple in ~5% of layers; seed 0.  One step = one full circuit on the
+device-resident state.  The state (16 GiB) is far larger than L2, so no L2
+flush is needed between steps.
+
+metric  statevector_gbps: effective bandwidth = sum over gates of
+        2 * 16 B * (amplitudes the gate must touch) / circuit time
+e2e     the same metric through pyquafu_gb300.qfvm.simulate_circuit (the
+        reference's API) with the input state in pinned host memory: H2D of
+        the state, the run, and D2H of the result are inside the timed region.
+
+--impl reference times the reference algorithm on the host cores instead (the
+CPU restatement in oracle/, OpenMP over all cores) on a bounded sample of the
+same circuit and state size.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_QUBITS = int(os.environ.get("QFVM_BENCH_QUBITS", "30"))
+DEPTH = 40
+SEED = 0
+S128 = 16
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM = 6800.0
+FP64_PEAK_INSTR = 0.596e12  # measured FP64 FMA instructions/s on this GPU model (profiles/gb300_arith_peaks.md)
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM, "fallback"
+
+
+def workload(n=N_QUBITS, depth=DEPTH, seed=SEED):
+    from pyquafu_gb300 import workloads
+
+    return workloads.random_layers(n, depth, seed, extras=True)
+
+
+def fp64_ops(ops, n):
+    """FP64 arithmetic instructions of one circuit under the engine's kernels
+    (mul/fma/add per touched amplitude component)."""
+    N = float(2 ** n)
+    total = 0.0
+    for o in ops:
+        c = 2.0 ** -o.ncontrols
+        name = o.name
+        if name in ("h", "ry", "rx"):
+            total += 4 * N * c
+        elif name in ("rz", "rzz"):
+            total += 4 * N
+        elif name in ("t", "tdg", "p", "cp"):
+            total += 2 * N * c
+        elif o.matrix is not None and name not in ("swap",):
+            total += 8 * N * c
+    return total
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(ops, n, seconds=12.0, threads=None):
+    """Time the CPU restatement of the reference (oracle/) on the host cores:
+    apply the circuit's gates in order to a 2^n complex128 state until
+    `seconds` have elapsed; returns (gbps, gates applied, cores)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    cores = threads or os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    oracle.build()
+    psi = np.zeros(1 << n, dtype=np.complex128)
+    psi[0] = 1.0
+    from pyquafu_gb300 import workloads  # noqa: F401
+
+    gate_bytes = gate_equiv_bytes(ops, n)
+    done = 0
+    bytes_done = 0.0
+    t0 = time.perf_counter()
+    for i, o in enumerate(ops):
+        oracle.apply_op(psi, o)
+        done += 1
+        bytes_done += gate_bytes[i]
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    return bytes_done / dt / 1e9, done, dt, cores
+
+
+def gate_equiv_bytes(ops, n, S=S128):
+    """Per-gate algorithmic bytes: 2 * S * amplitudes the gate must touch."""
+    N = float(2 ** n)
+    out = []
+    for o in ops:
+        amps = N / 2.0 ** o.ncontrols
+        if o.name in ("s", "sdg", "t", "tdg", "p", "cp", "z", "cz"):
+            amps *= 0.5
+        elif o.name == "swap":
+            amps *= 0.5
+        out.append(2.0 * S * amps)
+    return out
+
+
+def run_reference(args):
+    rank = env_int("RANK", 0)
+    if rank != 0:
+        return 0
+    ops = workload()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build()
+    cores = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(cores)
+    n = N_QUBITS
+    gb = gate_equiv_bytes(ops, n)
+    per_step = max(1, env_int("QFVM_REF_GATES_PER_STEP", 6))
+    psi = np.zeros(1 << n, dtype=np.complex128)
+    psi[0] = 1.0
+    pos = 0
+
+    def step():
+        nonlocal pos
+        b = 0.0
+        for _ in range(per_step):
+            oracle.apply_op(psi, ops[pos])
+            b += gb[pos]
+            pos = (pos + 1) % len(ops)
+        return b
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    tot = 0.0
+    for _ in range(args.steps):
+        tot += step()
+    dt = time.perf_counter() - t0
+    v = tot / dt / 1e9
+    sample = (f"{per_step} consecutive gates of the 30-qubit circuit per step on a 16 GiB complex128 state "
+              f"(oracle/qsv_oracle.c, OpenMP {cores} threads)")
+    line = {"impl": "reference", "metric": "statevector_gbps", "value": round(v, 3), "unit": "GB/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "random_layers_30q_c128_depth40_extras", "qubits": n, "depth": DEPTH,
+                       "seed": SEED, "l2": "state 16 GiB >> L2 (no flush needed)"},
+            "cpu_baseline": {"value": round(v, 3), "unit": "GB/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(v, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    from pyquafu_gb300 import _native as nat
+    from pyquafu_gb300 import engine, ir, qfvm, workloads
+    from pyquafu_gb300.builder import build
+
+    world = env_int("WORLD_SIZE", 1)
+    rank = env_int("RANK", 0)
+    local = env_int("LOCAL_RANK", 0)
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    build()
+    nat.load()
+    n = N_QUBITS
+    ops = workload()
+    gb = sum(gate_equiv_bytes(ops, n))
+    fp64 = fp64_ops(ops, n)
+    plan = engine.Plan(n, ops, "c128")
+    st_plan = plan.stats()
+    state = engine.DeviceState(n, "c128").set_zero()
+    stream = torch.cuda.ExternalStream(state.stream())
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        plan.run(state)
+    barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    l0 = nat.launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    pass_ms, pass_ty = [], []
+    for _ in range(args.steps):
+        ms, ty = plan.run_timed(state)
+        pass_ms.append(ms)
+        pass_ty.append(ty)
+    ev1.record(stream)
+    barrier()
+    launches = nat.launch_count() - l0
+    clk = clocks.stop()
+    total_ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = world * gb / (ms_step * 1e-3) / 1e9
+    pass_ms = np.concatenate(pass_ms)
+    pass_ty = np.concatenate(pass_ty)
+    tile_ms = pass_ms[pass_ty == 0]
+    pass_bytes = 2.0 * S128 * 2 ** n
+    peak, peak_kind = hbm_peak()
+    avg_tile = float(tile_ms.mean()) if tile_ms.size else float(pass_ms.mean())
+    achieved = pass_bytes / (avg_tile * 1e-3) / 1e9
+    fp64_rate = fp64 / (ms_step * 1e-3)
+
+    # --- complex64 variant of the same circuit ---
+    c64 = {}
+    if not args.skip_variants:
+        plan64 = engine.Plan(n, ops, "c64")
+        st64 = engine.DeviceState(n, "c64").set_zero()
+        s64 = torch.cuda.ExternalStream(st64.stream())
+        for _ in range(max(1, args.warmup)):
+            plan64.run(st64)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s64)
+        ms64 = []
+        for _ in range(args.steps):
+            m, t = plan64.run_timed(st64)
+            ms64.append(m[t == 0])
+        e1.record(s64)
+        torch.cuda.synchronize()
+        step64 = e0.elapsed_time(e1) / args.steps
+        gb64 = sum(gate_equiv_bytes(ops, n, 8))
+        t64 = float(np.concatenate(ms64).mean())
+        c64 = {"value": round(gb64 / (step64 * 1e-3) / 1e9, 2), "unit": "GB/s", "ms_per_step": round(step64, 3),
+               "passes": plan64.stats()["passes"],
+               "tile_pass_gbps": round(2.0 * 8 * 2 ** n / (t64 * 1e-3) / 1e9, 1),
+               "tile_pass_frac_hbm": round(2.0 * 8 * 2 ** n / (t64 * 1e-3) / 1e9 / peak, 3)}
+        st64.close()
+        plan64.close()
+
+    # --- end to end through the reference-shaped API (host buffers) ---
+    state.close()
+    host = torch.empty(2 * 2 ** n, dtype=torch.float64, pin_memory=True)
+    psi = host.numpy().view(np.complex128)
+    psi[:] = 0
+    psi[0] = 1.0
+    circuit = workloads.as_protocol(n, ops)
+    for _ in range(max(1, min(args.warmup, 1))):
+        qfvm.simulate_circuit(circuit, psi, 0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        qfvm.simulate_circuit(circuit, psi, 0)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e = {"value": round(world * gb / e2e_s / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": int(S128 * 2 ** n),
+           "d2h_bytes_per_step": int(S128 * 2 ** n), "ms_per_step": round(e2e_s * 1e3, 2),
+           "api": "pyquafu_gb300.qfvm.simulate_circuit(circuit, pinned complex128 state, shots=0)"}
+    del psi, host
+
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        cgbps, gates_done, cdt, cores = cpu_sample(ops, n, seconds=args.cpu_seconds)
+        cpu = {"value": round(cgbps, 3), "unit": "GB/s", "cores": cores, "kind": "port",
+               "sample": f"first {gates_done} gates of the circuit on the 30-qubit complex128 state "
+                         f"({cdt:.1f} s, oracle/qsv_oracle.c with OpenMP)"}
+
+    if rank == 0:
+        line = {
+            "metric": "statevector_gbps", "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "random_layers_30q_c128_depth40_extras", "qubits": n, "depth": DEPTH,
+                       "seed": SEED, "gates": len(ops), "passes": st_plan["passes"],
+                       "rounds": st_plan["rounds"], "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "state 16 GiB >> L2 (no flush needed)"},
+            "roofline": {"bound": "hbm", "kernel": "k_pass<P64,12,4>", "achieved": round(achieved, 1),
+                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "peak_kind": peak_kind, "traffic": None,
+                         "bytes_per_launch": pass_bytes, "avg_launch_ms": round(avg_tile, 3)},
+            "fp64": {"instr_per_s": fp64_rate, "frac_of_measured_peak": round(fp64_rate / FP64_PEAK_INSTR, 3)},
+            "pass_gbps": round(st_plan["pass_bytes"] / (ms_step * 1e-3) / 1e9, 1),
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "complex64": c64,
+            "clocks": clk,
+            "gpu_launches": int(launches),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-variants", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -153,6 +153,11 @@ int qfvm_plan_destroy(qfvm_plan* plan);
 int qfvm_plan_stats(const qfvm_plan* plan, int64_t* passes, int64_t* rounds, int64_t* gates,
                     double* pass_bytes, double* gate_bytes);
 int qfvm_plan_run(qfvm_plan* plan, qfvm_sv* sv);
+/* Run the plan with a CUDA event recorded on the state's stream around every
+ * pass launch; waits for completion and writes each pass's device time (ms)
+ * to pass_ms[0..passes-1] and its type (0 tile, 1 whole-state, 2 k-target)
+ * to pass_type. */
+int qfvm_plan_run_timed(qfvm_plan* plan, qfvm_sv* sv, float* pass_ms, int32_t* pass_type);
 
 /* Host-only planning (no device needed): build the fused schedule and copy
  * its records out, for inspection and for testing the fuser.  Records are the

@@ -16,7 +16,8 @@ import numpy as np
 from .builder import LIB
 
 QFVM_C128, QFVM_C64, QFVM_C128_DS = 0, 1, 2
-PRECISIONS = {"c128": QFVM_C128, "complex128": QFVM_C128, "c64": QFVM_C64, "complex64": QFVM_C64}
+PRECISIONS = {"c128": QFVM_C128, "complex128": QFVM_C128, "c64": QFVM_C64, "complex64": QFVM_C64,
+              "c128_ds": QFVM_C128_DS}
 
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory",
@@ -67,6 +68,7 @@ PROTOTYPES = {
     "qfvm_plan_stats": (ctypes.c_int, [c_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                        ctypes.POINTER(ctypes.c_int64), c_dp, c_dp]),
     "qfvm_plan_run": (ctypes.c_int, [c_vp, c_vp]),
+    "qfvm_plan_run_timed": (ctypes.c_int, [c_vp, c_vp, ctypes.POINTER(ctypes.c_float), c_i32p]),
     "qfvm_plan_host_build": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int64, c_dp,
                                             ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(c_vp)]),
     "qfvm_plan_host_counts": (ctypes.c_int, [c_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32)]),

@@ -85,6 +85,7 @@ struct qfvm_sv {
 
 struct qfvm_plan {
     HostPlan hp;
+    std::vector<cudaEvent_t> events;  // for timed runs
     void* dbuf = nullptr;
     PassDesc* dpass = nullptr;
     StepDesc* dsteps = nullptr;
@@ -100,11 +101,13 @@ size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
 
 int upload_plan(qfvm_plan* p) {
     const HostPlan& hp = p->hp;
-    const bool f32 = hp.precision == QFVM_C64;
+    const bool f32 = hp.arith == QFVM_C64;
+    const bool dsp = hp.arith == QFVM_C128_DS;
     const size_t b_pass = align256(hp.passes.size() * sizeof(PassDesc));
     const size_t b_steps = align256(std::max<size_t>(hp.steps.size(), 1) * sizeof(StepDesc));
     const size_t b_ops = align256(std::max<size_t>(hp.ops.size(), 1) * sizeof(KOp));
     const size_t b_coef = align256(std::max<size_t>(hp.coef.size(), 1) * (f32 ? sizeof(float) : sizeof(double)));
+    // (a double-single coefficient is a float pair: same 8 bytes as a double)
     const size_t total = b_pass + b_steps + b_ops + b_coef;
     std::vector<unsigned char> host(total, 0);
     std::memcpy(host.data(), hp.passes.data(), hp.passes.size() * sizeof(PassDesc));
@@ -114,6 +117,13 @@ int upload_plan(qfvm_plan* p) {
     if (f32) {
         float* f = reinterpret_cast<float*>(cdst);
         for (size_t i = 0; i < hp.coef.size(); ++i) f[i] = static_cast<float>(hp.coef[i]);
+    } else if (dsp) {
+        float* f = reinterpret_cast<float*>(cdst);
+        for (size_t i = 0; i < hp.coef.size(); ++i) {
+            const float h = static_cast<float>(hp.coef[i]);
+            f[2 * i] = h;
+            f[2 * i + 1] = static_cast<float>(hp.coef[i] - static_cast<double>(h));
+        }
     } else if (!hp.coef.empty()) {
         std::memcpy(cdst, hp.coef.data(), hp.coef.size() * sizeof(double));
     }
@@ -139,13 +149,15 @@ int make_plan(int n, int precision, const qfvm_op* ops, int64_t n_ops, const dou
         int dT, dR;
         default_shape(n, sp, &dT, &dR);
         const int tt = T > 0 ? T : dT, rr = R > 0 ? R : dR;
-        if (!pass_shape_supported(sp, tt, rr)) return fail(QFVM_ERR_INVALID, "tile shape not compiled in");
+        if (!pass_shape_supported(precision == QFVM_C128_DS ? QFVM_C128_DS : sp, tt, rr))
+            return fail(QFVM_ERR_INVALID, "tile shape not compiled in");
     }
     qfvm_plan* p = new qfvm_plan();
     if (!build_plan(n, sp, gops, T, R, &p->hp, &err)) {
         delete p;
         return fail(QFVM_ERR_INVALID, err);
     }
+    p->hp.arith = (precision == QFVM_C128_DS) ? QFVM_C128_DS : sp;
     int rc = upload_plan(p);
     if (rc != QFVM_OK) {
         if (p->dbuf) cudaFree(p->dbuf);
@@ -158,27 +170,34 @@ int make_plan(int n, int precision, const qfvm_op* ops, int64_t n_ops, const dou
 
 void free_plan(qfvm_plan* p) {
     if (!p) return;
+    for (cudaEvent_t e : p->events) cudaEventDestroy(e);
     if (p->dbuf) cudaFree(p->dbuf);
     delete p;
 }
 
-int run_plan(qfvm_plan* p, qfvm_sv* sv) {
+int run_plan(qfvm_plan* p, qfvm_sv* sv, bool timed = false) {
     const HostPlan& hp = p->hp;
     if (hp.n != sv->n || hp.precision != sv->precision) return fail(QFVM_ERR_INVALID, "plan/state mismatch");
+    if (timed && p->events.size() != hp.passes.size() + 1) {
+        for (cudaEvent_t e : p->events) cudaEventDestroy(e);
+        p->events.assign(hp.passes.size() + 1, nullptr);
+        for (auto& e : p->events) QSV_CUDA(cudaEventCreate(&e), "event");
+    }
+    if (timed) QSV_CUDA(cudaEventRecord(p->events[0], sv->stream), "event record");
     for (size_t i = 0; i < hp.passes.size(); ++i) {
         const PassDesc& pd = hp.passes[i];
         cudaError_t e = cudaSuccess;
         if (pd.type == PASS_TILE) {
-            e = launch_tile_pass(sv->precision, hp.T, hp.R, sv->d, p->dpass + i, p->dsteps, p->dops, p->dcoef, hp.n,
-                                 pd.H, sv->stream);
+            e = launch_tile_pass(hp.arith, hp.T, hp.R, sv->d, p->dpass + i, p->dsteps, p->dops, p->dcoef, hp.n, pd.H,
+                                 sv->stream);
         } else if (pd.type == PASS_SMALL) {
-            e = launch_small(sv->precision, sv->d, 0, 1, hp.n, p->dops + pd.op_begin, pd.op_count, p->dcoef,
-                             sv->stream);
+            e = launch_small(hp.arith, sv->d, 0, 1, hp.n, p->dops + pd.op_begin, pd.op_count, p->dcoef, sv->stream);
         } else {
-            e = launch_globalop(sv->precision, sv->d, hp.n, p->dops + pd.op_begin, p->dcoef, sv->stream);
+            e = launch_globalop(hp.arith, sv->d, hp.n, p->dops + pd.op_begin, p->dcoef, sv->stream);
         }
         g_launches.fetch_add(1, std::memory_order_relaxed);
         if (e != cudaSuccess) return fail(QFVM_ERR_CUDA, std::string("pass launch: ") + cudaGetErrorString(e));
+        if (timed) QSV_CUDA(cudaEventRecord(p->events[i + 1], sv->stream), "event record");
     }
     return QFVM_OK;
 }
@@ -509,6 +528,20 @@ int qfvm_plan_run(qfvm_plan* plan, qfvm_sv* sv) {
     if (!plan || !sv) return fail(QFVM_ERR_INVALID, "null argument");
     if (!plan->dbuf) return fail(QFVM_ERR_INVALID, "host-only plan cannot run");
     return run_plan(plan, sv);
+}
+
+int qfvm_plan_run_timed(qfvm_plan* plan, qfvm_sv* sv, float* pass_ms, int32_t* pass_type) {
+    if (!plan || !sv) return fail(QFVM_ERR_INVALID, "null argument");
+    if (!plan->dbuf) return fail(QFVM_ERR_INVALID, "host-only plan cannot run");
+    QSV_TRY(run_plan(plan, sv, true));
+    QSV_CUDA(cudaEventSynchronize(plan->events.back()), "timed run sync");
+    for (size_t i = 0; i < plan->hp.passes.size(); ++i) {
+        float ms = 0.f;
+        QSV_CUDA(cudaEventElapsedTime(&ms, plan->events[i], plan->events[i + 1]), "elapsed");
+        if (pass_ms) pass_ms[i] = ms;
+        if (pass_type) pass_type[i] = plan->hp.passes[i].type;
+    }
+    return QFVM_OK;
 }
 
 int qfvm_plan_host_build(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int64_t n_ops,

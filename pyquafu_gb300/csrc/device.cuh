@@ -131,8 +131,11 @@ __device__ __forceinline__ void reg_swap(typename P::A (&a)[1 << R], const KOp& 
         constexpr int B0 = decltype(b0)::value;
         with_bit<R>(op.t1, [&](auto b1) {
             constexpr int B1 = decltype(b1)::value;
-            if constexpr (B0 < B1) {
-                reg_quads<P, R, B0, B1, CTRL>(
+            // SWAP is symmetric in its two targets: order the register bits
+            if constexpr (B0 != B1) {
+                constexpr int LO = B0 < B1 ? B0 : B1;
+                constexpr int HI = B0 < B1 ? B1 : B0;
+                reg_quads<P, R, LO, HI, CTRL>(
                     a, creg, [](typename P::A&, typename P::A& v1, typename P::A& v2, typename P::A&) {
                         typename P::A t = v1;
                         v1 = v2;

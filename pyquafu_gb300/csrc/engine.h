@@ -100,6 +100,7 @@ struct PlanStats {
 // Host-side plan (built by plan.cpp, executed by kernels.cu).
 struct HostPlan {
     int n = 0, precision = QFVM_C128, T = 0, R = 0, L = 0;
+    int arith = QFVM_C128;  // kernel arithmetic: QFVM_C128 (FP64), QFVM_C64 (FP32), QFVM_C128_DS
     std::vector<PassDesc> passes;
     std::vector<StepDesc> steps;
     std::vector<KOp> ops;

@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(256) k_globalop(typename P::G* __restrict__ st
             uint64_t idx = i;
             for (int j = 0; j < k; ++j)
                 if ((m >> j) & 1) idx |= 1ULL << op.tk[j];
-            in[m] = P::g2s(state[idx]);
+            in[m] = P::s2a(P::g2s(state[idx]));
         }
         for (uint32_t r = 0; r < dim; ++r) {
             typename P::R xr = P::mul(P::coef(coef, op.coef + 2 * (r * dim)), in[0].x);
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(256) k_globalop(typename P::G* __restrict__ st
             A o;
             o.x = xr;
             o.y = xi;
-            state[idx] = P::s2g(o);
+            state[idx] = P::s2g(P::a2s(o));
         }
     }
 }
@@ -357,39 +357,39 @@ __global__ void k_sample_exact(const typename P::G* __restrict__ state, uint64_t
 // Host launchers
 // ---------------------------------------------------------------------------
 bool pass_shape_supported(int precision, int T, int R) {
-    return precision == QFVM_C64 ? pass_shape_c64(T, R) : pass_shape_c128(T, R);
+    if (precision == QFVM_C64) return pass_shape_c64(T, R);
+    if (precision == QFVM_C128_DS) return pass_shape_ds(T, R);
+    return pass_shape_c128(T, R);
 }
 
 cudaError_t launch_tile_pass(int precision, int T, int R, void* state, const PassDesc* dpass,
                              const StepDesc* dsteps, const KOp* dops, const void* dcoef, int n, int H,
                              cudaStream_t st) {
     if (precision == QFVM_C64) return launch_pass_c64(T, R, state, dpass, dsteps, dops, dcoef, n, H, st);
+    if (precision == QFVM_C128_DS) return launch_pass_ds(T, R, state, dpass, dsteps, dops, dcoef, n, H, st);
     return launch_pass_c128(T, R, state, dpass, dsteps, dops, dcoef, n, H, st);
+}
+
+template <class P>
+static cudaError_t launch_small_p(void* state, uint64_t stride, int batch, int n, const KOp* dops, int nops,
+                                  const void* dcoef, cudaStream_t st) {
+    const int threads = n >= 10 ? 512 : 256;
+    const size_t smem = sizeof(typename P::S) << n;
+    if (smem > 48 * 1024) {
+        cudaError_t e =
+            cudaFuncSetAttribute(k_small<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+    }
+    k_small<P><<<batch, threads, smem, st>>>(static_cast<typename P::G*>(state), stride, n, dops, nops,
+                                            static_cast<const typename P::C*>(dcoef));
+    return cudaGetLastError();
 }
 
 cudaError_t launch_small(int precision, void* state, uint64_t stride, int batch, int n, const KOp* dops, int nops,
                          const void* dcoef, cudaStream_t st) {
-    const int threads = n >= 10 ? 512 : 256;
-    if (precision == QFVM_C64) {
-        const size_t smem = sizeof(float2) << n;
-        if (smem > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(k_small<P32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 static_cast<int>(smem));
-            if (e != cudaSuccess) return e;
-        }
-        k_small<P32><<<batch, threads, smem, st>>>(static_cast<float2*>(state), stride, n, dops, nops,
-                                                  static_cast<const float*>(dcoef));
-    } else {
-        const size_t smem = sizeof(double2) << n;
-        if (smem > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(k_small<P64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 static_cast<int>(smem));
-            if (e != cudaSuccess) return e;
-        }
-        k_small<P64><<<batch, threads, smem, st>>>(static_cast<double2*>(state), stride, n, dops, nops,
-                                                  static_cast<const double*>(dcoef));
-    }
-    return cudaGetLastError();
+    if (precision == QFVM_C64) return launch_small_p<P32>(state, stride, batch, n, dops, nops, dcoef, st);
+    if (precision == QFVM_C128_DS) return launch_small_p<PDS>(state, stride, batch, n, dops, nops, dcoef, st);
+    return launch_small_p<P64>(state, stride, batch, n, dops, nops, dcoef, st);
 }
 
 cudaError_t launch_globalop(int precision, void* state, int n, const KOp* dop, const void* dcoef,
@@ -398,6 +398,8 @@ cudaError_t launch_globalop(int precision, void* state, int n, const KOp* dop, c
     const unsigned blocks = static_cast<unsigned>(groups / 256 < 152 * 16 ? (groups + 255) / 256 : 152 * 16);
     if (precision == QFVM_C64)
         k_globalop<P32><<<blocks, 256, 0, st>>>(static_cast<float2*>(state), n, dop, static_cast<const float*>(dcoef));
+    else if (precision == QFVM_C128_DS)
+        k_globalop<PDS><<<blocks, 256, 0, st>>>(static_cast<double2*>(state), n, dop, static_cast<const ds*>(dcoef));
     else
         k_globalop<P64><<<blocks, 256, 0, st>>>(static_cast<double2*>(state), n, dop,
                                                static_cast<const double*>(dcoef));

@@ -13,6 +13,9 @@ constexpr int REDUCE_BLOCKS = 152 * 4;
 bool pass_shape_supported(int precision, int T, int R);
 bool pass_shape_c128(int T, int R);
 bool pass_shape_c64(int T, int R);
+bool pass_shape_ds(int T, int R);
+cudaError_t launch_pass_ds(int T, int R, void* state, const PassDesc* dpass, const StepDesc* dsteps,
+                           const KOp* dops, const void* dcoef, int n, int H, cudaStream_t st);
 cudaError_t launch_pass_c128(int T, int R, void* state, const PassDesc* dpass, const StepDesc* dsteps,
                              const KOp* dops, const void* dcoef, int n, int H, cudaStream_t st);
 cudaError_t launch_pass_c64(int T, int R, void* state, const PassDesc* dpass, const StepDesc* dsteps,

@@ -66,6 +66,79 @@ struct P32 {
 };
 
 // ------------------------------------------------------------------------
+// PDS : complex128 storage, double-single arithmetic.  Each real is carried
+// as an unevaluated sum h + l of two floats (about 48 significand bits) and
+// combined with error-free transformations (TwoSum, FMA-based TwoProd)
+// on the FP32 pipes, which on this GPU issue ~57x faster than FP64.
+// Conversions to and from FP64 happen once per pass, at the shared-memory
+// staging of a tile.
+// ------------------------------------------------------------------------
+struct ds {
+    float h, l;
+};
+struct ds2 {
+    ds x, y;
+};
+
+__device__ __forceinline__ ds ds_from_double(double v) {
+    const float h = __double2float_rn(v);
+    const float l = __double2float_rn(__dsub_rn(v, static_cast<double>(h)));
+    return {h, l};
+}
+__device__ __forceinline__ double ds_to_double(ds a) {
+    return __dadd_rn(static_cast<double>(a.h), static_cast<double>(a.l));
+}
+// a + b with TwoSum on the high parts
+__device__ __forceinline__ ds ds_add(ds a, ds b) {
+    const float s = __fadd_rn(a.h, b.h);
+    const float v = __fsub_rn(s, a.h);
+    float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, v)), __fsub_rn(b.h, v));
+    e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+    const float h = __fadd_rn(s, e);
+    return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+// c * x, unnormalised (p + e) via FMA TwoProd plus the cross terms
+__device__ __forceinline__ ds ds_mul_raw(ds c, ds x) {
+    const float p = __fmul_rn(c.h, x.h);
+    float e = __fmaf_rn(c.h, x.h, -p);
+    e = __fmaf_rn(c.h, x.l, e);
+    e = __fmaf_rn(c.l, x.h, e);
+    return {p, e};
+}
+
+struct PDS {
+    using R = ds;
+    using C = ds;
+    using A = ds2;
+    using S = float4;   // (re.h, re.l, im.h, im.l)
+    using G = double2;
+    static constexpr int SBYTES = 16;
+    static constexpr int GBITS = 3;
+    __device__ static __forceinline__ A s2a(S s) { return {{s.x, s.y}, {s.z, s.w}}; }
+    __device__ static __forceinline__ S a2s(A a) { return make_float4(a.x.h, a.x.l, a.y.h, a.y.l); }
+    __device__ static __forceinline__ S g2s(G g) {
+        const ds r = ds_from_double(g.x), i = ds_from_double(g.y);
+        return make_float4(r.h, r.l, i.h, i.l);
+    }
+    __device__ static __forceinline__ G s2g(S s) {
+        return make_double2(ds_to_double({s.x, s.y}), ds_to_double({s.z, s.w}));
+    }
+    __device__ static __forceinline__ R mul(C c, R x) {
+        const ds p = ds_mul_raw(c, x);
+        const float h = __fadd_rn(p.h, p.l);
+        return {h, __fsub_rn(p.l, __fsub_rn(h, p.h))};
+    }
+    __device__ static __forceinline__ R madd(C c, R x, R acc) { return ds_add(acc, ds_mul_raw(c, x)); }
+    __device__ static __forceinline__ R add(R x, R y) { return ds_add(x, y); }
+    __device__ static __forceinline__ R neg(R x) { return {-x.h, -x.l}; }
+    __device__ static __forceinline__ C cneg(C c) { return {-c.h, -c.l}; }
+    __device__ static __forceinline__ C coef(const C* pool, uint32_t i) {
+        const float2 v = __ldg(reinterpret_cast<const float2*>(pool) + i);
+        return {v.x, v.y};
+    }
+};
+
+// ------------------------------------------------------------------------
 // Gate math on amplitude pairs, written once over the policy primitives.
 // ------------------------------------------------------------------------
 

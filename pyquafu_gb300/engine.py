@@ -166,6 +166,15 @@ class Plan:
         """Enqueue the plan on the state's stream (asynchronous)."""
         nat.check(self._lib.qfvm_plan_run(self._h, state.handle), "plan run")
 
+    def run_timed(self, state: DeviceState) -> tuple[np.ndarray, np.ndarray]:
+        """Run with CUDA events around every pass; returns (ms per pass, pass type)."""
+        npass = self.stats()["passes"]
+        ms = np.zeros(npass, dtype=np.float32)
+        ty = np.zeros(npass, dtype=np.int32)
+        nat.check(self._lib.qfvm_plan_run_timed(self._h, state.handle, ms.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                nat.i32ptr(ty)), "plan run (timed)")
+        return ms, ty
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.qfvm_plan_destroy(self._h)

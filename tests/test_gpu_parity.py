@@ -65,6 +65,37 @@ def test_tile_shapes_c128(T, R):
         assert err <= TOL128, (n, T, R, err)
 
 
+@pytest.mark.parametrize("T,R", [(11, 4), (12, 4), (12, 5), (13, 5)])
+def test_tile_shapes_double_single(T, R):
+    # complex128 storage with double-single arithmetic: same 1e-12 bound
+    for n in (T, T + 3):
+        ops = workloads.random_layers(n, 6, seed=3000 + n, extras=True, extra_rate=0.6)
+        got = run(n, ops, "c128_ds", T=T, R=R)
+        err = np.abs(got - oracle.simulate(n, ops)).max()
+        assert err <= TOL128, (n, T, R, err)
+
+
+def test_golden_circuits_double_single(golden):
+    meta, states = golden
+    for case in meta["cases"]:
+        ops = [helpers.op_from_json(d) for d in case["ops"]]
+        got = run(case["n"], [o for o in ops if o.is_gate], "c128_ds", psi_in=states.get(f"{case['tag']}__in"))
+        err = np.abs(got - states[f"{case['tag']}__out"]).max()
+        assert err <= TOL128, (case["tag"], err)
+
+
+def test_swap_register_order():
+    # swaps whose targets land in either register order inside one round
+    n = 14
+    ops = []
+    for a, b in [(0, 3), (3, 0), (12, 5), (5, 12), (13, 1), (2, 11)]:
+        ops += [workloads.named("h", (a,)), workloads.named("ry", (b,), (0.4,)),
+                workloads.matrix_gate("swap", (a, b), workloads.SWAP)]
+    for prec in ("c128", "c128_ds"):
+        got = run(n, ops, prec, T=12, R=4)
+        assert np.abs(got - oracle.simulate(n, ops)).max() <= TOL128, prec
+
+
 @pytest.mark.parametrize("T,R", [(12, 5), (13, 5), (13, 6), (14, 6)])
 def test_tile_shapes_c64(T, R):
     n = T + 2
