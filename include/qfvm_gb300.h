@@ -115,6 +115,27 @@ int qfvm_sampling_statevec(const double* state, uint64_t state_len, const double
 int qfvm_expect_statevec(const double* state, uint64_t state_len, const uint64_t* x_masks,
                          const uint64_t* z_masks, const int32_t* y_counts, int64_t n_terms, double* out);
 
+/* Allocation-free expectation (no counterpart in the reference).
+ * For callers that cannot allocate GPU memory while they run -- processes
+ * that reserve all of HBM for their own pool at start-up, or hot loops where
+ * cudaMalloc/cudaFree would synchronise the device -- this computes the same
+ * unweighted <P_k> as qfvm_expect_statevec on a state that already lives in
+ * device memory the caller owns (`dev_state`, state_len amplitudes of
+ * complex128 or complex64 per `precision`), issuing its work on `stream`
+ * (NULL = default stream) and waiting for it.  It allocates nothing: its
+ * scratch is a fixed 64 KiB __device__ array in the library, which every GPU
+ * that loads the library holds until exit.  At most QFVM_NOALLOC_MAX_TERMS
+ * terms per call (larger requests are rejected).  All calls on a device share
+ * that scratch, so calls that overlap on the GPU race and must be serialised
+ * by the caller.  The first call on each device resolves the scratch address
+ * (with that device current); make it before any stream capture.  On failure
+ * the message is in qfvm_noalloc_last_error(). */
+#define QFVM_NOALLOC_MAX_TERMS 1024
+int qfvm_expect_device_noalloc(const void* dev_state, uint64_t state_len, int32_t precision,
+                               const uint64_t* x_masks, const uint64_t* z_masks, const int32_t* y_counts,
+                               int64_t n_terms, double* out, void* stream);
+const char* qfvm_noalloc_last_error(void);
+
 /* ------------------------------------------------------------------ */
 /* Device-resident statevector (engine-owned HBM buffer)               */
 /* ------------------------------------------------------------------ */

@@ -51,6 +51,9 @@ PROTOTYPES = {
     "qfvm_applyop_statevec": (ctypes.c_int, [c_vp, c_dp, ctypes.c_int64, c_dp, ctypes.c_uint64]),
     "qfvm_sampling_statevec": (ctypes.c_int, [c_dp, ctypes.c_uint64, c_dp, ctypes.c_int64, c_u64p]),
     "qfvm_expect_statevec": (ctypes.c_int, [c_dp, ctypes.c_uint64, c_u64p, c_u64p, c_i32p, ctypes.c_int64, c_dp]),
+    "qfvm_expect_device_noalloc": (ctypes.c_int, [c_vp, ctypes.c_uint64, ctypes.c_int32, c_u64p, c_u64p, c_i32p,
+                                                  ctypes.c_int64, c_dp, c_vp]),
+    "qfvm_noalloc_last_error": (ctypes.c_char_p, []),
     "qfvm_sv_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(c_vp)]),
     "qfvm_sv_destroy": (ctypes.c_int, [c_vp]),
     "qfvm_sv_set_zero": (ctypes.c_int, [c_vp]),
