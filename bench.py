@@ -227,11 +227,62 @@ def run_reference(args):
     return 0
 
 
+S_OF = {"c128": 16, "c128_ds": 16, "c64": 8}
+KERNEL_OF = {"c128": "k_pass<P64,12,4>", "c128_ds": "k_pass<PDS,12,4>", "c64": "k_pass<P32,13,5>"}
+
+
+def measure(precision, ops, n, steps, warmup, per_pass=True):
+    """Device-resident measurement of one precision: returns a dict."""
+    import torch
+
+    from pyquafu_gb300 import _native as nat
+    from pyquafu_gb300 import engine
+
+    S = S_OF[precision]
+    plan = engine.Plan(n, ops, precision)
+    st_plan = plan.stats()
+    state = engine.DeviceState(n, precision).set_zero()
+    stream = torch.cuda.ExternalStream(state.stream())
+    for _ in range(warmup):
+        plan.run(state)
+    torch.cuda.synchronize()
+    l0 = nat.launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    pass_ms, pass_ty = [], []
+    for _ in range(steps):
+        if per_pass:
+            ms, ty = plan.run_timed(state)
+            pass_ms.append(ms)
+            pass_ty.append(ty)
+        else:
+            plan.run(state)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = nat.launch_count() - l0
+    ms_step = ev0.elapsed_time(ev1) / steps
+    gb = sum(gate_equiv_bytes(ops, n, S))
+    out = {"precision": precision, "ms_per_step": ms_step, "gbps": gb / (ms_step * 1e-3) / 1e9,
+           "passes": st_plan["passes"], "rounds": st_plan["rounds"], "gates": st_plan["gates"],
+           "pass_bytes": st_plan["pass_bytes"], "launches": int(launches)}
+    if per_pass:
+        pm = np.concatenate(pass_ms)
+        pt = np.concatenate(pass_ty)
+        tile = pm[pt == 0]
+        out["avg_tile_ms"] = float(tile.mean()) if tile.size else float(pm.mean())
+        out["tile_bytes"] = 2.0 * S * 2 ** n
+        out["tile_gbps"] = out["tile_bytes"] / (out["avg_tile_ms"] * 1e-3) / 1e9
+    state.close()
+    plan.close()
+    return out
+
+
 def run_gpu(args):
     import torch
 
     from pyquafu_gb300 import _native as nat
-    from pyquafu_gb300 import engine, ir, qfvm, workloads
+    from pyquafu_gb300 import qfvm, workloads
     from pyquafu_gb300.builder import build
 
     world = env_int("WORLD_SIZE", 1)
@@ -246,12 +297,7 @@ def run_gpu(args):
     nat.load()
     n = N_QUBITS
     ops = workload()
-    gb = sum(gate_equiv_bytes(ops, n))
-    fp64 = fp64_ops(ops, n)
-    plan = engine.Plan(n, ops, "c128")
-    st_plan = plan.stats()
-    state = engine.DeviceState(n, "c128").set_zero()
-    stream = torch.cuda.ExternalStream(state.stream())
+    peak, peak_kind = hbm_peak()
 
     def barrier():
         torch.cuda.synchronize()
@@ -260,25 +306,13 @@ def run_gpu(args):
 
             dist.barrier()
 
-    for _ in range(args.warmup):
-        plan.run(state)
     barrier()
     clocks = ClockSampler()
     clocks.start()
-    l0 = nat.launch_count()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    pass_ms, pass_ty = [], []
-    for _ in range(args.steps):
-        ms, ty = plan.run_timed(state)
-        pass_ms.append(ms)
-        pass_ty.append(ty)
-    ev1.record(stream)
-    barrier()
-    launches = nat.launch_count() - l0
+    main = measure(args.precision, ops, n, args.steps, args.warmup)
     clk = clocks.stop()
-    total_ms = ev0.elapsed_time(ev1)
+    barrier()
+    total_ms = main["ms_per_step"] * args.steps
     if world > 1:
         import torch.distributed as dist
 
@@ -286,93 +320,73 @@ def run_gpu(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     ms_step = total_ms / args.steps
+    S = S_OF[args.precision]
+    gb = sum(gate_equiv_bytes(ops, n, S))
     value = world * gb / (ms_step * 1e-3) / 1e9
-    pass_ms = np.concatenate(pass_ms)
-    pass_ty = np.concatenate(pass_ty)
-    tile_ms = pass_ms[pass_ty == 0]
-    pass_bytes = 2.0 * S128 * 2 ** n
-    peak, peak_kind = hbm_peak()
-    avg_tile = float(tile_ms.mean()) if tile_ms.size else float(pass_ms.mean())
-    achieved = pass_bytes / (avg_tile * 1e-3) / 1e9
-    fp64_rate = fp64 / (ms_step * 1e-3)
+    achieved = main["tile_gbps"]
+    fp64 = fp64_ops(ops, n)
 
-    # --- complex64 variant of the same circuit ---
-    c64 = {}
-    if not args.skip_variants:
-        plan64 = engine.Plan(n, ops, "c64")
-        st64 = engine.DeviceState(n, "c64").set_zero()
-        s64 = torch.cuda.ExternalStream(st64.stream())
-        for _ in range(max(1, args.warmup)):
-            plan64.run(st64)
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(s64)
-        ms64 = []
-        for _ in range(args.steps):
-            m, t = plan64.run_timed(st64)
-            ms64.append(m[t == 0])
-        e1.record(s64)
-        torch.cuda.synchronize()
-        step64 = e0.elapsed_time(e1) / args.steps
-        gb64 = sum(gate_equiv_bytes(ops, n, 8))
-        t64 = float(np.concatenate(ms64).mean())
-        c64 = {"value": round(gb64 / (step64 * 1e-3) / 1e9, 2), "unit": "GB/s", "ms_per_step": round(step64, 3),
-               "passes": plan64.stats()["passes"],
-               "tile_pass_gbps": round(2.0 * 8 * 2 ** n / (t64 * 1e-3) / 1e9, 1),
-               "tile_pass_frac_hbm": round(2.0 * 8 * 2 ** n / (t64 * 1e-3) / 1e9 / peak, 3)}
-        st64.close()
-        plan64.close()
+    variants = {}
+    for v in [x for x in args.variants.split(",") if x and x != args.precision]:
+        r = measure(v, ops, n, args.steps, max(1, min(args.warmup, 3)))
+        variants[v] = {"value": round(r["gbps"], 2), "unit": "GB/s", "ms_per_step": round(r["ms_per_step"], 3),
+                       "passes": r["passes"], "tile_kernel": KERNEL_OF[v], "tile_pass_gbps": round(r["tile_gbps"], 1),
+                       "tile_pass_frac_hbm": round(r["tile_gbps"] / peak, 4)}
 
     # --- end to end through the reference-shaped API (host buffers) ---
-    state.close()
-    host = torch.empty(2 * 2 ** n, dtype=torch.float64, pin_memory=True)
-    psi = host.numpy().view(np.complex128)
-    psi[:] = 0
-    psi[0] = 1.0
-    circuit = workloads.as_protocol(n, ops)
-    for _ in range(max(1, min(args.warmup, 1))):
+    e2e = None
+    if not args.skip_e2e:
+        host = torch.empty(2 * 2 ** n, dtype=torch.float64, pin_memory=True)
+        psi = host.numpy().view(np.complex128)
+        psi[:] = 0
+        psi[0] = 1.0
+        circuit = workloads.as_protocol(n, ops)
         qfvm.simulate_circuit(circuit, psi, 0)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        qfvm.simulate_circuit(circuit, psi, 0)
-    torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    e2e = {"value": round(world * gb / e2e_s / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": int(S128 * 2 ** n),
-           "d2h_bytes_per_step": int(S128 * 2 ** n), "ms_per_step": round(e2e_s * 1e3, 2),
-           "api": "pyquafu_gb300.qfvm.simulate_circuit(circuit, pinned complex128 state, shots=0)"}
-    del psi, host
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            qfvm.simulate_circuit(circuit, psi, 0)
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        gb128 = sum(gate_equiv_bytes(ops, n, 16))
+        e2e = {"value": round(world * gb128 / e2e_s / 1e9, 2), "unit": "GB/s",
+               "h2d_bytes_per_step": int(16 * 2 ** n), "d2h_bytes_per_step": int(16 * 2 ** n),
+               "ms_per_step": round(e2e_s * 1e3, 2),
+               "api": "pyquafu_gb300.qfvm.simulate_circuit(circuit, pinned complex128 state, shots=0)"}
+        del psi, host
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
         cgbps, gates_done, cdt, cores = cpu_sample(ops, n, seconds=args.cpu_seconds)
         cpu = {"value": round(cgbps, 3), "unit": "GB/s", "cores": cores, "kind": "port",
-               "sample": f"first {gates_done} gates of the circuit on the 30-qubit complex128 state "
+               "sample": f"first {gates_done} gates of the circuit on the {n}-qubit complex128 state "
                          f"({cdt:.1f} s, oracle/qsv_oracle.c with OpenMP)"}
 
     if rank == 0:
         line = {
             "metric": "statevector_gbps", "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": {"c128": "f64", "c128_ds": "f32x2", "c64": "f32"}[args.precision],
             "data": "synthetic",
-            "config": {"workload": "random_layers_30q_c128_depth40_extras", "qubits": n, "depth": DEPTH,
-                       "seed": SEED, "gates": len(ops), "passes": st_plan["passes"],
-                       "rounds": st_plan["rounds"], "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "state 16 GiB >> L2 (no flush needed)"},
-            "roofline": {"bound": "hbm", "kernel": "k_pass<P64,12,4>", "achieved": round(achieved, 1),
-                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                         "peak_kind": peak_kind, "traffic": None,
-                         "bytes_per_launch": pass_bytes, "avg_launch_ms": round(avg_tile, 3)},
-            "fp64": {"instr_per_s": fp64_rate, "frac_of_measured_peak": round(fp64_rate / FP64_PEAK_INSTR, 3)},
-            "pass_gbps": round(st_plan["pass_bytes"] / (ms_step * 1e-3) / 1e9, 1),
+            "config": {"workload": f"random_layers_{n}q_c128_depth40_extras", "qubits": n, "depth": DEPTH,
+                       "seed": SEED, "gates": len(ops), "precision": args.precision, "passes": main["passes"],
+                       "rounds": main["rounds"], "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "state >> L2 (no flush needed)"},
+            "roofline": {"bound": "hbm", "kernel": KERNEL_OF[args.precision], "achieved": round(achieved, 1),
+                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                         "traffic": None, "bytes_per_launch": main["tile_bytes"],
+                         "avg_launch_ms": round(main["avg_tile_ms"], 3)},
+            "pass_gbps": round(main["pass_bytes"] / (ms_step * 1e-3) / 1e9, 1),
             "e2e": e2e,
             "cpu_baseline": cpu,
-            "complex64": c64,
+            "variants": variants,
             "clocks": clk,
-            "gpu_launches": int(launches),
+            "gpu_launches": int(main["launches"]),
         }
+        if args.precision == "c128":
+            line["fp64"] = {"instr_per_s": fp64 / (ms_step * 1e-3),
+                            "frac_of_measured_peak": round(fp64 / (ms_step * 1e-3) / FP64_PEAK_INSTR, 3)}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -387,10 +401,15 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="c128", choices=["c128", "c128_ds", "c64"])
+    ap.add_argument("--variants", default="c128_ds,c64")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-variants", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     args = ap.parse_args()
+    if args.skip_variants:
+        args.variants = ""
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

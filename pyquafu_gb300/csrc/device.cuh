@@ -52,7 +52,16 @@ __device__ __forceinline__ void reg_pairs(typename P::A (&a)[1 << R], uint32_t c
 #pragma unroll
     for (int j = 0; j < (1 << R); ++j) {
         if (j & (1 << TB)) continue;
-        if (!CTRL || ((static_cast<uint32_t>(j) & creg) == creg)) f(a[j], a[j | (1 << TB)]);
+        if constexpr (!CTRL) {
+            f(a[j], a[j | (1 << TB)]);
+        } else {
+            // controls inside the registers: compute, then select (no branch)
+            typename P::A x = a[j], y = a[j | (1 << TB)];
+            f(x, y);
+            const bool ok = (static_cast<uint32_t>(j) & creg) == creg;
+            a[j] = ok ? x : a[j];
+            a[j | (1 << TB)] = ok ? y : a[j | (1 << TB)];
+        }
     }
 }
 
@@ -146,44 +155,75 @@ __device__ __forceinline__ void reg_swap(typename P::A (&a)[1 << R], const KOp& 
     });
 }
 
+// Accumulated thread-uniform phase of a register round.
+template <class P>
+struct RoundPhase {
+    typename P::A f;
+    bool on;
+};
+
+template <class P>
+__device__ __forceinline__ void phase_mul(typename P::A& f, typename P::C dr, typename P::C di) {
+    amp_phase<P>(f, dr, di, P::cneg(di));
+}
+
+// Diagonal ops.  Three shapes, chosen by the planner:
+//  F_UNIFORM  no parity or control bit in the registers: one factor per
+//             thread, folded into the round's phase (it commutes with every
+//             op of the round) and applied once when the round ends;
+//  F_ONEBIT   exactly one parity bit in the registers (t0), no register
+//             control: two factors per thread, bit position compile-time;
+//  otherwise  per-amplitude parity and control, branch-free selects.
 template <class P, int R>
 __device__ __forceinline__ void reg_diag(typename P::A (&a)[1 << R], const KOp& op, uint64_t gthr,
-                                         const typename P::C* coef) {
+                                         const typename P::C* coef, RoundPhase<P>& ph) {
     using C = typename P::C;
-    const uint32_t creg = op.creg, preg = op.preg;
     const int pt = __popcll(gthr & op.pthr) & 1;
-    if (op.flags & F_D1_SPEC) {
-        const int sp = op.special;
-#pragma unroll
-        for (int j = 0; j < (1 << R); ++j) {
-            if ((static_cast<uint32_t>(j) & creg) != creg) continue;
-            if ((pt ^ (__popc(static_cast<uint32_t>(j) & preg) & 1)) == 0) continue;
-            amp_special<P>(a[j], sp);
-        }
+    const bool d0one = (op.flags & F_D0_ONE) != 0;
+    if (op.flags & F_UNIFORM) {
+        if (pt == 0 && d0one) return;
+        const uint32_t o = op.coef + (pt ? 2u : 0u);
+        phase_mul<P>(ph.f, P::coef(coef, o), P::coef(coef, o + 1));
+        ph.on = true;
         return;
     }
+    if (op.flags & F_ONEBIT) {
+        with_bit<R>(op.t0, [&](auto tb) {
+            constexpr int TB = decltype(tb)::value;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int idx = pt ^ h;
+                if (idx == 0 && d0one) continue;
+                const uint32_t o = op.coef + (idx ? 2u : 0u);
+                const C dr = P::coef(coef, o), di = P::coef(coef, o + 1), ndi = P::cneg(di);
+#pragma unroll
+                for (int j = 0; j < (1 << R); ++j)
+                    if (((j >> TB) & 1) == h) amp_phase<P>(a[j], dr, di, ndi);
+            }
+        });
+        return;
+    }
+    const uint32_t creg = op.creg, preg = op.preg;
     const C d0r = P::coef(coef, op.coef), d0i = P::coef(coef, op.coef + 1);
     const C d1r = P::coef(coef, op.coef + 2), d1i = P::coef(coef, op.coef + 3);
-    const C nd0i = P::cneg(d0i), nd1i = P::cneg(d1i);
-    const bool d0one = (op.flags & F_D0_ONE) != 0;
 #pragma unroll
     for (int j = 0; j < (1 << R); ++j) {
-        if ((static_cast<uint32_t>(j) & creg) != creg) continue;
-        const int par = pt ^ (__popc(static_cast<uint32_t>(j) & preg) & 1);
-        if (par) {
-            amp_phase<P>(a[j], d1r, d1i, nd1i);
-        } else if (!d0one) {
-            amp_phase<P>(a[j], d0r, d0i, nd0i);
-        }
+        const bool ok = (static_cast<uint32_t>(j) & creg) == creg;
+        const bool par = (pt ^ (__popc(static_cast<uint32_t>(j) & preg) & 1)) != 0;
+        const C dr = par ? d1r : d0r;
+        const C di = par ? d1i : d0i;
+        typename P::A v = a[j];
+        amp_phase<P>(v, dr, di, P::cneg(di));
+        a[j] = ok ? v : a[j];
     }
 }
 
 template <class P, int R>
 __device__ __forceinline__ void reg_apply(typename P::A (&a)[1 << R], const KOp& op, uint64_t gthr,
-                                          const typename P::C* coef) {
+                                          const typename P::C* coef, RoundPhase<P>& ph) {
     if ((gthr & op.cthr) != op.cthr) return;  // a control outside the registers is 0
     switch (op.kind) {
-        case K_DIAG: reg_diag<P, R>(a, op, gthr, coef); break;
+        case K_DIAG: reg_diag<P, R>(a, op, gthr, coef, ph); break;
         case K_SWAP:
             if (op.creg) reg_swap<P, R, true>(a, op);
             else reg_swap<P, R, false>(a, op);
@@ -336,12 +376,19 @@ __device__ __forceinline__ void small_apply(typename P::S* sm, int n, const KOp&
 }
 
 // ---------------------------------------------------------------------------
-// Fused tile pass.  One CTA per tile of 2^T amplitudes: tile-local bit k is
-// global qubit tq[k]; the low L qubits are contiguous so every global access
-// is a run of 2^L amplitudes.  The tile is staged in shared memory, then each
-// register round loads 2^R amplitudes per thread, applies its gates in
-// registers and writes them back.
+// Fused tile pass (persistent, double-buffered).
+//
+// A tile is 2^T amplitudes: tile-local bit k is global qubit tq[k], and the
+// low L qubits are the contiguous qubits 0..L-1, so every global access is a
+// run of 2^L amplitudes.  Each CTA walks tiles blockIdx.x, +gridDim.x, ...:
+// while it computes tile i in one shared-memory buffer, the asynchronous
+// copies (cp.async, 8 or 16 bytes per element, written straight to the
+// swizzled slot) of tile i+1 land in the other.  A tile's gates run in
+// register rounds: each thread loads 2^R amplitudes that differ in the
+// round's R register qubits, applies every gate of the round in registers and
+// writes them back.  Two-target dense gates run as shared-memory steps.
 // ---------------------------------------------------------------------------
+
 // Shared-memory step of a tile pass (kept out of line so its registers do not
 // weigh on the register rounds).
 template <class P>
@@ -353,114 +400,153 @@ __device__ __noinline__ void tile_smem_op(typename P::S* sm, int T, uint64_t bas
     }
 }
 
-template <int T, int R, int SB>
-struct PassOcc {
-    // CTAs per SM the register budget is sized for
-    static constexpr int value = 1;
-};
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem_dst, const void* gmem_src) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+    if constexpr (BYTES == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(gmem_src), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+__device__ __forceinline__ uint64_t tile_base(uint64_t b, int L, int H, const uint8_t* tq) {
+    uint64_t base = b << L;
+    for (int k = 0; k < H; ++k) base = insert0(base, tq[L + k]);
+    return base;
+}
+
+// Raw global elements of a tile -> shared memory, asynchronously.
+template <class P, int T, int NT>
+__device__ __forceinline__ void tile_prefetch(typename P::S* buf, const typename P::G* state, uint64_t base,
+                                              const uint64_t* choff, int L) {
+    static_assert(sizeof(typename P::G) == sizeof(typename P::S), "raw staging needs equal element sizes");
+    const uint32_t lmask = (1u << L) - 1;
+#pragma unroll 4
+    for (int k = 0; k < (1 << T) / NT; ++k) {
+        const uint32_t s = static_cast<uint32_t>(k * NT + threadIdx.x);
+        cp_async<sizeof(typename P::G)>(buf + swz<P::GBITS>(s), state + (base | choff[s >> L] | (s & lmask)));
+    }
+    cp_async_commit();
+}
 
 template <class P, int T, int R>
-__global__ void __launch_bounds__(1 << (T - R), PassOcc<T, R, P::SBYTES>::value) k_pass(typename P::G* __restrict__ state,
-                                                       const PassDesc* __restrict__ pdp,
-                                                       const StepDesc* __restrict__ steps,
-                                                       const KOp* __restrict__ ops,
-                                                       const typename P::C* __restrict__ coef) {
+__global__ void __launch_bounds__(1 << (T - R), 1) k_pass(typename P::G* __restrict__ state, uint64_t ntiles,
+                                                        const PassDesc* __restrict__ pdp,
+                                                        const StepDesc* __restrict__ steps,
+                                                        const KOp* __restrict__ ops,
+                                                        const typename P::C* __restrict__ coef) {
     constexpr int NT = 1 << (T - R);
     constexpr int NA = 1 << R;
     constexpr int GB = P::GBITS;
+    constexpr int PER = (1 << T) / NT;  // elements per thread
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    typename P::S* sm = reinterpret_cast<typename P::S*>(smem_raw);
-    uint64_t* choff = reinterpret_cast<uint64_t*>(smem_raw + (sizeof(typename P::S) << T));
+    typename P::S* bufs[2] = {reinterpret_cast<typename P::S*>(smem_raw),
+                              reinterpret_cast<typename P::S*>(smem_raw) + (1 << T)};
+    uint64_t* choff = reinterpret_cast<uint64_t*>(smem_raw + 2 * (sizeof(typename P::S) << T));
 
     const int tid = threadIdx.x;
     const int L = pdp->L;
     const int H = pdp->H;
-    uint64_t base = static_cast<uint64_t>(blockIdx.x) << L;
-    for (int k = 0; k < H; ++k) base = insert0(base, pdp->tq[L + k]);
-
+    const uint8_t* tq = pdp->tq;
     for (int c = tid; c < (1 << H); c += NT) {
         uint64_t off = 0;
         for (int k = 0; k < H; ++k)
-            if ((c >> k) & 1) off |= 1ULL << pdp->tq[L + k];
+            if ((c >> k) & 1) off |= 1ULL << tq[L + k];
         choff[c] = off;
     }
     __syncthreads();
-
     const uint32_t lmask = (1u << L) - 1;
-    constexpr int PER = (1 << T) / NT;  // elements per thread (>= 2^R)
-    constexpr int BATCH = PER < 8 ? PER : 8;
-#pragma unroll 1
-    for (int it = 0; it < PER; it += BATCH) {
-        typename P::G v[BATCH];
-#pragma unroll
-        for (int u = 0; u < BATCH; ++u) {
-            const uint32_t s = static_cast<uint32_t>((it + u) * NT + tid);
-            v[u] = __ldcs(state + (base | choff[s >> L] | (s & lmask)));
-        }
-#pragma unroll
-        for (int u = 0; u < BATCH; ++u) {
-            const uint32_t s = static_cast<uint32_t>((it + u) * NT + tid);
-            sm[swz<GB>(s)] = P::g2s(v[u]);
-        }
-    }
-    __syncthreads();
-
     const int nsteps = pdp->step_count;
-    const StepDesc* sd = steps + pdp->step_begin;
-    for (int si = 0; si < nsteps; ++si, ++sd) {
-        if (sd->type == STEP_SMEM) {
-            // dense multi-target gate applied in shared memory over the tile
-            for (int oi = 0; oi < sd->op_count; ++oi) {
-                tile_smem_op<P>(sm, T, base, ops[sd->op_begin + oi], coef);
-                __syncthreads();
-            }
-            continue;
-        }
-        uint32_t sb = 0;
-        uint64_t gthr = base;
-#pragma unroll
-        for (int k = 0; k < T - R; ++k) {
-            if ((tid >> k) & 1) {
-                sb |= 1u << sd->tpos[k];
-                gthr |= 1ULL << sd->tglob[k];
-            }
-        }
-        const uint32_t psb = swz<GB>(sb);
-        uint32_t rsw[R];
-#pragma unroll
-        for (int k = 0; k < R; ++k) rsw[k] = swz<GB>(1u << sd->rpos[k]);
-        typename P::A a[NA];
-#pragma unroll
-        for (int j = 0; j < NA; ++j) {
-            uint32_t ad = psb;
-#pragma unroll
-            for (int k = 0; k < R; ++k)
-                if ((j >> k) & 1) ad ^= rsw[k];
-            a[j] = P::s2a(sm[ad]);
-        }
-        const KOp* op = ops + sd->op_begin;
-        const int nop = sd->op_count;
-        for (int oi = 0; oi < nop; ++oi) {
-            const KOp o = op[oi];
-            reg_apply<P, R>(a, o, gthr, coef);
-        }
-        uint32_t psb2 = psb;
-        asm volatile("" : "+r"(psb2));  // recompute the addresses instead of keeping 2^R of them live
-#pragma unroll
-        for (int j = 0; j < NA; ++j) {
-            uint32_t ad = psb2;
-#pragma unroll
-            for (int k = 0; k < R; ++k)
-                if ((j >> k) & 1) ad ^= rsw[k];
-            sm[ad] = P::a2s(a[j]);
+
+    uint64_t b = blockIdx.x;
+    if (b < ntiles) tile_prefetch<P, T, NT>(bufs[0], state, tile_base(b, L, H, tq), choff, L);
+    for (int it = 0; b < ntiles; ++it, b += gridDim.x) {
+        typename P::S* sm = bufs[it & 1];
+        const uint64_t base = tile_base(b, L, H, tq);
+        const uint64_t bn = b + gridDim.x;
+        if (bn < ntiles) {
+            tile_prefetch<P, T, NT>(bufs[(it + 1) & 1], state, tile_base(bn, L, H, tq), choff, L);
+            cp_async_wait<1>();  // this tile's group is complete; the next one may be in flight
+        } else {
+            cp_async_wait<0>();
         }
         __syncthreads();
-    }
+        if constexpr (P::RAW_STAGING) {  // convert the raw FP64 tile to the register format in place
+#pragma unroll 4
+            for (int k = 0; k < PER; ++k) {
+                const uint32_t ad = swz<GB>(static_cast<uint32_t>(k * NT + tid));
+                sm[ad] = P::g2s(P::raw_to_g(sm[ad]));
+            }
+            __syncthreads();
+        }
 
-#pragma unroll 8
-    for (int it = 0; it < PER; ++it) {
-        const uint32_t s = static_cast<uint32_t>(it * NT + tid);
-        __stcs(state + (base | choff[s >> L] | (s & lmask)), P::s2g(sm[swz<GB>(s)]));
+        const StepDesc* sd = steps + pdp->step_begin;
+        for (int si = 0; si < nsteps; ++si, ++sd) {
+            if (sd->type == STEP_SMEM) {
+                // dense multi-target gate applied in shared memory over the tile
+                for (int oi = 0; oi < sd->op_count; ++oi) {
+                    tile_smem_op<P>(sm, T, base, ops[sd->op_begin + oi], coef);
+                    __syncthreads();
+                }
+                continue;
+            }
+            uint32_t sb = 0;
+            uint64_t gthr = base;
+#pragma unroll
+            for (int k = 0; k < T - R; ++k) {
+                if ((tid >> k) & 1) {
+                    sb |= 1u << sd->tpos[k];
+                    gthr |= 1ULL << sd->tglob[k];
+                }
+            }
+            const uint32_t psb = swz<GB>(sb);
+            uint32_t rsw[R];
+#pragma unroll
+            for (int k = 0; k < R; ++k) rsw[k] = swz<GB>(1u << sd->rpos[k]);
+            typename P::A a[NA];
+#pragma unroll
+            for (int j = 0; j < NA; ++j) {
+                uint32_t ad = psb;
+#pragma unroll
+                for (int k = 0; k < R; ++k)
+                    if ((j >> k) & 1) ad ^= rsw[k];
+                a[j] = P::s2a(sm[ad]);
+            }
+            const KOp* op = ops + sd->op_begin;
+            const int nop = sd->op_count;
+            RoundPhase<P> ph;
+            ph.f = P::one();
+            ph.on = false;
+            for (int oi = 0; oi < nop; ++oi) {
+                const KOp o = op[oi];
+                reg_apply<P, R>(a, o, gthr, coef, ph);
+            }
+            if (ph.on) {
+#pragma unroll
+                for (int j = 0; j < NA; ++j) amp_phase<P>(a[j], ph.f.x, ph.f.y, P::cneg(ph.f.y));
+            }
+            uint32_t psb2 = psb;
+            asm volatile("" : "+r"(psb2));  // recompute the addresses instead of keeping 2^R of them live
+#pragma unroll
+            for (int j = 0; j < NA; ++j) {
+                uint32_t ad = psb2;
+#pragma unroll
+                for (int k = 0; k < R; ++k)
+                    if ((j >> k) & 1) ad ^= rsw[k];
+                sm[ad] = P::a2s(a[j]);
+            }
+            __syncthreads();
+        }
+
+#pragma unroll 4
+        for (int k = 0; k < PER; ++k) {
+            const uint32_t s = static_cast<uint32_t>(k * NT + tid);
+            __stcs(state + (base | choff[s >> L] | (s & lmask)), P::s2g(sm[swz<GB>(s)]));
+        }
+        __syncthreads();  // the buffer is re-filled by the prefetch two tiles later
     }
 }
 

@@ -9,17 +9,24 @@ namespace {
 template <class P, int T, int R>
 cudaError_t launch_pass_t(void* state, const PassDesc* dpass, const StepDesc* dsteps, const KOp* dops,
                           const void* dcoef, int n, int H, cudaStream_t st) {
-    const size_t smem = (sizeof(typename P::S) << T) + (sizeof(uint64_t) << H);
-    static bool attr_set = false;  // per instantiation
-    if (!attr_set) {
+    // two tile buffers + the chunk-offset table
+    const size_t smem = 2 * (sizeof(typename P::S) << T) + (sizeof(uint64_t) << H);
+    static int grid_cap = 0;  // per instantiation: SMs x resident CTAs per SM
+    if (grid_cap == 0) {
         cudaError_t e = cudaFuncSetAttribute(k_pass<P, T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             static_cast<int>(smem + 4096));
+                                             static_cast<int>(2 * (sizeof(typename P::S) << T) + (8 << 12)));
         if (e != cudaSuccess) return e;
-        attr_set = true;
+        int dev = 0, nsm = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pass<P, T, R>, 1 << (T - R), smem);
+        if (e != cudaSuccess) return e;
+        grid_cap = (nsm > 0 ? nsm : 1) * (per_sm > 0 ? per_sm : 1);
     }
     const uint64_t tiles = 1ULL << (n - T);
-    k_pass<P, T, R><<<static_cast<unsigned>(tiles), 1 << (T - R), smem, st>>>(
-        static_cast<typename P::G*>(state), dpass, dsteps, dops, static_cast<const typename P::C*>(dcoef));
+    const unsigned grid = static_cast<unsigned>(tiles < static_cast<uint64_t>(grid_cap) ? tiles : grid_cap);
+    k_pass<P, T, R><<<grid, 1 << (T - R), smem, st>>>(static_cast<typename P::G*>(state), tiles, dpass, dsteps,
+                                                       dops, static_cast<const typename P::C*>(dcoef));
     return cudaGetLastError();
 }
 
@@ -34,10 +41,9 @@ cudaError_t launch_pass_ds(int T, int R, void* state, const PassDesc* dpass, con
     QSV_SHAPE(11, 4)
     QSV_SHAPE(12, 4)
     QSV_SHAPE(12, 5)
-    QSV_SHAPE(13, 5)
     return cudaErrorInvalidValue;
 }
 
-bool pass_shape_ds(int T, int R) { return (T == 11 && R == 4) || (T == 12 && (R == 4 || R == 5)) || (T == 13 && R == 5); }
+bool pass_shape_ds(int T, int R) { return (T == 11 && R == 4) || (T == 12 && (R == 4 || R == 5)); }
 
 }  // namespace qsv

@@ -631,6 +631,14 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
                         else ko.pthr |= b;
                     }
                 }
+                if (g.kind == K_DIAG && ko.creg == 0) {
+                    if (ko.preg == 0) {
+                        ko.flags |= F_UNIFORM;  // one factor per thread, folded into the round phase
+                    } else if (__builtin_popcount(ko.preg) == 1) {
+                        ko.flags |= F_ONEBIT;
+                        ko.t0 = static_cast<uint8_t>(__builtin_ctz(ko.preg));
+                    }
+                }
                 ko.coef = push_coef(plan, g);
                 plan->ops.push_back(ko);
             }

@@ -20,6 +20,7 @@ struct P64 {
     using G = double2;  // global-memory element
     static constexpr int SBYTES = 16;
     static constexpr int GBITS = 3;  // log2(elements per 128-byte wavefront)
+    static constexpr bool RAW_STAGING = false;  // shared memory holds the global format
     __device__ static __forceinline__ A s2a(S s) { return s; }
     __device__ static __forceinline__ S a2s(A a) { return a; }
     __device__ static __forceinline__ S g2s(G g) { return g; }
@@ -33,6 +34,7 @@ struct P64 {
     }
     __device__ static __forceinline__ C cneg(C c) { return -c; }
     __device__ static __forceinline__ C coef(const C* pool, uint32_t i) { return __ldg(pool + i); }
+    __device__ static __forceinline__ A one() { return make_double2(1.0, 0.0); }
     __device__ static __forceinline__ double to_d_re(A a) { return a.x; }
     __device__ static __forceinline__ double to_d_im(A a) { return a.y; }
     __device__ static __forceinline__ G make_g(double re, double im) { return make_double2(re, im); }
@@ -48,6 +50,7 @@ struct P32 {
     using G = float2;
     static constexpr int SBYTES = 8;
     static constexpr int GBITS = 4;
+    static constexpr bool RAW_STAGING = false;
     __device__ static __forceinline__ A s2a(S s) { return s; }
     __device__ static __forceinline__ S a2s(A a) { return a; }
     __device__ static __forceinline__ S g2s(G g) { return g; }
@@ -58,6 +61,7 @@ struct P32 {
     __device__ static __forceinline__ R neg(R x) { return __int_as_float(__float_as_int(x) ^ 0x80000000); }
     __device__ static __forceinline__ C cneg(C c) { return -c; }
     __device__ static __forceinline__ C coef(const C* pool, uint32_t i) { return __ldg(pool + i); }
+    __device__ static __forceinline__ A one() { return make_float2(1.f, 0.f); }
     __device__ static __forceinline__ G make_g(double re, double im) {
         return make_float2(static_cast<float>(re), static_cast<float>(im));
     }
@@ -114,6 +118,12 @@ struct PDS {
     using G = double2;
     static constexpr int SBYTES = 16;
     static constexpr int GBITS = 3;
+    // tiles arrive in shared memory as raw FP64 and are converted in place
+    static constexpr bool RAW_STAGING = true;
+    __device__ static __forceinline__ G raw_to_g(S s) {
+        return make_double2(__hiloint2double(__float_as_int(s.y), __float_as_int(s.x)),
+                            __hiloint2double(__float_as_int(s.w), __float_as_int(s.z)));
+    }
     __device__ static __forceinline__ A s2a(S s) { return {{s.x, s.y}, {s.z, s.w}}; }
     __device__ static __forceinline__ S a2s(A a) { return make_float4(a.x.h, a.x.l, a.y.h, a.y.l); }
     __device__ static __forceinline__ S g2s(G g) {
@@ -132,6 +142,7 @@ struct PDS {
     __device__ static __forceinline__ R add(R x, R y) { return ds_add(x, y); }
     __device__ static __forceinline__ R neg(R x) { return {-x.h, -x.l}; }
     __device__ static __forceinline__ C cneg(C c) { return {-c.h, -c.l}; }
+    __device__ static __forceinline__ A one() { return {{1.f, 0.f}, {0.f, 0.f}}; }
     __device__ static __forceinline__ C coef(const C* pool, uint32_t i) {
         const float2 v = __ldg(reinterpret_cast<const float2*>(pool) + i);
         return {v.x, v.y};
