@@ -278,6 +278,53 @@ def measure(precision, ops, n, steps, warmup, per_pass=True):
     return out
 
 
+def measure_adjoint(n=24, layers=20, ps_params=6):
+    """Adjoint gradients of a hardware-efficient ansatz (ry, rz on every qubit
+    then a cx ladder, 2 * n * layers parameters; observable sum a_i Z_i Z_i+1 +
+    sum b_i X_i): time per full gradient for each precision, the same GPU's
+    parameter-shift rate (timed on `ps_params` parameters, 2 forward runs each,
+    extrapolated), and each precision's gradient error against complex128."""
+    import torch
+
+    from pyquafu_gb300 import gradients, workloads
+
+    ops, _ = workloads.hea(n, layers, seed=0)
+    terms = workloads.zz_x_hamiltonian(n, seed=0)
+    nparam = 2 * n * layers
+    out = {"workload": f"hea_{n}q_{layers}layers_{nparam}params_{len(terms)}terms"}
+    ref = None
+    for prec in ("c128", "c128_ds", "c64"):
+        gradients.adjoint(n, ops, terms, prec)  # warm-up (plans, allocation)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = 2
+        for _ in range(reps):
+            e, g = gradients.adjoint(n, ops, terms, prec)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / reps
+        item = {"s_per_gradient": round(dt, 4), "grads_per_s": round(nparam / dt, 1), "energy": e}
+        if ref is None:
+            ref = g
+        else:
+            item["max_abs_err_vs_c128"] = float(np.abs(g - ref).max())
+        out[prec] = item
+    # parameter shift on the plain GPU path (complex128), a subset of parameters
+    sub = [o for o in ops]
+    keep = set(range(ps_params))
+    sub = [o if (o.slot in keep or o.slot < 0) else workloads.named(o.name, o.qubits, o.params) for o in ops]
+    t0 = time.perf_counter()
+    ps = gradients.param_shift(n, sub, terms, "c128")
+    dt = time.perf_counter() - t0
+    per_param = dt / max(1, len(keep))
+    out["param_shift_c128"] = {"s_per_parameter": round(per_param, 4),
+                               "s_per_gradient_extrapolated": round(per_param * nparam, 2),
+                               "params_timed": len(keep),
+                               "max_abs_diff_vs_adjoint": float(np.abs(ps[: len(keep)] - ref[: len(keep)]).max())}
+    out["adjoint_speedup_vs_param_shift"] = {
+        p: round(per_param * nparam / out[p]["s_per_gradient"], 1) for p in ("c128", "c128_ds", "c64")}
+    return out
+
+
 def run_gpu(args):
     import torch
 
@@ -355,6 +402,10 @@ def run_gpu(args):
                "api": "pyquafu_gb300.qfvm.simulate_circuit(circuit, pinned complex128 state, shots=0)"}
         del psi, host
 
+    adj = None
+    if not args.skip_adjoint:
+        adj = measure_adjoint(args.adjoint_qubits)
+
     cpu = None
     if rank == 0 and not args.skip_cpu:
         cgbps, gates_done, cdt, cores = cpu_sample(ops, n, seconds=args.cpu_seconds)
@@ -381,6 +432,7 @@ def run_gpu(args):
             "e2e": e2e,
             "cpu_baseline": cpu,
             "variants": variants,
+            "adjoint": adj,
             "clocks": clk,
             "gpu_launches": int(main["launches"]),
         }
@@ -406,6 +458,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-variants", action="store_true")
+    ap.add_argument("--skip-adjoint", action="store_true")
+    ap.add_argument("--adjoint-qubits", type=int, default=24)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     args = ap.parse_args()
     if args.skip_variants:

@@ -60,6 +60,11 @@ enum {
     QFVM_C128_DS = 2 /* complex128 storage, double-single (FP32 pair) arithmetic */
 };
 
+/* Generators of parameterised matrix gates (dG/dtheta = -i/2 Q G): Q is the
+ * Pauli X, Y or Z string on the targets with the controls as a projector, or
+ * (QFVM_GEN_PHASE) -2 times the projector onto targets and controls all 1. */
+enum { QFVM_GEN_NONE = 0, QFVM_GEN_X = 1, QFVM_GEN_Y = 2, QFVM_GEN_Z = 3, QFVM_GEN_PHASE = 4 };
+
 /* One gate of a packed circuit (128 bytes). */
 typedef struct qfvm_op {
     int32_t kind;      /* QFVM_OP_* */
@@ -68,7 +73,7 @@ typedef struct qfvm_op {
     int32_t mat_dim;   /* QFVM_OP_MATRIX: 2^targets; else 0 */
     int32_t qubits[QFVM_MAX_OP_QUBITS];
     int32_t slot;      /* parameter slot for batched/adjoint runs, -1 if none */
-    int32_t reserved;
+    int32_t gen;       /* QFVM_OP_MATRIX with a slot: generator, QFVM_GEN_* (0 for named gates) */
     double params[4];  /* gate angles (params[0] is the rotation angle) */
     int64_t mat_offset; /* complex index of the matrix in the pool, -1 if none */
 } qfvm_op;
@@ -114,6 +119,20 @@ int qfvm_sampling_statevec(const double* state, uint64_t state_len, const double
  * the number of Y factors. */
 int qfvm_expect_statevec(const double* state, uint64_t state_len, const uint64_t* x_masks,
                          const uint64_t* z_masks, const int32_t* y_counts, int64_t n_terms, double* out);
+
+/* Adjoint gradient: grad_adjoint of quafu/algorithms/gradients/gradiant.py:144-173.
+ * Runs the gates from |0..0> (or from psi_in, 2^n host complex128 amplitudes
+ * when not NULL), evaluates E = sum_t coeffs[t] <P_t> (Pauli terms as for
+ * qfvm_expect_statevec), forms lam = H psi and sweeps the gates backwards
+ * through their inverses, un-applying each to psi and lam together.  For
+ * every gate with slot >= 0 it adds dE/dtheta = Im<lam| Q |psi> (Q the gate's
+ * generator: RX/RY/RZ/RZZ, P/CP, or QFVM_GEN_* for matrix gates) into
+ * grads[slot]; grads has n_slots entries and is overwritten.  precision:
+ * QFVM_C128 (FP64), QFVM_C128_DS or QFVM_C64 (FP32 gates, FP64 reductions). */
+int qfvm_adjoint(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int64_t n_ops, const double* matpool,
+                 int64_t matpool_len, const uint64_t* x_masks, const uint64_t* z_masks, const int32_t* y_counts,
+                 const double* coeffs, int64_t n_terms, const double* psi_in, double* energy, double* grads,
+                 int64_t n_slots);
 
 /* Allocation-free expectation (no counterpart in the reference).
  * For callers that cannot allocate GPU memory while they run -- processes
@@ -187,6 +206,11 @@ int qfvm_plan_run_timed(qfvm_plan* plan, qfvm_sv* sv, float* pass_ms, int32_t* p
 int qfvm_plan_host_build(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int64_t n_ops,
                          const double* matpool, int64_t matpool_len, int32_t tile_qubits, int32_t reg_qubits,
                          qfvm_plan** out);
+/* The reverse sweep qfvm_adjoint runs (probes and inverse gates), host only. */
+int qfvm_plan_host_build_adjoint(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int64_t n_ops,
+                                 const double* matpool, int64_t matpool_len, qfvm_plan** out);
+/* Parameter slot of each probe of an adjoint plan, in probe-id order. */
+int qfvm_plan_host_probe_slots(const qfvm_plan* plan, int32_t* slots);
 int qfvm_plan_host_counts(const qfvm_plan* plan, int64_t counts[4], int32_t shape[3]);
 int qfvm_plan_host_copy(const qfvm_plan* plan, void* passes, void* steps, void* kops, double* coef);
 

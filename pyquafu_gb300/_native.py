@@ -54,6 +54,8 @@ PROTOTYPES = {
     "qfvm_expect_device_noalloc": (ctypes.c_int, [c_vp, ctypes.c_uint64, ctypes.c_int32, c_u64p, c_u64p, c_i32p,
                                                   ctypes.c_int64, c_dp, c_vp]),
     "qfvm_noalloc_last_error": (ctypes.c_char_p, []),
+    "qfvm_adjoint": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int64, c_dp, ctypes.c_int64,
+                                    c_u64p, c_u64p, c_i32p, c_dp, ctypes.c_int64, c_dp, c_dp, c_dp, ctypes.c_int64]),
     "qfvm_sv_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(c_vp)]),
     "qfvm_sv_destroy": (ctypes.c_int, [c_vp]),
     "qfvm_sv_set_zero": (ctypes.c_int, [c_vp]),
@@ -75,6 +77,9 @@ PROTOTYPES = {
     "qfvm_plan_host_build": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int64, c_dp,
                                             ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(c_vp)]),
     "qfvm_plan_host_counts": (ctypes.c_int, [c_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32)]),
+    "qfvm_plan_host_build_adjoint": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int64, c_dp,
+                                                    ctypes.c_int64, ctypes.POINTER(c_vp)]),
+    "qfvm_plan_host_probe_slots": (ctypes.c_int, [c_vp, c_i32p]),
     "qfvm_plan_host_copy": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_dp]),
 }
 

@@ -1,0 +1,262 @@
+// Adjoint-method kernels: two states (psi, lam) swept backwards through the
+// inverse gates, with "probes" that accumulate Im<lam| Q |psi> for the
+// generator Q of every parameterised gate (quafu/algorithms/gradients/
+// gradiant.py:144-173 computes the same quantity one gate at a time).
+#pragma once
+#include "device.cuh"
+
+namespace qsv {
+
+// Probe accumulator type: FP64 for complex128 storage, FP32 per thread (then
+// FP64 across the warp, CTA and grid) for complex64.
+template <class P>
+struct ProbeMath;
+
+template <>
+struct ProbeMath<P64> {
+    using T = double;
+    __device__ static __forceinline__ void zc(const double2& l, const double2& w, T& zr, T& zi) {
+        zr = __fma_rn(l.x, w.x, __dmul_rn(l.y, w.y));   // Re conj(l) w
+        zi = __fma_rn(l.x, w.y, -__dmul_rn(l.y, w.x));  // Im conj(l) w
+    }
+};
+template <>
+struct ProbeMath<P32> {
+    using T = float;
+    __device__ static __forceinline__ void zc(const float2& l, const float2& w, T& zr, T& zi) {
+        zr = __fmaf_rn(l.x, w.x, __fmul_rn(l.y, w.y));
+        zi = __fmaf_rn(l.x, w.y, -__fmul_rn(l.y, w.x));
+    }
+};
+template <>
+struct ProbeMath<PDS> {
+    using T = double;
+    __device__ static __forceinline__ void zc(const ds2& l, const ds2& w, T& zr, T& zi) {
+        const double lr = ds_to_double(l.x), li = ds_to_double(l.y);
+        const double wr = ds_to_double(w.x), wi = ds_to_double(w.y);
+        zr = __fma_rn(lr, wr, __dmul_rn(li, wi));
+        zi = __fma_rn(lr, wi, -__dmul_rn(li, wr));
+    }
+};
+
+// Im(conj(l) * i^ny * w) from z = conj(l) w
+template <class T>
+__device__ __forceinline__ T im_rot(T zr, T zi, int ny) {
+    switch (ny & 3) {
+        case 0: return zi;
+        case 1: return zr;
+        case 2: return -zi;
+        default: return -zr;
+    }
+}
+
+// One thread's share of a probe in a register round.  The flip mask has at
+// most two register bits (generators of 1- and 2-qubit rotations); its bits
+// are dispatched at compile time so the partner amplitude is a register.
+template <class P, int R, int XM>
+__device__ __forceinline__ typename ProbeMath<P>::T probe_sum(const typename P::A (&psi)[1 << R],
+                                                              const typename P::A (&lam)[1 << R], const KOp& op,
+                                                              int pt) {
+    using T = typename ProbeMath<P>::T;
+    T acc = T(0);
+#pragma unroll
+    for (int j = 0; j < (1 << R); ++j) {
+        if ((static_cast<uint32_t>(j) & op.creg) != op.creg) continue;
+        const int jx = j ^ XM;
+        const int sgn = pt ^ (__popc(static_cast<uint32_t>(jx) & op.preg) & 1);
+        T zr, zi;
+        ProbeMath<P>::zc(lam[j], psi[jx], zr, zi);
+        const T v = im_rot<T>(zr, zi, op.special);
+        acc += sgn ? -v : v;
+    }
+    return acc;
+}
+
+template <class P, int R>
+__device__ __forceinline__ double reg_probe(const typename P::A (&psi)[1 << R], const typename P::A (&lam)[1 << R],
+                                            const KOp& op, uint64_t gthr) {
+    using T = typename ProbeMath<P>::T;
+    if ((gthr & op.cthr) != op.cthr) return 0.0;
+    const int pt = __popcll(gthr & op.pthr) & 1;
+    T acc = T(0);
+    const uint32_t x = op.xreg;
+    if (x == 0) {
+        acc = probe_sum<P, R, 0>(psi, lam, op, pt);
+    } else if ((x & (x - 1)) == 0) {
+        with_bit<R>(__ffs(x) - 1, [&](auto b) {
+            constexpr int B = decltype(b)::value;
+            acc = probe_sum<P, R, (1 << B)>(psi, lam, op, pt);
+        });
+    } else {
+        const int b0 = __ffs(x) - 1;
+        const int b1 = __ffs(x & (x - 1)) - 1;
+        with_bit<R>(b0, [&](auto c0) {
+            constexpr int B0 = decltype(c0)::value;
+            with_bit<R>(b1, [&](auto c1) {
+                constexpr int B1 = decltype(c1)::value;
+                if constexpr (B0 != B1) acc = probe_sum<P, R, (1 << B0) | (1 << B1)>(psi, lam, op, pt);
+            });
+        });
+    }
+    return static_cast<double>(acc);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// Two-state fused tile pass (persistent, double-buffered, like k_pass).
+// Gates apply to both states; probes add their warp sums into pacc[warp][p]
+// in a fixed order, and at the end every CTA writes its per-probe total to
+// partial[p * gridDim.x + blockIdx.x].
+// ---------------------------------------------------------------------------
+template <class P, int T, int R>
+__global__ void __launch_bounds__(1 << (T - R), 1)
+    k_pass2(typename P::G* __restrict__ psi_g, typename P::G* __restrict__ lam_g, uint64_t ntiles,
+            const PassDesc* __restrict__ pdp, const StepDesc* __restrict__ steps, const KOp* __restrict__ ops,
+            const typename P::C* __restrict__ coef, double* __restrict__ partial) {
+    constexpr int NT = 1 << (T - R);
+    constexpr int NW = NT / 32;
+    constexpr int NA = 1 << R;
+    constexpr int GB = P::GBITS;
+    constexpr int PER = (1 << T) / NT;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    typename P::S* base_s = reinterpret_cast<typename P::S*>(smem_raw);
+    // buffers: [slot][state]
+    uint64_t* choff = reinterpret_cast<uint64_t*>(smem_raw + 4 * (sizeof(typename P::S) << T));
+    double* pacc = reinterpret_cast<double*>(choff + (1 << pdp->H));
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int L = pdp->L, H = pdp->H;
+    const uint8_t* tq = pdp->tq;
+    const int np = pdp->nprobe;
+    for (int c = tid; c < (1 << H); c += NT) {
+        uint64_t off = 0;
+        for (int k = 0; k < H; ++k)
+            if ((c >> k) & 1) off |= 1ULL << tq[L + k];
+        choff[c] = off;
+    }
+    for (int i = tid; i < NW * MAX_PASS_PROBES; i += NT) pacc[i] = 0.0;
+    __syncthreads();
+    const uint32_t lmask = (1u << L) - 1;
+    const int nsteps = pdp->step_count;
+    auto buf = [&](int slot, int st) { return base_s + (2 * slot + st) * (1 << T); };
+
+    uint64_t b = blockIdx.x;
+    if (b < ntiles) {
+        const uint64_t bb = tile_base(b, L, H, tq);
+        tile_prefetch<P, T, NT>(buf(0, 0), psi_g, bb, choff, L);
+        tile_prefetch<P, T, NT>(buf(0, 1), lam_g, bb, choff, L);
+    }
+    for (int it = 0; b < ntiles; ++it, b += gridDim.x) {
+        typename P::S* sm[2] = {buf(it & 1, 0), buf(it & 1, 1)};
+        const uint64_t base = tile_base(b, L, H, tq);
+        const uint64_t bn = b + gridDim.x;
+        if (bn < ntiles) {
+            const uint64_t nb = tile_base(bn, L, H, tq);
+            tile_prefetch<P, T, NT>(buf((it + 1) & 1, 0), psi_g, nb, choff, L);
+            tile_prefetch<P, T, NT>(buf((it + 1) & 1, 1), lam_g, nb, choff, L);
+            cp_async_wait<2>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        if constexpr (P::RAW_STAGING) {
+#pragma unroll 4
+            for (int k = 0; k < PER; ++k) {
+                const uint32_t ad = swz<GB>(static_cast<uint32_t>(k * NT + tid));
+                sm[0][ad] = P::g2s(P::raw_to_g(sm[0][ad]));
+                sm[1][ad] = P::g2s(P::raw_to_g(sm[1][ad]));
+            }
+            __syncthreads();
+        }
+        const StepDesc* sd = steps + pdp->step_begin;
+        for (int si = 0; si < nsteps; ++si, ++sd) {
+            if (sd->type == STEP_SMEM) {
+                for (int oi = 0; oi < sd->op_count; ++oi) {
+                    tile_smem_op<P>(sm[0], T, base, ops[sd->op_begin + oi], coef);
+                    tile_smem_op<P>(sm[1], T, base, ops[sd->op_begin + oi], coef);
+                    __syncthreads();
+                }
+                continue;
+            }
+            uint32_t sb = 0;
+            uint64_t gthr = base;
+#pragma unroll
+            for (int k = 0; k < T - R; ++k) {
+                if ((tid >> k) & 1) {
+                    sb |= 1u << sd->tpos[k];
+                    gthr |= 1ULL << sd->tglob[k];
+                }
+            }
+            const uint32_t psb = swz<GB>(sb);
+            uint32_t rsw[R];
+#pragma unroll
+            for (int k = 0; k < R; ++k) rsw[k] = swz<GB>(1u << sd->rpos[k]);
+            typename P::A a[2][NA];
+#pragma unroll
+            for (int j = 0; j < NA; ++j) {
+                uint32_t ad = psb;
+#pragma unroll
+                for (int k = 0; k < R; ++k)
+                    if ((j >> k) & 1) ad ^= rsw[k];
+                a[0][j] = P::s2a(sm[0][ad]);
+                a[1][j] = P::s2a(sm[1][ad]);
+            }
+            RoundPhase<P> ph[2];
+            ph[0].f = ph[1].f = P::one();
+            ph[0].on = ph[1].on = false;
+            const KOp* op = ops + sd->op_begin;
+            for (int oi = 0; oi < sd->op_count; ++oi) {
+                const KOp o = op[oi];
+                if (o.kind == K_PROBE) {
+                    // pending uniform phases act on both states alike, so the
+                    // probe (a product of conj(lam) and psi) is unaffected by them
+                    const double v = warp_sum(reg_probe<P, R>(a[0], a[1], o, gthr));
+                    if (lane == 0) pacc[warp * MAX_PASS_PROBES + o.probe] += v * P::coef_d(coef, o.coef);
+                } else {
+                    reg_apply<P, R>(a[0], o, gthr, coef, ph[0]);
+                    reg_apply<P, R>(a[1], o, gthr, coef, ph[1]);
+                }
+            }
+#pragma unroll
+            for (int s2 = 0; s2 < 2; ++s2) {
+                if (ph[s2].on) {
+#pragma unroll
+                    for (int j = 0; j < NA; ++j) amp_phase<P>(a[s2][j], ph[s2].f.x, ph[s2].f.y, P::cneg(ph[s2].f.y));
+                }
+            }
+            uint32_t psb2 = psb;
+            asm volatile("" : "+r"(psb2));
+#pragma unroll
+            for (int j = 0; j < NA; ++j) {
+                uint32_t ad = psb2;
+#pragma unroll
+                for (int k = 0; k < R; ++k)
+                    if ((j >> k) & 1) ad ^= rsw[k];
+                sm[0][ad] = P::a2s(a[0][j]);
+                sm[1][ad] = P::a2s(a[1][j]);
+            }
+            __syncthreads();
+        }
+#pragma unroll 4
+        for (int k = 0; k < PER; ++k) {
+            const uint32_t s = static_cast<uint32_t>(k * NT + tid);
+            const uint64_t g = base | choff[s >> L] | (s & lmask);
+            __stcs(psi_g + g, P::s2g(sm[0][swz<GB>(s)]));
+            __stcs(lam_g + g, P::s2g(sm[1][swz<GB>(s)]));
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    for (int p = tid; p < np; p += NT) {
+        double s = 0.0;
+        for (int w = 0; w < NW; ++w) s += pacc[w * MAX_PASS_PROBES + p];
+        partial[static_cast<size_t>(p) * gridDim.x + blockIdx.x] = s;
+    }
+}
+
+}  // namespace qsv

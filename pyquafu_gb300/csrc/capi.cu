@@ -137,6 +137,8 @@ int upload_plan(qfvm_plan* p) {
     return QFVM_OK;
 }
 
+int make_plan_gops(int n, int precision, const std::vector<GOp>& gops, int T, int R, qfvm_plan** out);
+
 int make_plan(int n, int precision, const qfvm_op* ops, int64_t n_ops, const double* matpool, int64_t matpool_len,
               int T, int R, qfvm_plan** out) {
     if (n < 1 || n > QFVM_MAX_QUBITS) return fail(QFVM_ERR_INVALID, "qubit count out of range");
@@ -152,6 +154,12 @@ int make_plan(int n, int precision, const qfvm_op* ops, int64_t n_ops, const dou
         if (!pass_shape_supported(precision == QFVM_C128_DS ? QFVM_C128_DS : sp, tt, rr))
             return fail(QFVM_ERR_INVALID, "tile shape not compiled in");
     }
+    return make_plan_gops(n, precision, gops, T, R, out);
+}
+
+int make_plan_gops(int n, int precision, const std::vector<GOp>& gops, int T, int R, qfvm_plan** out) {
+    std::string err;
+    const int sp = store_precision(precision);
     qfvm_plan* p = new qfvm_plan();
     if (!build_plan(n, sp, gops, T, R, &p->hp, &err)) {
         delete p;
@@ -569,6 +577,32 @@ int qfvm_plan_host_build(int32_t num_qubits, int32_t precision, const qfvm_op* o
     return QFVM_OK;
 }
 
+int qfvm_plan_host_build_adjoint(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int64_t n_ops,
+                                 const double* matpool, int64_t matpool_len, qfvm_plan** out) {
+    if (!out) return fail(QFVM_ERR_INVALID, "null output");
+    if (num_qubits < 1 || num_qubits > QFVM_MAX_QUBITS) return fail(QFVM_ERR_INVALID, "qubit count out of range");
+    std::vector<GOp> gops, sweep;
+    std::string err;
+    if (!classify(num_qubits, ops, n_ops, matpool, matpool_len, &gops, &err)) return fail(QFVM_ERR_INVALID, err);
+    if (!build_adjoint_sweep(gops, &sweep, &err)) return fail(QFVM_ERR_INVALID, err);
+    int aT = 0, aR = 0;
+    adjoint_shape(precision, &aT, &aR);
+    qfvm_plan* p = new qfvm_plan();
+    if (!build_plan(num_qubits, store_precision(precision), sweep, aT, aR, &p->hp, &err)) {
+        delete p;
+        return fail(QFVM_ERR_INVALID, err);
+    }
+    p->hp.arith = precision;
+    *out = p;
+    return QFVM_OK;
+}
+
+int qfvm_plan_host_probe_slots(const qfvm_plan* plan, int32_t* slots) {
+    if (!plan || !slots) return fail(QFVM_ERR_INVALID, "null argument");
+    for (size_t i = 0; i < plan->hp.probe_slot.size(); ++i) slots[i] = plan->hp.probe_slot[i];
+    return QFVM_OK;
+}
+
 int qfvm_plan_host_counts(const qfvm_plan* plan, int64_t counts[4], int32_t shape[3]) {
     if (!plan || !counts || !shape) return fail(QFVM_ERR_INVALID, "null argument");
     counts[0] = static_cast<int64_t>(plan->hp.passes.size());
@@ -638,6 +672,151 @@ int qfvm_sampling_statevec(const double* state, uint64_t state_len, const double
     QSV_TRY(cached_state(n, QFVM_C128, &sv));
     QSV_TRY(sv_upload(sv, state, sv->N));
     return sv_sample(sv, uniforms, shots, out_indices);
+}
+
+int qfvm_adjoint(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int64_t n_ops, const double* matpool,
+                 int64_t matpool_len, const uint64_t* x_masks, const uint64_t* z_masks, const int32_t* y_counts,
+                 const double* coeffs, int64_t n_terms, const double* psi_in, double* energy, double* grads,
+                 int64_t n_slots) {
+    std::lock_guard<std::mutex> lk(g_boundary_mu);
+    const int n = num_qubits;
+    if (n < 1 || n > QFVM_MAX_QUBITS) return fail(QFVM_ERR_INVALID, "qubit count out of range");
+    if (n_terms < 1 || !x_masks || !z_masks || !y_counts || !coeffs)
+        return fail(QFVM_ERR_INVALID, "the observable needs at least one Pauli term");
+    if (n_slots < 0 || (n_slots > 0 && !grads)) return fail(QFVM_ERR_INVALID, "bad gradient buffer");
+    if (precision != QFVM_C128 && precision != QFVM_C64 && precision != QFVM_C128_DS)
+        return fail(QFVM_ERR_INVALID, "unknown precision");
+    QSV_TRY(check_device());
+    const uint64_t lim = n >= 64 ? ~0ULL : ((1ULL << n) - 1);
+    for (int64_t t = 0; t < n_terms; ++t)
+        if ((x_masks[t] | z_masks[t]) & ~lim) return fail(QFVM_ERR_INVALID, "Pauli term acts outside the state");
+    std::vector<GOp> gops;
+    std::string err;
+    if (!classify(n, ops, n_ops, matpool, matpool_len, &gops, &err)) return fail(QFVM_ERR_INVALID, err);
+    for (const GOp& g : gops)
+        if (g.slot >= n_slots) return fail(QFVM_ERR_INVALID, "parameter slot beyond n_slots");
+    std::vector<GOp> sweep;
+    if (!build_adjoint_sweep(gops, &sweep, &err)) return fail(QFVM_ERR_INVALID, err);
+    for (const GOp& g : sweep)
+        if (g.kind == K_PROBE && __builtin_popcountll(g.xmask) > 2)
+            return fail(QFVM_ERR_UNSUPPORTED, "generators flipping more than two qubits are not supported");
+    const int storage = store_precision(precision);
+    const int arith = precision;
+
+    // forward pass on psi
+    qfvm_plan* fwd = nullptr;
+    QSV_TRY(make_plan_gops(n, precision, gops, 0, 0, &fwd));
+    int aT = 0, aR = 0;
+    adjoint_shape(arith, &aT, &aR);
+    qfvm_plan* rev = nullptr;
+    int rc = make_plan_gops(n, precision, sweep, aT, aR, &rev);
+    if (rc != QFVM_OK) {
+        free_plan(fwd);
+        return rc;
+    }
+    auto done = [&](int code) {
+        free_plan(fwd);
+        free_plan(rev);
+        return code;
+    };
+#define ADJ_CUDA(call, what)                                                                          \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) return done(fail(QFVM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e_))); \
+    } while (0)
+    qfvm_sv* psi = nullptr;
+    rc = cached_state(n, storage, &psi);
+    if (rc != QFVM_OK) return done(rc);
+    static qfvm_sv* lam_cache[2] = {nullptr, nullptr};
+    const int ck = storage == QFVM_C64 ? 1 : 0;
+    if (!lam_cache[ck] || lam_cache[ck]->n != n) {
+        if (lam_cache[ck]) sv_free(lam_cache[ck]);
+        lam_cache[ck] = nullptr;
+        rc = sv_create(n, storage, &lam_cache[ck]);
+        if (rc != QFVM_OK) return done(rc);
+    }
+    qfvm_sv* lam = lam_cache[ck];
+    rc = psi_in ? sv_upload(psi, psi_in, psi->N) : sv_set_zero(psi);
+    if (rc == QFVM_OK) rc = run_plan(fwd, psi);
+    if (rc != QFVM_OK) return done(rc);
+
+    // energy = sum_t c_t <P_t>
+    std::vector<double> ev(static_cast<size_t>(n_terms));
+    rc = sv_expect(psi, x_masks, z_masks, y_counts, n_terms, ev.data());
+    if (rc != QFVM_OK) return done(rc);
+    double e = 0.0;
+    for (int64_t t = 0; t < n_terms; ++t) e += coeffs[t] * ev[t];
+    if (energy) *energy = e;
+
+    // lam = H psi (terms sorted by flip mask so the kernel reuses loads)
+    std::vector<int64_t> ord(static_cast<size_t>(n_terms));
+    for (int64_t t = 0; t < n_terms; ++t) ord[t] = t;
+    std::stable_sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return x_masks[a] < x_masks[b]; });
+    const size_t nt = static_cast<size_t>(n_terms);
+    std::vector<uint64_t> hx(nt), hz(nt);
+    std::vector<int32_t> hy(nt);
+    std::vector<double> hc(nt);
+    for (size_t i = 0; i < nt; ++i) {
+        hx[i] = x_masks[ord[i]];
+        hz[i] = z_masks[ord[i]];
+        hy[i] = y_counts[ord[i]];
+        hc[i] = coeffs[ord[i]];
+    }
+    const size_t nprobe = rev->hp.probe_slot.size();
+    const int gcap = pass2_grid_cap();
+    const size_t b8 = align256(nt * 8), b4 = align256(nt * 4);
+    const size_t bvals = align256(std::max<size_t>(nprobe, 1) * 8);
+    const size_t bpart = align256(static_cast<size_t>(MAX_PASS_PROBES) * gcap * 8);
+    rc = lam->masks.ensure(3 * b8 + b4 + bvals + bpart);
+    if (rc != QFVM_OK) return done(rc);
+    char* mb = static_cast<char*>(lam->masks.p);
+    uint64_t* dx = reinterpret_cast<uint64_t*>(mb);
+    uint64_t* dz = reinterpret_cast<uint64_t*>(mb + b8);
+    double* dc = reinterpret_cast<double*>(mb + 2 * b8);
+    int32_t* dy = reinterpret_cast<int32_t*>(mb + 3 * b8);
+    double* dvals = reinterpret_cast<double*>(mb + 3 * b8 + b4);
+    double* dpart = reinterpret_cast<double*>(mb + 3 * b8 + b4 + bvals);
+    cudaStream_t st = psi->stream;
+    ADJ_CUDA(cudaStreamSynchronize(lam->stream), "adjoint sync");
+    ADJ_CUDA(cudaMemcpyAsync(dx, hx.data(), nt * 8, cudaMemcpyHostToDevice, st), "term upload");
+    ADJ_CUDA(cudaMemcpyAsync(dz, hz.data(), nt * 8, cudaMemcpyHostToDevice, st), "term upload");
+    ADJ_CUDA(cudaMemcpyAsync(dc, hc.data(), nt * 8, cudaMemcpyHostToDevice, st), "term upload");
+    ADJ_CUDA(cudaMemcpyAsync(dy, hy.data(), nt * 4, cudaMemcpyHostToDevice, st), "term upload");
+    ADJ_CUDA(launch_hamiltonian(storage, psi->d, lam->d, psi->N, dx, dz, dy, dc, static_cast<int>(nt), st),
+             "hamiltonian");
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+
+    // reverse sweep over both states
+    const HostPlan& hp = rev->hp;
+    for (size_t i = 0; i < hp.passes.size(); ++i) {
+        const PassDesc& pd = hp.passes[i];
+        cudaError_t ce = cudaSuccess;
+        if (pd.type == PASS_TILE) {
+            int grid = 0;
+            ce = launch_pass2(arith, psi->d, lam->d, rev->dpass + i, rev->dsteps, rev->dops, rev->dcoef, n, pd.H,
+                              dpart, &grid, st);
+            g_launches.fetch_add(1, std::memory_order_relaxed);
+            if (ce == cudaSuccess && pd.nprobe > 0) {
+                ce = launch_probe_reduce(dpart, grid, pd.nprobe, dvals + pd.probe_base, st);
+                g_launches.fetch_add(1, std::memory_order_relaxed);
+            }
+        } else if (pd.type == PASS_SMALL) {
+            ce = launch_small2(arith, psi->d, lam->d, n, rev->dops + pd.op_begin, pd.op_count, rev->dcoef, dvals, st);
+            g_launches.fetch_add(1, std::memory_order_relaxed);
+        } else {
+            ce = launch_globalop(arith, psi->d, n, rev->dops + pd.op_begin, rev->dcoef, st);
+            if (ce == cudaSuccess) ce = launch_globalop(arith, lam->d, n, rev->dops + pd.op_begin, rev->dcoef, st);
+            g_launches.fetch_add(2, std::memory_order_relaxed);
+        }
+        if (ce != cudaSuccess) return done(fail(QFVM_ERR_CUDA, std::string("adjoint pass: ") + cudaGetErrorString(ce)));
+    }
+    std::vector<double> vals(nprobe);
+    if (nprobe) ADJ_CUDA(cudaMemcpyAsync(vals.data(), dvals, nprobe * 8, cudaMemcpyDeviceToHost, st), "probe download");
+    ADJ_CUDA(cudaStreamSynchronize(st), "adjoint sync");
+    for (int64_t k = 0; k < n_slots; ++k) grads[k] = 0.0;
+    for (size_t p = 0; p < nprobe; ++p) grads[hp.probe_slot[p]] += vals[p];
+    return done(QFVM_OK);
+#undef ADJ_CUDA
 }
 
 int qfvm_expect_statevec(const double* state, uint64_t state_len, const uint64_t* x_masks, const uint64_t* z_masks,

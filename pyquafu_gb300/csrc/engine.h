@@ -23,7 +23,8 @@ enum GKind : uint8_t {
     K_Y = 6,      // [[0,-i],[i,0]] on t0
     K_SWAP = 7,   // exchange qubits t0 and t1
     K_DENSE2 = 8, // 4x4 complex on (t0 = bit 0, t1 = bit 1), 32 coefs
-    K_DENSEK = 9  // 2^k x 2^k complex on tk[0..k-1] (bit j = tk[j]), 2*4^k coefs
+    K_DENSEK = 9, // 2^k x 2^k complex on tk[0..k-1] (bit j = tk[j]), 2*4^k coefs
+    K_PROBE = 10  // adjoint sweep: accumulate Im<lam| Q |psi> (reads both states, changes neither)
 };
 
 // DIAG flags
@@ -48,6 +49,15 @@ struct GOp {
     std::vector<double> coef;
     int src = -1;   // index of the circuit op it came from
     int slot = -1;  // parameter slot (batched / adjoint runs)
+    // Generator of a parameterised gate: dG/dtheta = -i/2 Q G with
+    // Q = scale * proj(gcmask) * (Pauli with flip mask gx, phase mask gz, gny Y factors).
+    bool has_gen = false;
+    uint64_t gx = 0, gz = 0, gcmask = 0;
+    int gny = 0;
+    double gscale = 1.0;
+    // K_PROBE: xmask = flip bits, pmask = Z bits, cmask = projector bits,
+    // special = number of Y factors, coef = {scale}
+    uint64_t xmask = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -59,12 +69,14 @@ struct GOp {
 // thread's base index.  For whole-state kernels all masks are global.
 struct KOp {
     uint8_t kind, flags, special, k;
-    uint8_t t0, t1, pad0, pad1;
+    uint8_t t0, t1;
+    uint16_t probe;  // K_PROBE: index of the probe within its pass
     uint32_t creg, preg;
     uint64_t cthr, pthr;
     uint32_t coef;  // offset into the coefficient pool (in reals)
     uint8_t tk[MAXK];
     uint8_t pad2[2];
+    uint32_t xreg;  // K_PROBE: flip mask over register bits (or over global bits in whole-state passes)
 };
 static_assert(sizeof(KOp) == 48, "KOp layout");
 
@@ -77,10 +89,12 @@ struct PassDesc {
     int32_t T, L, H;
     int32_t step_begin, step_count;
     int32_t op_begin, op_count;  // PASS_SMALL / PASS_GLOBALOP: ops applied
+    int32_t probe_base, nprobe;  // adjoint sweeps: probes evaluated in this pass
     uint8_t tq[16];
 };
 enum : int32_t { PASS_TILE = 0, PASS_SMALL = 1, PASS_GLOBALOP = 2 };
-static_assert(sizeof(PassDesc) == 48, "PassDesc layout");
+static_assert(sizeof(PassDesc) == 56, "PassDesc layout");
+constexpr int MAX_PASS_PROBES = 64;
 
 // One register round inside a tile pass: register bit k holds tile-local
 // position rpos[k]; thread-index bit k selects tile-local position tpos[k].
@@ -102,6 +116,7 @@ struct PlanStats {
 // Host-side plan (built by plan.cpp, executed by kernels.cu).
 struct HostPlan {
     int n = 0, precision = QFVM_C128, T = 0, R = 0, L = 0;
+    std::vector<int> probe_slot;  // adjoint sweeps: parameter slot of every probe, by probe id
     int arith = QFVM_C128;  // kernel arithmetic: QFVM_C128 (FP64), QFVM_C64 (FP32), QFVM_C128_DS
     std::vector<PassDesc> passes;
     std::vector<StepDesc> steps;
@@ -120,6 +135,10 @@ bool classify(int n, const qfvm_op* ops, int64_t n_ops, const double* matpool, i
               std::vector<GOp>* out, std::string* err);
 bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R, HostPlan* plan,
                 std::string* err);
+// Reverse sweep of the adjoint method: for each gate from last to first, a
+// probe of its generator (if it carries a parameter slot) and its inverse.
+bool build_adjoint_sweep(const std::vector<GOp>& gops, std::vector<GOp>* out, std::string* err);
+GOp gop_dagger(const GOp& g);
 // Gate-equivalent bytes of one gop: 2 * bytes per amplitude * amplitudes it
 // must touch.
 double gop_bytes(const GOp& g, int n, int precision);

@@ -42,3 +42,18 @@ cudaError_t launch_sample_exact(int precision, const void* state, uint64_t N, co
                                 const int64_t* dord, int64_t m, uint64_t* dout, cudaStream_t st);
 
 }  // namespace qsv
+
+namespace qsv {
+// adjoint.cu
+void adjoint_shape(int arith, int* T, int* R);
+int adjoint_small_max(int arith);
+cudaError_t launch_pass2(int arith, void* psi, void* lam, const PassDesc* dpass, const StepDesc* dsteps,
+                         const KOp* dops, const void* dcoef, int n, int H, double* partial, int* grid_out,
+                         cudaStream_t st);
+int pass2_grid_cap();
+cudaError_t launch_small2(int arith, void* psi, void* lam, int n, const KOp* dops, int nops, const void* dcoef,
+                          double* probe_out, cudaStream_t st);
+cudaError_t launch_hamiltonian(int storage, const void* psi, void* lam, uint64_t N, const uint64_t* dx,
+                               const uint64_t* dz, const int32_t* dny, const double* dc, int nterms, cudaStream_t st);
+cudaError_t launch_probe_reduce(const double* partial, int grid, int np, double* out, cudaStream_t st);
+}  // namespace qsv

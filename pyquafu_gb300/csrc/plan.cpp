@@ -283,6 +283,34 @@ bool classify(int n, const qfvm_op* ops, int64_t n_ops, const double* matpool, i
                 return false;
             }
         }
+        // generator of a parameterised gate: dG/dtheta = -i/2 Q G
+        // (rotations exp(-i theta Q / 2); phase gates diag(1, e^{i l}) give Q = -2 proj)
+        {
+            const uint64_t b0 = 1ULL << q[0];
+            switch (o.kind) {
+                case QFVM_OP_RX: g.has_gen = true; g.gx = b0; break;
+                case QFVM_OP_RY: g.has_gen = true; g.gx = b0; g.gz = b0; g.gny = 1; break;
+                case QFVM_OP_RZ: g.has_gen = true; g.gz = b0; break;
+                case QFVM_OP_RZZ: g.has_gen = true; g.gz = b0 | (1ULL << q[1]); break;
+                case QFVM_OP_P: g.has_gen = true; g.gcmask = b0; g.gscale = -2.0; break;
+                case QFVM_OP_CP: g.has_gen = true; g.gcmask = b0 | (1ULL << q[1]); g.gscale = -2.0; break;
+                case QFVM_OP_MATRIX: {
+                    uint64_t tm = 0, cm = 0;
+                    for (int j = 0; j < o.ncontrols; ++j) cm |= 1ULL << q[j];
+                    for (int j = o.ncontrols; j < nq; ++j) tm |= 1ULL << q[j];
+                    const int nt = nq - o.ncontrols;
+                    switch (o.gen) {
+                        case QFVM_GEN_X: g.has_gen = true; g.gx = tm; g.gcmask = cm; break;
+                        case QFVM_GEN_Y: g.has_gen = true; g.gx = tm; g.gz = tm; g.gny = nt; g.gcmask = cm; break;
+                        case QFVM_GEN_Z: g.has_gen = true; g.gz = tm; g.gcmask = cm; break;
+                        case QFVM_GEN_PHASE: g.has_gen = true; g.gcmask = tm | cm; g.gscale = -2.0; break;
+                        default: break;
+                    }
+                    break;
+                }
+                default: break;
+            }
+        }
         out->push_back(std::move(g));
     }
     return true;
@@ -328,6 +356,14 @@ void gop_actions(const GOp& g, std::vector<std::pair<int, uint8_t>>* acts) {
         case K_DENSEK:
             for (int j = 0; j < g.k; ++j) acts->push_back({g.tk[j], A_G});
             break;
+        case K_PROBE:
+            // a probe of Q commutes with a gate that commutes with Q: Z bits and
+            // the projector act diagonally, pure flip bits as X, Y bits as both
+            for (int q = 0; q < 64; ++q) {
+                const uint64_t b = 1ULL << q;
+                if (g.xmask & b) acts->push_back({q, (g.pmask & b) ? A_G : A_X});
+            }
+            break;
         default: acts->push_back({g.t0, A_G}); break;
     }
 }
@@ -350,6 +386,10 @@ void gop_targets(const GOp& g, std::vector<int>* t) {
             break;
         case K_DENSEK:
             for (int j = 0; j < g.k; ++j) t->push_back(g.tk[j]);
+            break;
+        case K_PROBE:  // flipped qubits pair amplitudes: they must be register bits
+            for (int q = 0; q < 64; ++q)
+                if (g.xmask & (1ULL << q)) t->push_back(q);
             break;
         default: t->push_back(g.t0); break;
     }
@@ -375,6 +415,11 @@ KOp global_kop(HostPlan* p, const GOp& g) {
     for (int j = 0; j < g.k; ++j) k.tk[j] = static_cast<uint8_t>(g.tk[j]);
     k.cthr = g.cmask;
     k.pthr = g.pmask;
+    if (g.kind == K_PROBE) {
+        k.xreg = static_cast<uint32_t>(g.xmask);  // whole-state kernels: global flip bits (n <= 14)
+        k.probe = static_cast<uint16_t>(p->probe_slot.size());
+        p->probe_slot.push_back(g.slot);
+    }
     k.coef = push_coef(p, g);
     return k;
 }
@@ -438,6 +483,8 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
         pd.op_begin = 0;
         for (const auto& g : gops) plan->ops.push_back(global_kop(plan, g));
         pd.op_count = static_cast<int32_t>(plan->ops.size());
+        pd.probe_base = 0;
+        pd.nprobe = static_cast<int32_t>(plan->probe_slot.size());
         plan->passes.push_back(pd);
         st.passes = 1;
         st.rounds = 0;
@@ -465,12 +512,14 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
         uint8_t blocked[64] = {0};
         std::vector<int> high;  // global qubits >= L in the tile
         std::vector<int> sched, rest;
+        int probes = 0;
         for (int gi : pending) {
             const GOp& g = gops[gi];
             gop_actions(g, &acts);
             bool conflict = false;
             for (auto& a : acts) conflict |= act_conflict(blocked[a.first], a.second);
             bool ok = !conflict && g.kind != K_DENSEK;
+            if (ok && g.kind == K_PROBE && probes >= MAX_PASS_PROBES) ok = false;
             if (ok) {
                 gop_targets(g, &targ);
                 std::vector<int> add;
@@ -486,6 +535,7 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
             }
             if (ok) {
                 sched.push_back(gi);
+                if (g.kind == K_PROBE) ++probes;
             } else {
                 for (auto& a : acts) blocked[a.first] |= a.second;
                 rest.push_back(gi);
@@ -528,6 +578,7 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
             local_of[high[k]] = L + k;
         }
         pd.step_begin = static_cast<int32_t>(plan->steps.size());
+        pd.probe_base = static_cast<int32_t>(plan->probe_slot.size());
 
         // ---- split the pass's gates into register rounds ----
         // Two-target dense gates run as shared-memory steps of the tile (in
@@ -631,6 +682,12 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
                         else ko.pthr |= b;
                     }
                 }
+                if (g.kind == K_PROBE) {
+                    for (int q = 0; q < n; ++q)
+                        if (g.xmask & (1ULL << q)) ko.xreg |= 1u << reg_of_local[local_of[q]];
+                    ko.probe = static_cast<uint16_t>(plan->probe_slot.size() - pd.probe_base);
+                    plan->probe_slot.push_back(g.slot);
+                }
                 if (g.kind == K_DIAG && ko.creg == 0) {
                     if (ko.preg == 0) {
                         ko.flags |= F_UNIFORM;  // one factor per thread, folded into the round phase
@@ -648,10 +705,66 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
             todo = left;
         }
         pd.step_count = static_cast<int32_t>(plan->steps.size()) - pd.step_begin;
+        pd.nprobe = static_cast<int32_t>(plan->probe_slot.size()) - pd.probe_base;
         plan->passes.push_back(pd);
         st.passes += 1;
         st.pass_bytes += 2.0 * Sb * N;
         pending = rest;
+    }
+    return true;
+}
+
+GOp gop_dagger(const GOp& g) {
+    GOp d = g;
+    auto conj_transpose = [&](int dim) {
+        std::vector<double> c(g.coef.size());
+        for (int r = 0; r < dim; ++r)
+            for (int k = 0; k < dim; ++k) {
+                c[2 * (r * dim + k)] = g.coef[2 * (k * dim + r)];
+                c[2 * (r * dim + k) + 1] = -g.coef[2 * (k * dim + r) + 1];
+            }
+        d.coef = c;
+    };
+    switch (g.kind) {
+        case K_REAL: d.coef = {g.coef[0], g.coef[2], g.coef[1], g.coef[3]}; break;  // real unitary: transpose
+        case K_RX: d.coef = {g.coef[0], -g.coef[1]}; break;
+        case K_DENSE: conj_transpose(2); break;
+        case K_DENSE2: conj_transpose(4); break;
+        case K_DENSEK: conj_transpose(1 << g.k); break;
+        case K_DIAG:
+            d.coef = {g.coef[0], -g.coef[1], g.coef[2], -g.coef[3]};
+            if (g.flags & F_D1_SPEC) {
+                if (g.special == SP_I) d.special = SP_NEGI;
+                else if (g.special == SP_NEGI) d.special = SP_I;
+            }
+            break;
+        default: break;  // X, Y, SWAP are self-inverse
+    }
+    return d;
+}
+
+bool build_adjoint_sweep(const std::vector<GOp>& gops, std::vector<GOp>* out, std::string* err) {
+    out->clear();
+    out->reserve(gops.size() * 2);
+    for (size_t r = gops.size(); r-- > 0;) {
+        const GOp& g = gops[r];
+        if (g.slot >= 0) {
+            if (!g.has_gen) {
+                *err = "op " + std::to_string(g.src) + " carries a parameter slot but has no generator";
+                return false;
+            }
+            GOp pr;
+            pr.kind = K_PROBE;
+            pr.xmask = g.gx;
+            pr.pmask = g.gz;
+            pr.cmask = g.gcmask;
+            pr.special = static_cast<uint8_t>(g.gny & 3);
+            pr.coef = {g.gscale};
+            pr.slot = g.slot;
+            pr.src = g.src;
+            out->push_back(pr);
+        }
+        out->push_back(gop_dagger(g));
     }
     return true;
 }

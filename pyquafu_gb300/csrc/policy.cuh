@@ -35,6 +35,7 @@ struct P64 {
     __device__ static __forceinline__ C cneg(C c) { return -c; }
     __device__ static __forceinline__ C coef(const C* pool, uint32_t i) { return __ldg(pool + i); }
     __device__ static __forceinline__ A one() { return make_double2(1.0, 0.0); }
+    __device__ static __forceinline__ double coef_d(const C* pool, uint32_t i) { return __ldg(pool + i); }
     __device__ static __forceinline__ double to_d_re(A a) { return a.x; }
     __device__ static __forceinline__ double to_d_im(A a) { return a.y; }
     __device__ static __forceinline__ G make_g(double re, double im) { return make_double2(re, im); }
@@ -62,6 +63,9 @@ struct P32 {
     __device__ static __forceinline__ C cneg(C c) { return -c; }
     __device__ static __forceinline__ C coef(const C* pool, uint32_t i) { return __ldg(pool + i); }
     __device__ static __forceinline__ A one() { return make_float2(1.f, 0.f); }
+    __device__ static __forceinline__ double coef_d(const C* pool, uint32_t i) {
+        return static_cast<double>(__ldg(pool + i));
+    }
     __device__ static __forceinline__ G make_g(double re, double im) {
         return make_float2(static_cast<float>(re), static_cast<float>(im));
     }
@@ -143,6 +147,7 @@ struct PDS {
     __device__ static __forceinline__ R neg(R x) { return {-x.h, -x.l}; }
     __device__ static __forceinline__ C cneg(C c) { return {-c.h, -c.l}; }
     __device__ static __forceinline__ A one() { return {{1.f, 0.f}, {0.f, 0.f}}; }
+    __device__ static __forceinline__ double coef_d(const C* pool, uint32_t i) { return ds_to_double(coef(pool, i)); }
     __device__ static __forceinline__ C coef(const C* pool, uint32_t i) {
         const float2 v = __ldg(reinterpret_cast<const float2*>(pool) + i);
         return {v.x, v.y};

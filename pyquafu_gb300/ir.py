@@ -41,6 +41,27 @@ SKIPPED = {"barrier", "delay", "id"}
 
 MAX_OP_QUBITS = 16
 
+# generators of parameterised matrix gates (QFVM_GEN_* of include/qfvm_gb300.h)
+GEN_NONE, GEN_X, GEN_Y, GEN_Z, GEN_PHASE = 0, 1, 2, 3, 4
+
+
+def generator_of(name: str, kind: int) -> int:
+    """dG/dtheta = -i/2 Q G for the rotation families pyquafu defines
+    (element_gates.py: RX/RY/RZ, RXX/RYY/RZZ, CRX/CRY/CRZ, MCRX/MCRY/MCRZ,
+    P/CP); named OPMAP gates carry their generator implicitly."""
+    if kind != OP_MATRIX:
+        return GEN_NONE
+    n = name.lower()
+    if n.endswith("rx") or n.endswith("rxx"):
+        return GEN_X
+    if n.endswith("ry") or n.endswith("ryy"):
+        return GEN_Y
+    if n.endswith("rz") or n.endswith("rzz"):
+        return GEN_Z
+    if n in ("p", "cp", "mcp", "phase"):
+        return GEN_PHASE
+    return GEN_NONE
+
 # numpy mirror of ``qfvm_op`` (include/qfvm_gb300.h); 128 bytes, 8-byte aligned
 OP_DTYPE = np.dtype(
     [
@@ -50,7 +71,7 @@ OP_DTYPE = np.dtype(
         ("mat_dim", "<i4"),
         ("qubits", "<i4", (MAX_OP_QUBITS,)),
         ("slot", "<i4"),
-        ("reserved", "<i4"),
+        ("gen", "<i4"),
         ("params", "<f8", (4,)),
         ("mat_offset", "<i8"),
     ],
@@ -62,11 +83,11 @@ assert OP_DTYPE.itemsize == 128
 class Op:
     """One instruction of the packed list (a gate, or a measure/reset/cif)."""
 
-    __slots__ = ("name", "kind", "qubits", "ncontrols", "params", "matrix", "slot",
+    __slots__ = ("name", "kind", "qubits", "ncontrols", "params", "matrix", "slot", "gen",
                  "qbits", "cbits", "condition", "body")
 
     def __init__(self, name, kind, qubits=(), ncontrols=0, params=(), matrix=None, slot=-1,
-                 qbits=(), cbits=(), condition=0, body=()):
+                 qbits=(), cbits=(), condition=0, body=(), gen=None):
         self.name = name
         self.kind = kind
         self.qubits = tuple(int(q) for q in qubits)
@@ -74,6 +95,7 @@ class Op:
         self.params = tuple(float(p) for p in params)
         self.matrix = matrix
         self.slot = int(slot)
+        self.gen = generator_of(name, kind) if gen is None else int(gen)
         self.qbits = tuple(int(q) for q in qbits)
         self.cbits = tuple(int(c) for c in cbits)
         self.condition = int(condition)
@@ -200,6 +222,7 @@ def pack(ops) -> tuple[np.ndarray, np.ndarray]:
         r["nqubits"] = len(o.qubits)
         r["qubits"][: len(o.qubits)] = o.qubits
         r["slot"] = o.slot
+        r["gen"] = o.gen
         p = list(o.params)[:4]
         r["params"][: len(p)] = p
         if o.matrix is not None:

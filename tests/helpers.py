@@ -32,27 +32,34 @@ def load_golden():
 # ------------------------- engine record layouts -------------------------
 
 PASS_DT = np.dtype([("type", "<i4"), ("T", "<i4"), ("L", "<i4"), ("H", "<i4"), ("step_begin", "<i4"),
-                    ("step_count", "<i4"), ("op_begin", "<i4"), ("op_count", "<i4"), ("tq", "u1", (16,))])
+                    ("step_count", "<i4"), ("op_begin", "<i4"), ("op_count", "<i4"), ("probe_base", "<i4"),
+                    ("nprobe", "<i4"), ("tq", "u1", (16,))])
 STEP_DT = np.dtype([("type", "<i4"), ("op_begin", "<i4"), ("op_count", "<i4"), ("rpos", "u1", (8,)),
                     ("tpos", "u1", (16,)), ("tglob", "u1", (16,))])
 KOP_DT = np.dtype([("kind", "u1"), ("flags", "u1"), ("special", "u1"), ("k", "u1"), ("t0", "u1"), ("t1", "u1"),
-                   ("pad0", "u1"), ("pad1", "u1"), ("creg", "<u4"), ("preg", "<u4"), ("cthr", "<u8"),
-                   ("pthr", "<u8"), ("coef", "<u4"), ("tk", "u1", (6,)), ("pad2", "u1", (2,))], align=True)
-assert PASS_DT.itemsize == 48 and STEP_DT.itemsize == 52 and KOP_DT.itemsize == 48
+                   ("probe", "<u2"), ("creg", "<u4"), ("preg", "<u4"), ("cthr", "<u8"),
+                   ("pthr", "<u8"), ("coef", "<u4"), ("tk", "u1", (6,)), ("pad2", "u1", (2,)), ("xreg", "<u4")],
+                  align=True)
+assert PASS_DT.itemsize == 56 and STEP_DT.itemsize == 52 and KOP_DT.itemsize == 48
 
-K_DENSE, K_REAL, K_RX, K_DIAG, K_X, K_Y, K_SWAP, K_DENSE2, K_DENSEK = range(1, 10)
+K_DENSE, K_REAL, K_RX, K_DIAG, K_X, K_Y, K_SWAP, K_DENSE2, K_DENSEK, K_PROBE = range(1, 11)
 PASS_TILE, PASS_SMALL, PASS_GLOBALOP = 0, 1, 2
 STEP_ROUND, STEP_SMEM = 0, 1
 
 
-def host_plan(n, ops, precision=0, T=0, R=0):
+def host_plan(n, ops, precision=0, T=0, R=0, adjoint=False):
     from pyquafu_gb300 import _native as nat
 
     lib = nat.load()
     arr, pool = ir.pack(ops)
     h = ctypes.c_void_p()
-    nat.check(lib.qfvm_plan_host_build(n, precision, nat.vptr(arr), arr.size, nat.dptr(pool.view(np.float64)),
-                                       pool.size, T, R, ctypes.byref(h)), "host plan")
+    if adjoint:
+        nat.check(lib.qfvm_plan_host_build_adjoint(n, precision, nat.vptr(arr), arr.size,
+                                                   nat.dptr(pool.view(np.float64)), pool.size, ctypes.byref(h)),
+                  "host adjoint plan")
+    else:
+        nat.check(lib.qfvm_plan_host_build(n, precision, nat.vptr(arr), arr.size, nat.dptr(pool.view(np.float64)),
+                                           pool.size, T, R, ctypes.byref(h)), "host plan")
     counts = (ctypes.c_int64 * 4)()
     shape = (ctypes.c_int32 * 3)()
     nat.check(lib.qfvm_plan_host_counts(h, counts, shape))
@@ -61,9 +68,13 @@ def host_plan(n, ops, precision=0, T=0, R=0):
     kops = np.zeros(max(counts[2], 1), KOP_DT)
     coef = np.zeros(max(counts[3], 1), np.float64)
     nat.check(lib.qfvm_plan_host_copy(h, nat.vptr(passes), nat.vptr(steps), nat.vptr(kops), nat.dptr(coef)))
+    nprobe = int(sum(int(p["nprobe"]) for p in passes))
+    slots = np.zeros(max(nprobe, 1), dtype=np.int32)
+    if nprobe:
+        nat.check(lib.qfvm_plan_host_probe_slots(h, nat.i32ptr(slots)))
     lib.qfvm_plan_destroy(h)
     return {"passes": passes, "steps": steps[: counts[1]], "ops": kops[: counts[2]], "coef": coef,
-            "T": shape[0], "R": shape[1], "L": shape[2]}
+            "T": shape[0], "R": shape[1], "L": shape[2], "probe_slots": slots[:nprobe]}
 
 
 def _bits(mask):
@@ -141,6 +152,77 @@ def apply_global(psi, kind, t, cmask, pmask, flags, special, coef, off, tk=()):
     else:
         raise ValueError(kind)
     psi[i0], psi[i1] = na, nb
+
+
+def probe_value(psi, lam, xmask, zmask, cmask, ny, scale):
+    """Im <lam| Q |psi> with (Q psi)[i] = scale i^ny (-1)^popc((i^x)&z) psi[i^x] on controls."""
+    idx = np.arange(psi.size, dtype=np.int64)
+    ix = idx ^ xmask
+    par = np.zeros(psi.size, dtype=np.int64)
+    for q in _bits(zmask):
+        par ^= (ix >> q) & 1
+    w = psi[ix] * np.where(par == 1, -1.0, 1.0) * (1j ** ny)
+    ok = (idx & cmask) == cmask
+    return float(scale * np.sum(np.where(ok, np.conj(lam) * w, 0)).imag)
+
+
+def interpret2(plan, psi, lam):
+    """Execute an adjoint sweep plan on (psi, lam); returns the probe values."""
+    states = [psi.copy(), lam.copy()]
+    vals = np.zeros(len(plan["probe_slots"]))
+    coef = plan["coef"]
+
+    def apply_both(kind, t, cm, pm, flags, special, off, tk=()):
+        for st in states:
+            apply_global(st, kind, t, cm, pm, flags, special, coef, off, tk)
+
+    for pd in plan["passes"]:
+        if pd["type"] in (PASS_SMALL, PASS_GLOBALOP):
+            for o in plan["ops"][pd["op_begin"]: pd["op_begin"] + pd["op_count"]]:
+                if o["kind"] == K_PROBE:
+                    vals[o["probe"]] = probe_value(states[0], states[1], int(o["xreg"]), int(o["pthr"]),
+                                                   int(o["cthr"]), int(o["special"]), coef[o["coef"]])
+                    continue
+                tk = [int(x) for x in o["tk"][: o["k"]]]
+                t = (int(o["t0"]), int(o["t1"])) if o["kind"] in (K_SWAP, K_DENSE2) else int(o["t0"])
+                apply_both(int(o["kind"]), t, int(o["cthr"]), int(o["pthr"]), int(o["flags"]), int(o["special"]),
+                           int(o["coef"]), tk)
+            continue
+        T = int(pd["T"])
+        tq = [int(x) for x in pd["tq"][:T]]
+        for sd in plan["steps"][pd["step_begin"]: pd["step_begin"] + pd["step_count"]]:
+            ops = plan["ops"][sd["op_begin"]: sd["op_begin"] + sd["op_count"]]
+            if sd["type"] == STEP_SMEM:
+                for o in ops:
+                    cm = int(o["cthr"])
+                    for b in _bits(o["creg"]):
+                        cm |= 1 << tq[b]
+                    apply_both(int(o["kind"]), (tq[o["t0"]], tq[o["t1"]]), cm, 0, 0, 0, int(o["coef"]))
+                continue
+            R = plan["R"]
+            g_of_reg = [tq[p] for p in [int(x) for x in sd["rpos"][:R]]]
+            for o in ops:
+                cm, pm = int(o["cthr"]), int(o["pthr"])
+                for b in _bits(o["creg"]):
+                    cm |= 1 << g_of_reg[b]
+                for b in _bits(o["preg"]):
+                    pm |= 1 << g_of_reg[b]
+                kind = int(o["kind"])
+                if kind == K_PROBE:
+                    xm = 0
+                    for b in _bits(o["xreg"]):
+                        xm |= 1 << g_of_reg[b]
+                    vals[int(pd["probe_base"]) + int(o["probe"])] = probe_value(
+                        states[0], states[1], xm, pm, cm, int(o["special"]), coef[o["coef"]])
+                    continue
+                if kind == K_SWAP:
+                    t = (g_of_reg[o["t0"]], g_of_reg[o["t1"]])
+                elif kind == K_DIAG:
+                    t = 0
+                else:
+                    t = g_of_reg[o["t0"]]
+                apply_both(kind, t, cm, pm, int(o["flags"]), int(o["special"]), int(o["coef"]))
+    return vals
 
 
 def interpret(plan, psi):
