@@ -199,9 +199,55 @@ int qfvm_plan_run(qfvm_plan* plan, qfvm_sv* sv);
  * to pass_type. */
 int qfvm_plan_run_timed(qfvm_plan* plan, qfvm_sv* sv, float* pass_ms, int32_t* pass_type);
 
+/* ---------------------------------------------------------------------------
+ * Batched runs.  Replaces the reference's per-sample Python loops over
+ * Estimator.run: quafu/algorithms/interface/torch.py:76-78 (ExecuteCircuits
+ * forward), quafu/algorithms/gradients/vjp.py:93-103 (jacobian via
+ * ParamShift per sample and observable) and quafu/algorithms/estimator.py:186-229.
+ *
+ * A batch holds groups.  A group is n_items circuits on num_qubits qubits
+ * that share one gate list `ops` and one set of n_obs observables; they
+ * differ only in the angles of their slotted rx/ry/rz/p/cp/rzz gates, which a
+ * run reads from values[item * n_slots + slot] (ops[k].params give the
+ * structure only).  Every item starts in |0...0>.  Observable o is the sum of
+ * the terms t with obs_index[t] == o (obs_index NULL: one observable), term t
+ * being coeffs[t] * P_t with P_t given by x/z masks and y count as in
+ * qfvm_expect_statevec.
+ *
+ * A run takes the slot values of all groups back to back (group order, then
+ * item-major) and writes expvals[item * n_obs + o] = <O_o> (FP64 sums) for all
+ * groups back to back.  Mode 1 (batch created with QFVM_BATCH_GRADS) also
+ * writes grads[item * n_slots + s] = d(sum_o w[item, o] <O_o>)/d value[s], by
+ * the adjoint method, with weights w laid out like expvals (NULL: all 1).
+ * Groups run concurrently on their own streams; the first run of a mode is
+ * issued directly, the second is captured into a CUDA graph and every later
+ * run of that mode replays it as a single graph launch.  A batch is used by
+ * one thread at a time.
+ * ------------------------------------------------------------------------- */
+typedef struct qfvm_batch qfvm_batch;
+#define QFVM_BATCH_GRADS 1    /* prepare gradient (mode 1) runs */
+#define QFVM_BATCH_NO_GRAPH 2 /* always issue runs directly (no CUDA graph) */
+/* tile_qubits / reg_qubits: fused-pass shape of the forward passes (0: default). */
+int qfvm_batch_create(int32_t precision, int32_t flags, int32_t tile_qubits, int32_t reg_qubits, qfvm_batch** out);
+int qfvm_batch_add_group(qfvm_batch* batch, int32_t num_qubits, const qfvm_op* ops, int64_t n_ops,
+                         const double* matpool, int64_t matpool_len, const uint64_t* x_masks, const uint64_t* z_masks,
+                         const int32_t* y_counts, const double* coeffs, const int32_t* obs_index, int64_t n_terms,
+                         int64_t n_obs, int64_t n_items, int64_t n_slots);
+int qfvm_batch_run(qfvm_batch* batch, int32_t mode, const double* values, const double* weights, double* expvals,
+                   double* grads);
+/* As qfvm_batch_run, plus the device time of the run (uploads, kernels and
+ * downloads) from CUDA events on the batch's stream. */
+int qfvm_batch_run_timed(qfvm_batch* batch, int32_t mode, const double* values, const double* weights,
+                         double* expvals, double* grads, float* device_ms);
+/* Sizes of the value / result arrays; per mode: kernels one run launches and
+ * whether its graph has been captured. */
+int qfvm_batch_info(const qfvm_batch* batch, int64_t* n_groups, int64_t* n_values, int64_t* n_expvals,
+                    int64_t* n_grads, int64_t kernels_per_run[2], int32_t graph_ready[2]);
+int qfvm_batch_destroy(qfvm_batch* batch);
+
 /* Host-only planning (no device needed): build the fused schedule and copy
  * its records out, for inspection and for testing the fuser.  Records are the
- * engine's internal layouts: 48-byte pass, 52-byte step and 48-byte op
+ * engine's internal layouts: 56-byte pass, 52-byte step and 48-byte op
  * records; counts[] receives passes, steps, ops, coefficients. */
 int qfvm_plan_host_build(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int64_t n_ops,
                          const double* matpool, int64_t matpool_len, int32_t tile_qubits, int32_t reg_qubits,
@@ -209,6 +255,14 @@ int qfvm_plan_host_build(int32_t num_qubits, int32_t precision, const qfvm_op* o
 /* The reverse sweep qfvm_adjoint runs (probes and inverse gates), host only. */
 int qfvm_plan_host_build_adjoint(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int64_t n_ops,
                                  const double* matpool, int64_t matpool_len, qfvm_plan** out);
+/* The forward plan (adjoint == 0) or reverse sweep (adjoint != 0) that a
+ * batch group runs, host only: value-dependent fast paths of slotted gates are
+ * dropped and the pool blocks a run rewrites per item are recorded. */
+int qfvm_plan_host_build_batched(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int64_t n_ops,
+                                 const double* matpool, int64_t matpool_len, int32_t adjoint, qfvm_plan** out);
+/* Bind records of a plan: 4 int32 each (pool offset, gate kind, angle sign,
+ * slot); records may be NULL to query the count. */
+int qfvm_plan_host_binds(const qfvm_plan* plan, int64_t* count, int32_t* records);
 /* Parameter slot of each probe of an adjoint plan, in probe-id order. */
 int qfvm_plan_host_probe_slots(const qfvm_plan* plan, int32_t* slots);
 int qfvm_plan_host_counts(const qfvm_plan* plan, int64_t counts[4], int32_t shape[3]);

@@ -74,11 +74,26 @@ PROTOTYPES = {
                                        ctypes.POINTER(ctypes.c_int64), c_dp, c_dp]),
     "qfvm_plan_run": (ctypes.c_int, [c_vp, c_vp]),
     "qfvm_plan_run_timed": (ctypes.c_int, [c_vp, c_vp, ctypes.POINTER(ctypes.c_float), c_i32p]),
+    "qfvm_batch_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                         ctypes.POINTER(c_vp)]),
+    "qfvm_batch_add_group": (ctypes.c_int, [c_vp, ctypes.c_int32, c_vp, ctypes.c_int64, c_dp, ctypes.c_int64,
+                                            c_u64p, c_u64p, c_i32p, c_dp, c_i32p, ctypes.c_int64, ctypes.c_int64,
+                                            ctypes.c_int64, ctypes.c_int64]),
+    "qfvm_batch_run": (ctypes.c_int, [c_vp, ctypes.c_int32, c_dp, c_dp, c_dp, c_dp]),
+    "qfvm_batch_run_timed": (ctypes.c_int, [c_vp, ctypes.c_int32, c_dp, c_dp, c_dp, c_dp,
+                                            ctypes.POINTER(ctypes.c_float)]),
+    "qfvm_batch_info": (ctypes.c_int, [c_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                       ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                       ctypes.POINTER(ctypes.c_int64), c_i32p]),
+    "qfvm_batch_destroy": (ctypes.c_int, [c_vp]),
     "qfvm_plan_host_build": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int64, c_dp,
                                             ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(c_vp)]),
     "qfvm_plan_host_counts": (ctypes.c_int, [c_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32)]),
     "qfvm_plan_host_build_adjoint": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int64, c_dp,
                                                     ctypes.c_int64, ctypes.POINTER(c_vp)]),
+    "qfvm_plan_host_build_batched": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int64, c_dp,
+                                                    ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(c_vp)]),
+    "qfvm_plan_host_binds": (ctypes.c_int, [c_vp, ctypes.POINTER(ctypes.c_int64), c_i32p]),
     "qfvm_plan_host_probe_slots": (ctypes.c_int, [c_vp, c_i32p]),
     "qfvm_plan_host_copy": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_dp]),
 }

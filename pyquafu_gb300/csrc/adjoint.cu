@@ -7,12 +7,18 @@ namespace qsv {
 
 // Whole-state two-state pass for small states: psi and lam both live in the
 // shared memory of one CTA; a probe is reduced over the CTA in a fixed order
-// and written straight to probe_out[probe].
+// and written straight to probe_out[probe].  CTA b handles item b of a batch:
+// states at offset b << n, coefficients at coef0 + b * cstride, probe values
+// at probe_out + b * pstride.
 template <class P>
-__global__ void __launch_bounds__(512) k_small2(typename P::G* __restrict__ psi_g, typename P::G* __restrict__ lam_g,
+__global__ void __launch_bounds__(512) k_small2(typename P::G* __restrict__ psi0, typename P::G* __restrict__ lam0,
                                                 int n, const KOp* __restrict__ ops, int nops,
-                                                const typename P::C* __restrict__ coef,
-                                                double* __restrict__ probe_out) {
+                                                const typename P::C* __restrict__ coef0, uint64_t cstride,
+                                                double* __restrict__ probe0, uint64_t pstride) {
+    typename P::G* psi_g = psi0 + (static_cast<uint64_t>(blockIdx.x) << n);
+    typename P::G* lam_g = lam0 + (static_cast<uint64_t>(blockIdx.x) << n);
+    const typename P::C* coef = coef0 + blockIdx.x * cstride;
+    double* probe_out = probe0 + blockIdx.x * pstride;
     constexpr int GB = P::GBITS;
     using T = typename ProbeMath<P>::T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -105,7 +111,8 @@ namespace {
 
 template <class P, int T, int R>
 cudaError_t launch_pass2_t(void* psi, void* lam, const PassDesc* dpass, const StepDesc* dsteps, const KOp* dops,
-                           const void* dcoef, int n, int H, double* partial, int* grid_out, cudaStream_t st) {
+                           const void* dcoef, int n, int H, int items, uint64_t cstride, int per_tile,
+                           double* partial, int* grid_out, cudaStream_t st) {
     constexpr int NT = 1 << (T - R);
     const size_t smem = 4 * (sizeof(typename P::S) << T) + (sizeof(uint64_t) << H) +
                         sizeof(double) * (NT / 32) * MAX_PASS_PROBES;
@@ -122,26 +129,28 @@ cudaError_t launch_pass2_t(void* psi, void* lam, const PassDesc* dpass, const St
         if (e != cudaSuccess) return e;
         grid_cap = (nsm > 0 ? nsm : 1) * (per_sm > 0 ? per_sm : 1);
     }
-    const uint64_t tiles = 1ULL << (n - T);
+    const uint64_t tiles = static_cast<uint64_t>(items) << (n - T);
     const unsigned grid = static_cast<unsigned>(tiles < static_cast<uint64_t>(grid_cap) ? tiles : grid_cap);
     *grid_out = static_cast<int>(grid);
     k_pass2<P, T, R><<<grid, NT, smem, st>>>(static_cast<typename P::G*>(psi), static_cast<typename P::G*>(lam), tiles,
-                                            dpass, dsteps, dops, static_cast<const typename P::C*>(dcoef), partial);
+                                            dpass, dsteps, dops, static_cast<const typename P::C*>(dcoef), cstride,
+                                            n - T, per_tile, partial);
     return cudaGetLastError();
 }
 
 template <class P>
-cudaError_t launch_small2_p(void* psi, void* lam, int n, const KOp* dops, int nops, const void* dcoef,
-                            double* probe_out, cudaStream_t st) {
+cudaError_t launch_small2_p(void* psi, void* lam, int n, const KOp* dops, int nops, const void* dcoef, int items,
+                            uint64_t cstride, double* probe_out, uint64_t pstride, cudaStream_t st) {
     const size_t smem = 2 * (sizeof(typename P::S) << n);
     if (smem > 48 * 1024) {
         cudaError_t e =
             cudaFuncSetAttribute(k_small2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
     }
-    k_small2<P><<<1, n >= 10 ? 512 : 256, smem, st>>>(static_cast<typename P::G*>(psi),
-                                                      static_cast<typename P::G*>(lam), n, dops, nops,
-                                                      static_cast<const typename P::C*>(dcoef), probe_out);
+    k_small2<P><<<items, n >= 10 ? 512 : 256, smem, st>>>(static_cast<typename P::G*>(psi),
+                                                          static_cast<typename P::G*>(lam), n, dops, nops,
+                                                          static_cast<const typename P::C*>(dcoef), cstride,
+                                                          probe_out, pstride);
     return cudaGetLastError();
 }
 
@@ -160,22 +169,27 @@ void adjoint_shape(int arith, int* T, int* R) {
 int adjoint_small_max(int arith) { return arith == QFVM_C64 ? 11 : 10; }
 
 cudaError_t launch_pass2(int arith, void* psi, void* lam, const PassDesc* dpass, const StepDesc* dsteps,
-                         const KOp* dops, const void* dcoef, int n, int H, double* partial, int* grid_out,
-                         cudaStream_t st) {
+                         const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride, int per_tile,
+                         double* partial, int* grid_out, cudaStream_t st) {
     if (arith == QFVM_C64)
-        return launch_pass2_t<P32, 12, 5>(psi, lam, dpass, dsteps, dops, dcoef, n, H, partial, grid_out, st);
+        return launch_pass2_t<P32, 12, 5>(psi, lam, dpass, dsteps, dops, dcoef, n, H, items, cstride, per_tile,
+                                          partial, grid_out, st);
     if (arith == QFVM_C128_DS)
-        return launch_pass2_t<PDS, 11, 4>(psi, lam, dpass, dsteps, dops, dcoef, n, H, partial, grid_out, st);
-    return launch_pass2_t<P64, 11, 4>(psi, lam, dpass, dsteps, dops, dcoef, n, H, partial, grid_out, st);
+        return launch_pass2_t<PDS, 11, 4>(psi, lam, dpass, dsteps, dops, dcoef, n, H, items, cstride, per_tile,
+                                          partial, grid_out, st);
+    return launch_pass2_t<P64, 11, 4>(psi, lam, dpass, dsteps, dops, dcoef, n, H, items, cstride, per_tile, partial,
+                                      grid_out, st);
 }
 
 int pass2_grid_cap() { return 152 * 4; }
 
 cudaError_t launch_small2(int arith, void* psi, void* lam, int n, const KOp* dops, int nops, const void* dcoef,
-                          double* probe_out, cudaStream_t st) {
-    if (arith == QFVM_C64) return launch_small2_p<P32>(psi, lam, n, dops, nops, dcoef, probe_out, st);
-    if (arith == QFVM_C128_DS) return launch_small2_p<PDS>(psi, lam, n, dops, nops, dcoef, probe_out, st);
-    return launch_small2_p<P64>(psi, lam, n, dops, nops, dcoef, probe_out, st);
+                          int items, uint64_t cstride, double* probe_out, uint64_t pstride, cudaStream_t st) {
+    if (arith == QFVM_C64)
+        return launch_small2_p<P32>(psi, lam, n, dops, nops, dcoef, items, cstride, probe_out, pstride, st);
+    if (arith == QFVM_C128_DS)
+        return launch_small2_p<PDS>(psi, lam, n, dops, nops, dcoef, items, cstride, probe_out, pstride, st);
+    return launch_small2_p<P64>(psi, lam, n, dops, nops, dcoef, items, cstride, probe_out, pstride, st);
 }
 
 cudaError_t launch_hamiltonian(int storage, const void* psi, void* lam, uint64_t N, const uint64_t* dx,

@@ -110,14 +110,18 @@ __device__ __forceinline__ double warp_sum(double v) {
 // ---------------------------------------------------------------------------
 // Two-state fused tile pass (persistent, double-buffered, like k_pass).
 // Gates apply to both states; probes add their warp sums into pacc[warp][p]
-// in a fixed order, and at the end every CTA writes its per-probe total to
-// partial[p * gridDim.x + blockIdx.x].
+// in a fixed order.  Single state (per_tile == 0): at the end every CTA writes
+// its per-probe total to partial[p * gridDim.x + blockIdx.x].  Batched states
+// (per_tile == 1): tile b belongs to item b >> ishift, reads that item's
+// coefficients at coef0 + item * cstride, and writes its own per-probe sums to
+// partial[p * ntiles + b], so sums never mix items.
 // ---------------------------------------------------------------------------
 template <class P, int T, int R>
 __global__ void __launch_bounds__(1 << (T - R), 1)
     k_pass2(typename P::G* __restrict__ psi_g, typename P::G* __restrict__ lam_g, uint64_t ntiles,
             const PassDesc* __restrict__ pdp, const StepDesc* __restrict__ steps, const KOp* __restrict__ ops,
-            const typename P::C* __restrict__ coef, double* __restrict__ partial) {
+            const typename P::C* __restrict__ coef0, uint64_t cstride, int ishift, int per_tile,
+            double* __restrict__ partial) {
     constexpr int NT = 1 << (T - R);
     constexpr int NW = NT / 32;
     constexpr int NA = 1 << R;
@@ -154,6 +158,7 @@ __global__ void __launch_bounds__(1 << (T - R), 1)
     for (int it = 0; b < ntiles; ++it, b += gridDim.x) {
         typename P::S* sm[2] = {buf(it & 1, 0), buf(it & 1, 1)};
         const uint64_t base = tile_base(b, L, H, tq);
+        const typename P::C* coef = coef0 + (b >> ishift) * cstride;
         const uint64_t bn = b + gridDim.x;
         if (bn < ntiles) {
             const uint64_t nb = tile_base(bn, L, H, tq);
@@ -250,7 +255,19 @@ __global__ void __launch_bounds__(1 << (T - R), 1)
             __stcs(lam_g + g, P::s2g(sm[1][swz<GB>(s)]));
         }
         __syncthreads();
+        if (per_tile) {
+            for (int p = tid; p < np; p += NT) {
+                double s = 0.0;
+                for (int w = 0; w < NW; ++w) {
+                    s += pacc[w * MAX_PASS_PROBES + p];
+                    pacc[w * MAX_PASS_PROBES + p] = 0.0;
+                }
+                partial[static_cast<size_t>(p) * ntiles + b] = s;
+            }
+            __syncthreads();
+        }
     }
+    if (per_tile) return;
     __syncthreads();
     for (int p = tid; p < np; p += NT) {
         double s = 0.0;

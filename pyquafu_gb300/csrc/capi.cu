@@ -12,34 +12,20 @@
 #include "engine.h"
 #include "kernels.h"
 #include "qfvm_gb300.h"
+#include "capi_internal.h"
 
 using namespace qsv;
 
-namespace {
+namespace qsv_capi {
 
 thread_local std::string g_err;
 std::atomic<uint64_t> g_launches{0};
-std::mutex g_boundary_mu;  // serialises the host-buffer entry points (shared cached state)
+std::mutex g_boundary_mu;
 
 int fail(int code, const std::string& msg) {
     g_err = msg;
     return code;
 }
-
-#define QSV_CUDA(call, what)                                                                        \
-    do {                                                                                           \
-        cudaError_t e_ = (call);                                                                   \
-        if (e_ != cudaSuccess) {                                                                   \
-            return fail(e_ == cudaErrorMemoryAllocation ? QFVM_ERR_NOMEM : QFVM_ERR_CUDA,           \
-                        std::string(what) + ": " + cudaGetErrorString(e_));                        \
-        }                                                                                          \
-    } while (0)
-
-#define QSV_TRY(expr)          \
-    do {                       \
-        int rc_ = (expr);      \
-        if (rc_ != QFVM_OK) return rc_; \
-    } while (0)
 
 int check_device() {
     int count = 0;
@@ -48,56 +34,12 @@ int check_device() {
     return QFVM_OK;
 }
 
-// Growable device scratch buffer.
-struct DevBuf {
-    void* p = nullptr;
-    size_t cap = 0;
-    int ensure(size_t bytes) {
-        if (bytes <= cap) return QFVM_OK;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        size_t want = std::max<size_t>(bytes, 256);
-        QSV_CUDA(cudaMalloc(&p, want), "scratch allocation");
-        cap = want;
-        return QFVM_OK;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-    template <class T>
-    T* as() {
-        return static_cast<T*>(p);
-    }
-};
+}  // namespace qsv_capi
 
-}  // namespace
+using namespace qsv_capi;
 
-struct qfvm_sv {
-    int n = 0, precision = QFVM_C128;
-    uint64_t N = 0;
-    void* d = nullptr;
-    cudaStream_t stream = nullptr;
-    DevBuf red, masks, sample_blk, sample_shots, staging;
-};
 
-struct qfvm_plan {
-    HostPlan hp;
-    std::vector<cudaEvent_t> events;  // for timed runs
-    void* dbuf = nullptr;
-    PassDesc* dpass = nullptr;
-    StepDesc* dsteps = nullptr;
-    KOp* dops = nullptr;
-    void* dcoef = nullptr;
-};
-
-namespace {
-
-int store_precision(int precision) { return precision == QFVM_C64 ? QFVM_C64 : QFVM_C128; }
-
-size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+namespace qsv_capi {
 
 int upload_plan(qfvm_plan* p) {
     const HostPlan& hp = p->hp;
@@ -197,11 +139,11 @@ int run_plan(qfvm_plan* p, qfvm_sv* sv, bool timed = false) {
         cudaError_t e = cudaSuccess;
         if (pd.type == PASS_TILE) {
             e = launch_tile_pass(hp.arith, hp.T, hp.R, sv->d, p->dpass + i, p->dsteps, p->dops, p->dcoef, hp.n, pd.H,
-                                 sv->stream);
+                                 1, 0, sv->stream);
         } else if (pd.type == PASS_SMALL) {
-            e = launch_small(hp.arith, sv->d, 0, 1, hp.n, p->dops + pd.op_begin, pd.op_count, p->dcoef, sv->stream);
+            e = launch_small(hp.arith, sv->d, 0, 1, hp.n, p->dops + pd.op_begin, pd.op_count, p->dcoef, 0, sv->stream);
         } else {
-            e = launch_globalop(hp.arith, sv->d, hp.n, p->dops + pd.op_begin, p->dcoef, sv->stream);
+            e = launch_globalop(hp.arith, sv->d, hp.n, p->dops + pd.op_begin, p->dcoef, 1, 0, sv->stream);
         }
         g_launches.fetch_add(1, std::memory_order_relaxed);
         if (e != cudaSuccess) return fail(QFVM_ERR_CUDA, std::string("pass launch: ") + cudaGetErrorString(e));
@@ -597,6 +539,44 @@ int qfvm_plan_host_build_adjoint(int32_t num_qubits, int32_t precision, const qf
     return QFVM_OK;
 }
 
+int qfvm_plan_host_build_batched(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int64_t n_ops,
+                                 const double* matpool, int64_t matpool_len, int32_t adjoint, qfvm_plan** out) {
+    if (!out) return fail(QFVM_ERR_INVALID, "null output");
+    if (num_qubits < 1 || num_qubits > QFVM_MAX_QUBITS) return fail(QFVM_ERR_INVALID, "qubit count out of range");
+    std::vector<GOp> gops, sweep;
+    std::string err;
+    if (!classify(num_qubits, ops, n_ops, matpool, matpool_len, &gops, &err)) return fail(QFVM_ERR_INVALID, err);
+    if (!unfix_bound(&gops, &err)) return fail(QFVM_ERR_UNSUPPORTED, err);
+    int T = 0, R = 0;
+    if (adjoint) {
+        if (!build_adjoint_sweep(gops, &sweep, &err)) return fail(QFVM_ERR_INVALID, err);
+        adjoint_shape(precision, &T, &R);
+    }
+    qfvm_plan* p = new qfvm_plan();
+    if (!build_plan(num_qubits, store_precision(precision), adjoint ? sweep : gops, T, R, &p->hp, &err)) {
+        delete p;
+        return fail(QFVM_ERR_INVALID, err);
+    }
+    p->hp.arith = precision;
+    *out = p;
+    return QFVM_OK;
+}
+
+int qfvm_plan_host_binds(const qfvm_plan* plan, int64_t* count, int32_t* records) {
+    if (!plan || !count) return fail(QFVM_ERR_INVALID, "null argument");
+    *count = static_cast<int64_t>(plan->hp.binds.size());
+    if (records) {
+        for (size_t i = 0; i < plan->hp.binds.size(); ++i) {
+            const Bind& b = plan->hp.binds[i];
+            records[4 * i] = static_cast<int32_t>(b.off);
+            records[4 * i + 1] = b.kind;
+            records[4 * i + 2] = b.sign;
+            records[4 * i + 3] = b.slot;
+        }
+    }
+    return QFVM_OK;
+}
+
 int qfvm_plan_host_probe_slots(const qfvm_plan* plan, int32_t* slots) {
     if (!plan || !slots) return fail(QFVM_ERR_INVALID, "null argument");
     for (size_t i = 0; i < plan->hp.probe_slot.size(); ++i) slots[i] = plan->hp.probe_slot[i];
@@ -793,19 +773,20 @@ int qfvm_adjoint(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int6
         cudaError_t ce = cudaSuccess;
         if (pd.type == PASS_TILE) {
             int grid = 0;
-            ce = launch_pass2(arith, psi->d, lam->d, rev->dpass + i, rev->dsteps, rev->dops, rev->dcoef, n, pd.H,
-                              dpart, &grid, st);
+            ce = launch_pass2(arith, psi->d, lam->d, rev->dpass + i, rev->dsteps, rev->dops, rev->dcoef, n, pd.H, 1, 0,
+                              0, dpart, &grid, st);
             g_launches.fetch_add(1, std::memory_order_relaxed);
             if (ce == cudaSuccess && pd.nprobe > 0) {
                 ce = launch_probe_reduce(dpart, grid, pd.nprobe, dvals + pd.probe_base, st);
                 g_launches.fetch_add(1, std::memory_order_relaxed);
             }
         } else if (pd.type == PASS_SMALL) {
-            ce = launch_small2(arith, psi->d, lam->d, n, rev->dops + pd.op_begin, pd.op_count, rev->dcoef, dvals, st);
+            ce = launch_small2(arith, psi->d, lam->d, n, rev->dops + pd.op_begin, pd.op_count, rev->dcoef, 1, 0,
+                               dvals, 0, st);
             g_launches.fetch_add(1, std::memory_order_relaxed);
         } else {
-            ce = launch_globalop(arith, psi->d, n, rev->dops + pd.op_begin, rev->dcoef, st);
-            if (ce == cudaSuccess) ce = launch_globalop(arith, lam->d, n, rev->dops + pd.op_begin, rev->dcoef, st);
+            ce = launch_globalop(arith, psi->d, n, rev->dops + pd.op_begin, rev->dcoef, 1, 0, st);
+            if (ce == cudaSuccess) ce = launch_globalop(arith, lam->d, n, rev->dops + pd.op_begin, rev->dcoef, 1, 0, st);
             g_launches.fetch_add(2, std::memory_order_relaxed);
         }
         if (ce != cudaSuccess) return done(fail(QFVM_ERR_CUDA, std::string("adjoint pass: ") + cudaGetErrorString(ce)));

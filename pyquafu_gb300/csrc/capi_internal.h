@@ -1,0 +1,88 @@
+// Internals of the C ABI shared by its translation units (capi.cu, batch_capi.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+#include "qfvm_gb300.h"
+
+namespace qsv_capi {
+
+extern std::atomic<uint64_t> g_launches;
+extern std::mutex g_boundary_mu;  // serialises the host-buffer entry points (shared cached state)
+
+int fail(int code, const std::string& msg);
+int check_device();
+
+#define QSV_CUDA(call, what)                                                                        \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) {                                                                   \
+            return ::qsv_capi::fail(e_ == cudaErrorMemoryAllocation ? QFVM_ERR_NOMEM : QFVM_ERR_CUDA, \
+                                    std::string(what) + ": " + cudaGetErrorString(e_));            \
+        }                                                                                          \
+    } while (0)
+
+#define QSV_TRY(expr)                   \
+    do {                                \
+        int rc_ = (expr);               \
+        if (rc_ != QFVM_OK) return rc_; \
+    } while (0)
+
+// Growable device scratch buffer.
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes) {
+        if (bytes <= cap) return QFVM_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(bytes, 256);
+        QSV_CUDA(cudaMalloc(&p, want), "scratch allocation");
+        cap = want;
+        return QFVM_OK;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <class T>
+    T* as() {
+        return static_cast<T*>(p);
+    }
+};
+
+inline int store_precision(int precision) { return precision == QFVM_C64 ? QFVM_C64 : QFVM_C128; }
+inline size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+
+}  // namespace qsv_capi
+
+struct qfvm_sv {
+    int n = 0, precision = QFVM_C128;
+    uint64_t N = 0;
+    void* d = nullptr;
+    cudaStream_t stream = nullptr;
+    qsv_capi::DevBuf red, masks, sample_blk, sample_shots, staging;
+};
+
+struct qfvm_plan {
+    qsv::HostPlan hp;
+    std::vector<cudaEvent_t> events;  // for timed runs
+    void* dbuf = nullptr;
+    qsv::PassDesc* dpass = nullptr;
+    qsv::StepDesc* dsteps = nullptr;
+    qsv::KOp* dops = nullptr;
+    void* dcoef = nullptr;
+};
+
+namespace qsv_capi {
+int make_plan_gops(int n, int precision, const std::vector<qsv::GOp>& gops, int T, int R, qfvm_plan** out);
+void free_plan(qfvm_plan* p);
+}  // namespace qsv_capi

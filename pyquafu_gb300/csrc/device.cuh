@@ -437,7 +437,10 @@ __global__ void __launch_bounds__(1 << (T - R), 1) k_pass(typename P::G* __restr
                                                         const PassDesc* __restrict__ pdp,
                                                         const StepDesc* __restrict__ steps,
                                                         const KOp* __restrict__ ops,
-                                                        const typename P::C* __restrict__ coef) {
+                                                        const typename P::C* __restrict__ coef0,
+                                                        uint64_t cstride, int ishift) {
+    // batched runs: tile b belongs to item b >> ishift, whose coefficients
+    // start at coef0 + item * cstride (cstride = 0 for a single state)
     constexpr int NT = 1 << (T - R);
     constexpr int NA = 1 << R;
     constexpr int GB = P::GBITS;
@@ -466,6 +469,7 @@ __global__ void __launch_bounds__(1 << (T - R), 1) k_pass(typename P::G* __restr
     for (int it = 0; b < ntiles; ++it, b += gridDim.x) {
         typename P::S* sm = bufs[it & 1];
         const uint64_t base = tile_base(b, L, H, tq);
+        const typename P::C* coef = coef0 + (b >> ishift) * cstride;
         const uint64_t bn = b + gridDim.x;
         if (bn < ntiles) {
             tile_prefetch<P, T, NT>(bufs[(it + 1) & 1], state, tile_base(bn, L, H, tq), choff, L);

@@ -58,7 +58,23 @@ struct GOp {
     // K_PROBE: xmask = flip bits, pmask = Z bits, cmask = projector bits,
     // special = number of Y factors, coef = {scale}
     uint64_t xmask = 0;
+    // Batched runs: a slotted RX/RY/RZ/P/CP/RZZ is re-bound per item from its
+    // slot value; bkind is the circuit op kind (QFVM_OP_*), bsign = -1 for the
+    // inverse gate of a reverse sweep (angle -theta).
+    uint8_t bkind = 0;
+    int8_t bsign = 1;
 };
+
+// One coefficient block of the pool that a batched run rewrites per item:
+// coef[off ..] = coefficients of gate kind `kind` at angle sign * value[slot].
+struct Bind {
+    uint32_t off;
+    uint8_t kind;
+    int8_t sign;
+    uint16_t pad;
+    int32_t slot;
+};
+static_assert(sizeof(Bind) == 12, "Bind layout");
 
 // ---------------------------------------------------------------------------
 // Device-side plan records (POD, uploaded once per plan)
@@ -122,6 +138,7 @@ struct HostPlan {
     std::vector<StepDesc> steps;
     std::vector<KOp> ops;
     std::vector<double> coef;  // FP64 coefficient pool
+    std::vector<Bind> binds;   // pool blocks that depend on a slot value
     PlanStats stats;
 };
 
@@ -139,6 +156,13 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
 // probe of its generator (if it carries a parameter slot) and its inverse.
 bool build_adjoint_sweep(const std::vector<GOp>& gops, std::vector<GOp>* out, std::string* err);
 GOp gop_dagger(const GOp& g);
+// Batched runs: drop the fast paths that depend on a bindable gate's value
+// (special phases, unit first diagonal entry of RZ/RZZ) so one plan serves
+// every value.  Returns false (with a message) for a slotted gate that
+// cannot be re-bound on the device.
+bool unfix_bound(std::vector<GOp>* gops, std::string* err);
+// Coefficients of a bindable gate kind at angle th (2 or 4 doubles).
+int bind_coef(int kind, double th, double* c);
 // Gate-equivalent bytes of one gop: 2 * bytes per amplitude * amplitudes it
 // must touch.
 double gop_bytes(const GOp& g, int n, int precision);

@@ -11,11 +11,12 @@ namespace qsv {
 template <class P>
 __global__ void __launch_bounds__(512) k_small(typename P::G* __restrict__ state, uint64_t stride, int n,
                                                const KOp* __restrict__ ops, int nops,
-                                               const typename P::C* __restrict__ coef) {
+                                               const typename P::C* __restrict__ coef0, uint64_t cstride) {
     constexpr int GB = P::GBITS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     typename P::S* sm = reinterpret_cast<typename P::S*>(smem_raw);
     typename P::G* st = state + stride * blockIdx.x;
+    const typename P::C* coef = coef0 + cstride * blockIdx.x;  // item blockIdx.x's coefficient pool
     const uint32_t N = 1u << n;
     for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) sm[swz<GB>(i)] = P::g2s(st[i]);
     __syncthreads();
@@ -31,8 +32,9 @@ __global__ void __launch_bounds__(512) k_small(typename P::G* __restrict__ state
 // Dense gate on k targets straight on global memory (large states; rare).
 // ---------------------------------------------------------------------------
 template <class P>
-__global__ void __launch_bounds__(256) k_globalop(typename P::G* __restrict__ state, int n,
-                                                  const KOp* __restrict__ opp, const typename P::C* __restrict__ coef) {
+__global__ void __launch_bounds__(256) k_globalop(typename P::G* __restrict__ state, int n, int items,
+                                                  const KOp* __restrict__ opp, const typename P::C* __restrict__ coef0,
+                                                  uint64_t cstride) {
     using A = typename P::A;
     using C = typename P::C;
     const KOp op = *opp;
@@ -46,12 +48,14 @@ __global__ void __launch_bounds__(256) k_globalop(typename P::G* __restrict__ st
             srt[y] = srt[y - 1];
             srt[y - 1] = t;
         }
-    const uint64_t groups = 1ULL << (n - k);
+    // batched states: the item index sits above the n gate qubits
+    const uint64_t groups = static_cast<uint64_t>(items) << (n - k);
     for (uint64_t g = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; g < groups;
          g += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
         uint64_t i = g;
         for (int j = 0; j < k; ++j) i = insert0(i, srt[j]);
         if ((i & op.cthr) != op.cthr) continue;
+        const typename P::C* coef = coef0 + (i >> n) * cstride;
         A in[1 << MAXK];
         for (uint32_t m = 0; m < dim; ++m) {
             uint64_t idx = i;
@@ -270,15 +274,15 @@ bool pass_shape_supported(int precision, int T, int R) {
 
 cudaError_t launch_tile_pass(int precision, int T, int R, void* state, const PassDesc* dpass,
                              const StepDesc* dsteps, const KOp* dops, const void* dcoef, int n, int H,
-                             cudaStream_t st) {
-    if (precision == QFVM_C64) return launch_pass_c64(T, R, state, dpass, dsteps, dops, dcoef, n, H, st);
-    if (precision == QFVM_C128_DS) return launch_pass_ds(T, R, state, dpass, dsteps, dops, dcoef, n, H, st);
-    return launch_pass_c128(T, R, state, dpass, dsteps, dops, dcoef, n, H, st);
+                             int items, uint64_t cstride, cudaStream_t st) {
+    if (precision == QFVM_C64) return launch_pass_c64(T, R, state, dpass, dsteps, dops, dcoef, n, H, items, cstride, st);
+    if (precision == QFVM_C128_DS) return launch_pass_ds(T, R, state, dpass, dsteps, dops, dcoef, n, H, items, cstride, st);
+    return launch_pass_c128(T, R, state, dpass, dsteps, dops, dcoef, n, H, items, cstride, st);
 }
 
 template <class P>
 static cudaError_t launch_small_p(void* state, uint64_t stride, int batch, int n, const KOp* dops, int nops,
-                                  const void* dcoef, cudaStream_t st) {
+                                  const void* dcoef, uint64_t cstride, cudaStream_t st) {
     const int threads = n >= 10 ? 512 : 256;
     const size_t smem = sizeof(typename P::S) << n;
     if (smem > 48 * 1024) {
@@ -287,28 +291,30 @@ static cudaError_t launch_small_p(void* state, uint64_t stride, int batch, int n
         if (e != cudaSuccess) return e;
     }
     k_small<P><<<batch, threads, smem, st>>>(static_cast<typename P::G*>(state), stride, n, dops, nops,
-                                            static_cast<const typename P::C*>(dcoef));
+                                            static_cast<const typename P::C*>(dcoef), cstride);
     return cudaGetLastError();
 }
 
 cudaError_t launch_small(int precision, void* state, uint64_t stride, int batch, int n, const KOp* dops, int nops,
-                         const void* dcoef, cudaStream_t st) {
-    if (precision == QFVM_C64) return launch_small_p<P32>(state, stride, batch, n, dops, nops, dcoef, st);
-    if (precision == QFVM_C128_DS) return launch_small_p<PDS>(state, stride, batch, n, dops, nops, dcoef, st);
-    return launch_small_p<P64>(state, stride, batch, n, dops, nops, dcoef, st);
+                         const void* dcoef, uint64_t cstride, cudaStream_t st) {
+    if (precision == QFVM_C64) return launch_small_p<P32>(state, stride, batch, n, dops, nops, dcoef, cstride, st);
+    if (precision == QFVM_C128_DS) return launch_small_p<PDS>(state, stride, batch, n, dops, nops, dcoef, cstride, st);
+    return launch_small_p<P64>(state, stride, batch, n, dops, nops, dcoef, cstride, st);
 }
 
-cudaError_t launch_globalop(int precision, void* state, int n, const KOp* dop, const void* dcoef,
-                            cudaStream_t st) {
-    const uint64_t groups = 1ULL << (n - 1);
+cudaError_t launch_globalop(int precision, void* state, int n, const KOp* dop, const void* dcoef, int items,
+                            uint64_t cstride, cudaStream_t st) {
+    const uint64_t groups = static_cast<uint64_t>(items) << (n - 1);
     const unsigned blocks = static_cast<unsigned>(groups / 256 < 152 * 16 ? (groups + 255) / 256 : 152 * 16);
     if (precision == QFVM_C64)
-        k_globalop<P32><<<blocks, 256, 0, st>>>(static_cast<float2*>(state), n, dop, static_cast<const float*>(dcoef));
+        k_globalop<P32><<<blocks, 256, 0, st>>>(static_cast<float2*>(state), n, items, dop,
+                                               static_cast<const float*>(dcoef), cstride);
     else if (precision == QFVM_C128_DS)
-        k_globalop<PDS><<<blocks, 256, 0, st>>>(static_cast<double2*>(state), n, dop, static_cast<const ds*>(dcoef));
+        k_globalop<PDS><<<blocks, 256, 0, st>>>(static_cast<double2*>(state), n, items, dop,
+                                               static_cast<const ds*>(dcoef), cstride);
     else
-        k_globalop<P64><<<blocks, 256, 0, st>>>(static_cast<double2*>(state), n, dop,
-                                               static_cast<const double*>(dcoef));
+        k_globalop<P64><<<blocks, 256, 0, st>>>(static_cast<double2*>(state), n, items, dop,
+                                               static_cast<const double*>(dcoef), cstride);
     return cudaGetLastError();
 }
 

@@ -15,19 +15,22 @@ bool pass_shape_c128(int T, int R);
 bool pass_shape_c64(int T, int R);
 bool pass_shape_ds(int T, int R);
 cudaError_t launch_pass_ds(int T, int R, void* state, const PassDesc* dpass, const StepDesc* dsteps,
-                           const KOp* dops, const void* dcoef, int n, int H, cudaStream_t st);
+                           const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride,
+                            cudaStream_t st);
 cudaError_t launch_pass_c128(int T, int R, void* state, const PassDesc* dpass, const StepDesc* dsteps,
-                             const KOp* dops, const void* dcoef, int n, int H, cudaStream_t st);
+                             const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride,
+                            cudaStream_t st);
 cudaError_t launch_pass_c64(int T, int R, void* state, const PassDesc* dpass, const StepDesc* dsteps,
-                            const KOp* dops, const void* dcoef, int n, int H, cudaStream_t st);
+                            const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride,
+                            cudaStream_t st);
 
 cudaError_t launch_tile_pass(int precision, int T, int R, void* state, const PassDesc* dpass,
                              const StepDesc* dsteps, const KOp* dops, const void* dcoef, int n, int H,
-                             cudaStream_t st);
+                             int items, uint64_t cstride, cudaStream_t st);
 cudaError_t launch_small(int precision, void* state, uint64_t stride, int batch, int n, const KOp* dops, int nops,
-                         const void* dcoef, cudaStream_t st);
-cudaError_t launch_globalop(int precision, void* state, int n, const KOp* dop, const void* dcoef,
-                            cudaStream_t st);
+                         const void* dcoef, uint64_t cstride, cudaStream_t st);
+cudaError_t launch_globalop(int precision, void* state, int n, const KOp* dop, const void* dcoef, int items,
+                            uint64_t cstride, cudaStream_t st);
 cudaError_t launch_set_basis(int precision, void* state, uint64_t N, uint64_t index, cudaStream_t st);
 cudaError_t launch_convert(bool to64, const void* in, void* out, uint64_t n, cudaStream_t st);
 cudaError_t launch_expect_z(int precision, const void* state, uint64_t N, const uint64_t* dzm, int nterms,
@@ -48,12 +51,31 @@ namespace qsv {
 void adjoint_shape(int arith, int* T, int* R);
 int adjoint_small_max(int arith);
 cudaError_t launch_pass2(int arith, void* psi, void* lam, const PassDesc* dpass, const StepDesc* dsteps,
-                         const KOp* dops, const void* dcoef, int n, int H, double* partial, int* grid_out,
-                         cudaStream_t st);
+                         const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride, int per_tile,
+                         double* partial, int* grid_out, cudaStream_t st);
 int pass2_grid_cap();
 cudaError_t launch_small2(int arith, void* psi, void* lam, int n, const KOp* dops, int nops, const void* dcoef,
-                          double* probe_out, cudaStream_t st);
+                          int items, uint64_t cstride, double* probe_out, uint64_t pstride, cudaStream_t st);
 cudaError_t launch_hamiltonian(int storage, const void* psi, void* lam, uint64_t N, const uint64_t* dx,
                                const uint64_t* dz, const int32_t* dny, const double* dc, int nterms, cudaStream_t st);
 cudaError_t launch_probe_reduce(const double* partial, int grid, int np, double* out, cudaStream_t st);
+}  // namespace qsv
+
+namespace qsv {
+// batch.cu
+cudaError_t launch_bind(int arith, void* pool, uint64_t cstride, const Bind* dbinds, int nb, const double* dvals,
+                        int nslots, int items, cudaStream_t st);
+cudaError_t launch_replicate(int arith, void* pool, uint64_t cstride, uint64_t len, int items, cudaStream_t st);
+cudaError_t launch_zero_items(int storage, void* state, int n, int items, cudaStream_t st);
+uint64_t hamiltonian_chunk(int n);
+cudaError_t launch_expect_seg(int storage, const void* psi, int n, int items, const uint64_t* dx, const uint64_t* dz,
+                              const int32_t* dny, const double* dc, const int32_t* doptr, int nobs, double* epart,
+                              double* out, cudaStream_t st);
+cudaError_t launch_lambda_seg(int storage, const void* psi, void* lam, int n, int items, const uint64_t* dx,
+                              const uint64_t* dz, const int32_t* dny, const double* dc, const int32_t* dtobs,
+                              int nterms, int nobs, const double* dw, cudaStream_t st);
+cudaError_t launch_probe_reduce_seg(const double* partial, uint64_t ntiles, int tpi, int items, int np, double* out,
+                                    int ostride, int ooff, cudaStream_t st);
+cudaError_t launch_slot_gather(const double* vals, int nprobe, int items, const int32_t* sptr, const int32_t* sidx,
+                               int nslots, double* grads, cudaStream_t st);
 }  // namespace qsv

@@ -95,6 +95,9 @@ bool classify(int n, const qfvm_op* ops, int64_t n_ops, const double* matpool, i
         GOp g;
         g.src = static_cast<int>(i);
         g.slot = o.slot;
+        if (o.slot >= 0 && (o.kind == QFVM_OP_RX || o.kind == QFVM_OP_RY || o.kind == QFVM_OP_RZ ||
+                            o.kind == QFVM_OP_P || o.kind == QFVM_OP_CP || o.kind == QFVM_OP_RZZ))
+            g.bkind = static_cast<uint8_t>(o.kind);
         const int* q = o.qubits;
         auto need = [&](int k) {
             if (nq < k) {
@@ -399,6 +402,8 @@ void gop_targets(const GOp& g, std::vector<int>* t) {
 uint32_t push_coef(HostPlan* p, const GOp& g) {
     uint32_t off = static_cast<uint32_t>(p->coef.size());
     p->coef.insert(p->coef.end(), g.coef.begin(), g.coef.end());
+    if (g.bkind != 0 && g.slot >= 0 && g.kind != K_PROBE)
+        p->binds.push_back(Bind{off, g.bkind, g.bsign, 0, g.slot});
     return off;
 }
 
@@ -716,6 +721,7 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
 
 GOp gop_dagger(const GOp& g) {
     GOp d = g;
+    d.bsign = static_cast<int8_t>(-g.bsign);
     auto conj_transpose = [&](int dim) {
         std::vector<double> c(g.coef.size());
         for (int r = 0; r < dim; ++r)
@@ -765,6 +771,53 @@ bool build_adjoint_sweep(const std::vector<GOp>& gops, std::vector<GOp>* out, st
             out->push_back(pr);
         }
         out->push_back(gop_dagger(g));
+    }
+    return true;
+}
+
+int bind_coef(int kind, double th, double* c) {
+    switch (kind) {
+        case QFVM_OP_RX:
+            c[0] = std::cos(th / 2);
+            c[1] = std::sin(th / 2);
+            return 2;
+        case QFVM_OP_RY:
+            c[0] = std::cos(th / 2);
+            c[1] = -std::sin(th / 2);
+            c[2] = std::sin(th / 2);
+            c[3] = std::cos(th / 2);
+            return 4;
+        case QFVM_OP_RZ:
+        case QFVM_OP_RZZ:
+            c[0] = std::cos(-th / 2);
+            c[1] = std::sin(-th / 2);
+            c[2] = std::cos(th / 2);
+            c[3] = std::sin(th / 2);
+            return 4;
+        case QFVM_OP_P:
+        case QFVM_OP_CP:
+            c[0] = 1.0;
+            c[1] = 0.0;
+            c[2] = std::cos(th);
+            c[3] = std::sin(th);
+            return 4;
+        default: return 0;
+    }
+}
+
+bool unfix_bound(std::vector<GOp>* gops, std::string* err) {
+    for (GOp& g : *gops) {
+        if (g.slot < 0) continue;
+        if (g.bkind == 0) {
+            *err = "op " + std::to_string(g.src) +
+                   ": only rx/ry/rz/p/cp/rzz gates can carry a per-item parameter in a batched run";
+            return false;
+        }
+        if (g.kind == K_DIAG) {
+            g.flags &= static_cast<uint8_t>(~F_D1_SPEC);
+            g.special = 0;
+            if (g.bkind == QFVM_OP_RZ || g.bkind == QFVM_OP_RZZ) g.flags &= static_cast<uint8_t>(~F_D0_ONE);
+        }
     }
     return true;
 }

@@ -47,13 +47,17 @@ PASS_TILE, PASS_SMALL, PASS_GLOBALOP = 0, 1, 2
 STEP_ROUND, STEP_SMEM = 0, 1
 
 
-def host_plan(n, ops, precision=0, T=0, R=0, adjoint=False):
+def host_plan(n, ops, precision=0, T=0, R=0, adjoint=False, batched=False):
     from pyquafu_gb300 import _native as nat
 
     lib = nat.load()
     arr, pool = ir.pack(ops)
     h = ctypes.c_void_p()
-    if adjoint:
+    if batched:
+        nat.check(lib.qfvm_plan_host_build_batched(n, precision, nat.vptr(arr), arr.size,
+                                                   nat.dptr(pool.view(np.float64)), pool.size, int(adjoint),
+                                                   ctypes.byref(h)), "host batched plan")
+    elif adjoint:
         nat.check(lib.qfvm_plan_host_build_adjoint(n, precision, nat.vptr(arr), arr.size,
                                                    nat.dptr(pool.view(np.float64)), pool.size, ctypes.byref(h)),
                   "host adjoint plan")
@@ -72,9 +76,13 @@ def host_plan(n, ops, precision=0, T=0, R=0, adjoint=False):
     slots = np.zeros(max(nprobe, 1), dtype=np.int32)
     if nprobe:
         nat.check(lib.qfvm_plan_host_probe_slots(h, nat.i32ptr(slots)))
+    nb = ctypes.c_int64()
+    nat.check(lib.qfvm_plan_host_binds(h, ctypes.byref(nb), None))
+    binds = np.zeros((max(nb.value, 1), 4), dtype=np.int32)
+    nat.check(lib.qfvm_plan_host_binds(h, ctypes.byref(nb), nat.i32ptr(binds)))
     lib.qfvm_plan_destroy(h)
     return {"passes": passes, "steps": steps[: counts[1]], "ops": kops[: counts[2]], "coef": coef,
-            "T": shape[0], "R": shape[1], "L": shape[2], "probe_slots": slots[:nprobe]}
+            "T": shape[0], "R": shape[1], "L": shape[2], "probe_slots": slots[:nprobe], "binds": binds[: nb.value]}
 
 
 def _bits(mask):
