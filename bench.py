@@ -325,6 +325,196 @@ def measure_adjoint(n=24, layers=20, ps_params=6):
     return out
 
 
+def measure_uneven_batch(reps=5, check_items=8, cpu=True, cpu_seconds=8.0, tune=True):
+    """2048 circuits of 10..18 qubits (ry encoding + 6 HEA layers), complex64
+    with FP64 reductions: per-circuit <Z_0> and full gradient in one CUDA-graph
+    launch.  Device time of the graph launch (uploads and downloads
+    included), wall time through BatchSession.run, algorithmic bytes, and the
+    complex64 error against the complex128 batched path on a subset."""
+    from pyquafu_gb300 import batch as bmod
+    from pyquafu_gb300 import workloads
+
+    groups = workloads.uneven_batch()
+    keys = sorted(groups)
+    values = [groups[n][1] for n in keys]
+    obs = [(1.0, "Z", [0])]
+    tuned = {}
+    if tune:
+        from pyquafu_gb300 import autotune
+
+        t0 = time.perf_counter()
+        for n in keys:
+            r = autotune.tune_batch_group(n, groups[n][0], groups[n][1], obs, "c64", reps=2)
+            tuned[n] = [list(r["forward"]), list(r["reverse"])]
+        tuned["seconds"] = round(time.perf_counter() - t0, 1)
+    bs = bmod.BatchSession("c64", grads=True)
+    nbytes = 0.0
+    for n in keys:
+        ops, vals = groups[n]
+        bs.add_group(n, ops, obs, vals.shape[0], vals.shape[1])
+        fp, rp = bmod.group_passes(n, ops, "c64")
+        nbytes += bmod.algorithmic_bytes(n, vals.shape[0], fp, rp, 8)
+    for _ in range(3):  # direct, capture + replay, replay
+        bs.run(values, grads=True)
+    dev = []
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        exps, grads, ms = bs.run(values, grads=True, timed=True)
+        dev.append(ms)
+    wall = (time.perf_counter() - t0) / reps
+    info = bs.info()
+    bs.close()
+    ncirc = sum(v.shape[0] for v in values)
+    ngrad = sum(v.size for v in values)
+    dev_s = float(np.median(dev)) * 1e-3
+    # complex64 error against the complex128 batched path (first items of every group)
+    ref = bmod.BatchSession("c128", grads=True)
+    sub = [v[:check_items] for v in values]
+    for n, v in zip(keys, sub):
+        ref.add_group(n, groups[n][0], obs, v.shape[0], v.shape[1])
+    re_, rg_ = ref.run(sub, grads=True)
+    ref.close()
+    err_e = max(float(np.abs(e[:check_items] - r).max()) for e, r in zip(exps, re_))
+    err_g = max(float(np.abs(g[:check_items] - r).max()) for g, r in zip(grads, rg_))
+    out = {"workload": "uneven_batch_2048_circuits_10to18q_ry_encoding_6hea_layers_c64",
+           "circuits": ncirc, "gradient_entries": ngrad, "groups": len(keys),
+           "graph_launches_per_run": 1, "kernels_per_graph": int(info["kernels_per_run"][1]),
+           "device_ms_per_run": round(dev_s * 1e3, 3), "wall_ms_per_run": round(wall * 1e3, 3),
+           "circuits_per_s": round(ncirc / dev_s, 1), "grads_per_s": round(ngrad / dev_s, 1),
+           "e2e_circuits_per_s": round(ncirc / wall, 1),
+           "algorithmic_gb": round(nbytes / 1e9, 3), "achieved_gbps": round(nbytes / dev_s / 1e9, 1),
+           "max_abs_err_vs_c128": {"expval": err_e, "grad": err_g, "items_checked": check_items * len(keys)},
+           "autotuned_shapes": tuned}
+    if cpu:
+        out["cpu_baseline"] = cpu_batch_sample(groups, obs, cpu_seconds)
+    return out
+
+
+def cpu_batch_sample(groups, obs, seconds):
+    """Reference algorithm on the host: the oracle port of grad_adjoint
+    (gradiant.py:144-173) over the circuits of the smallest groups, until
+    `seconds` have passed; circuits/s extrapolated by state size."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    from pyquafu_gb300 import gradients
+
+    oracle.build()
+    done, cost_done, t0 = 0, 0.0, time.perf_counter()
+    total_cost = sum(v.shape[0] * (2 ** n) for n, (_, v) in groups.items())
+    for n in sorted(groups):
+        ops, vals = groups[n]
+        for v in vals:
+            bound = gradients.bind(ops, v)
+            oracle.grad_adjoint(n, bound, [o.slot for o in bound], obs)
+            done += 1
+            cost_done += 2 ** n
+            if time.perf_counter() - t0 > seconds:
+                break
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    rate = done / dt
+    return {"value": round(rate * cost_done / done * sum(v.shape[0] for _, v in groups.values()) / total_cost, 2),
+            "unit": "circuits/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{done} circuits (smallest qubit counts first) in {dt:.1f} s through the oracle's "
+                      f"adjoint; rate scaled to the batch's size mix by 2^n"}
+
+
+def measure_qnn(steps=5, warmup=3, ps_forwards=20, tune=True):
+    """QNN training step: 1024 samples x 16 qubits, 12 HEA layers (384 shared
+    weights), MSE of <Z_0> against sign(w . x) labels; forward and adjoint
+    backward through the torch binding (complex64, FP64 reductions), SGD
+    update.  Compared with parameter shift on the plain GPU path:
+    B * (1 + 2 * 384) single-circuit forward runs, timed on `ps_forwards`."""
+    import torch
+
+    from pyquafu_gb300 import batch as bmod
+    from pyquafu_gb300 import gradients, workloads
+    from pyquafu_gb300.engine import DeviceState
+    from pyquafu_gb300.interface import QuantumLayer
+
+    n, layers, B = 16, 12, 1024
+    ops, w0, x, y = workloads.qnn_batch(batch=B, n=n, layers=layers)
+    nw = 2 * n * layers
+    tuned = None
+    if tune:
+        from pyquafu_gb300 import autotune
+
+        v0 = np.concatenate([np.broadcast_to(w0, (B, nw)), x], axis=1)
+        r = autotune.tune_batch_group(n, ops, v0, [(1.0, "Z", [0])], "c64", reps=2)
+        tuned = {"forward": list(r["forward"]), "reverse": list(r["reverse"]), "forward_ms": r["forward_ms"],
+                 "run_ms": r["run_ms"], "seconds": r["tuning_s"]}
+    layer = QuantumLayer(n, ops, [(1.0, "Z", [0])], np.arange(nw), nw + np.arange(n), init=w0, precision="c64")
+    opt = torch.optim.SGD(layer.parameters(), lr=0.05)
+    xt, yt = torch.tensor(x), torch.tensor(y)
+
+    def step():
+        opt.zero_grad()
+        out = layer(xt)
+        loss = torch.mean((out[:, 0] - yt) ** 2)
+        loss.backward()
+        opt.step()
+        return float(loss.detach())
+
+    for _ in range(warmup):
+        step()
+    t0 = time.perf_counter()
+    losses = [step() for _ in range(steps)]
+    dt = (time.perf_counter() - t0) / steps
+    # device time of one forward + adjoint run of the batch
+    runner = layer.runner(B)
+    vals = np.concatenate([np.broadcast_to(layer.weight.detach().numpy(), (B, nw)), x], axis=1)
+    dev = []
+    for _ in range(3):
+        dev.append(runner.session.run([vals], grads=True, timed=True)[2])
+    dev_s = float(np.median(dev)) * 1e-3
+    fp, rp = bmod.group_passes(n, ops, "c64")
+    nbytes = bmod.algorithmic_bytes(n, B, fp, rp, 8)
+    # parameter shift on the plain path: one forward per evaluation
+    st = DeviceState(n, "c64")
+    terms = [(1.0, "Z", [0])]
+    bound = gradients.bind(ops, vals[0])
+    gradients.energy(n, bound, terms, "c64", st)
+    t1 = time.perf_counter()
+    for _ in range(ps_forwards):
+        gradients.energy(n, bound, terms, "c64", st)
+    fwd_s = (time.perf_counter() - t1) / ps_forwards
+    st.close()
+    ps_step = B * (1 + 2 * nw) * fwd_s
+    return {"workload": "qnn_1024x16q_12hea_layers_384_weights_mse_z0_c64",
+            "s_per_step": round(dt, 5), "steps_per_s": round(1 / dt, 2),
+            "device_ms_forward_adjoint": round(dev_s * 1e3, 3),
+            "algorithmic_gb": round(nbytes / 1e9, 3), "achieved_gbps": round(nbytes / dev_s / 1e9, 1),
+            "passes": {"forward": fp, "reverse": rp}, "loss_first_last": [losses[0], losses[-1]],
+            "param_shift_plain_path": {"s_per_forward": round(fwd_s, 6), "forwards_per_step": B * (1 + 2 * nw),
+                                       "s_per_step_extrapolated": round(ps_step, 1)},
+            "speedup_vs_param_shift": round(ps_step / dt, 1), "autotuned": tuned}
+
+
+def autotune_all(args, n, ops):
+    """Pick the fused-pass shapes for every workload of this run with the
+    project autotuner (pyquafu_gb300.autotune); tuning time is reported and
+    is outside every timed region."""
+    from pyquafu_gb300 import autotune, workloads
+
+    t0 = time.perf_counter()
+    out = {}
+    proxy = min(n, 26)
+    pops = workload(proxy)
+    for prec in [args.precision] + [v for v in args.variants.split(",") if v and v != args.precision]:
+        r = autotune.tune_plan(proxy, pops, prec, reps=2, apply_to=[n])
+        out[f"plan_{prec}"] = {"tuned_on_qubits": proxy, "shape": r["shape"], "times_ms": r["times_ms"]}
+    if not args.skip_adjoint:
+        aops, _ = workloads.hea(args.adjoint_qubits, 20, seed=0)
+        terms = workloads.zz_x_hamiltonian(args.adjoint_qubits, seed=0)
+        for prec in ("c128", "c128_ds", "c64"):
+            r = autotune.tune_adjoint(args.adjoint_qubits, aops, terms, prec, reps=1)
+            out[f"adjoint_{prec}"] = {"shape": r["shape"], "times_ms": r["times_ms"]}
+    out["seconds"] = round(time.perf_counter() - t0, 1)
+    return out
+
+
 def run_gpu(args):
     import torch
 
@@ -353,6 +543,7 @@ def run_gpu(args):
 
             dist.barrier()
 
+    tuning = None if args.no_autotune else autotune_all(args, n, ops)
     barrier()
     clocks = ClockSampler()
     clocks.start()
@@ -405,6 +596,11 @@ def run_gpu(args):
     adj = None
     if not args.skip_adjoint:
         adj = measure_adjoint(args.adjoint_qubits)
+    batched = None
+    if not args.skip_batch:
+        batched = {"uneven_2048": measure_uneven_batch(cpu=rank == 0 and not args.skip_cpu,
+                                                       tune=not args.no_autotune),
+                   "qnn_training_step": measure_qnn(tune=not args.no_autotune)}
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -433,6 +629,8 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "variants": variants,
             "adjoint": adj,
+            "batched": batched,
+            "autotune": tuning,
             "clocks": clk,
             "gpu_launches": int(main["launches"]),
         }
@@ -460,6 +658,8 @@ def main():
     ap.add_argument("--skip-variants", action="store_true")
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--adjoint-qubits", type=int, default=24)
+    ap.add_argument("--skip-batch", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     args = ap.parse_args()
     if args.skip_variants:

@@ -227,8 +227,20 @@ int qfvm_plan_run_timed(qfvm_plan* plan, qfvm_sv* sv, float* pass_ms, int32_t* p
 typedef struct qfvm_batch qfvm_batch;
 #define QFVM_BATCH_GRADS 1    /* prepare gradient (mode 1) runs */
 #define QFVM_BATCH_NO_GRAPH 2 /* always issue runs directly (no CUDA graph) */
-/* tile_qubits / reg_qubits: fused-pass shape of the forward passes (0: default). */
-int qfvm_batch_create(int32_t precision, int32_t flags, int32_t tile_qubits, int32_t reg_qubits, qfvm_batch** out);
+/* shapes: NULL (defaults) or {tile qubits, register qubits} of the forward
+ * passes then of the reverse-sweep passes, 0 for a default entry; an
+ * uncompiled shape is QFVM_ERR_INVALID (qfvm_shape_supported lists them). */
+int qfvm_batch_create(int32_t precision, int32_t flags, const int32_t* shapes, qfvm_batch** out);
+/* Whether a fused-pass shape is compiled in: kind 0 = one-state passes
+ * (qfvm_plan_create, batch forward), 1 = two-state reverse-sweep passes. */
+int32_t qfvm_shape_supported(int32_t precision, int32_t kind, int32_t tile_qubits, int32_t reg_qubits);
+/* Process-wide shape for plans of `num_qubits` qubits that do not name one
+ * (every entry point above and batch groups without explicit shapes), set by
+ * the autotuner (pyquafu_gb300.autotune); tile_qubits 0 restores the
+ * built-in default. */
+int qfvm_set_tuned_shape(int32_t precision, int32_t kind, int32_t num_qubits, int32_t tile_qubits,
+                         int32_t reg_qubits);
+int qfvm_get_shape(int32_t precision, int32_t kind, int32_t num_qubits, int32_t* tile_qubits, int32_t* reg_qubits);
 int qfvm_batch_add_group(qfvm_batch* batch, int32_t num_qubits, const qfvm_op* ops, int64_t n_ops,
                          const double* matpool, int64_t matpool_len, const uint64_t* x_masks, const uint64_t* z_masks,
                          const int32_t* y_counts, const double* coeffs, const int32_t* obs_index, int64_t n_terms,

@@ -74,8 +74,11 @@ PROTOTYPES = {
                                        ctypes.POINTER(ctypes.c_int64), c_dp, c_dp]),
     "qfvm_plan_run": (ctypes.c_int, [c_vp, c_vp]),
     "qfvm_plan_run_timed": (ctypes.c_int, [c_vp, c_vp, ctypes.POINTER(ctypes.c_float), c_i32p]),
-    "qfvm_batch_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
-                                         ctypes.POINTER(c_vp)]),
+    "qfvm_batch_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, c_i32p, ctypes.POINTER(c_vp)]),
+    "qfvm_shape_supported": (ctypes.c_int32, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "qfvm_set_tuned_shape": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                            ctypes.c_int32]),
+    "qfvm_get_shape": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, c_i32p, c_i32p]),
     "qfvm_batch_add_group": (ctypes.c_int, [c_vp, ctypes.c_int32, c_vp, ctypes.c_int64, c_dp, ctypes.c_int64,
                                             c_u64p, c_u64p, c_i32p, c_dp, c_i32p, ctypes.c_int64, ctypes.c_int64,
                                             ctypes.c_int64, ctypes.c_int64]),

@@ -43,15 +43,19 @@ class BatchSession:
     """Owns a ``qfvm_batch``: groups of same-structure circuits evaluated in
     one device run.  ``grads=True`` prepares adjoint-gradient runs."""
 
-    def __init__(self, precision="c64", grads: bool = True, graph: bool = True, tile=None):
+    def __init__(self, precision="c64", grads: bool = True, graph: bool = True, tile=None, adjoint_tile=None):
+        """``tile`` / ``adjoint_tile``: (tile qubits, register qubits) of the
+        forward / reverse-sweep passes (None: the engine's defaults)."""
         lib = nat.load()
         self._lib = lib
         self.precision = precision
         self.grads = bool(grads)
         flags = (GRADS if grads else 0) | (0 if graph else NO_GRAPH)
         t, r = tile if tile else (0, 0)
+        at, ar = adjoint_tile if adjoint_tile else (0, 0)
+        shapes = np.array([t, r, at, ar], dtype=np.int32)
         h = ctypes.c_void_p()
-        nat.check(lib.qfvm_batch_create(_precision(precision), flags, int(t), int(r), ctypes.byref(h)),
+        nat.check(lib.qfvm_batch_create(_precision(precision), flags, nat.i32ptr(shapes), ctypes.byref(h)),
                   "batch create")
         self._h = h
         self.groups = []  # (n, items, slots, nobs)
@@ -165,3 +169,36 @@ class BatchSession:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def group_passes(n: int, ops, precision="c64") -> tuple[int, int]:
+    """(forward passes, reverse-sweep passes) of the plans a group runs
+    (host planning only)."""
+    lib = nat.load()
+    gates = [o for o in ops if o.is_gate]
+    arr, pool = ir.pack(gates)
+    out = []
+    for adjoint in (0, 1):
+        h = ctypes.c_void_p()
+        nat.check(lib.qfvm_plan_host_build_batched(int(n), _precision(precision), nat.vptr(arr), arr.size,
+                                                   nat.dptr(pool.view(np.float64)), pool.size, adjoint,
+                                                   ctypes.byref(h)), "host batched plan")
+        counts = (ctypes.c_int64 * 4)()
+        shape = (ctypes.c_int32 * 3)()
+        nat.check(lib.qfvm_plan_host_counts(h, counts, shape))
+        lib.qfvm_plan_destroy(h)
+        out.append(int(counts[0]))
+    return out[0], out[1]
+
+
+def algorithmic_bytes(n: int, items: int, fwd_passes: int, rev_passes: int, amp_bytes: int = 8,
+                      grads: bool = True) -> float:
+    """HBM bytes a run of one group must move at least: zero-fill (write),
+    forward passes (read + write), the expectation (read); with gradients
+    lam = H psi (read + write) and reverse passes over psi and lam (2 x read +
+    write)."""
+    sn = float(amp_bytes) * items * (1 << n)
+    b = sn + 2 * sn * fwd_passes + sn
+    if grads:
+        b += 2 * sn + 4 * sn * rev_passes
+    return b

@@ -116,8 +116,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 // coefficients at coef0 + item * cstride, and writes its own per-probe sums to
 // partial[p * ntiles + b], so sums never mix items.
 // ---------------------------------------------------------------------------
-template <class P, int T, int R>
-__global__ void __launch_bounds__(1 << (T - R), 1)
+template <class P, int T, int R, int NB, int MINB>
+__global__ void __launch_bounds__(1 << (T - R), MINB)
     k_pass2(typename P::G* __restrict__ psi_g, typename P::G* __restrict__ lam_g, uint64_t ntiles,
             const PassDesc* __restrict__ pdp, const StepDesc* __restrict__ steps, const KOp* __restrict__ ops,
             const typename P::C* __restrict__ coef0, uint64_t cstride, int ishift, int per_tile,
@@ -129,8 +129,8 @@ __global__ void __launch_bounds__(1 << (T - R), 1)
     constexpr int PER = (1 << T) / NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     typename P::S* base_s = reinterpret_cast<typename P::S*>(smem_raw);
-    // buffers: [slot][state]
-    uint64_t* choff = reinterpret_cast<uint64_t*>(smem_raw + 4 * (sizeof(typename P::S) << T));
+    // buffers: [slot][state], NB slots
+    uint64_t* choff = reinterpret_cast<uint64_t*>(smem_raw + 2 * NB * (sizeof(typename P::S) << T));
     double* pacc = reinterpret_cast<double*>(choff + (1 << pdp->H));
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -147,26 +147,32 @@ __global__ void __launch_bounds__(1 << (T - R), 1)
     __syncthreads();
     const uint32_t lmask = (1u << L) - 1;
     const int nsteps = pdp->step_count;
-    auto buf = [&](int slot, int st) { return base_s + (2 * slot + st) * (1 << T); };
+    auto buf = [&](int slot, int st) { return base_s + (2 * (slot & (NB - 1)) + st) * (1 << T); };
 
     uint64_t b = blockIdx.x;
-    if (b < ntiles) {
+    if (NB == 2 && b < ntiles) {
         const uint64_t bb = tile_base(b, L, H, tq);
         tile_prefetch<P, T, NT>(buf(0, 0), psi_g, bb, choff, L);
         tile_prefetch<P, T, NT>(buf(0, 1), lam_g, bb, choff, L);
     }
     for (int it = 0; b < ntiles; ++it, b += gridDim.x) {
-        typename P::S* sm[2] = {buf(it & 1, 0), buf(it & 1, 1)};
+        typename P::S* sm[2] = {buf(it, 0), buf(it, 1)};
         const uint64_t base = tile_base(b, L, H, tq);
         const typename P::C* coef = coef0 + (b >> ishift) * cstride;
-        const uint64_t bn = b + gridDim.x;
-        if (bn < ntiles) {
-            const uint64_t nb = tile_base(bn, L, H, tq);
-            tile_prefetch<P, T, NT>(buf((it + 1) & 1, 0), psi_g, nb, choff, L);
-            tile_prefetch<P, T, NT>(buf((it + 1) & 1, 1), lam_g, nb, choff, L);
-            cp_async_wait<2>();
-        } else {
+        if constexpr (NB == 1) {
+            tile_prefetch<P, T, NT>(sm[0], psi_g, base, choff, L);
+            tile_prefetch<P, T, NT>(sm[1], lam_g, base, choff, L);
             cp_async_wait<0>();
+        } else {
+            const uint64_t bn = b + gridDim.x;
+            if (bn < ntiles) {
+                const uint64_t nb = tile_base(bn, L, H, tq);
+                tile_prefetch<P, T, NT>(buf(it + 1, 0), psi_g, nb, choff, L);
+                tile_prefetch<P, T, NT>(buf(it + 1, 1), lam_g, nb, choff, L);
+                cp_async_wait<2>();
+            } else {
+                cp_async_wait<0>();
+            }
         }
         __syncthreads();
         if constexpr (P::RAW_STAGING) {

@@ -69,7 +69,7 @@ size_t coef_elem_bytes(int arith) { return arith == QFVM_C64 ? 4 : 8; }
 }  // namespace
 
 struct qfvm_batch {
-    int precision = QFVM_C64, flags = 0, T = 0, R = 0;
+    int precision = QFVM_C64, flags = 0, T = 0, R = 0, aT = 0, aR = 0;
     std::vector<BatchGroup*> groups;
     int64_t nvals = 0, nweight = 0, nexp = 0, ngrad = 0;
     cudaStream_t main = nullptr;
@@ -170,8 +170,8 @@ int add_group(qfvm_batch* b, int n, const qfvm_op* ops, int64_t n_ops, const dou
     int rc = make_plan_gops(n, arith, gops, b->T, b->R, &g->fwd);
     if (rc != QFVM_OK) return bail(rc);
     if (grads) {
-        int aT = 0, aR = 0;
-        adjoint_shape(arith, &aT, &aR);
+        int aT = b->aT, aR = b->aR;
+        if (aT == 0) resolve_shape(arith, 1, n, &aT, &aR);
         rc = make_plan_gops(n, arith, sweep, aT, aR, &g->rev);
         if (rc != QFVM_OK) return bail(rc);
         g->nprobe = static_cast<int>(g->rev->hp.probe_slot.size());
@@ -342,7 +342,7 @@ int enqueue_group(qfvm_batch* b, BatchGroup* g, int mode, uint64_t* nk) {
         const PassDesc& pd = rp.passes[i];
         if (pd.type == PASS_TILE) {
             int grid = 0;
-            QSV_LAUNCH(launch_pass2(arith, g->psi.p, g->lam.p, g->rev->dpass + i, g->rev->dsteps, g->rev->dops,
+            QSV_LAUNCH(launch_pass2(arith, rp.T, rp.R, g->psi.p, g->lam.p, g->rev->dpass + i, g->rev->dsteps, g->rev->dops,
                                     g->rpool.p, n, pd.H, items, g->rstride, 1, g->partial, &grid, st),
                        "batched adjoint pass");
             if (pd.nprobe > 0) {
@@ -478,24 +478,39 @@ void free_batch(qfvm_batch* b) {
 
 extern "C" {
 
-int qfvm_batch_create(int32_t precision, int32_t flags, int32_t tile_qubits, int32_t reg_qubits, qfvm_batch** out) {
+int qfvm_batch_create(int32_t precision, int32_t flags, const int32_t* shapes, qfvm_batch** out) {
     if (!out) return fail(QFVM_ERR_INVALID, "null output handle");
     *out = nullptr;
     if (precision != QFVM_C128 && precision != QFVM_C64 && precision != QFVM_C128_DS)
         return fail(QFVM_ERR_INVALID, "unknown precision");
     if (flags & ~(QFVM_BATCH_GRADS | QFVM_BATCH_NO_GRAPH)) return fail(QFVM_ERR_INVALID, "unknown batch flags");
-    if (tile_qubits > 0 || reg_qubits > 0) {
+    int sh[4] = {0, 0, 0, 0};
+    if (shapes)
+        for (int k = 0; k < 4; ++k) sh[k] = shapes[k];
+    if (sh[0] > 0 || sh[1] > 0) {
         int dT = 0, dR = 0;
         default_shape(20, store_precision(precision), &dT, &dR);
-        if (!pass_shape_supported(precision, tile_qubits > 0 ? tile_qubits : dT, reg_qubits > 0 ? reg_qubits : dR))
-            return fail(QFVM_ERR_INVALID, "tile shape not compiled in");
+        if (sh[0] <= 0) sh[0] = dT;
+        if (sh[1] <= 0) sh[1] = dR;
+        if (!pass_shape_supported(precision, sh[0], sh[1]))
+            return fail(QFVM_ERR_INVALID, "forward tile shape not compiled in");
+    }
+    if (sh[2] > 0 || sh[3] > 0) {
+        int dT = 0, dR = 0;
+        adjoint_shape(precision, &dT, &dR);
+        if (sh[2] <= 0) sh[2] = dT;
+        if (sh[3] <= 0) sh[3] = dR;
+        if (!pass2_shape_supported(precision, sh[2], sh[3]))
+            return fail(QFVM_ERR_INVALID, "reverse-sweep tile shape not compiled in");
     }
     QSV_TRY(check_device());
     qfvm_batch* b = new qfvm_batch();
     b->precision = precision;
     b->flags = flags;
-    b->T = tile_qubits;
-    b->R = reg_qubits;
+    b->T = sh[0];
+    b->R = sh[1];
+    b->aT = sh[2];
+    b->aR = sh[3];
     if (cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreate(&b->t0) != cudaSuccess || cudaEventCreate(&b->t1) != cudaSuccess) {
@@ -539,6 +554,31 @@ int qfvm_batch_info(const qfvm_batch* batch, int64_t* n_groups, int64_t* n_value
         if (graph_ready) graph_ready[m] = batch->exec[m] ? 1 : 0;
     }
     return QFVM_OK;
+}
+
+int qfvm_set_tuned_shape(int32_t precision, int32_t kind, int32_t num_qubits, int32_t tile_qubits,
+                         int32_t reg_qubits) {
+    if (precision != QFVM_C128 && precision != QFVM_C64 && precision != QFVM_C128_DS)
+        return fail(QFVM_ERR_INVALID, "unknown precision");
+    if (!set_tuned_shape(precision, kind, num_qubits, tile_qubits, reg_qubits))
+        return fail(QFVM_ERR_INVALID, "shape not compiled in, or bad kind / qubit count");
+    return QFVM_OK;
+}
+
+int qfvm_get_shape(int32_t precision, int32_t kind, int32_t num_qubits, int32_t* tile_qubits, int32_t* reg_qubits) {
+    if (!tile_qubits || !reg_qubits) return fail(QFVM_ERR_INVALID, "null argument");
+    int T = 0, R = 0;
+    resolve_shape(precision, kind, num_qubits, &T, &R);
+    *tile_qubits = T;
+    *reg_qubits = R;
+    return QFVM_OK;
+}
+
+int32_t qfvm_shape_supported(int32_t precision, int32_t kind, int32_t tile_qubits, int32_t reg_qubits) {
+    if (precision != QFVM_C128 && precision != QFVM_C64 && precision != QFVM_C128_DS) return 0;
+    if (kind == 0) return pass_shape_supported(precision, tile_qubits, reg_qubits) ? 1 : 0;
+    if (kind == 1) return pass2_shape_supported(precision, tile_qubits, reg_qubits) ? 1 : 0;
+    return 0;
 }
 
 int qfvm_batch_destroy(qfvm_batch* batch) {

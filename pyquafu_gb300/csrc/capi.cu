@@ -102,6 +102,7 @@ int make_plan(int n, int precision, const qfvm_op* ops, int64_t n_ops, const dou
 int make_plan_gops(int n, int precision, const std::vector<GOp>& gops, int T, int R, qfvm_plan** out) {
     std::string err;
     const int sp = store_precision(precision);
+    if (T <= 0 && R <= 0) resolve_shape(precision, 0, n, &T, &R);
     qfvm_plan* p = new qfvm_plan();
     if (!build_plan(n, sp, gops, T, R, &p->hp, &err)) {
         delete p;
@@ -509,6 +510,8 @@ int qfvm_plan_host_build(int32_t num_qubits, int32_t precision, const qfvm_op* o
         const int tt = tile_qubits > 0 ? tile_qubits : dT, rr = reg_qubits > 0 ? reg_qubits : dR;
         if (!pass_shape_supported(store_precision(precision), tt, rr))
             return fail(QFVM_ERR_INVALID, "tile shape not compiled in");
+    } else {
+        resolve_shape(precision, 0, num_qubits, &tile_qubits, &reg_qubits);
     }
     qfvm_plan* p = new qfvm_plan();
     if (!build_plan(num_qubits, store_precision(precision), gops, tile_qubits, reg_qubits, &p->hp, &err)) {
@@ -528,7 +531,7 @@ int qfvm_plan_host_build_adjoint(int32_t num_qubits, int32_t precision, const qf
     if (!classify(num_qubits, ops, n_ops, matpool, matpool_len, &gops, &err)) return fail(QFVM_ERR_INVALID, err);
     if (!build_adjoint_sweep(gops, &sweep, &err)) return fail(QFVM_ERR_INVALID, err);
     int aT = 0, aR = 0;
-    adjoint_shape(precision, &aT, &aR);
+    resolve_shape(precision, 1, num_qubits, &aT, &aR);
     qfvm_plan* p = new qfvm_plan();
     if (!build_plan(num_qubits, store_precision(precision), sweep, aT, aR, &p->hp, &err)) {
         delete p;
@@ -550,7 +553,7 @@ int qfvm_plan_host_build_batched(int32_t num_qubits, int32_t precision, const qf
     int T = 0, R = 0;
     if (adjoint) {
         if (!build_adjoint_sweep(gops, &sweep, &err)) return fail(QFVM_ERR_INVALID, err);
-        adjoint_shape(precision, &T, &R);
+        resolve_shape(precision, 1, num_qubits, &T, &R);
     }
     qfvm_plan* p = new qfvm_plan();
     if (!build_plan(num_qubits, store_precision(precision), adjoint ? sweep : gops, T, R, &p->hp, &err)) {
@@ -687,7 +690,7 @@ int qfvm_adjoint(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int6
     qfvm_plan* fwd = nullptr;
     QSV_TRY(make_plan_gops(n, precision, gops, 0, 0, &fwd));
     int aT = 0, aR = 0;
-    adjoint_shape(arith, &aT, &aR);
+    resolve_shape(arith, 1, n, &aT, &aR);
     qfvm_plan* rev = nullptr;
     int rc = make_plan_gops(n, precision, sweep, aT, aR, &rev);
     if (rc != QFVM_OK) {
@@ -773,7 +776,7 @@ int qfvm_adjoint(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int6
         cudaError_t ce = cudaSuccess;
         if (pd.type == PASS_TILE) {
             int grid = 0;
-            ce = launch_pass2(arith, psi->d, lam->d, rev->dpass + i, rev->dsteps, rev->dops, rev->dcoef, n, pd.H, 1, 0,
+            ce = launch_pass2(arith, hp.T, hp.R, psi->d, lam->d, rev->dpass + i, rev->dsteps, rev->dops, rev->dcoef, n, pd.H, 1, 0,
                               0, dpart, &grid, st);
             g_launches.fetch_add(1, std::memory_order_relaxed);
             if (ce == cudaSuccess && pd.nprobe > 0) {

@@ -432,8 +432,11 @@ __device__ __forceinline__ void tile_prefetch(typename P::S* buf, const typename
     cp_async_commit();
 }
 
-template <class P, int T, int R>
-__global__ void __launch_bounds__(1 << (T - R), 1) k_pass(typename P::G* __restrict__ state, uint64_t ntiles,
+// NB = tile buffers: 2 overlaps the next tile's load with this tile's rounds
+// (one resident CTA per SM); 1 leaves that overlap to the other CTAs resident
+// on the SM, which MINB (the launch-bounds minimum) makes room for.
+template <class P, int T, int R, int NB, int MINB>
+__global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __restrict__ state, uint64_t ntiles,
                                                         const PassDesc* __restrict__ pdp,
                                                         const StepDesc* __restrict__ steps,
                                                         const KOp* __restrict__ ops,
@@ -447,8 +450,8 @@ __global__ void __launch_bounds__(1 << (T - R), 1) k_pass(typename P::G* __restr
     constexpr int PER = (1 << T) / NT;  // elements per thread
     extern __shared__ __align__(16) unsigned char smem_raw[];
     typename P::S* bufs[2] = {reinterpret_cast<typename P::S*>(smem_raw),
-                              reinterpret_cast<typename P::S*>(smem_raw) + (1 << T)};
-    uint64_t* choff = reinterpret_cast<uint64_t*>(smem_raw + 2 * (sizeof(typename P::S) << T));
+                              reinterpret_cast<typename P::S*>(smem_raw) + (NB - 1) * (1 << T)};
+    uint64_t* choff = reinterpret_cast<uint64_t*>(smem_raw + NB * (sizeof(typename P::S) << T));
 
     const int tid = threadIdx.x;
     const int L = pdp->L;
@@ -465,17 +468,22 @@ __global__ void __launch_bounds__(1 << (T - R), 1) k_pass(typename P::G* __restr
     const int nsteps = pdp->step_count;
 
     uint64_t b = blockIdx.x;
-    if (b < ntiles) tile_prefetch<P, T, NT>(bufs[0], state, tile_base(b, L, H, tq), choff, L);
+    if (NB == 2 && b < ntiles) tile_prefetch<P, T, NT>(bufs[0], state, tile_base(b, L, H, tq), choff, L);
     for (int it = 0; b < ntiles; ++it, b += gridDim.x) {
         typename P::S* sm = bufs[it & 1];
         const uint64_t base = tile_base(b, L, H, tq);
         const typename P::C* coef = coef0 + (b >> ishift) * cstride;
-        const uint64_t bn = b + gridDim.x;
-        if (bn < ntiles) {
-            tile_prefetch<P, T, NT>(bufs[(it + 1) & 1], state, tile_base(bn, L, H, tq), choff, L);
-            cp_async_wait<1>();  // this tile's group is complete; the next one may be in flight
-        } else {
+        if constexpr (NB == 1) {
+            tile_prefetch<P, T, NT>(sm, state, base, choff, L);
             cp_async_wait<0>();
+        } else {
+            const uint64_t bn = b + gridDim.x;
+            if (bn < ntiles) {
+                tile_prefetch<P, T, NT>(bufs[(it + 1) & 1], state, tile_base(bn, L, H, tq), choff, L);
+                cp_async_wait<1>();  // this tile's group is complete; the next one may be in flight
+            } else {
+                cp_async_wait<0>();
+            }
         }
         __syncthreads();
         if constexpr (P::RAW_STAGING) {  // convert the raw FP64 tile to the register format in place

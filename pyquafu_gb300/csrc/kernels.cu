@@ -2,6 +2,8 @@
 // FP64 reductions (Pauli expectation, norms) and the sampling pipeline (block
 // sums, block prefix, per-shot locate, exact fallback).  The fused tile-pass
 // kernel is instantiated per precision in pass_c128.cu / pass_c64.cu.
+#include <atomic>
+
 #include "device.cuh"
 #include "kernels.h"
 #include "reduce.cuh"
@@ -266,6 +268,37 @@ __global__ void k_sample_exact(const typename P::G* __restrict__ state, uint64_t
 // ---------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------
+// Shapes picked by the autotuner per (arithmetic, pass kind, qubit count),
+// packed as T | R << 8; 0 means the built-in default.
+static std::atomic<int32_t> g_tuned[3][2][QFVM_MAX_QUBITS + 1];
+
+void resolve_shape(int arith, int kind, int n, int* T, int* R) {
+    const int a = (arith == QFVM_C64) ? 1 : (arith == QFVM_C128_DS ? 2 : 0);
+    const int32_t v = (n >= 0 && n <= QFVM_MAX_QUBITS && (kind == 0 || kind == 1))
+                          ? g_tuned[a][kind][n].load(std::memory_order_relaxed)
+                          : 0;
+    if (v) {
+        *T = v & 0xff;
+        *R = (v >> 8) & 0xff;
+        return;
+    }
+    if (kind == 1) adjoint_shape(arith, T, R);
+    else default_shape(n, arith == QFVM_C64 ? QFVM_C64 : QFVM_C128, T, R);
+}
+
+bool set_tuned_shape(int arith, int kind, int n, int T, int R) {
+    if (n < 0 || n > QFVM_MAX_QUBITS || (kind != 0 && kind != 1)) return false;
+    const int a = (arith == QFVM_C64) ? 1 : (arith == QFVM_C128_DS ? 2 : 0);
+    if (T == 0) {
+        g_tuned[a][kind][n].store(0);
+        return true;
+    }
+    const bool ok = kind == 0 ? pass_shape_supported(arith, T, R) : pass2_shape_supported(arith, T, R);
+    if (!ok) return false;
+    g_tuned[a][kind][n].store(T | (R << 8));
+    return true;
+}
+
 bool pass_shape_supported(int precision, int T, int R) {
     if (precision == QFVM_C64) return pass_shape_c64(T, R);
     if (precision == QFVM_C128_DS) return pass_shape_ds(T, R);

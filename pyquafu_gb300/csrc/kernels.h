@@ -11,6 +11,10 @@ constexpr int EXPECT_BATCH = 8;   // Pauli terms reduced per kernel launch
 constexpr int REDUCE_BLOCKS = 152 * 4;
 
 bool pass_shape_supported(int precision, int T, int R);
+// Shape of a pass kind (0 one-state, 1 two-state reverse sweep) for n qubits:
+// the autotuned one if set, else the built-in default.
+void resolve_shape(int arith, int kind, int n, int* T, int* R);
+bool set_tuned_shape(int arith, int kind, int n, int T, int R);
 bool pass_shape_c128(int T, int R);
 bool pass_shape_c64(int T, int R);
 bool pass_shape_ds(int T, int R);
@@ -50,7 +54,8 @@ namespace qsv {
 // adjoint.cu
 void adjoint_shape(int arith, int* T, int* R);
 int adjoint_small_max(int arith);
-cudaError_t launch_pass2(int arith, void* psi, void* lam, const PassDesc* dpass, const StepDesc* dsteps,
+bool pass2_shape_supported(int arith, int T, int R);
+cudaError_t launch_pass2(int arith, int T, int R, void* psi, void* lam, const PassDesc* dpass, const StepDesc* dsteps,
                          const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride, int per_tile,
                          double* partial, int* grid_out, cudaStream_t st);
 int pass2_grid_cap();

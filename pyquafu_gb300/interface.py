@@ -1,0 +1,180 @@
+"""PyTorch binding of the batched adjoint engine.
+
+The reference's torch layer (quafu/algorithms/interface/torch.py:65-89,
+``ExecuteCircuits``) runs one Estimator evaluation per sample in its forward
+pass (torch.py:76-78) and, in its backward pass, a parameter-shift Jacobian:
+two more evaluations per parameter, sample and observable
+(quafu/algorithms/gradients/vjp.py:60-103), contracted with ``grad_out``
+(vjp.py:106-140).  Here both directions are single batched device runs:
+
+* forward: every sample's expectation values in one run of a
+  ``BatchSession`` (states of all samples side by side in HBM);
+* backward: with one observable, the per-sample gradients come from the same
+  run as the forward values (the adjoint sweep costs about two forward
+  passes) and the vector-Jacobian product is ``grad_out * J``; with several
+  observables the backward pass is one weighted adjoint run whose observable
+  is sum_o grad_out[b, o] O_o, which gives the vector-Jacobian product
+  directly (no Jacobian of size B x n_obs x P is ever formed).
+
+``TorchTransformer.execute`` mirrors the reference's entry point of the same
+name (torch.py:39-62) for circuits whose parameterised gates take plain
+``Parameter`` objects; ``QuantumLayer`` is a module with shared weights and
+per-sample angle-encoded inputs (the QNN training workload).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+from torch import nn
+
+from . import ir
+from .batch import BatchSession
+
+
+class BatchRunner:
+    """A batch session for one circuit structure and one batch size."""
+
+    def __init__(self, n: int, ops, observables, items: int, slots: int, precision: str = "c64", tile=None,
+                 adjoint_tile=None):
+        self.n, self.items, self.slots = int(n), int(items), int(slots)
+        self.session = BatchSession(precision, grads=True, tile=tile, adjoint_tile=adjoint_tile)
+        self.session.add_group(n, ops, observables, items, slots)
+        self.nobs = self.session.groups[0][3]
+
+    def close(self):
+        self.session.close()
+
+
+class BatchedExpval(torch.autograd.Function):
+    """values (items, slots) -> expectation values (items, n_obs)."""
+
+    @staticmethod
+    def forward(ctx, values, runner):  # pylint: disable=arguments-differ
+        v = np.ascontiguousarray(values.detach().to("cpu", torch.float64).numpy())
+        ctx.runner = runner
+        if runner.nobs == 1:
+            e, g = runner.session.run([v], grads=True)
+            ctx.jac = torch.from_numpy(g[0])
+            ctx.v = None
+        else:
+            e = runner.session.run([v])
+            ctx.jac = None
+            ctx.v = v
+        return torch.from_numpy(e[0]).to(device=values.device, dtype=values.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_out):  # pylint: disable=arguments-differ
+        go = grad_out.detach().to("cpu", torch.float64)
+        if ctx.jac is not None:
+            gv = go[:, :1] * ctx.jac
+        else:
+            _, g = ctx.runner.session.run([ctx.v], grads=True, weights=[go.numpy()])
+            gv = torch.from_numpy(g[0])
+        return gv.to(device=grad_out.device, dtype=grad_out.dtype), None
+
+
+class QuantumLayer(nn.Module):
+    """Shared trainable weights and per-sample inputs bound to the slots of
+    one circuit; forward(x) returns the (batch, n_obs) expectation values.
+    ``weight_slots[k]`` is the slot of weight k, ``input_slots[j]`` the slot
+    of input feature j."""
+
+    def __init__(self, n: int, ops, observables, weight_slots, input_slots, init=None, precision: str = "c64",
+                 tile=None, adjoint_tile=None):
+        super().__init__()
+        self.n, self.ops, self.observables = n, [o for o in ops if o.is_gate], observables
+        self.precision, self.tile, self.adjoint_tile = precision, tile, adjoint_tile
+        self.slots = max([o.slot for o in self.ops] + [-1]) + 1
+        self.register_buffer("_wslots", torch.as_tensor(np.asarray(weight_slots), dtype=torch.long))
+        self.register_buffer("_xslots", torch.as_tensor(np.asarray(input_slots), dtype=torch.long))
+        w0 = np.zeros(len(weight_slots)) if init is None else np.asarray(init, dtype=np.float64)
+        self.weight = nn.Parameter(torch.tensor(w0, dtype=torch.float64))
+        self._runners: dict[int, BatchRunner] = {}
+
+    def runner(self, batch: int) -> BatchRunner:
+        r = self._runners.get(batch)
+        if r is None:
+            r = BatchRunner(self.n, self.ops, self.observables, batch, self.slots, self.precision, self.tile,
+                            self.adjoint_tile)
+            self._runners[batch] = r
+        return r
+
+    def forward(self, x):
+        b = x.shape[0]
+        values = torch.zeros(b, self.slots, dtype=torch.float64, device=x.device)
+        values = values.index_copy(1, self._wslots, self.weight.unsqueeze(0).expand(b, -1))
+        values = values.index_copy(1, self._xslots, x.to(torch.float64))
+        return BatchedExpval.apply(values, self.runner(b))
+
+
+# ----------------------------------------------------------- reference drop-in
+
+
+def _z_observables(n):
+    """_generate_expval_z (vjp.py:25-30): <Z_i> for every qubit."""
+    return [[(1.0, "Z", [q])] for q in range(n)]
+
+
+class _CircuitBinding:
+    """Gate slots of a circuit: gate i of ``circ.gates`` whose angle is a
+    ``Parameter`` reads variable ``var_of_slot[slot]``."""
+
+    def __init__(self, circ):
+        parsed = ir.read_circuit(circ)
+        gates = [o for o in parsed.ops if o.is_gate]
+        if len(gates) != len(circ.gates):
+            raise ValueError("circuits with wrapped sub-circuits are not supported here: unwrap them first")
+        variables = list(circ.variables)
+        index = {id(v): k for k, v in enumerate(variables)}
+        var_of_slot = []
+        for i, g in enumerate(circ.gates):
+            paras = list(getattr(g, "paras", []) or [])
+            kinds = [type(p).__name__ for p in paras]
+            if "ParameterExpression" in kinds:
+                raise NotImplementedError("gate angles given as ParameterExpression are not batched: use "
+                                          "Parameter objects")
+            if kinds and kinds[0] == "Parameter":
+                gates[i].slot = len(var_of_slot)
+                var_of_slot.append(index[id(paras[0])])
+        self.n = parsed.num_qubits
+        self.gates = gates
+        self.num_vars = len(variables)
+        self.var_of_slot = torch.as_tensor(var_of_slot, dtype=torch.long)
+
+
+class TorchTransformer:
+    """Drop-in for quafu.algorithms.interface.torch.TorchTransformer with the
+    batched adjoint engine behind ``method="adjoint"`` (the reference's
+    ``method`` hook, torch.py:45)."""
+
+    _bindings: dict = {}
+
+    @staticmethod
+    def init_weights(shape):
+        """Return torch gradient tensor with specified shape (torch.py:31-34)."""
+        return torch.randn(*shape, requires_grad=True, dtype=torch.double)
+
+    @staticmethod
+    def execute(circ, parameters: torch.Tensor, run_fn=None, grad_fn=None, method="adjoint", estimator=None,
+                precision: str = "c64"):
+        """(batch, n_variables) variable values -> (batch, circ.num) <Z_i>."""
+        del run_fn, grad_fn, estimator  # the reference's hooks; the engine runs both directions
+        if method not in ("adjoint", "internal"):
+            raise ValueError(f"unknown method {method!r}")
+        key = (id(circ), precision)
+        ent = TorchTransformer._bindings.get(key)
+        if ent is None or ent[0] is not circ:
+            ent = (circ, _CircuitBinding(circ), {})
+            TorchTransformer._bindings[key] = ent
+        _, bind, runners = ent
+        params = parameters if parameters.dim() == 2 else parameters.reshape(1, -1)
+        if params.shape[1] != bind.num_vars:
+            raise ValueError(f"expected {bind.num_vars} parameters per sample, got {params.shape[1]}")
+        b = params.shape[0]
+        runner = runners.get(b)
+        if runner is None:
+            runner = BatchRunner(bind.n, bind.gates, _z_observables(bind.n), b, len(bind.var_of_slot), precision)
+            runners[b] = runner
+        values = params.to(torch.float64).index_select(1, bind.var_of_slot.to(params.device))
+        return BatchedExpval.apply(values, runner)

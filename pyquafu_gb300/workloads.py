@@ -10,6 +10,14 @@ Hardware-efficient ansatz (the gradient workloads):
   ``layers`` x (ry on every qubit, rz on every qubit) followed by a cx ladder
   0->1->...->n-1, optionally preceded by an ry angle-encoding layer.
 
+Batched gradient workloads:
+  ``uneven_batch``: circuits with qubit counts uniform in [nmin, nmax], each
+  an ry(x_j) encoding layer (x ~ U[-pi, pi]) then ``layers`` HEA layers with
+  angles ~ U[0, 2*pi); grouped by qubit count for the batched engine.
+  ``qnn_batch``: a QNN on n qubits with ``layers`` HEA layers of shared
+  weights, inputs x ~ N(0, 1) angle-encoded by ry, labels sign(w . x) for a
+  fixed random w; the loss is the MSE of <Z_0> against the labels.
+
 Circuits are returned as ``pyquafu_gb300.ir.Op`` lists (the engine's packed
 input), and ``as_protocol`` wraps them in objects with the attributes the
 reference's circuit reader uses (.instructions, .num, .cbits_num; ops with
@@ -84,6 +92,36 @@ def hea(n: int, layers: int, seed: int = 0, encode: np.ndarray | None = None):
     return ops, params
 
 
+def uneven_batch(circuits: int = 2048, nmin: int = 10, nmax: int = 18, layers: int = 6, seed: int = 0):
+    """Returns {n: (ops, values)} with values[item] the slot vector of one
+    circuit: its 2 * n * layers HEA angles, then its n encoding angles."""
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(nmin, nmax + 1, size=circuits)
+    groups = {}
+    for n in range(nmin, nmax + 1):
+        count = int(np.sum(ns == n))
+        if count == 0:
+            continue
+        ops, _ = hea(n, layers, seed=0, encode=np.zeros(n))
+        nw = 2 * n * layers
+        vals = np.empty((count, nw + n))
+        vals[:, :nw] = rng.uniform(0.0, 2 * np.pi, (count, nw))
+        vals[:, nw:] = rng.uniform(-np.pi, np.pi, (count, n))
+        groups[n] = (ops, vals)
+    return groups
+
+
+def qnn_batch(batch: int = 1024, n: int = 16, layers: int = 12, seed: int = 0):
+    """Returns (ops, weights, x, y): ops with slots 0..2*n*layers-1 for the
+    shared weights and 2*n*layers + j for input feature j."""
+    rng = np.random.default_rng(seed)
+    x = rng.normal(size=(batch, n))
+    w = rng.normal(size=n)
+    y = np.where(x @ w >= 0, 1.0, -1.0)
+    ops, weights = hea(n, layers, seed=seed, encode=np.zeros(n))
+    return ops, weights, x, y
+
+
 def zz_x_hamiltonian(n: int, seed: int = 0):
     """sum_i a_i Z_i Z_{i+1} + sum_i b_i X_i with a, b ~ N(0, 1): list of
     (coeff, paulistr, pos)."""
@@ -98,12 +136,26 @@ def zz_x_hamiltonian(n: int, seed: int = 0):
 # ------------------------- circuit-protocol wrappers -------------------------
 
 
+class Parameter:
+    """Stand-in with the reference Parameter's protocol (a named value that
+    converts to float; quafu/elements/parameters.py:256-280)."""
+
+    def __init__(self, name: str, value: float = 0.0):
+        self.name = name
+        self.value = float(value)
+
+    def __float__(self):
+        return self.value
+
+
 class _ProtoGate:
-    def __init__(self, op: ir.Op):
+    def __init__(self, op: ir.Op, variables=None):
         self.name = op.name.upper()
         self.pos = list(op.qubits)
         self._paras = list(op.params)
-        self.paras = list(op.params)
+        if variables is not None and op.slot >= 0:
+            self._paras[0] = variables[op.slot]
+        self.paras = list(self._paras)
         if op.ncontrols:
             self.ctrls = list(op.qubits[: op.ncontrols])
         if op.matrix is not None:
@@ -121,14 +173,36 @@ class _ProtoMeasure:
 class ProtoCircuit:
     """Minimal object with the circuit protocol the qfvm reader consumes."""
 
-    def __init__(self, num: int, ops, measures=None, cbits_num=None):
+    def __init__(self, num: int, ops, measures=None, cbits_num=None, parameters: bool = False):
         self.num = num
         self.cbits_num = num if cbits_num is None else cbits_num
-        self.instructions = [_ProtoGate(o) for o in ops]
+        # with ``parameters``, op slot k becomes the shared Parameter "theta_k"
+        nslot = max([o.slot for o in ops] + [-1]) + 1
+        self._vars = [Parameter(f"theta_{k}") for k in range(nslot)] if parameters else None
+        if self._vars is not None:
+            for o in ops:
+                if o.slot >= 0:
+                    self._vars[o.slot].value = o.params[0]
+        self.instructions = [_ProtoGate(o, self._vars) for o in ops]
+        self.gates = [g for g in self.instructions]
         if measures:
             q, c = zip(*measures)
             self.instructions.append(_ProtoMeasure(q, c))
         self.measures = dict(measures or [])
+
+    def get_parameter_grads(self):
+        """{Parameter: [[(gate index, para index), d angle / d parameter]]}
+        in order of first use (quantum_circuit.py:255-283)."""
+        out = {}
+        for i, g in enumerate(self.gates):
+            for j, p in enumerate(getattr(g, "paras", [])):
+                if isinstance(p, Parameter):
+                    out.setdefault(p, []).append([(i, j), 1.0])
+        return out
+
+    @property
+    def variables(self):
+        return list(self.get_parameter_grads().keys())
 
 
 def as_protocol(num: int, ops, measures=None) -> ProtoCircuit:

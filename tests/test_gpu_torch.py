@@ -1,0 +1,57 @@
+"""The torch binding of the batched engine on the GPU: QuantumLayer (shared
+weights + per-sample inputs, one observable: Jacobian from the forward run)
+and the TorchTransformer.execute drop-in (<Z_i> of every qubit: weighted
+adjoint run in backward), both against the oracle."""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from pyquafu_gb300 import gradients, workloads
+from pyquafu_gb300.interface import QuantumLayer, TorchTransformer
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision,tol", [("c128", 1e-10), ("c64", 2e-5)])
+def test_quantum_layer_mse_gradient(precision, tol):
+    n, layers, batch = 8, 2, 12
+    ops, w0, x, y = workloads.qnn_batch(batch=batch, n=n, layers=layers, seed=1)
+    nw = 2 * n * layers
+    layer = QuantumLayer(n, ops, [(1.0, "Z", [0])], np.arange(nw), nw + np.arange(n), init=w0, precision=precision)
+    xt = torch.tensor(x)
+    out = layer(xt)
+    loss = torch.mean((out[:, 0] - torch.tensor(y)) ** 2)
+    loss.backward()
+    e_ref = np.zeros(batch)
+    g_ref = np.zeros(nw)
+    for b in range(batch):
+        v = np.concatenate([w0, x[b]])
+        bound = gradients.bind(ops, v)
+        psi = oracle.simulate(n, bound)
+        e_ref[b] = oracle.expect_pauli(psi, "Z", [0])
+        g = oracle.grad_adjoint(n, bound, [o.slot for o in bound], [(1.0, "Z", [0])])
+        g_ref += 2.0 * (e_ref[b] - y[b]) / batch * g[:nw]
+    np.testing.assert_allclose(out[:, 0].detach().numpy(), e_ref, atol=tol)
+    np.testing.assert_allclose(layer.weight.grad.numpy(), g_ref, atol=tol)
+
+
+def test_transformer_execute_dropin():
+    n, batch = 6, 5
+    ops, _ = workloads.hea(n, 2, seed=3)
+    circ = workloads.ProtoCircuit(n, ops, parameters=True)
+    nvar = len(circ.variables)
+    rng = np.random.default_rng(3)
+    params = torch.tensor(rng.uniform(0, 2 * np.pi, (batch, nvar)), requires_grad=True)
+    out = TorchTransformer.execute(circ, params, method="adjoint", precision="c128")
+    go = torch.tensor(rng.normal(size=(batch, n)))
+    (out * go).sum().backward()
+    for b in range(batch):
+        bound = gradients.bind(ops, params[b].detach().numpy())
+        psi = oracle.simulate(n, bound)
+        for q in range(n):
+            assert abs(out[b, q].item() - oracle.expect_pauli(psi, "Z", [q])) < 1e-12
+        terms = [(float(go[b, q]), "Z", [q]) for q in range(n)]
+        g = oracle.grad_adjoint(n, bound, [o.slot for o in bound], terms)
+        np.testing.assert_allclose(params.grad[b].numpy(), g, atol=1e-10)
