@@ -73,10 +73,11 @@ __device__ __forceinline__ typename ProbeMath<P>::T probe_sum(const typename P::
 }
 
 template <class P, int R>
-__device__ __forceinline__ double reg_probe(const typename P::A (&psi)[1 << R], const typename P::A (&lam)[1 << R],
-                                            const KOp& op, uint64_t gthr) {
+__device__ __forceinline__ typename ProbeMath<P>::T reg_probe(const typename P::A (&psi)[1 << R],
+                                                              const typename P::A (&lam)[1 << R], const KOp& op,
+                                                              uint64_t gthr) {
     using T = typename ProbeMath<P>::T;
-    if ((gthr & op.cthr) != op.cthr) return 0.0;
+    if ((gthr & op.cthr) != op.cthr) return T(0);
     const int pt = __popcll(gthr & op.pthr) & 1;
     T acc = T(0);
     const uint32_t x = op.xreg;
@@ -98,10 +99,11 @@ __device__ __forceinline__ double reg_probe(const typename P::A (&psi)[1 << R], 
             });
         });
     }
-    return static_cast<double>(acc);
+    return acc;
 }
 
-__device__ __forceinline__ double warp_sum(double v) {
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
@@ -217,29 +219,24 @@ __global__ void __launch_bounds__(1 << (T - R), MINB)
                 a[0][j] = P::s2a(sm[0][ad]);
                 a[1][j] = P::s2a(sm[1][ad]);
             }
-            RoundPhase<P> ph[2];
-            ph[0].f = ph[1].f = P::one();
-            ph[0].on = ph[1].on = false;
+            RoundPhase<P> ph;
+            ph.f = P::one();
+            ph.on = false;
             const KOp* op = ops + sd->op_begin;
             for (int oi = 0; oi < sd->op_count; ++oi) {
                 const KOp o = op[oi];
                 if (o.kind == K_PROBE) {
                     // pending uniform phases act on both states alike, so the
-                    // probe (a product of conj(lam) and psi) is unaffected by them
-                    const double v = warp_sum(reg_probe<P, R>(a[0], a[1], o, gthr));
+                    // probe (a product of conj(lam) and psi) is unaffected by
+                    // them; the warp sum runs in the probe type (FP32 for
+                    // complex64), FP64 from the warp total on
+                    const double v = static_cast<double>(warp_sum(reg_probe<P, R>(a[0], a[1], o, gthr)));
                     if (lane == 0) pacc[warp * MAX_PASS_PROBES + o.probe] += v * P::coef_d(coef, o.coef);
                 } else {
-                    reg_apply<P, R>(a[0], o, gthr, coef, ph[0]);
-                    reg_apply<P, R>(a[1], o, gthr, coef, ph[1]);
+                    reg_apply<P, R, 2>(a, o, gthr, coef, ph);
                 }
             }
-#pragma unroll
-            for (int s2 = 0; s2 < 2; ++s2) {
-                if (ph[s2].on) {
-#pragma unroll
-                    for (int j = 0; j < NA; ++j) amp_phase<P>(a[s2][j], ph[s2].f.x, ph[s2].f.y, P::cneg(ph[s2].f.y));
-                }
-            }
+            reg_finish_phase<P, R, 2>(a, ph);
             uint32_t psb2 = psb;
             asm volatile("" : "+r"(psb2));
 #pragma unroll

@@ -44,37 +44,38 @@ __device__ __forceinline__ void with_bit(int b, F&& f) {
 }
 
 // ---------------------------------------------------------------------------
-// Register-round operations: a thread holds 2^R amplitudes that differ in the
-// R register bits; target bits are compile-time after the with_bit dispatch.
+// Register-round operations: a thread holds 2^R amplitudes of each of NS
+// states (the adjoint sweep carries psi and lam together); they differ in the
+// R register bits, and target bits are compile-time after the with_bit
+// dispatch.  One dispatch serves all NS states, whose arithmetic interleaves.
 // ---------------------------------------------------------------------------
-template <class P, int R, int TB, bool CTRL, class F>
-__device__ __forceinline__ void reg_pairs(typename P::A (&a)[1 << R], uint32_t creg, F&& f) {
+template <class P, int R, int NS>
+using RegState = typename P::A[NS][1 << R];
+
+template <class P, int R, int NS, int TB, bool CTRL, class F>
+__device__ __forceinline__ void reg_pairs(RegState<P, R, NS>& a, uint32_t creg, F&& f) {
 #pragma unroll
     for (int j = 0; j < (1 << R); ++j) {
         if (j & (1 << TB)) continue;
-        if constexpr (!CTRL) {
-            f(a[j], a[j | (1 << TB)]);
-        } else {
-            // controls inside the registers: compute, then select (no branch)
-            typename P::A x = a[j], y = a[j | (1 << TB)];
-            f(x, y);
-            const bool ok = (static_cast<uint32_t>(j) & creg) == creg;
-            a[j] = ok ? x : a[j];
-            a[j | (1 << TB)] = ok ? y : a[j | (1 << TB)];
-        }
+        // controls inside the registers: creg is warp-uniform, so this
+        // branch never diverges
+        if (CTRL && (static_cast<uint32_t>(j) & creg) != creg) continue;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) f(a[s][j], a[s][j | (1 << TB)]);
     }
 }
 
-template <class P, int R, bool CTRL>
-__device__ __forceinline__ void reg_op1(typename P::A (&a)[1 << R], const KOp& op, const typename P::C* coef) {
+template <class P, int R, int NS, bool CTRL>
+__device__ __forceinline__ void reg_op1(RegState<P, R, NS>& a, const KOp& op, const typename P::C* coef) {
     using C = typename P::C;
+    using A = typename P::A;
     const uint32_t creg = op.creg;
     switch (op.kind) {
         case K_X:
             with_bit<R>(op.t0, [&](auto tb) {
                 constexpr int TB = decltype(tb)::value;
-                reg_pairs<P, R, TB, CTRL>(a, creg, [](typename P::A& x, typename P::A& y) {
-                    typename P::A t = x;
+                reg_pairs<P, R, NS, TB, CTRL>(a, creg, [](A& x, A& y) {
+                    A t = x;
                     x = y;
                     y = t;
                 });
@@ -83,7 +84,7 @@ __device__ __forceinline__ void reg_op1(typename P::A (&a)[1 << R], const KOp& o
         case K_Y:
             with_bit<R>(op.t0, [&](auto tb) {
                 constexpr int TB = decltype(tb)::value;
-                reg_pairs<P, R, TB, CTRL>(a, creg, [](typename P::A& x, typename P::A& y) { pair_y<P>(x, y); });
+                reg_pairs<P, R, NS, TB, CTRL>(a, creg, [](A& x, A& y) { pair_y<P>(x, y); });
             });
             break;
         case K_REAL: {
@@ -91,8 +92,7 @@ __device__ __forceinline__ void reg_op1(typename P::A (&a)[1 << R], const KOp& o
             const C m2 = P::coef(coef, op.coef + 2), m3 = P::coef(coef, op.coef + 3);
             with_bit<R>(op.t0, [&](auto tb) {
                 constexpr int TB = decltype(tb)::value;
-                reg_pairs<P, R, TB, CTRL>(
-                    a, creg, [&](typename P::A& x, typename P::A& y) { pair_real<P>(x, y, m0, m1, m2, m3); });
+                reg_pairs<P, R, NS, TB, CTRL>(a, creg, [&](A& x, A& y) { pair_real<P>(x, y, m0, m1, m2, m3); });
             });
             break;
         }
@@ -101,8 +101,7 @@ __device__ __forceinline__ void reg_op1(typename P::A (&a)[1 << R], const KOp& o
             const C ns = P::cneg(s);
             with_bit<R>(op.t0, [&](auto tb) {
                 constexpr int TB = decltype(tb)::value;
-                reg_pairs<P, R, TB, CTRL>(a, creg,
-                                          [&](typename P::A& x, typename P::A& y) { pair_rx<P>(x, y, c, s, ns); });
+                reg_pairs<P, R, NS, TB, CTRL>(a, creg, [&](A& x, A& y) { pair_rx<P>(x, y, c, s, ns); });
             });
             break;
         }
@@ -114,8 +113,7 @@ __device__ __forceinline__ void reg_op1(typename P::A (&a)[1 << R], const KOp& o
             for (int i = 0; i < 4; ++i) nmi[i] = P::cneg(m[2 * i + 1]);
             with_bit<R>(op.t0, [&](auto tb) {
                 constexpr int TB = decltype(tb)::value;
-                reg_pairs<P, R, TB, CTRL>(a, creg,
-                                          [&](typename P::A& x, typename P::A& y) { pair_dense<P>(x, y, m, nmi); });
+                reg_pairs<P, R, NS, TB, CTRL>(a, creg, [&](A& x, A& y) { pair_dense<P>(x, y, m, nmi); });
             });
             break;
         }
@@ -123,18 +121,8 @@ __device__ __forceinline__ void reg_op1(typename P::A (&a)[1 << R], const KOp& o
     }
 }
 
-template <class P, int R, int B0, int B1, bool CTRL, class F>
-__device__ __forceinline__ void reg_quads(typename P::A (&a)[1 << R], uint32_t creg, F&& f) {
-#pragma unroll
-    for (int j = 0; j < (1 << R); ++j) {
-        if (j & ((1 << B0) | (1 << B1))) continue;
-        if (!CTRL || ((static_cast<uint32_t>(j) & creg) == creg))
-            f(a[j], a[j | (1 << B0)], a[j | (1 << B1)], a[j | (1 << B0) | (1 << B1)]);
-    }
-}
-
-template <class P, int R, bool CTRL>
-__device__ __forceinline__ void reg_swap(typename P::A (&a)[1 << R], const KOp& op) {
+template <class P, int R, int NS, bool CTRL>
+__device__ __forceinline__ void reg_swap(RegState<P, R, NS>& a, const KOp& op) {
     const uint32_t creg = op.creg;
     with_bit<R>(op.t0, [&](auto b0) {
         constexpr int B0 = decltype(b0)::value;
@@ -144,18 +132,24 @@ __device__ __forceinline__ void reg_swap(typename P::A (&a)[1 << R], const KOp& 
             if constexpr (B0 != B1) {
                 constexpr int LO = B0 < B1 ? B0 : B1;
                 constexpr int HI = B0 < B1 ? B1 : B0;
-                reg_quads<P, R, LO, HI, CTRL>(
-                    a, creg, [](typename P::A&, typename P::A& v1, typename P::A& v2, typename P::A&) {
-                        typename P::A t = v1;
-                        v1 = v2;
-                        v2 = t;
-                    });
+#pragma unroll
+                for (int j = 0; j < (1 << R); ++j) {
+                    if (j & ((1 << LO) | (1 << HI))) continue;
+                    if (CTRL && (static_cast<uint32_t>(j) & creg) != creg) continue;
+#pragma unroll
+                    for (int s = 0; s < NS; ++s) {
+                        typename P::A t = a[s][j | (1 << LO)];
+                        a[s][j | (1 << LO)] = a[s][j | (1 << HI)];
+                        a[s][j | (1 << HI)] = t;
+                    }
+                }
             }
         });
     });
 }
 
-// Accumulated thread-uniform phase of a register round.
+// Accumulated thread-uniform phase of a register round (the same for every
+// state of the round: all states see the same gates).
 template <class P>
 struct RoundPhase {
     typename P::A f;
@@ -174,8 +168,8 @@ __device__ __forceinline__ void phase_mul(typename P::A& f, typename P::C dr, ty
 //  F_ONEBIT   exactly one parity bit in the registers (t0), no register
 //             control: two factors per thread, bit position compile-time;
 //  otherwise  per-amplitude parity and control, branch-free selects.
-template <class P, int R>
-__device__ __forceinline__ void reg_diag(typename P::A (&a)[1 << R], const KOp& op, uint64_t gthr,
+template <class P, int R, int NS>
+__device__ __forceinline__ void reg_diag(RegState<P, R, NS>& a, const KOp& op, uint64_t gthr,
                                          const typename P::C* coef, RoundPhase<P>& ph) {
     using C = typename P::C;
     const int pt = __popcll(gthr & op.pthr) & 1;
@@ -198,7 +192,10 @@ __device__ __forceinline__ void reg_diag(typename P::A (&a)[1 << R], const KOp& 
                 const C dr = P::coef(coef, o), di = P::coef(coef, o + 1), ndi = P::cneg(di);
 #pragma unroll
                 for (int j = 0; j < (1 << R); ++j)
-                    if (((j >> TB) & 1) == h) amp_phase<P>(a[j], dr, di, ndi);
+                    if (((j >> TB) & 1) == h) {
+#pragma unroll
+                        for (int s = 0; s < NS; ++s) amp_phase<P>(a[s][j], dr, di, ndi);
+                    }
             }
         });
         return;
@@ -206,33 +203,46 @@ __device__ __forceinline__ void reg_diag(typename P::A (&a)[1 << R], const KOp& 
     const uint32_t creg = op.creg, preg = op.preg;
     const C d0r = P::coef(coef, op.coef), d0i = P::coef(coef, op.coef + 1);
     const C d1r = P::coef(coef, op.coef + 2), d1i = P::coef(coef, op.coef + 3);
+    const C nd0i = P::cneg(d0i), nd1i = P::cneg(d1i);
 #pragma unroll
     for (int j = 0; j < (1 << R); ++j) {
-        const bool ok = (static_cast<uint32_t>(j) & creg) == creg;
+        if ((static_cast<uint32_t>(j) & creg) != creg) continue;  // warp-uniform
+        // the parity depends on the thread: selects, no divergent branch
         const bool par = (pt ^ (__popc(static_cast<uint32_t>(j) & preg) & 1)) != 0;
         const C dr = par ? d1r : d0r;
         const C di = par ? d1i : d0i;
-        typename P::A v = a[j];
-        amp_phase<P>(v, dr, di, P::cneg(di));
-        a[j] = ok ? v : a[j];
+        const C ndi = par ? nd1i : nd0i;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) amp_phase<P>(a[s][j], dr, di, ndi);
     }
 }
 
-template <class P, int R>
-__device__ __forceinline__ void reg_apply(typename P::A (&a)[1 << R], const KOp& op, uint64_t gthr,
+template <class P, int R, int NS>
+__device__ __forceinline__ void reg_apply(RegState<P, R, NS>& a, const KOp& op, uint64_t gthr,
                                           const typename P::C* coef, RoundPhase<P>& ph) {
     if ((gthr & op.cthr) != op.cthr) return;  // a control outside the registers is 0
     switch (op.kind) {
-        case K_DIAG: reg_diag<P, R>(a, op, gthr, coef, ph); break;
+        case K_DIAG: reg_diag<P, R, NS>(a, op, gthr, coef, ph); break;
         case K_SWAP:
-            if (op.creg) reg_swap<P, R, true>(a, op);
-            else reg_swap<P, R, false>(a, op);
+            if (op.creg) reg_swap<P, R, NS, true>(a, op);
+            else reg_swap<P, R, NS, false>(a, op);
             break;
         default:
-            if (op.creg) reg_op1<P, R, true>(a, op, coef);
-            else reg_op1<P, R, false>(a, op, coef);
+            if (op.creg) reg_op1<P, R, NS, true>(a, op, coef);
+            else reg_op1<P, R, NS, false>(a, op, coef);
             break;
     }
+}
+
+// Applies a round's accumulated phase to every state.
+template <class P, int R, int NS>
+__device__ __forceinline__ void reg_finish_phase(RegState<P, R, NS>& a, const RoundPhase<P>& ph) {
+    if (!ph.on) return;
+    const typename P::C nfi = P::cneg(ph.f.y);
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+#pragma unroll
+        for (int j = 0; j < (1 << R); ++j) amp_phase<P>(a[s][j], ph.f.x, ph.f.y, nfi);
 }
 
 // ---------------------------------------------------------------------------
@@ -518,14 +528,14 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
             uint32_t rsw[R];
 #pragma unroll
             for (int k = 0; k < R; ++k) rsw[k] = swz<GB>(1u << sd->rpos[k]);
-            typename P::A a[NA];
+            typename P::A a[1][NA];
 #pragma unroll
             for (int j = 0; j < NA; ++j) {
                 uint32_t ad = psb;
 #pragma unroll
                 for (int k = 0; k < R; ++k)
                     if ((j >> k) & 1) ad ^= rsw[k];
-                a[j] = P::s2a(sm[ad]);
+                a[0][j] = P::s2a(sm[ad]);
             }
             const KOp* op = ops + sd->op_begin;
             const int nop = sd->op_count;
@@ -534,12 +544,9 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
             ph.on = false;
             for (int oi = 0; oi < nop; ++oi) {
                 const KOp o = op[oi];
-                reg_apply<P, R>(a, o, gthr, coef, ph);
+                reg_apply<P, R, 1>(a, o, gthr, coef, ph);
             }
-            if (ph.on) {
-#pragma unroll
-                for (int j = 0; j < NA; ++j) amp_phase<P>(a[j], ph.f.x, ph.f.y, P::cneg(ph.f.y));
-            }
+            reg_finish_phase<P, R, 1>(a, ph);
             uint32_t psb2 = psb;
             asm volatile("" : "+r"(psb2));  // recompute the addresses instead of keeping 2^R of them live
 #pragma unroll
@@ -548,7 +555,7 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
 #pragma unroll
                 for (int k = 0; k < R; ++k)
                     if ((j >> k) & 1) ad ^= rsw[k];
-                sm[ad] = P::a2s(a[j]);
+                sm[ad] = P::a2s(a[0][j]);
             }
             __syncthreads();
         }
