@@ -259,7 +259,7 @@ int qfvm_batch_destroy(qfvm_batch* batch);
 
 /* Host-only planning (no device needed): build the fused schedule and copy
  * its records out, for inspection and for testing the fuser.  Records are the
- * engine's internal layouts: 56-byte pass, 52-byte step and 48-byte op
+ * engine's internal layouts: 56-byte pass, 100-byte step and 48-byte op
  * records; counts[] receives passes, steps, ops, coefficients. */
 int qfvm_plan_host_build(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int64_t n_ops,
                          const double* matpool, int64_t matpool_len, int32_t tile_qubits, int32_t reg_qubits,

@@ -50,26 +50,32 @@ __device__ __forceinline__ T im_rot(T zr, T zi, int ny) {
     }
 }
 
-// One thread's share of a probe in a register round.  The flip mask has at
-// most two register bits (generators of 1- and 2-qubit rotations); its bits
-// are dispatched at compile time so the partner amplitude is a register.
-template <class P, int R, int XM>
-__device__ __forceinline__ typename ProbeMath<P>::T probe_sum(const typename P::A (&psi)[1 << R],
-                                                              const typename P::A (&lam)[1 << R], const KOp& op,
-                                                              int pt) {
+// One thread's share of a probe in a register round:
+//   sum_j (-1)^parity((j ^ XM) & Z) conj(lam_j) psi_(j ^ XM)   (j over the registers)
+// accumulated as a complex pair, so the i^ny rotation and the thread's own
+// parity bit are applied once per probe, not per amplitude.  XM (flip bits)
+// is compile-time; ZM >= 0 is the compile-time Z mask, ZM < 0 reads `zrt`.
+template <class P, int R, int XM, int ZM>
+__device__ __forceinline__ void probe_sum(const typename P::A (&psi)[1 << R], const typename P::A (&lam)[1 << R],
+                                          uint32_t creg, uint32_t zrt, typename ProbeMath<P>::T& ar,
+                                          typename ProbeMath<P>::T& ai) {
     using T = typename ProbeMath<P>::T;
-    T acc = T(0);
 #pragma unroll
     for (int j = 0; j < (1 << R); ++j) {
-        if ((static_cast<uint32_t>(j) & op.creg) != op.creg) continue;
+        if ((static_cast<uint32_t>(j) & creg) != creg) continue;  // warp-uniform
         const int jx = j ^ XM;
-        const int sgn = pt ^ (__popc(static_cast<uint32_t>(jx) & op.preg) & 1);
+        const bool neg = ZM >= 0 ? ((__popc(static_cast<uint32_t>(jx & (ZM < 0 ? 0 : ZM))) & 1) != 0)
+                                 : ((__popc(static_cast<uint32_t>(jx) & zrt) & 1) != 0);
         T zr, zi;
         ProbeMath<P>::zc(lam[j], psi[jx], zr, zi);
-        const T v = im_rot<T>(zr, zi, op.special);
-        acc += sgn ? -v : v;
+        if (neg) {
+            ar -= zr;
+            ai -= zi;
+        } else {
+            ar += zr;
+            ai += zi;
+        }
     }
-    return acc;
 }
 
 template <class P, int R>
@@ -79,14 +85,25 @@ __device__ __forceinline__ typename ProbeMath<P>::T reg_probe(const typename P::
     using T = typename ProbeMath<P>::T;
     if ((gthr & op.cthr) != op.cthr) return T(0);
     const int pt = __popcll(gthr & op.pthr) & 1;
-    T acc = T(0);
-    const uint32_t x = op.xreg;
+    T ar = T(0), ai = T(0);
+    const uint32_t x = op.xreg, z = op.preg, c = op.creg;
     if (x == 0) {
-        acc = probe_sum<P, R, 0>(psi, lam, op, pt);
+        if (z == 0) {
+            probe_sum<P, R, 0, 0>(psi, lam, c, z, ar, ai);
+        } else if ((z & (z - 1)) == 0) {
+            with_bit<R>(__ffs(z) - 1, [&](auto b) {
+                constexpr int B = decltype(b)::value;
+                probe_sum<P, R, 0, (1 << B)>(psi, lam, c, z, ar, ai);
+            });
+        } else {
+            probe_sum<P, R, 0, -1>(psi, lam, c, z, ar, ai);
+        }
     } else if ((x & (x - 1)) == 0) {
         with_bit<R>(__ffs(x) - 1, [&](auto b) {
             constexpr int B = decltype(b)::value;
-            acc = probe_sum<P, R, (1 << B)>(psi, lam, op, pt);
+            if (z == 0) probe_sum<P, R, (1 << B), 0>(psi, lam, c, z, ar, ai);
+            else if (z == x) probe_sum<P, R, (1 << B), (1 << B)>(psi, lam, c, z, ar, ai);
+            else probe_sum<P, R, (1 << B), -1>(psi, lam, c, z, ar, ai);
         });
     } else {
         const int b0 = __ffs(x) - 1;
@@ -95,11 +112,12 @@ __device__ __forceinline__ typename ProbeMath<P>::T reg_probe(const typename P::
             constexpr int B0 = decltype(c0)::value;
             with_bit<R>(b1, [&](auto c1) {
                 constexpr int B1 = decltype(c1)::value;
-                if constexpr (B0 != B1) acc = probe_sum<P, R, (1 << B0) | (1 << B1)>(psi, lam, op, pt);
+                if constexpr (B0 != B1) probe_sum<P, R, (1 << B0) | (1 << B1), -1>(psi, lam, c, z, ar, ai);
             });
         });
     }
-    return acc;
+    const T v = im_rot<T>(ar, ai, op.special);
+    return pt ? -v : v;
 }
 
 template <class T>
@@ -136,6 +154,7 @@ __global__ void __launch_bounds__(1 << (T - R), MINB)
     double* pacc = reinterpret_cast<double*>(choff + (1 << pdp->H));
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t stid = swz<GB>(static_cast<uint32_t>(tid));
     const int L = pdp->L, H = pdp->H;
     const uint8_t* tq = pdp->tq;
     const int np = pdp->nprobe;
@@ -178,9 +197,9 @@ __global__ void __launch_bounds__(1 << (T - R), MINB)
         }
         __syncthreads();
         if constexpr (P::RAW_STAGING) {
-#pragma unroll 4
+#pragma unroll
             for (int k = 0; k < PER; ++k) {
-                const uint32_t ad = swz<GB>(static_cast<uint32_t>(k * NT + tid));
+                const uint32_t ad = swz<GB>(static_cast<uint32_t>(k * NT)) ^ stid;
                 sm[0][ad] = P::g2s(P::raw_to_g(sm[0][ad]));
                 sm[1][ad] = P::g2s(P::raw_to_g(sm[1][ad]));
             }
@@ -196,19 +215,20 @@ __global__ void __launch_bounds__(1 << (T - R), MINB)
                 }
                 continue;
             }
-            uint32_t sb = 0;
+            // the thread's swizzled base offset and global index: the
+            // swizzle is XOR-linear, so both are sums over its index bits
+            uint32_t psb = 0;
             uint64_t gthr = base;
 #pragma unroll
             for (int k = 0; k < T - R; ++k) {
                 if ((tid >> k) & 1) {
-                    sb |= 1u << sd->tpos[k];
+                    psb ^= sd->tsw[k];
                     gthr |= 1ULL << sd->tglob[k];
                 }
             }
-            const uint32_t psb = swz<GB>(sb);
             uint32_t rsw[R];
 #pragma unroll
-            for (int k = 0; k < R; ++k) rsw[k] = swz<GB>(1u << sd->rpos[k]);
+            for (int k = 0; k < R; ++k) rsw[k] = sd->rsw[k];
             typename P::A a[2][NA];
 #pragma unroll
             for (int j = 0; j < NA; ++j) {
@@ -250,12 +270,13 @@ __global__ void __launch_bounds__(1 << (T - R), MINB)
             }
             __syncthreads();
         }
-#pragma unroll 4
+#pragma unroll
         for (int k = 0; k < PER; ++k) {
-            const uint32_t s = static_cast<uint32_t>(k * NT + tid);
+            const uint32_t s = static_cast<uint32_t>(k * NT) | tid;
             const uint64_t g = base | choff[s >> L] | (s & lmask);
-            __stcs(psi_g + g, P::s2g(sm[0][swz<GB>(s)]));
-            __stcs(lam_g + g, P::s2g(sm[1][swz<GB>(s)]));
+            const uint32_t ad = swz<GB>(static_cast<uint32_t>(k * NT)) ^ stid;
+            __stcs(psi_g + g, P::s2g(sm[0][ad]));
+            __stcs(lam_g + g, P::s2g(sm[1][ad]));
         }
         __syncthreads();
         if (per_tile) {

@@ -72,6 +72,27 @@ __device__ __forceinline__ void reg_op1(RegState<P, R, NS>& a, const KOp& op, co
     const uint32_t creg = op.creg;
     switch (op.kind) {
         case K_X:
+            if (CTRL && (creg & (creg - 1)) == 0) {
+                // one register control (cx): the swapped pairs are known at
+                // compile time after dispatching the control bit as well
+                with_bit<R>(__ffs(creg) - 1, [&](auto cb) {
+                    constexpr int CB = decltype(cb)::value;
+                    with_bit<R>(op.t0, [&](auto tb) {
+                        constexpr int TB = decltype(tb)::value;
+#pragma unroll
+                        for (int j = 0; j < (1 << R); ++j) {
+                            if ((j & (1 << TB)) || !(j & (1 << CB))) continue;
+#pragma unroll
+                            for (int s = 0; s < NS; ++s) {
+                                A t = a[s][j];
+                                a[s][j] = a[s][j | (1 << TB)];
+                                a[s][j | (1 << TB)] = t;
+                            }
+                        }
+                    });
+                });
+                break;
+            }
             with_bit<R>(op.t0, [&](auto tb) {
                 constexpr int TB = decltype(tb)::value;
                 reg_pairs<P, R, NS, TB, CTRL>(a, creg, [](A& x, A& y) {
@@ -434,10 +455,15 @@ __device__ __forceinline__ void tile_prefetch(typename P::S* buf, const typename
                                               const uint64_t* choff, int L) {
     static_assert(sizeof(typename P::G) == sizeof(typename P::S), "raw staging needs equal element sizes");
     const uint32_t lmask = (1u << L) - 1;
-#pragma unroll 4
+    const uint32_t tid = threadIdx.x;
+    const uint32_t stid = swz<P::GBITS>(tid);
+    // k * NT and tid share no bits and the swizzle is XOR-linear: the
+    // swizzled offset is a compile-time constant XOR the thread's own part
+#pragma unroll
     for (int k = 0; k < (1 << T) / NT; ++k) {
-        const uint32_t s = static_cast<uint32_t>(k * NT + threadIdx.x);
-        cp_async<sizeof(typename P::G)>(buf + swz<P::GBITS>(s), state + (base | choff[s >> L] | (s & lmask)));
+        const uint32_t s = static_cast<uint32_t>(k * NT) | tid;
+        cp_async<sizeof(typename P::G)>(buf + (swz<P::GBITS>(static_cast<uint32_t>(k * NT)) ^ stid),
+                                        state + (base | choff[s >> L] | (s & lmask)));
     }
     cp_async_commit();
 }
@@ -464,6 +490,7 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
     uint64_t* choff = reinterpret_cast<uint64_t*>(smem_raw + NB * (sizeof(typename P::S) << T));
 
     const int tid = threadIdx.x;
+    const uint32_t stid = swz<GB>(static_cast<uint32_t>(tid));
     const int L = pdp->L;
     const int H = pdp->H;
     const uint8_t* tq = pdp->tq;
@@ -497,9 +524,9 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
         }
         __syncthreads();
         if constexpr (P::RAW_STAGING) {  // convert the raw FP64 tile to the register format in place
-#pragma unroll 4
+#pragma unroll
             for (int k = 0; k < PER; ++k) {
-                const uint32_t ad = swz<GB>(static_cast<uint32_t>(k * NT + tid));
+                const uint32_t ad = swz<GB>(static_cast<uint32_t>(k * NT)) ^ stid;
                 sm[ad] = P::g2s(P::raw_to_g(sm[ad]));
             }
             __syncthreads();
@@ -515,19 +542,20 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
                 }
                 continue;
             }
-            uint32_t sb = 0;
+            // the thread's swizzled base offset and global index: the
+            // swizzle is XOR-linear, so both are sums over its index bits
+            uint32_t psb = 0;
             uint64_t gthr = base;
 #pragma unroll
             for (int k = 0; k < T - R; ++k) {
                 if ((tid >> k) & 1) {
-                    sb |= 1u << sd->tpos[k];
+                    psb ^= sd->tsw[k];
                     gthr |= 1ULL << sd->tglob[k];
                 }
             }
-            const uint32_t psb = swz<GB>(sb);
             uint32_t rsw[R];
 #pragma unroll
-            for (int k = 0; k < R; ++k) rsw[k] = swz<GB>(1u << sd->rpos[k]);
+            for (int k = 0; k < R; ++k) rsw[k] = sd->rsw[k];
             typename P::A a[1][NA];
 #pragma unroll
             for (int j = 0; j < NA; ++j) {
@@ -560,10 +588,10 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
             __syncthreads();
         }
 
-#pragma unroll 4
+#pragma unroll
         for (int k = 0; k < PER; ++k) {
-            const uint32_t s = static_cast<uint32_t>(k * NT + tid);
-            __stcs(state + (base | choff[s >> L] | (s & lmask)), P::s2g(sm[swz<GB>(s)]));
+            const uint32_t s = static_cast<uint32_t>(k * NT) | tid;
+            __stcs(state + (base | choff[s >> L] | (s & lmask)), P::s2g(sm[swz<GB>(static_cast<uint32_t>(k * NT)) ^ stid]));
         }
         __syncthreads();  // the buffer is re-filled by the prefetch two tiles later
     }

@@ -114,15 +114,20 @@ constexpr int MAX_PASS_PROBES = 64;
 
 // One register round inside a tile pass: register bit k holds tile-local
 // position rpos[k]; thread-index bit k selects tile-local position tpos[k].
+// rsw / tsw are the swizzled shared-memory offsets of those positions (the
+// swizzle is XOR-linear, so a thread's base offset is the XOR of the tsw of
+// its set index bits).
 struct StepDesc {
     int32_t type;  // STEP_*
     int32_t op_begin, op_count;
     uint8_t rpos[8];
     uint8_t tpos[16];
     uint8_t tglob[16];  // global qubit of thread bit k (= tq[tpos[k]])
+    uint16_t rsw[8];
+    uint16_t tsw[16];
 };
 enum : int32_t { STEP_ROUND = 0, STEP_SMEM = 1 };
-static_assert(sizeof(StepDesc) == 52, "StepDesc layout");
+static_assert(sizeof(StepDesc) == 100, "StepDesc layout");
 
 struct PlanStats {
     int64_t passes = 0, rounds = 0, gates = 0;

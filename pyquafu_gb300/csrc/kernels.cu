@@ -283,7 +283,7 @@ void resolve_shape(int arith, int kind, int n, int* T, int* R) {
         return;
     }
     if (kind == 1) adjoint_shape(arith, T, R);
-    else default_shape(n, arith == QFVM_C64 ? QFVM_C64 : QFVM_C128, T, R);
+    else default_shape(n, arith, T, R);
 }
 
 bool set_tuned_shape(int arith, int kind, int n, int T, int R) {

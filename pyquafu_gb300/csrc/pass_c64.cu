@@ -2,7 +2,7 @@
 #include "pass_launch.cuh"
 
 // shapes: (tile qubits, register qubits, tile buffers, min CTAs per SM)
-#define QSV_SHAPES(X) X(12, 5, 2, 1) X(13, 5, 2, 1) X(13, 6, 2, 1) X(12, 4, 1, 2) X(13, 4, 1, 1)
+#define QSV_SHAPES(X) X(12, 5, 2, 1) X(13, 5, 2, 1) X(12, 4, 1, 2) X(13, 4, 1, 1)
 
 namespace qsv {
 

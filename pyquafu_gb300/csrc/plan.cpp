@@ -23,12 +23,17 @@ int amp_bytes(int precision) { return precision == QFVM_C64 ? 8 : 16; }
 // Largest state handled by the whole-state (single CTA, shared memory) kernel.
 int small_max_qubits(int precision) { return precision == QFVM_C64 ? 14 : 13; }
 
+// Built-in shapes (the autotuner's choices on GB300 for the random-layer and
+// hardware-efficient workloads; a tuned table entry overrides them).
 void default_shape(int n, int precision, int* T, int* R) {
     if (precision == QFVM_C64) {
         *T = 13;
-        *R = 5;
-    } else {
+        *R = 4;
+    } else if (precision == QFVM_C128_DS) {
         *T = 12;
+        *R = 3;
+    } else {
+        *T = 11;
         *R = 4;
     }
     (void)n;
@@ -429,6 +434,15 @@ KOp global_kop(HostPlan* p, const GOp& g) {
     return k;
 }
 
+// Shared-memory swizzle of the tile kernels (swz in device.cuh): the higher
+// gbits-wide groups of an element index are XOR-folded onto the lowest group.
+uint32_t swizzle(uint32_t s, int gbits) {
+    const uint32_t m = (1u << gbits) - 1;
+    uint32_t x = s;
+    for (int k = 1; k * gbits < 32; ++k) x ^= (s >> (k * gbits)) & m;
+    return x;
+}
+
 // Thread-bit order for a register round: the first lanes get positions whose
 // residues modulo `gbits` are all distinct, which makes the shared-memory
 // swizzle of the kernels map each wavefront to distinct bank groups.
@@ -660,7 +674,9 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
             for (size_t k = 0; k < freep.size(); ++k) {
                 sd.tpos[k] = static_cast<uint8_t>(freep[k]);
                 sd.tglob[k] = pd.tq[freep[k]];
+                sd.tsw[k] = static_cast<uint16_t>(swizzle(1u << freep[k], gbits));
             }
+            for (int k = 0; k < R; ++k) sd.rsw[k] = static_cast<uint16_t>(swizzle(1u << regs[k], gbits));
             int reg_of_local[MAX_TILE];
             for (int p = 0; p < MAX_TILE; ++p) reg_of_local[p] = -1;
             for (int k = 0; k < R; ++k) reg_of_local[regs[k]] = k;

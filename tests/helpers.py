@@ -35,12 +35,12 @@ PASS_DT = np.dtype([("type", "<i4"), ("T", "<i4"), ("L", "<i4"), ("H", "<i4"), (
                     ("step_count", "<i4"), ("op_begin", "<i4"), ("op_count", "<i4"), ("probe_base", "<i4"),
                     ("nprobe", "<i4"), ("tq", "u1", (16,))])
 STEP_DT = np.dtype([("type", "<i4"), ("op_begin", "<i4"), ("op_count", "<i4"), ("rpos", "u1", (8,)),
-                    ("tpos", "u1", (16,)), ("tglob", "u1", (16,))])
+                    ("tpos", "u1", (16,)), ("tglob", "u1", (16,)), ("rsw", "<u2", (8,)), ("tsw", "<u2", (16,))])
 KOP_DT = np.dtype([("kind", "u1"), ("flags", "u1"), ("special", "u1"), ("k", "u1"), ("t0", "u1"), ("t1", "u1"),
                    ("probe", "<u2"), ("creg", "<u4"), ("preg", "<u4"), ("cthr", "<u8"),
                    ("pthr", "<u8"), ("coef", "<u4"), ("tk", "u1", (6,)), ("pad2", "u1", (2,)), ("xreg", "<u4")],
                   align=True)
-assert PASS_DT.itemsize == 56 and STEP_DT.itemsize == 52 and KOP_DT.itemsize == 48
+assert PASS_DT.itemsize == 56 and STEP_DT.itemsize == 100 and KOP_DT.itemsize == 48
 
 K_DENSE, K_REAL, K_RX, K_DIAG, K_X, K_Y, K_SWAP, K_DENSE2, K_DENSEK, K_PROBE = range(1, 11)
 PASS_TILE, PASS_SMALL, PASS_GLOBALOP = 0, 1, 2
@@ -82,7 +82,18 @@ def host_plan(n, ops, precision=0, T=0, R=0, adjoint=False, batched=False):
     nat.check(lib.qfvm_plan_host_binds(h, ctypes.byref(nb), nat.i32ptr(binds)))
     lib.qfvm_plan_destroy(h)
     return {"passes": passes, "steps": steps[: counts[1]], "ops": kops[: counts[2]], "coef": coef,
-            "T": shape[0], "R": shape[1], "L": shape[2], "probe_slots": slots[:nprobe], "binds": binds[: nb.value]}
+            "T": shape[0], "R": shape[1], "L": shape[2], "probe_slots": slots[:nprobe], "binds": binds[: nb.value],
+            "gbits": 4 if precision == 1 else 3}
+
+
+def swizzle(s, gbits):
+    """The kernels' shared-memory swizzle (XOR fold of higher gbits groups)."""
+    x = s
+    k = 1
+    while k * gbits < 32:
+        x ^= (s >> (k * gbits)) & ((1 << gbits) - 1)
+        k += 1
+    return x
 
 
 def _bits(mask):
@@ -264,6 +275,9 @@ def interpret(plan, psi):
             tpos = [int(x) for x in sd["tpos"][: T - R]]
             assert sorted(rpos + tpos) == list(range(T)), (rpos, tpos)
             assert [int(x) for x in sd["tglob"][: T - R]] == [tq[p] for p in tpos]
+            gb = plan["gbits"]
+            assert [int(x) for x in sd["tsw"][: T - R]] == [swizzle(1 << p, gb) for p in tpos]
+            assert [int(x) for x in sd["rsw"][:R]] == [swizzle(1 << p, gb) for p in rpos]
             g_of_reg = [tq[p] for p in rpos]
             for o in ops:
                 cm = int(o["cthr"])

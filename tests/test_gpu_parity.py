@@ -56,7 +56,7 @@ def test_golden_single_gates(golden):
         assert err <= TOL128, (case["tag"], err)
 
 
-@pytest.mark.parametrize("T,R", [(11, 4), (12, 4), (12, 5)])
+@pytest.mark.parametrize("T,R", [(11, 4), (12, 4), (12, 5), (12, 3), (11, 3)])
 def test_tile_shapes_c128(T, R):
     for n in (T, T + 3):
         ops = workloads.random_layers(n, 6, seed=1000 + n, extras=True, extra_rate=0.6)
@@ -65,7 +65,7 @@ def test_tile_shapes_c128(T, R):
         assert err <= TOL128, (n, T, R, err)
 
 
-@pytest.mark.parametrize("T,R", [(11, 4), (12, 4), (12, 5)])
+@pytest.mark.parametrize("T,R", [(11, 4), (12, 4), (12, 5), (12, 3)])
 def test_tile_shapes_double_single(T, R):
     # complex128 storage with double-single arithmetic: same 1e-12 bound
     for n in (T, T + 3):
@@ -96,7 +96,7 @@ def test_swap_register_order():
         assert np.abs(got - oracle.simulate(n, ops)).max() <= TOL128, prec
 
 
-@pytest.mark.parametrize("T,R", [(12, 5), (13, 5), (13, 6)])
+@pytest.mark.parametrize("T,R", [(12, 5), (13, 5), (12, 4), (13, 4)])
 def test_tile_shapes_c64(T, R):
     n = T + 2
     ops = workloads.random_layers(n, 5, seed=2000 + n, extras=True, extra_rate=0.6)

@@ -9,8 +9,8 @@ import oracle
 from pyquafu_gb300 import workloads
 
 
-SHAPES_C128 = [(11, 4), (12, 4), (12, 5)]
-SHAPES_C64 = [(12, 5), (13, 5), (13, 6)]
+SHAPES_C128 = [(11, 4), (12, 4), (12, 5), (12, 3), (11, 3)]
+SHAPES_C64 = [(12, 5), (13, 5), (12, 4), (13, 4)]
 
 
 @pytest.mark.parametrize("T,R", SHAPES_C128)
