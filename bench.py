@@ -228,7 +228,16 @@ def run_reference(args):
 
 
 S_OF = {"c128": 16, "c128_ds": 16, "c64": 8}
-KERNEL_OF = {"c128": "k_pass<P64,12,4>", "c128_ds": "k_pass<PDS,12,4>", "c64": "k_pass<P32,13,5>"}
+POLICY_OF = {"c128": "P64", "c128_ds": "PDS", "c64": "P32"}
+
+
+def kernel_name(precision, n):
+    """The one-state pass kernel a plan of n qubits runs (shape as resolved
+    by the engine: tuned or built-in)."""
+    from pyquafu_gb300 import autotune
+
+    t, r = autotune.current(precision, 0, n)
+    return f"k_pass<{POLICY_OF[precision]},{t},{r}>"
 
 
 def measure(precision, ops, n, steps, warmup, per_pass=True):
@@ -568,7 +577,7 @@ def run_gpu(args):
     for v in [x for x in args.variants.split(",") if x and x != args.precision]:
         r = measure(v, ops, n, args.steps, max(1, min(args.warmup, 3)))
         variants[v] = {"value": round(r["gbps"], 2), "unit": "GB/s", "ms_per_step": round(r["ms_per_step"], 3),
-                       "passes": r["passes"], "tile_kernel": KERNEL_OF[v], "tile_pass_gbps": round(r["tile_gbps"], 1),
+                       "passes": r["passes"], "tile_kernel": kernel_name(v, n), "tile_pass_gbps": round(r["tile_gbps"], 1),
                        "tile_pass_frac_hbm": round(r["tile_gbps"] / peak, 4)}
 
     # --- end to end through the reference-shaped API (host buffers) ---
@@ -620,7 +629,7 @@ def run_gpu(args):
                        "seed": SEED, "gates": len(ops), "precision": args.precision, "passes": main["passes"],
                        "rounds": main["rounds"], "parallelism": "replicas" if world > 1 else "single",
                        "l2": "state >> L2 (no flush needed)"},
-            "roofline": {"bound": "hbm", "kernel": KERNEL_OF[args.precision], "achieved": round(achieved, 1),
+            "roofline": {"bound": "hbm", "kernel": kernel_name(args.precision, n), "achieved": round(achieved, 1),
                          "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                          "traffic": None, "bytes_per_launch": main["tile_bytes"],
                          "avg_launch_ms": round(main["avg_tile_ms"], 3)},

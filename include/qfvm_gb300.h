@@ -49,8 +49,9 @@ enum {
     QFVM_OP_TDG, QFVM_OP_P, QFVM_OP_RX, QFVM_OP_RY, QFVM_OP_RZ, QFVM_OP_CX, QFVM_OP_CZ,
     QFVM_OP_CP, QFVM_OP_CCX, QFVM_OP_RZZ,
     QFVM_OP_MATRIX = 32,  /* targ matrix in the pool: mat_dim x mat_dim, row-major complex128 */
-    QFVM_OP_MEASURE = 40, /* not accepted by the gate entry points */
-    QFVM_OP_RESET = 41
+    QFVM_OP_MEASURE = 40, /* qfvm_simulate_shots only (not a gate) */
+    QFVM_OP_RESET = 41,   /* qfvm_simulate_shots only */
+    QFVM_OP_CIF = 42      /* qfvm_simulate_shots only */
 };
 
 /* Precision of a device state. */
@@ -198,6 +199,29 @@ int qfvm_plan_run(qfvm_plan* plan, qfvm_sv* sv);
  * to pass_ms[0..passes-1] and its type (0 tile, 1 whole-state, 2 k-target)
  * to pass_type. */
 int qfvm_plan_run_timed(qfvm_plan* plan, qfvm_sv* sv, float* pass_ms, int32_t* pass_type);
+
+/* ---------------------------------------------------------------------------
+ * Per-shot trajectories: the branch of simulate_circuit for circuits with
+ * operations after a measurement (qfvm.cpp:104-133, dispatch of measure /
+ * reset / cif in simulator.hpp:95-111).  Every shot runs the whole circuit on
+ * its own copy of psi_in (|0...0> when NULL); shots run side by side on the
+ * device.  Besides gates, `ops` holds:
+ *   QFVM_OP_MEASURE  nqubits = k (1..8) qubits in qubits[0..k), the classical
+ *                    bits they write in qubits[8..8+k)
+ *   QFVM_OP_RESET    nqubits = k (1..8) qubits in qubits[0..k)
+ *   QFVM_OP_CIF      classical bits in qubits[0..nqubits), condition in
+ *                    params[0]; the next mat_dim ops (gates only) are its body,
+ *                    applied when the bits, first most significant, equal it
+ * Every measure and reset draws one uniform: uniforms[s * n_draws + d] is
+ * shot s's d-th draw (n_draws = measures + resets), and the outcome is the
+ * first joint outcome m with u * total < cumulative probability (FP64, in
+ * outcome order; bit j of m is qubits[j]).  outcomes[s] = the measured
+ * classical bits of shot s in ascending order, the first most significant
+ * (the reference's count key); final_state (optional, 2^n complex128)
+ * receives the last shot's state. */
+int qfvm_simulate_shots(int32_t num_qubits, int32_t num_cbits, const qfvm_op* ops, int64_t n_ops,
+                        const double* matpool, int64_t matpool_len, const double* psi_in, int64_t shots,
+                        const double* uniforms, int64_t n_draws, uint64_t* outcomes, double* final_state);
 
 /* ---------------------------------------------------------------------------
  * Batched runs.  Replaces the reference's per-sample Python loops over

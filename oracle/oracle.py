@@ -111,6 +111,125 @@ def simulate(n: int, ops, psi: np.ndarray | None = None) -> np.ndarray:
     return psi
 
 
+# ------------------------------------------------------------------
+# Circuits with mid-circuit measurement, reset and classically controlled
+# blocks: the per-shot branch of simulate_circuit (qfvm.cpp:104-133).  The
+# reference draws each outcome with std::discrete_distribution over an
+# rng seeded from std::random_device (statevector.hpp:1307-1341); here every
+# measure/reset consumes one given uniform u and picks the first outcome m
+# with u * total < cum[m], probabilities summed in FP64 in index order.
+# ------------------------------------------------------------------
+
+
+def _outcome_probs(psi, qbits):
+    """sample_measure_probs (statevector.hpp:1307-1341): probability of every
+    joint outcome m of qbits (bit j of m <-> qbits[j])."""
+    idx = np.arange(psi.size, dtype=np.int64)
+    m = np.zeros(psi.size, dtype=np.int64)
+    for j, q in enumerate(qbits):
+        m |= ((idx >> q) & 1) << j
+    p = (psi.real * psi.real + psi.imag * psi.imag)
+    probs = np.zeros(1 << len(qbits))
+    for k in range(probs.size):  # index order inside every outcome
+        sel = p[m == k]
+        acc = 0.0
+        for v in sel:
+            acc += float(v)
+        probs[k] = acc
+    return probs, m
+
+
+def choose_outcome(probs, u):
+    """First outcome m with u * total < cum[m] (FP64, outcome order); the
+    last outcome of nonzero probability when rounding leaves none."""
+    total = 0.0
+    for v in probs:
+        total += float(v)
+    r = float(u) * total
+    cum = 0.0
+    last = 0
+    for k, v in enumerate(probs):
+        cum += float(v)
+        if v > 0:
+            last = k
+        if r < cum:
+            return k
+    return last
+
+
+def _collapse(psi, qbits, m_of, outcome, prob, final):
+    """update (statevector.hpp:1192-1225): keep outcome, scale 1/sqrt(prob),
+    then move it to `final` (reset) by exchanging the two outcome blocks."""
+    scale = 1.0 / np.sqrt(prob)
+    keep = m_of == outcome
+    out = np.where(keep, psi * scale, 0)
+    if final != outcome:
+        moved = np.zeros_like(out)
+        delta = 0
+        for j, q in enumerate(qbits):
+            if ((outcome ^ final) >> j) & 1:
+                delta |= 1 << q
+        idx = np.arange(psi.size, dtype=np.int64)
+        moved[idx[keep] ^ delta] = out[keep]
+        out = moved
+    psi[:] = out
+
+
+def run_shot(n, ops, ncbits, uniforms, psi_in=None):
+    """One shot of the per-shot branch: returns (creg list, final state)."""
+    psi = zero_state(n) if psi_in is None or np.size(psi_in) == 0 else np.array(psi_in, dtype=np.complex128)
+    creg = [0] * max(ncbits, 1)
+    draw = 0
+
+    def run(seq):
+        nonlocal draw
+        for op in seq:
+            if op.kind == 40 or op.kind == 41:  # measure / reset
+                probs, m_of = _outcome_probs(psi, op.qbits)
+                k = choose_outcome(probs, uniforms[draw])
+                draw += 1
+                _collapse(psi, op.qbits, m_of, k, probs[k], 0 if op.kind == 41 else k)
+                if op.kind == 40:
+                    for j, c in enumerate(op.cbits):
+                        creg[c] = (k >> j) & 1
+            elif op.kind == 42:  # cif: check_cif (statevector.hpp:186-193)
+                out = 0
+                for c in op.cbits:
+                    out = out * 2 + creg[c]
+                if out == op.condition:
+                    run(op.body)
+            elif op.kind == 43:
+                continue
+            else:
+                apply_op(psi, op)
+
+    run(ops)
+    return creg, psi
+
+
+def simulate_shots(n, ops, ncbits, uniforms, psi_in=None):
+    """Per-shot loop of qfvm.cpp:104-133: outcome of every shot (measured
+    cbits in ascending order, the first one most significant) and the final
+    state of the last shot.  uniforms[s] holds shot s's draws in order."""
+    measured = sorted({c for op in _walk(ops) if op.kind == 40 for c in op.cbits})
+    outcomes = []
+    psi = None
+    for s in range(len(uniforms)):
+        creg, psi = run_shot(n, ops, ncbits, uniforms[s], psi_in)
+        v = 0
+        for c in measured:
+            v = v * 2 + creg[c]
+        outcomes.append(v)
+    return outcomes, psi
+
+
+def _walk(ops):
+    for op in ops:
+        yield op
+        if op.kind == 42:
+            yield from _walk(op.body)
+
+
 def pauli_masks(paulistr: str, pos) -> tuple[int, int, int]:
     """Flip/Z masks and Y count as in statevector.hpp:1252-1279."""
     xm = zm = 0

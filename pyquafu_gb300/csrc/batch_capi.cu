@@ -314,15 +314,15 @@ int enqueue_group(qfvm_batch* b, BatchGroup* g, int mode, uint64_t* nk) {
         const PassDesc& pd = fp.passes[i];
         if (pd.type == PASS_TILE)
             QSV_LAUNCH(launch_tile_pass(arith, fp.T, fp.R, g->psi.p, g->fwd->dpass + i, g->fwd->dsteps, g->fwd->dops,
-                                        g->fpool.p, n, pd.H, items, g->fstride, st),
+                                        g->fpool.p, n, pd.H, items, g->fstride, nullptr, st),
                        "batched pass");
         else if (pd.type == PASS_SMALL)
             QSV_LAUNCH(launch_small(arith, g->psi.p, 1ULL << n, items, n, g->fwd->dops + pd.op_begin, pd.op_count,
-                                    g->fpool.p, g->fstride, st),
+                                    g->fpool.p, g->fstride, nullptr, st),
                        "batched small pass");
         else
             QSV_LAUNCH(launch_globalop(arith, g->psi.p, n, g->fwd->dops + pd.op_begin, g->fpool.p, items, g->fstride,
-                                       st),
+                                       nullptr, st),
                        "batched global op");
     }
     QSV_LAUNCH(launch_expect_seg(storage, g->psi.p, n, items, g->dx, g->dz, g->dy, g->dc, g->doptr, g->nobs, g->epart,
@@ -357,10 +357,10 @@ int enqueue_group(qfvm_batch* b, BatchGroup* g, int mode, uint64_t* nk) {
                        "batched adjoint small pass");
         } else {
             QSV_LAUNCH(launch_globalop(arith, g->psi.p, n, g->rev->dops + pd.op_begin, g->rpool.p, items, g->rstride,
-                                       st),
+                                       nullptr, st),
                        "batched global op");
             QSV_LAUNCH(launch_globalop(arith, g->lam.p, n, g->rev->dops + pd.op_begin, g->rpool.p, items, g->rstride,
-                                       st),
+                                       nullptr, st),
                        "batched global op");
         }
     }

@@ -140,11 +140,11 @@ int run_plan(qfvm_plan* p, qfvm_sv* sv, bool timed = false) {
         cudaError_t e = cudaSuccess;
         if (pd.type == PASS_TILE) {
             e = launch_tile_pass(hp.arith, hp.T, hp.R, sv->d, p->dpass + i, p->dsteps, p->dops, p->dcoef, hp.n, pd.H,
-                                 1, 0, sv->stream);
+                                 1, 0, nullptr, sv->stream);
         } else if (pd.type == PASS_SMALL) {
-            e = launch_small(hp.arith, sv->d, 0, 1, hp.n, p->dops + pd.op_begin, pd.op_count, p->dcoef, 0, sv->stream);
+            e = launch_small(hp.arith, sv->d, 0, 1, hp.n, p->dops + pd.op_begin, pd.op_count, p->dcoef, 0, nullptr, sv->stream);
         } else {
-            e = launch_globalop(hp.arith, sv->d, hp.n, p->dops + pd.op_begin, p->dcoef, 1, 0, sv->stream);
+            e = launch_globalop(hp.arith, sv->d, hp.n, p->dops + pd.op_begin, p->dcoef, 1, 0, nullptr, sv->stream);
         }
         g_launches.fetch_add(1, std::memory_order_relaxed);
         if (e != cudaSuccess) return fail(QFVM_ERR_CUDA, std::string("pass launch: ") + cudaGetErrorString(e));
@@ -788,8 +788,8 @@ int qfvm_adjoint(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int6
                                dvals, 0, st);
             g_launches.fetch_add(1, std::memory_order_relaxed);
         } else {
-            ce = launch_globalop(arith, psi->d, n, rev->dops + pd.op_begin, rev->dcoef, 1, 0, st);
-            if (ce == cudaSuccess) ce = launch_globalop(arith, lam->d, n, rev->dops + pd.op_begin, rev->dcoef, 1, 0, st);
+            ce = launch_globalop(arith, psi->d, n, rev->dops + pd.op_begin, rev->dcoef, 1, 0, nullptr, st);
+            if (ce == cudaSuccess) ce = launch_globalop(arith, lam->d, n, rev->dops + pd.op_begin, rev->dcoef, 1, 0, nullptr, st);
             g_launches.fetch_add(2, std::memory_order_relaxed);
         }
         if (ce != cudaSuccess) return done(fail(QFVM_ERR_CUDA, std::string("adjoint pass: ") + cudaGetErrorString(ce)));

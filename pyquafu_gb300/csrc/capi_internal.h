@@ -83,6 +83,8 @@ struct qfvm_plan {
 };
 
 namespace qsv_capi {
+int make_plan(int n, int precision, const qfvm_op* ops, int64_t n_ops, const double* matpool, int64_t matpool_len,
+              int T, int R, qfvm_plan** out);
 int make_plan_gops(int n, int precision, const std::vector<qsv::GOp>& gops, int T, int R, qfvm_plan** out);
 void free_plan(qfvm_plan* p);
 }  // namespace qsv_capi

@@ -477,7 +477,10 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
                                                         const StepDesc* __restrict__ steps,
                                                         const KOp* __restrict__ ops,
                                                         const typename P::C* __restrict__ coef0,
-                                                        uint64_t cstride, int ishift) {
+                                                        uint64_t cstride, int ishift,
+                                                        const uint8_t* __restrict__ active) {
+    // active (optional): items whose tiles are written back; the others keep
+    // their state (classically controlled blocks of per-shot trajectories)
     // batched runs: tile b belongs to item b >> ishift, whose coefficients
     // start at coef0 + item * cstride (cstride = 0 for a single state)
     constexpr int NT = 1 << (T - R);
@@ -588,10 +591,13 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
             __syncthreads();
         }
 
+        if (active == nullptr || active[b >> ishift]) {
 #pragma unroll
-        for (int k = 0; k < PER; ++k) {
-            const uint32_t s = static_cast<uint32_t>(k * NT) | tid;
-            __stcs(state + (base | choff[s >> L] | (s & lmask)), P::s2g(sm[swz<GB>(static_cast<uint32_t>(k * NT)) ^ stid]));
+            for (int k = 0; k < PER; ++k) {
+                const uint32_t s = static_cast<uint32_t>(k * NT) | tid;
+                __stcs(state + (base | choff[s >> L] | (s & lmask)),
+                       P::s2g(sm[swz<GB>(static_cast<uint32_t>(k * NT)) ^ stid]));
+            }
         }
         __syncthreads();  // the buffer is re-filled by the prefetch two tiles later
     }

@@ -13,7 +13,9 @@ namespace qsv {
 template <class P>
 __global__ void __launch_bounds__(512) k_small(typename P::G* __restrict__ state, uint64_t stride, int n,
                                                const KOp* __restrict__ ops, int nops,
-                                               const typename P::C* __restrict__ coef0, uint64_t cstride) {
+                                               const typename P::C* __restrict__ coef0, uint64_t cstride,
+                                               const uint8_t* __restrict__ active) {
+    if (active && !active[blockIdx.x]) return;  // the whole block: item blockIdx.x keeps its state
     constexpr int GB = P::GBITS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     typename P::S* sm = reinterpret_cast<typename P::S*>(smem_raw);
@@ -36,7 +38,7 @@ __global__ void __launch_bounds__(512) k_small(typename P::G* __restrict__ state
 template <class P>
 __global__ void __launch_bounds__(256) k_globalop(typename P::G* __restrict__ state, int n, int items,
                                                   const KOp* __restrict__ opp, const typename P::C* __restrict__ coef0,
-                                                  uint64_t cstride) {
+                                                  uint64_t cstride, const uint8_t* __restrict__ active) {
     using A = typename P::A;
     using C = typename P::C;
     const KOp op = *opp;
@@ -57,6 +59,7 @@ __global__ void __launch_bounds__(256) k_globalop(typename P::G* __restrict__ st
         uint64_t i = g;
         for (int j = 0; j < k; ++j) i = insert0(i, srt[j]);
         if ((i & op.cthr) != op.cthr) continue;
+        if (active && !active[i >> n]) continue;
         const typename P::C* coef = coef0 + (i >> n) * cstride;
         A in[1 << MAXK];
         for (uint32_t m = 0; m < dim; ++m) {
@@ -307,15 +310,15 @@ bool pass_shape_supported(int precision, int T, int R) {
 
 cudaError_t launch_tile_pass(int precision, int T, int R, void* state, const PassDesc* dpass,
                              const StepDesc* dsteps, const KOp* dops, const void* dcoef, int n, int H,
-                             int items, uint64_t cstride, cudaStream_t st) {
-    if (precision == QFVM_C64) return launch_pass_c64(T, R, state, dpass, dsteps, dops, dcoef, n, H, items, cstride, st);
-    if (precision == QFVM_C128_DS) return launch_pass_ds(T, R, state, dpass, dsteps, dops, dcoef, n, H, items, cstride, st);
-    return launch_pass_c128(T, R, state, dpass, dsteps, dops, dcoef, n, H, items, cstride, st);
+                             int items, uint64_t cstride, const uint8_t* active, cudaStream_t st) {
+    if (precision == QFVM_C64) return launch_pass_c64(T, R, state, dpass, dsteps, dops, dcoef, n, H, items, cstride, active, st);
+    if (precision == QFVM_C128_DS) return launch_pass_ds(T, R, state, dpass, dsteps, dops, dcoef, n, H, items, cstride, active, st);
+    return launch_pass_c128(T, R, state, dpass, dsteps, dops, dcoef, n, H, items, cstride, active, st);
 }
 
 template <class P>
 static cudaError_t launch_small_p(void* state, uint64_t stride, int batch, int n, const KOp* dops, int nops,
-                                  const void* dcoef, uint64_t cstride, cudaStream_t st) {
+                                  const void* dcoef, uint64_t cstride, const uint8_t* active, cudaStream_t st) {
     const int threads = n >= 10 ? 512 : 256;
     const size_t smem = sizeof(typename P::S) << n;
     if (smem > 48 * 1024) {
@@ -324,30 +327,30 @@ static cudaError_t launch_small_p(void* state, uint64_t stride, int batch, int n
         if (e != cudaSuccess) return e;
     }
     k_small<P><<<batch, threads, smem, st>>>(static_cast<typename P::G*>(state), stride, n, dops, nops,
-                                            static_cast<const typename P::C*>(dcoef), cstride);
+                                            static_cast<const typename P::C*>(dcoef), cstride, active);
     return cudaGetLastError();
 }
 
 cudaError_t launch_small(int precision, void* state, uint64_t stride, int batch, int n, const KOp* dops, int nops,
-                         const void* dcoef, uint64_t cstride, cudaStream_t st) {
-    if (precision == QFVM_C64) return launch_small_p<P32>(state, stride, batch, n, dops, nops, dcoef, cstride, st);
-    if (precision == QFVM_C128_DS) return launch_small_p<PDS>(state, stride, batch, n, dops, nops, dcoef, cstride, st);
-    return launch_small_p<P64>(state, stride, batch, n, dops, nops, dcoef, cstride, st);
+                         const void* dcoef, uint64_t cstride, const uint8_t* active, cudaStream_t st) {
+    if (precision == QFVM_C64) return launch_small_p<P32>(state, stride, batch, n, dops, nops, dcoef, cstride, active, st);
+    if (precision == QFVM_C128_DS) return launch_small_p<PDS>(state, stride, batch, n, dops, nops, dcoef, cstride, active, st);
+    return launch_small_p<P64>(state, stride, batch, n, dops, nops, dcoef, cstride, active, st);
 }
 
 cudaError_t launch_globalop(int precision, void* state, int n, const KOp* dop, const void* dcoef, int items,
-                            uint64_t cstride, cudaStream_t st) {
+                            uint64_t cstride, const uint8_t* active, cudaStream_t st) {
     const uint64_t groups = static_cast<uint64_t>(items) << (n - 1);
     const unsigned blocks = static_cast<unsigned>(groups / 256 < 152 * 16 ? (groups + 255) / 256 : 152 * 16);
     if (precision == QFVM_C64)
         k_globalop<P32><<<blocks, 256, 0, st>>>(static_cast<float2*>(state), n, items, dop,
-                                               static_cast<const float*>(dcoef), cstride);
+                                               static_cast<const float*>(dcoef), cstride, active);
     else if (precision == QFVM_C128_DS)
         k_globalop<PDS><<<blocks, 256, 0, st>>>(static_cast<double2*>(state), n, items, dop,
-                                               static_cast<const ds*>(dcoef), cstride);
+                                               static_cast<const ds*>(dcoef), cstride, active);
     else
         k_globalop<P64><<<blocks, 256, 0, st>>>(static_cast<double2*>(state), n, items, dop,
-                                               static_cast<const double*>(dcoef), cstride);
+                                               static_cast<const double*>(dcoef), cstride, active);
     return cudaGetLastError();
 }
 

@@ -20,21 +20,21 @@ bool pass_shape_c64(int T, int R);
 bool pass_shape_ds(int T, int R);
 cudaError_t launch_pass_ds(int T, int R, void* state, const PassDesc* dpass, const StepDesc* dsteps,
                            const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride,
-                            cudaStream_t st);
+                            const uint8_t* active, cudaStream_t st);
 cudaError_t launch_pass_c128(int T, int R, void* state, const PassDesc* dpass, const StepDesc* dsteps,
                              const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride,
-                            cudaStream_t st);
+                            const uint8_t* active, cudaStream_t st);
 cudaError_t launch_pass_c64(int T, int R, void* state, const PassDesc* dpass, const StepDesc* dsteps,
                             const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride,
-                            cudaStream_t st);
+                            const uint8_t* active, cudaStream_t st);
 
 cudaError_t launch_tile_pass(int precision, int T, int R, void* state, const PassDesc* dpass,
                              const StepDesc* dsteps, const KOp* dops, const void* dcoef, int n, int H,
-                             int items, uint64_t cstride, cudaStream_t st);
+                             int items, uint64_t cstride, const uint8_t* active, cudaStream_t st);
 cudaError_t launch_small(int precision, void* state, uint64_t stride, int batch, int n, const KOp* dops, int nops,
-                         const void* dcoef, uint64_t cstride, cudaStream_t st);
+                         const void* dcoef, uint64_t cstride, const uint8_t* active, cudaStream_t st);
 cudaError_t launch_globalop(int precision, void* state, int n, const KOp* dop, const void* dcoef, int items,
-                            uint64_t cstride, cudaStream_t st);
+                            uint64_t cstride, const uint8_t* active, cudaStream_t st);
 cudaError_t launch_set_basis(int precision, void* state, uint64_t N, uint64_t index, cudaStream_t st);
 cudaError_t launch_convert(bool to64, const void* in, void* out, uint64_t n, cudaStream_t st);
 cudaError_t launch_expect_z(int precision, const void* state, uint64_t N, const uint64_t* dzm, int nterms,
@@ -83,4 +83,27 @@ cudaError_t launch_probe_reduce_seg(const double* partial, uint64_t ntiles, int 
                                     int ostride, int ooff, cudaStream_t st);
 cudaError_t launch_slot_gather(const double* vals, int nprobe, int items, const int32_t* sptr, const int32_t* sidx,
                                int nslots, double* grads, cudaStream_t st);
+}  // namespace qsv
+
+namespace qsv {
+// shots.cu: per-shot trajectories (mid-circuit measure / reset / cif)
+struct MeasureSpec {
+    uint8_t q[8];    // measured qubits, outcome bit order
+    uint8_t srt[8];  // the same, ascending
+    uint8_t cb[8];   // classical bits written (measure)
+    int32_t k;       // qubits measured
+    int32_t reset;   // 1: reset (final block 0), 0: measure
+};
+struct CifSpec {
+    uint8_t cb[16];
+    int32_t nc;
+    uint64_t condition;
+};
+int outcome_blocks_per_item(int n, int k);
+cudaError_t launch_measure(void* state, int n, const MeasureSpec& ms, int items, const double* duni, int draw,
+                           int ndraws, uint8_t* dcreg, int ncb, double* dpart, int32_t* doutcome, double* dscale,
+                           cudaStream_t st);
+cudaError_t launch_cif_mask(const uint8_t* dcreg, int ncb, int items, const CifSpec& cs, uint8_t* dactive,
+                            cudaStream_t st);
+cudaError_t launch_items_copy(void* state, int n, int items, const void* psi0, cudaStream_t st);
 }  // namespace qsv

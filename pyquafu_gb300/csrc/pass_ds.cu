@@ -9,7 +9,7 @@ namespace qsv {
 
 cudaError_t launch_pass_ds(int T, int R, void* state, const PassDesc* dpass, const StepDesc* dsteps,
                             const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride,
-                            cudaStream_t st) {
+                            const uint8_t* active, cudaStream_t st) {
     using P = PDS;
     QSV_SHAPES(QSV_LAUNCH_SHAPE)
     return cudaErrorInvalidValue;

@@ -10,7 +10,8 @@ namespace qsv {
 
 template <class P, int T, int R, int NB, int MINB>
 cudaError_t launch_pass_t(void* state, const PassDesc* dpass, const StepDesc* dsteps, const KOp* dops,
-                          const void* dcoef, int n, int H, int items, uint64_t cstride, cudaStream_t st) {
+                          const void* dcoef, int n, int H, int items, uint64_t cstride, const uint8_t* active,
+                          cudaStream_t st) {
     // NB tile buffers + the chunk-offset table
     const size_t smem = NB * (sizeof(typename P::S) << T) + (sizeof(uint64_t) << H);
     static int grid_cap = 0;  // per instantiation: SMs x resident CTAs per SM
@@ -30,7 +31,7 @@ cudaError_t launch_pass_t(void* state, const PassDesc* dpass, const StepDesc* ds
     k_pass<P, T, R, NB, MINB><<<grid, 1 << (T - R), smem, st>>>(static_cast<typename P::G*>(state), tiles, dpass,
                                                                  dsteps, dops,
                                                                  static_cast<const typename P::C*>(dcoef), cstride,
-                                                                 n - T);
+                                                                 n - T, active);
     return cudaGetLastError();
 }
 
@@ -38,6 +39,7 @@ cudaError_t launch_pass_t(void* state, const PassDesc* dpass, const StepDesc* ds
 
 #define QSV_LAUNCH_SHAPE(TT, RR, NBB, MB)                                                                  \
     if (T == TT && R == RR)                                                                                \
-        return launch_pass_t<P, TT, RR, NBB, MB>(state, dpass, dsteps, dops, dcoef, n, H, items, cstride, st);
+        return launch_pass_t<P, TT, RR, NBB, MB>(state, dpass, dsteps, dops, dcoef, n, H, items, cstride, active, \
+                                                 st);
 #define QSV_HAS_SHAPE(TT, RR, NBB, MB) \
     if (T == TT && R == RR) return true;

@@ -235,3 +235,57 @@ def pack(ops) -> tuple[np.ndarray, np.ndarray]:
             r["mat_offset"] = -1
     pool_arr = np.concatenate(pool) if pool else np.zeros(1, dtype=np.complex128)
     return arr, np.ascontiguousarray(pool_arr, dtype=np.complex128)
+
+
+def program_draws(ops) -> int:
+    """Uniform draws one shot of a program consumes (one per measure / reset)."""
+    return sum(1 for o in ops if o.kind in (OP_MEASURE, OP_RESET))
+
+
+def pack_program(ops) -> tuple[np.ndarray, np.ndarray]:
+    """Pack a whole program for qfvm_simulate_shots: gates as in ``pack``,
+    measure (qubits, then classical bits at qubits[8:]), reset, and cif
+    followed by its body (mat_dim = body length).  NOPs are dropped."""
+    flat = []
+    for o in ops:
+        if o.kind == OP_NOP:
+            continue
+        if o.kind == OP_CIF:
+            body = [b for b in o.body if b.kind != OP_NOP]
+            if any(not b.is_gate for b in body):
+                raise ValueError("a cif body holds gates only")
+            flat.append(o)
+            flat.extend(body)
+        else:
+            flat.append(o)
+    gates_arr, pool = pack([o for o in flat if o.is_gate])
+    arr = np.zeros(len(flat), dtype=OP_DTYPE)
+    gi = 0
+    for i, o in enumerate(flat):
+        r = arr[i]
+        if o.is_gate:
+            arr[i] = gates_arr[gi]
+            gi += 1
+            continue
+        r["kind"] = o.kind
+        r["mat_offset"] = -1
+        r["slot"] = -1
+        if o.kind == OP_MEASURE:
+            if len(o.qbits) > 8:
+                raise ValueError("a measure of more than 8 qubits at once")
+            r["nqubits"] = len(o.qbits)
+            r["qubits"][: len(o.qbits)] = o.qbits
+            r["qubits"][8: 8 + len(o.cbits)] = o.cbits
+        elif o.kind == OP_RESET:
+            if len(o.qbits) > 8:
+                raise ValueError("a reset of more than 8 qubits at once")
+            r["nqubits"] = len(o.qbits)
+            r["qubits"][: len(o.qbits)] = o.qbits
+        elif o.kind == OP_CIF:
+            if len(o.cbits) > 16:
+                raise ValueError("cif on more than 16 classical bits")
+            r["nqubits"] = len(o.cbits)
+            r["qubits"][: len(o.cbits)] = o.cbits
+            r["params"][0] = float(o.condition)
+            r["mat_dim"] = sum(1 for b in o.body if b.kind != OP_NOP)
+    return arr, pool

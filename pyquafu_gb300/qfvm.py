@@ -83,16 +83,31 @@ def _count(strings) -> dict:
 
 
 def _gate_ops(ops):
-    out = []
+    return [op for op in ops if op.is_gate and op.kind != ir.OP_NOP]
+
+
+def _has_classical(ops) -> bool:
+    return any(op.kind in (ir.OP_RESET, ir.OP_CIF) for op in ops)
+
+
+def _shots(n: int, ncbits: int, ops, psi: np.ndarray, shots: int):
+    """qfvm_simulate_shots: every shot's outcome and the last shot's state."""
     for op in ops:
-        if op.kind in (ir.OP_MEASURE,):
-            continue
-        if op.kind in (ir.OP_RESET, ir.OP_CIF):
-            raise QfvmError(f"'{op.name}' is not supported by the GB300 engine yet", 4)
-        if op.kind == ir.OP_NOP:
-            continue
-        out.append(op)
-    return out
+        if op.is_gate:
+            ir.validate([op], n)
+        elif op.kind == ir.OP_CIF:
+            ir.validate([b for b in op.body if b.is_gate and b.kind != ir.OP_NOP], n)
+    arr, pool = ir.pack_program(ops)
+    nd = ir.program_draws(ops)
+    uni = _uniforms(shots * nd) if nd else np.zeros(1)
+    out = np.zeros(shots, dtype=np.uint64)
+    final = np.empty(1 << n, dtype=np.complex128)
+    psi_p = nat.dptr(psi.view(np.float64)) if psi.size else None
+    rc = nat.load().qfvm_simulate_shots(n, int(ncbits), nat.vptr(arr), arr.size, nat.dptr(pool.view(np.float64)),
+                                        pool.size, psi_p, int(shots), nat.dptr(uni), nd, nat.u64ptr(out),
+                                        nat.dptr(final.view(np.float64)))
+    nat.check(rc, "simulate_circuit (per-shot trajectories)")
+    return out, final
 
 
 def _run(n: int, ops, state: np.ndarray, given: bool, shots: int) -> np.ndarray:
@@ -115,11 +130,38 @@ def simulate_circuit(circuit, inputstate=None, shots=None):
     circ = ir.read_circuit(circuit)
     psi = _as_state(inputstate)
     given = psi.size != 0
-    if not circ.final_measure:
-        raise QfvmError("circuits with operations after a measurement are not supported by the GB300 engine yet", 4)
     n = _qubits_of(psi.size) if given else circ.num_qubits
     if n < 1:
         raise QfvmError("a circuit needs at least one qubit")
+    if not circ.final_measure:
+        # per-shot branch (qfvm.cpp:104-133): one trajectory per shot; the
+        # returned state is the last shot's
+        if shots < 1:
+            raise QfvmError("circuits with operations after a measurement need shots >= 1", 1)
+        out, final = _shots(n, circ.cbits_num, circ.ops, psi, shots)
+        counts: dict = {}
+        for v in out.tolist():
+            counts[int(v)] = counts.get(int(v), 0) + 1
+        return counts, final
+    if _has_classical(circ.ops):
+        # measures only at the end but resets / cifs before them: one
+        # trajectory with the measures skipped (simulator.hpp:115-125), then
+        # the counts are sampled from its state as for any final measurement
+        prog = [op for op in circ.ops if op.kind != ir.OP_MEASURE]
+        _, final = _shots(n, circ.cbits_num, prog, psi, 1)
+        state = psi if given else final
+        if given:
+            state[:] = final
+        measures = circ.measure_vec
+        outcount: dict = {}
+        if measures and shots > 0:
+            idx = np.zeros(shots, dtype=np.uint64)
+            uni = _uniforms(shots)
+            nat.check(nat.load().qfvm_sampling_statevec(nat.dptr(state.view(np.float64)), state.size,
+                                                        nat.dptr(uni), shots, nat.u64ptr(idx)), "sampling")
+            for s_, c in _count(_bitstrings(idx, measures)).items():
+                outcount[int(s_, 2)] = c
+        return outcount, state
     ops = _gate_ops(circ.ops)
     ir.validate(ops, n)
     state = psi if given else np.empty(1 << n, dtype=np.complex128)

@@ -39,6 +39,11 @@ def op_to_json(o: ir.Op) -> dict:
     if o.matrix is not None:
         m = np.asarray(o.matrix, dtype=np.complex128)
         d["matrix"] = [m.real.tolist(), m.imag.tolist()]
+    if o.qbits or o.cbits:
+        d["qbits"], d["cbits"] = list(o.qbits), list(o.cbits)
+    if o.kind == ir.OP_CIF:
+        d["condition"] = o.condition
+        d["body"] = [op_to_json(b) for b in o.body]
     return d
 
 
@@ -200,6 +205,77 @@ def main():
     qc.measure([3, 1], [0, 1])
     counts_case("partial_measure", qc)
 
+    # circuits with operations after a measurement: the per-shot branch
+    # (qfvm.cpp:104-133), deterministic outcomes; the circuits are those of
+    # tests/quafu/simulator/classic_test.py:25-93 (the input-state case,
+    # classic_test.py:176-185, trips the reference's adopted-buffer bug and is
+    # left out)
+    mid_cases = []
+
+    def mid_case(tag, qc, shots=10):
+        counts, psi = ref.simulate_circuit(qc, np.zeros(0, dtype=np.complex128), shots)
+        circ = ir.read_circuit(qc)
+        mid_cases.append({"tag": tag, "n": qc.num, "cbits": qc.cbits_num, "ops": [op_to_json(o) for o in circ.ops],
+                          "final_measure": circ.final_measure, "shots": shots,
+                          "counts": {str(k): int(v) for k, v in dict(counts).items()}})
+        states[f"mid_{tag}"] = np.asarray(psi)
+
+    qc = QuantumCircuit(2, 2)
+    qc.x(0)
+    qc.measure([0], [0])
+    with qc.cif([0], 1):
+        qc.x(1)
+    qc.measure([1], [1])
+    mid_case("cif_true", qc)
+    qc = QuantumCircuit(2)
+    qc.measure([0], [0])
+    with qc.cif([0], 1):
+        qc.x(1)
+    qc.measure([1], [1])
+    mid_case("cif_false", qc)
+    qc = QuantumCircuit(3, 3)
+    qc.x(0)
+    qc.cx(0, 1)
+    qc.measure([0, 1], [0, 1])
+    with qc.cif([0, 1], 3):
+        qc.x(2)
+    qc.measure([2], [2])
+    mid_case("cif_list_true", qc)
+    qc = QuantumCircuit(3)
+    qc.x(0)
+    qc.cx(0, 1)
+    qc.measure([0, 1], [0, 1])
+    for cond in (0, 1, 2, 4):
+        with qc.cif([0, 1], cond):
+            qc.x(2)
+    qc.measure([2], [2])
+    mid_case("cif_list_false", qc)
+    qc = QuantumCircuit(2)
+    qc.x(0)
+    qc.measure([0], [0])
+    qc.reset([0])
+    qc.measure([0], [1])
+    mid_case("single_reset", qc)
+    qc = QuantumCircuit(4)
+    qc.x(0)
+    qc.cx(0, 1)
+    qc.measure([0, 1], [0, 1])
+    qc.reset([0, 1])
+    qc.measure([0, 1], [2, 3])
+    mid_case("multi_reset", qc)
+    qc = QuantumCircuit(3, 3)
+    qc.x(1)
+    qc.x(2)
+    qc.cx(2, 0)
+    qc.reset([1])
+    qc.x(0)
+    qc.measure([0], [0])
+    with qc.cif([0], 0):  # the reference reads no parameterised gate inside a cif
+        qc.x(1)
+        qc.h(2)
+    qc.measure([1], [1])
+    mid_case("reset_then_cif", qc, shots=1)
+
     # sampling_statevec on basis states: {bitstring: count}
     sampling_cases = []
     for idx, meas in [(5, {0: 0, 1: 1, 2: 2, 3: 3}), (6, {2: 0, 1: 1}), (9, {3: 1, 0: 0}), (12, {3: 0, 2: 1, 0: 2})]:
@@ -303,7 +379,7 @@ def main():
     grad_case("hea6_l3", n, hea(n, 3, 21), terms)
 
     meta = {"cases": out_cases, "apply": apply_cases, "counts": count_cases, "sampling": sampling_cases,
-            "gradients": grad_cases,
+            "gradients": grad_cases, "mid_circuit": mid_cases,
             "generator": "tests/golden/make_golden.py (reference qfvm.cpp via oracle/build_ref.sh)"}
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(meta, f)

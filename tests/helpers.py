@@ -19,7 +19,9 @@ def op_from_json(d) -> ir.Op:
     m = None
     if "matrix" in d:
         m = np.array(d["matrix"][0]) + 1j * np.array(d["matrix"][1])
-    return ir.Op(d["name"], d["kind"], d["qubits"], d["ncontrols"], d["params"], matrix=m, slot=d.get("slot", -1))
+    body = [op_from_json(b) for b in d.get("body", [])]
+    return ir.Op(d["name"], d["kind"], d["qubits"], d["ncontrols"], d["params"], matrix=m, slot=d.get("slot", -1),
+                 qbits=d.get("qbits", ()), cbits=d.get("cbits", ()), condition=d.get("condition", 0), body=body)
 
 
 def load_golden():

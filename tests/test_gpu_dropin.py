@@ -87,7 +87,18 @@ def test_errors_are_raised_not_crashes():
         qbits = [0]
         cbits = [0]
 
+    # a gate after a measurement takes the per-shot branch: it needs shots
     pc = proto(2, [workloads.named("h", (0,))])
     pc.instructions = [M()] + pc.instructions
+    with pytest.raises(qfvm.QfvmError):
+        qfvm.simulate_circuit(pc, None, 0)
+    counts, psi = qfvm.simulate_circuit(pc, None, 10)
+    assert counts == {0: 10} and abs(abs(psi[0]) - 2 ** -0.5) < 1e-15
+
+    class R:
+        name = "reset"
+        pos = [5]
+
+    pc.instructions = [R()] + pc.instructions
     with pytest.raises(qfvm.QfvmError):
         qfvm.simulate_circuit(pc, None, 10)

@@ -93,3 +93,31 @@ def test_known_answers_bell():
 
     psi = oracle.simulate(2, [workloads.named("h", (0,)), workloads.named("cx", (0, 1), ncontrols=1)])
     np.testing.assert_allclose(np.abs(psi) ** 2, [0.5, 0, 0, 0.5], atol=1e-15)
+
+
+def test_mid_circuit_golden(golden):
+    """Per-shot trajectories (qfvm.cpp:104-133) restated by the oracle agree
+    with the reference's counts and last-shot states; the circuits are the
+    reference's own classic_test.py cases (deterministic outcomes)."""
+    meta, states = golden
+    rng = np.random.default_rng(0)
+    for case in meta["mid_circuit"]:
+        ops = [helpers.op_from_json(d) for d in case["ops"]]
+        nd = sum(1 for o in ops if o.kind in (40, 41))
+        if case["final_measure"]:
+            continue
+        outcomes, psi = oracle.simulate_shots(case["n"], ops, case["cbits"], rng.random((case["shots"], nd)))
+        counts = {}
+        for v in outcomes:
+            counts[str(v)] = counts.get(str(v), 0) + 1
+        assert counts == case["counts"], case["tag"]
+        assert np.max(np.abs(psi - states["mid_" + case["tag"]])) < 1e-13, case["tag"]
+
+
+def test_outcome_choice_rule():
+    # first outcome m with u * total < cum[m]; zero-probability outcomes are
+    # never chosen, even at u = 0 or just below 1
+    assert oracle.choose_outcome([0.0, 0.5, 0.5], 0.0) == 1
+    assert oracle.choose_outcome([0.25, 0.25, 0.5, 0.0], 0.5) == 2
+    assert oracle.choose_outcome([0.25, 0.25, 0.5, 0.0], 0.9999999999999999) == 2
+    assert oracle.choose_outcome([1.0, 0.0], 0.3) == 0
