@@ -430,6 +430,43 @@ def cpu_batch_sample(groups, obs, seconds):
                       f"adjoint; rate scaled to the batch's size mix by 2^n"}
 
 
+def measure_trajectories(n=18, shots=4096, cpu=True):
+    """Per-shot trajectories: a random-layer circuit on n qubits with a
+    measurement of two qubits, a reset and a classically controlled block in
+    the middle, then a final measurement; every shot is one trajectory (the
+    per-shot branch of simulate_circuit), all shots through one call."""
+    from pyquafu_gb300 import ir, qfvm, workloads
+
+    ops = workloads.random_layers(n, 6, seed=7)
+    ops.append(ir.Op("measure", ir.OP_MEASURE, qbits=[0, 1], cbits=[0, 1]))
+    ops.append(ir.Op("reset", ir.OP_RESET, qbits=[2]))
+    ops.append(ir.Op("cif", ir.OP_CIF, cbits=[0, 1], condition=3,
+                     body=[workloads.named("x", (2,)), workloads.named("h", (3,))]))
+    ops += workloads.random_layers(n, 6, seed=8)
+    ops.append(ir.Op("measure", ir.OP_MEASURE, qbits=list(range(4)), cbits=list(range(2, 6))))
+    empty = np.zeros(0, dtype=np.complex128)
+    qfvm._shots(n, 6, ops, empty, 64)  # warm-up
+    t0 = time.perf_counter()
+    out, _ = qfvm._shots(n, 6, ops, empty, shots)
+    dt = time.perf_counter() - t0
+    res = {"workload": f"random_layers_{n}q_12layers_midcircuit_measure_reset_cif", "shots": shots,
+           "s_per_call": round(dt, 4), "shots_per_s": round(shots / dt, 1),
+           "distinct_outcomes": int(len(set(out.tolist())))}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        oracle.build()
+        k = 4
+        uni = np.random.default_rng(0).random((k, ir.program_draws(ops)))
+        t1 = time.perf_counter()
+        oracle.simulate_shots(n, ops, 6, uni)
+        cdt = (time.perf_counter() - t1) / k
+        res["cpu_baseline"] = {"value": round(1.0 / cdt, 2), "unit": "shots/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": f"{k} shots through the oracle's per-shot restatement"}
+    return res
+
+
 def measure_qnn(steps=5, warmup=3, ps_forwards=20, tune=True):
     """QNN training step: 1024 samples x 16 qubits, 12 HEA layers (384 shared
     weights), MSE of <Z_0> against sign(w . x) labels; forward and adjoint
@@ -491,7 +528,17 @@ def measure_qnn(steps=5, warmup=3, ps_forwards=20, tune=True):
     fwd_s = (time.perf_counter() - t1) / ps_forwards
     st.close()
     ps_step = B * (1 + 2 * nw) * fwd_s
+    # the same parameter-shift algorithm with every shifted evaluation an
+    # item of a batched run (4 samples timed, extrapolated to the batch)
+    sub = 4
+    gradients.jacobian_param_shift(n, ops, [(1.0, "Z", [0])], vals[:1], "c64")  # warm-up
+    t2 = time.perf_counter()
+    gradients.jacobian_param_shift(n, ops, [(1.0, "Z", [0])], vals[:sub], "c64")
+    psb = (time.perf_counter() - t2) / sub * B
     return {"workload": "qnn_1024x16q_12hea_layers_384_weights_mse_z0_c64",
+            "param_shift_batched": {"samples_timed": sub, "evaluations_per_sample": 1 + 2 * nw,
+                                    "s_per_step_extrapolated": round(psb, 2),
+                                    "adjoint_speedup": round(psb / dt, 1)},
             "s_per_step": round(dt, 5), "steps_per_s": round(1 / dt, 2),
             "device_ms_forward_adjoint": round(dev_s * 1e3, 3),
             "algorithmic_gb": round(nbytes / 1e9, 3), "achieved_gbps": round(nbytes / dev_s / 1e9, 1),
@@ -609,7 +656,8 @@ def run_gpu(args):
     if not args.skip_batch:
         batched = {"uneven_2048": measure_uneven_batch(cpu=rank == 0 and not args.skip_cpu,
                                                        tune=not args.no_autotune),
-                   "qnn_training_step": measure_qnn(tune=not args.no_autotune)}
+                   "qnn_training_step": measure_qnn(tune=not args.no_autotune),
+                   "trajectories": measure_trajectories(cpu=rank == 0 and not args.skip_cpu)}
 
     cpu = None
     if rank == 0 and not args.skip_cpu:

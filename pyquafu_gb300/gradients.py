@@ -143,3 +143,42 @@ def grad_para_shift(qc, hamiltonian, precision="c128"):
     para_grads = qc._calc_parameter_grads()
     n, gates, _ = _slotted_ops(qc)
     return _assemble(para_grads, param_shift(n, gates, _circuit_terms(hamiltonian), precision))
+
+
+# ---------------------------- batched parameter shift ----------------------------
+
+
+def jacobian_param_shift(n: int, ops, observables, values, precision="c64", chunk_items: int = 8192):
+    """The reference's parameter-shift Jacobian (ParamShift.grad,
+    param_shift.py:47-78, looped over samples and observables in vjp.py:60-103)
+    on the batched engine: every shifted evaluation (value[s] +- pi/2, one slot
+    at a time) is one item of a batch run, and all observables of an item come
+    from the same run.  values: (batch, slots).  Returns (expectation values
+    (batch, n_obs), Jacobian (batch, n_obs, slots))."""
+    from .batch import BatchSession
+
+    values = np.atleast_2d(np.asarray(values, dtype=np.float64))
+    b, s = values.shape
+    gates = [o for o in ops if o.is_gate]
+    # per sample: the unshifted point, then +pi/2 and -pi/2 on every slot
+    shifts = np.concatenate([np.zeros((1, s)), np.eye(s) * (np.pi / 2), -np.eye(s) * (np.pi / 2)])
+    per = shifts.shape[0]
+    evals = (values[:, None, :] + shifts[None, :, :]).reshape(b * per, s)
+    out = []
+    sessions = {}
+    try:
+        for c0 in range(0, evals.shape[0], chunk_items):
+            chunk = evals[c0: c0 + chunk_items]
+            bs = sessions.get(chunk.shape[0])
+            if bs is None:
+                bs = BatchSession(precision, grads=False)
+                bs.add_group(n, gates, observables, chunk.shape[0], s)
+                sessions[chunk.shape[0]] = bs
+            out.append(bs.run([chunk])[0])
+    finally:
+        for bs in sessions.values():
+            bs.close()
+    e = np.concatenate(out).reshape(b, per, -1)
+    expv = e[:, 0, :]
+    jac = (e[:, 1: 1 + s, :] - e[:, 1 + s:, :]) / 2.0  # (batch, slots, n_obs)
+    return expv, np.transpose(jac, (0, 2, 1))

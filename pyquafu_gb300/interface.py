@@ -158,9 +158,13 @@ class TorchTransformer:
     @staticmethod
     def execute(circ, parameters: torch.Tensor, run_fn=None, grad_fn=None, method="adjoint", estimator=None,
                 precision: str = "c64"):
-        """(batch, n_variables) variable values -> (batch, circ.num) <Z_i>."""
+        """(batch, n_variables) variable values -> (batch, circ.num) <Z_i>.
+        method "adjoint" (or the reference's default "internal"): the batched
+        adjoint engine; "param_shift": the reference's own algorithm (a
+        parameter-shift Jacobian, vjp.py:60-103) with every shifted evaluation
+        an item of one batched run."""
         del run_fn, grad_fn, estimator  # the reference's hooks; the engine runs both directions
-        if method not in ("adjoint", "internal"):
+        if method not in ("adjoint", "internal", "param_shift"):
             raise ValueError(f"unknown method {method!r}")
         key = (id(circ), precision)
         ent = TorchTransformer._bindings.get(key)
@@ -172,9 +176,33 @@ class TorchTransformer:
         if params.shape[1] != bind.num_vars:
             raise ValueError(f"expected {bind.num_vars} parameters per sample, got {params.shape[1]}")
         b = params.shape[0]
+        values = params.to(torch.float64).index_select(1, bind.var_of_slot.to(params.device))
+        if method == "param_shift":
+            return ParamShiftExpval.apply(values, bind, precision)
         runner = runners.get(b)
         if runner is None:
             runner = BatchRunner(bind.n, bind.gates, _z_observables(bind.n), b, len(bind.var_of_slot), precision)
             runners[b] = runner
-        values = params.to(torch.float64).index_select(1, bind.var_of_slot.to(params.device))
         return BatchedExpval.apply(values, runner)
+
+
+class ParamShiftExpval(torch.autograd.Function):
+    """Forward: <Z_i> per sample; backward: grad_out contracted with the
+    parameter-shift Jacobian (compute_vjp, vjp.py:106-140).  Shifts are per
+    gate slot, so a Parameter shared by several gates gets the exact chain-rule
+    sum of its gates' shifts."""
+
+    @staticmethod
+    def forward(ctx, values, bind, precision):  # pylint: disable=arguments-differ
+        from .gradients import jacobian_param_shift
+
+        v = values.detach().to("cpu", torch.float64).numpy()
+        e, jac = jacobian_param_shift(bind.n, bind.gates, _z_observables(bind.n), v, precision)
+        ctx.jac = torch.from_numpy(jac)
+        return torch.from_numpy(e).to(device=values.device, dtype=values.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_out):  # pylint: disable=arguments-differ
+        go = grad_out.detach().to("cpu", torch.float64)
+        gv = torch.einsum("bo,bos->bs", go, ctx.jac)
+        return gv.to(device=grad_out.device, dtype=grad_out.dtype), None, None

@@ -55,3 +55,31 @@ def test_transformer_execute_dropin():
         terms = [(float(go[b, q]), "Z", [q]) for q in range(n)]
         g = oracle.grad_adjoint(n, bound, [o.slot for o in bound], terms)
         np.testing.assert_allclose(params.grad[b].numpy(), g, atol=1e-10)
+
+
+def test_batched_param_shift_matches_adjoint():
+    from pyquafu_gb300 import gradients
+
+    n, batch = 7, 3
+    ops, _ = workloads.hea(n, 2, seed=5)
+    slots = max(o.slot for o in ops) + 1
+    rng = np.random.default_rng(5)
+    v = rng.uniform(0, 2 * np.pi, (batch, slots))
+    obs = [[(1.0, "Z", [q])] for q in range(n)]
+    e, jac = gradients.jacobian_param_shift(n, ops, obs, v, "c128", chunk_items=20)
+    assert jac.shape == (batch, n, slots)
+    for b in range(batch):
+        bound = gradients.bind(ops, v[b])
+        psi = oracle.simulate(n, bound)
+        for q in (0, 3, 6):
+            g = oracle.grad_adjoint(n, bound, [o.slot for o in bound], [(1.0, "Z", [q])])
+            np.testing.assert_allclose(jac[b, q], g, atol=1e-10)
+            assert abs(e[b, q] - oracle.expect_pauli(psi, "Z", [q])) < 1e-12
+    circ = workloads.ProtoCircuit(n, ops, parameters=True)
+    params = torch.tensor(v, requires_grad=True)
+    go = torch.tensor(rng.normal(size=(batch, n)))
+    (TorchTransformer.execute(circ, params, method="param_shift", precision="c128") * go).sum().backward()
+    g_ps = params.grad.clone()
+    params.grad = None
+    (TorchTransformer.execute(circ, params, method="adjoint", precision="c128") * go).sum().backward()
+    np.testing.assert_allclose(g_ps.numpy(), params.grad.numpy(), atol=1e-10)
