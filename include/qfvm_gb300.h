@@ -51,7 +51,9 @@ enum {
     QFVM_OP_MATRIX = 32,  /* targ matrix in the pool: mat_dim x mat_dim, row-major complex128 */
     QFVM_OP_MEASURE = 40, /* qfvm_simulate_shots only (not a gate) */
     QFVM_OP_RESET = 41,   /* qfvm_simulate_shots only */
-    QFVM_OP_CIF = 42      /* qfvm_simulate_shots only */
+    QFVM_OP_CIF = 42,     /* qfvm_simulate_shots only */
+    QFVM_OP_UCHANNEL = 44, /* qfvm_simulate_noise only: unitary channel */
+    QFVM_OP_KRAUS = 45     /* qfvm_simulate_noise only: Kraus channel */
 };
 
 /* Precision of a device state. */
@@ -222,6 +224,30 @@ int qfvm_plan_run_timed(qfvm_plan* plan, qfvm_sv* sv, float* pass_ms, int32_t* p
 int qfvm_simulate_shots(int32_t num_qubits, int32_t num_cbits, const qfvm_op* ops, int64_t n_ops,
                         const double* matpool, int64_t matpool_len, const double* psi_in, int64_t shots,
                         const double* uniforms, int64_t n_draws, uint64_t* outcomes, double* final_state);
+
+/* ---------------------------------------------------------------------------
+ * Noisy trajectories: NoiseSVSimulator.run (quafu/simulators/simulator.py:
+ * 148-225), the shots side by side on the device.  Besides gates, `ops` holds
+ * one-qubit channels on qubits[0] (nqubits = 1, mat_dim = 2) with m =
+ * params[0] operators (1..8) as m consecutive row-major 2x2 matrices at
+ * mat_offset in the pool:
+ *   QFVM_OP_UCHANNEL  unitary channel; the m pool entries after the matrices
+ *                     hold the probabilities (real parts); operator i is
+ *                     picked as np.random.choice does (first i with
+ *                     cumsum(p)[i] / sum(p) > u), noise.py:86-91
+ *   QFVM_OP_KRAUS     Kraus channel, the reference's rule (simulator.py:61-76):
+ *                     s += ||K_i psi|| / ||psi|| in order, the first i with
+ *                     u < s is applied as K_i psi / ||K_i psi||; none: no change
+ * Draws per shot (uniforms[s * n_draws + d]), in the reference's order: one per
+ * unitary channel (op order), one per Kraus channel (op order), one for the
+ * final sample; n_draws = unitary + Kraus channels + 1.  samples[s] is the
+ * basis index measure_samples' scan picks (first index whose running |a|^2
+ * sum exceeds u; 2^n when none); with n_terms > 0, expvals[s * n_terms + t] =
+ * coeffs[t] <P_t> of shot s's final state (FP64).  psi_in NULL: |0...0>. */
+int qfvm_simulate_noise(int32_t num_qubits, const qfvm_op* ops, int64_t n_ops, const double* matpool,
+                        int64_t matpool_len, const double* psi_in, int64_t shots, const double* uniforms,
+                        int64_t n_draws, uint64_t* samples, const uint64_t* x_masks, const uint64_t* z_masks,
+                        const int32_t* y_counts, const double* coeffs, int64_t n_terms, double* expvals);
 
 /* ---------------------------------------------------------------------------
  * Batched runs.  Replaces the reference's per-sample Python loops over

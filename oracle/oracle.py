@@ -223,6 +223,67 @@ def simulate_shots(n, ops, ncbits, uniforms, psi_in=None):
     return outcomes, psi
 
 
+# ------------------------------------------------------------------
+# Noisy trajectories: NoiseSVSimulator (quafu/simulators/simulator.py:148-225).
+# Per shot the reference draws one number per unitary channel while building
+# the sampled circuit (gen_circuit, :196-218, np.random.choice), then one per
+# Kraus channel while running it (_apply_op, :61-76, np.random.rand), then
+# samples one index (sampling_statevec); here those draws are given uniforms
+# in the same order.
+# ------------------------------------------------------------------
+
+
+def _apply_1q(psi, q, m):
+    from types import SimpleNamespace
+
+    apply_op(psi, SimpleNamespace(name="kraus_op", qubits=(q,), ncontrols=0, params=(), matrix=np.asarray(m)))
+
+
+def run_noisy_shot(n, ops, uniforms, psi_in=None):
+    """One shot: (sampled basis index, final state)."""
+    psi = zero_state(n) if psi_in is None or np.size(psi_in) == 0 else np.array(psi_in, dtype=np.complex128)
+    nu = sum(1 for o in ops if o.kind == 44)
+    iu, ik = 0, nu
+    for op in ops:
+        if op.kind == 44:  # UnitaryChannel.gen_gate: np.random.choice(gatelist, p=probs)
+            cdf = np.cumsum(np.asarray(op.params, dtype=np.float64))
+            cdf /= cdf[-1]
+            i = int(np.searchsorted(cdf, uniforms[iu], side="right"))
+            iu += 1
+            _apply_1q(psi, op.qubits[0], op.matrix[min(i, len(cdf) - 1)])
+        elif op.kind == 45:  # KrausChannel in _apply_op: s += ||K psi|| / ||psi||
+            r = uniforms[ik]
+            ik += 1
+            norm0 = np.linalg.norm(psi)
+            s = 0.0
+            for k in op.matrix:
+                t = psi.copy()
+                _apply_1q(t, op.qubits[0], k)
+                norm1 = np.linalg.norm(t)
+                s += norm1 / norm0
+                if r < s:
+                    psi[:] = t / norm1
+                    break
+        elif op.kind == 43:
+            continue
+        else:
+            apply_op(psi, op)
+    idx = int(sample_indices(psi, np.array([uniforms[len(uniforms) - 1]]))[0])
+    return idx, psi
+
+
+def simulate_noise(n, ops, uniforms, psi_in=None, terms=None):
+    """NoiseSVSimulator.run: per shot the sampled index and, with terms
+    [(coeff, paulistr, pos)], coeff * <P> of the shot's final state."""
+    samples, expv = [], []
+    for u in uniforms:
+        idx, psi = run_noisy_shot(n, ops, u, psi_in)
+        samples.append(idx)
+        if terms:
+            expv.append([c * expect_pauli(psi, p, pos) for c, p, pos in terms])
+    return samples, (np.array(expv) if terms else None)
+
+
 def _walk(ops):
     for op in ops:
         yield op

@@ -56,6 +56,9 @@ PROTOTYPES = {
     "qfvm_noalloc_last_error": (ctypes.c_char_p, []),
     "qfvm_simulate_shots": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int64, c_dp,
                                            ctypes.c_int64, c_dp, ctypes.c_int64, c_dp, ctypes.c_int64, c_u64p, c_dp]),
+    "qfvm_simulate_noise": (ctypes.c_int, [ctypes.c_int32, c_vp, ctypes.c_int64, c_dp, ctypes.c_int64, c_dp,
+                                           ctypes.c_int64, c_dp, ctypes.c_int64, c_u64p, c_u64p, c_u64p, c_i32p,
+                                           c_dp, ctypes.c_int64, c_dp]),
     "qfvm_adjoint": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int64, c_dp, ctypes.c_int64,
                                     c_u64p, c_u64p, c_i32p, c_dp, ctypes.c_int64, c_dp, c_dp, c_dp, ctypes.c_int64]),
     "qfvm_sv_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(c_vp)]),

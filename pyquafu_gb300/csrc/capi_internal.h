@@ -87,4 +87,7 @@ int make_plan(int n, int precision, const qfvm_op* ops, int64_t n_ops, const dou
               int T, int R, qfvm_plan** out);
 int make_plan_gops(int n, int precision, const std::vector<qsv::GOp>& gops, int T, int R, qfvm_plan** out);
 void free_plan(qfvm_plan* p);
+// Every pass of a plan over `items` states back to back (shared coefficients;
+// active = optional per-item write-back mask).
+int run_plan_items(qfvm_plan* p, void* state, int items, const uint8_t* active, cudaStream_t st);
 }  // namespace qsv_capi

@@ -107,3 +107,13 @@ cudaError_t launch_cif_mask(const uint8_t* dcreg, int ncb, int items, const CifS
                             cudaStream_t st);
 cudaError_t launch_items_copy(void* state, int n, int items, const void* psi0, cudaStream_t st);
 }  // namespace qsv
+
+namespace qsv {
+// noise.cu: per-shot noise channels on one qubit, per-item final sample
+constexpr int MAX_CHANNEL_OPS = 8;
+cudaError_t launch_channel(void* state, int n, int q, int m, int kraus, const double* dmats, const double* dprobs,
+                           int items, const double* duni, int draw, int ndraws, double* dpart, double* dimat,
+                           cudaStream_t st);
+cudaError_t launch_item_sample(const void* state, int n, int items, const double* duni, int draw, int ndraws,
+                               uint64_t* dout, cudaStream_t st);
+}  // namespace qsv

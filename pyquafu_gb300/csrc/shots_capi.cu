@@ -112,6 +112,10 @@ int parse_program(int n, int ncb, const qfvm_op* ops, int64_t n_ops, const doubl
     return flush();
 }
 
+}  // namespace
+
+namespace qsv_capi {
+
 // Every pass of a plan over `items` states (shared coefficient pool).
 int run_plan_items(qfvm_plan* p, void* state, int items, const uint8_t* active, cudaStream_t st) {
     const HostPlan& hp = p->hp;
@@ -132,7 +136,7 @@ int run_plan_items(qfvm_plan* p, void* state, int items, const uint8_t* active, 
     return QFVM_OK;
 }
 
-}  // namespace
+}  // namespace qsv_capi
 
 extern "C" {
 

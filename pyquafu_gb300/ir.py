@@ -28,6 +28,7 @@ OP_X, OP_Y, OP_Z, OP_H, OP_S, OP_SDG, OP_T, OP_TDG, OP_P = 1, 2, 3, 4, 5, 6, 7, 
 OP_RX, OP_RY, OP_RZ, OP_CX, OP_CZ, OP_CP, OP_CCX, OP_RZZ = 10, 11, 12, 13, 14, 15, 16, 17
 OP_MATRIX = 32
 OP_MEASURE, OP_RESET, OP_CIF, OP_NOP = 40, 41, 42, 43
+OP_UCHANNEL, OP_KRAUS = 44, 45  # noise channels (qfvm_simulate_noise)
 
 NAMED_KIND = {
     "x": OP_X, "y": OP_Y, "z": OP_Z, "h": OP_H, "s": OP_S, "sdg": OP_SDG, "t": OP_T,
@@ -289,3 +290,78 @@ def pack_program(ops) -> tuple[np.ndarray, np.ndarray]:
             r["params"][0] = float(o.condition)
             r["mat_dim"] = sum(1 for b in o.body if b.kind != OP_NOP)
     return arr, pool
+
+
+# ------------------------------------------------------------------ noise
+
+
+def channel_op(kind: int, qubit: int, matrices, probs=None) -> Op:
+    """A one-qubit channel: ``matrices`` (m, 2, 2); unitary channels also
+    carry the probabilities of their operators in ``params``."""
+    mats = np.ascontiguousarray(np.asarray(matrices, dtype=np.complex128).reshape(-1, 2, 2))
+    params = [] if probs is None else [float(p) for p in probs]
+    name = "unitary_channel" if kind == OP_UCHANNEL else "kraus_channel"
+    op = Op(name, kind, (qubit,), 0, (), matrix=mats)
+    op.params = tuple(params)
+    return op
+
+
+def _is_instance_named(obj, names) -> bool:
+    return any(c.__name__ in names for c in type(obj).__mro__)
+
+
+def read_noisy_op(pyop) -> Op | None:
+    """One instruction of a noisy circuit: UnitaryChannel (gatelist + probs,
+    quafu/elements/noise.py:71-91) and KrausChannel (gatelist, :26-68) become
+    channel ops; anything else is read as ``read_op`` does."""
+    if _is_instance_named(pyop, ("UnitaryChannel", "KrausChannel")):
+        mats = [_matrix_of(g) for g in pyop.gatelist]
+        q = pyop.pos[0] if not isinstance(pyop.pos, (int, np.integer)) else int(pyop.pos)
+        if _is_instance_named(pyop, ("UnitaryChannel",)):
+            return channel_op(OP_UCHANNEL, int(q), mats, list(pyop.probs))
+        return channel_op(OP_KRAUS, int(q), mats)
+    return read_op(pyop)
+
+
+def pack_noise(ops) -> tuple[np.ndarray, np.ndarray]:
+    """Pack gates and channels for qfvm_simulate_noise: a channel's matrices
+    (and, for unitary channels, its probabilities as the next m pool
+    entries) go to the matrix pool."""
+    gates_arr, gpool = pack([o for o in ops if o.is_gate])
+    pool = [gpool] if any(o.is_gate and o.matrix is not None for o in ops) else []
+    off = sum(p.size for p in pool)
+    arr = np.zeros(len([o for o in ops if o.kind != OP_NOP]), dtype=OP_DTYPE)
+    gi = 0
+    i = 0
+    for o in ops:
+        if o.kind == OP_NOP:
+            continue
+        if o.is_gate:
+            arr[i] = gates_arr[gi]
+            gi += 1
+        else:
+            if o.kind not in (OP_UCHANNEL, OP_KRAUS):
+                raise ValueError(f"'{o.name}' in a noisy circuit: gates and channels only")
+            m = o.matrix.shape[0]
+            r = arr[i]
+            r["kind"] = o.kind
+            r["nqubits"] = 1
+            r["qubits"][0] = o.qubits[0]
+            r["params"][0] = m
+            r["mat_dim"] = 2
+            r["mat_offset"] = off
+            r["slot"] = -1
+            block = [o.matrix.reshape(-1)]
+            if o.kind == OP_UCHANNEL:
+                block.append(np.asarray(o.params, dtype=np.complex128))
+            block = np.concatenate(block)
+            pool.append(block)
+            off += block.size
+        i += 1
+    pool_arr = np.concatenate(pool) if pool else np.zeros(1, dtype=np.complex128)
+    return arr, np.ascontiguousarray(pool_arr, dtype=np.complex128)
+
+
+def noise_draws(ops) -> int:
+    """Uniforms one noisy shot consumes: one per channel, one for the sample."""
+    return sum(1 for o in ops if o.kind in (OP_UCHANNEL, OP_KRAUS)) + 1

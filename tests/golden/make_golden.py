@@ -276,6 +276,45 @@ def main():
     qc.measure([1], [1])
     mid_case("reset_then_cif", qc, shots=1)
 
+    # noisy trajectories (NoiseSVSimulator.run, simulator.py:174-203) with
+    # numpy's generator seeded: per shot the reference draws one number per
+    # unitary channel, then one per Kraus channel, from np.random (replayable);
+    # its final sample uses the engine's own generator, so counts are recorded
+    # only for circuits whose final state is a basis state.  psi=None: the
+    # reference's `if not psi` rejects numpy arrays on this numpy.
+    from quafu.elements.noise import AmplitudeDamping, BitFlip, Decoherence, Dephasing, Depolarizing
+    from quafu.simulators.simulator import NoiseSVSimulator
+
+    noise_cases = []
+
+    def noise_case(tag, qc, terms, shots, seed, with_counts):
+        hamil = Hamiltonian.from_pauli_list(terms) if terms else None
+        np.random.seed(seed)
+        res = NoiseSVSimulator().run(qc, psi=None, shots=shots, hamiltonian=hamil)
+        ops = []
+        for ins in qc.instructions:
+            o = ir.read_noisy_op(ins)
+            if o is not None and o.kind != ir.OP_MEASURE:
+                ops.append(o)
+        case = {"tag": tag, "n": qc.num, "ops": [op_to_json(o) for o in ops], "shots": shots, "seed": seed,
+                "measures": [[int(q), int(c)] for q, c in qc.measures.items()],
+                "terms": [[t[0], float(t[1])] for t in terms],
+                "pauli_expects": [float(v) for v in res["pauli_expects"]]}
+        if with_counts:
+            case["counts"] = {str(k): int(v) for k, v in dict(res["counts"]).items()}
+        noise_cases.append(case)
+
+    qc = QuantumCircuit(3)
+    qc << eg.HGate(0) << eg.CXGate(0, 1) << Depolarizing(1, 0.3) << BitFlip(2, 0.4)
+    qc << AmplitudeDamping(0, 0.25) << eg.RYGate(2, 0.7) << Dephasing(0, 0.2) << Decoherence(1, 2.0, 30.0, 20.0)
+    qc << eg.CXGate(1, 2) << AmplitudeDamping(2, 0.5)
+    qc.measure([0, 1, 2])
+    noise_case("mixed_channels", qc, [("Z0", 1.0), ("X1 Z2", 0.5), ("Y0 Y1", -0.3), ("Z2", 0.8)], 40, 7, False)
+    qc = QuantumCircuit(2)
+    qc << eg.XGate(0) << BitFlip(1, 0.5) << Depolarizing(0, 0.6)
+    qc.measure([0, 1])
+    noise_case("basis_flips", qc, [("Z0", 1.0), ("Z1", 1.0)], 30, 11, True)
+
     # sampling_statevec on basis states: {bitstring: count}
     sampling_cases = []
     for idx, meas in [(5, {0: 0, 1: 1, 2: 2, 3: 3}), (6, {2: 0, 1: 1}), (9, {3: 1, 0: 0}), (12, {3: 0, 2: 1, 0: 2})]:
@@ -379,7 +418,7 @@ def main():
     grad_case("hea6_l3", n, hea(n, 3, 21), terms)
 
     meta = {"cases": out_cases, "apply": apply_cases, "counts": count_cases, "sampling": sampling_cases,
-            "gradients": grad_cases, "mid_circuit": mid_cases,
+            "gradients": grad_cases, "mid_circuit": mid_cases, "noise": noise_cases,
             "generator": "tests/golden/make_golden.py (reference qfvm.cpp via oracle/build_ref.sh)"}
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(meta, f)

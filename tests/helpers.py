@@ -322,3 +322,27 @@ def random_state(n, seed):
     rng = np.random.default_rng(seed)
     psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
     return (psi / np.linalg.norm(psi)).astype(np.complex128)
+
+
+def noise_uniforms(ops, shots, seed, extra_seed=123):
+    """The reference's draws per noisy shot (numpy's legacy global generator,
+    seeded): one per unitary channel, then one per Kraus channel; then one
+    draw for the final sample from a separate generator."""
+    nch = sum(1 for o in ops if o.kind in (44, 45))
+    np.random.seed(seed)
+    extra = np.random.default_rng(extra_seed)
+    out = np.zeros((shots, nch + 1))
+    for s in range(shots):
+        for k in range(nch):
+            out[s, k] = np.random.random_sample()
+        out[s, nch] = extra.random()
+    return out
+
+
+def noise_terms(pairs):
+    """[("X1 Z2", coeff)] -> [(coeff, "XZ", [1, 2])]."""
+    terms = []
+    for pstr, c in pairs:
+        parts = pstr.split()
+        terms.append((c, "".join(t[0] for t in parts), [int(t[1:]) for t in parts]))
+    return terms

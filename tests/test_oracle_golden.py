@@ -121,3 +121,22 @@ def test_outcome_choice_rule():
     assert oracle.choose_outcome([0.25, 0.25, 0.5, 0.0], 0.5) == 2
     assert oracle.choose_outcome([0.25, 0.25, 0.5, 0.0], 0.9999999999999999) == 2
     assert oracle.choose_outcome([1.0, 0.0], 0.3) == 0
+
+
+def test_noise_golden(golden):
+    """Noisy trajectories (NoiseSVSimulator) restated by the oracle replay the
+    reference's seeded channel draws: averaged Pauli expectations and, where
+    the final state is a basis state, the counts."""
+    meta, _ = golden
+    for case in meta["noise"]:
+        ops = [helpers.op_from_json(d) for d in case["ops"]]
+        uni = helpers.noise_uniforms(ops, case["shots"], case["seed"])
+        terms = helpers.noise_terms(case["terms"])
+        samples, expv = oracle.simulate_noise(case["n"], ops, uni, terms=terms)
+        np.testing.assert_allclose(expv.mean(axis=0), case["pauli_expects"], atol=1e-12, err_msg=case["tag"])
+        if "counts" in case:
+            strings = oracle.bitstrings(samples, [tuple(m) for m in case["measures"]])
+            counts = {}
+            for st in strings:
+                counts[st] = counts.get(st, 0) + 1
+            assert counts == case["counts"], case["tag"]
