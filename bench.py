@@ -467,6 +467,49 @@ def measure_trajectories(n=18, shots=4096, cpu=True):
     return res
 
 
+def measure_noise(n=16, shots=2048, cpu=True):
+    """Noisy trajectories (the NoiseSVSimulator workload): 8 random layers on
+    n qubits with a depolarizing channel and an amplitude-damping channel on
+    every qubit after every second layer; one sample and 3 Pauli terms per
+    shot, all shots in one call."""
+    from pyquafu_gb300 import ir, noise, workloads
+
+    X = np.array([[0, 1], [1, 0]], dtype=complex)
+    Y = np.array([[0, -1j], [1j, 0]])
+    Z = np.diag([1.0, -1.0]).astype(complex)
+    p, g = 0.02, 0.05
+    ops = []
+    for layer in range(8):
+        ops += workloads.random_layers(n, 1, seed=100 + layer)
+        if layer % 2:
+            for q in range(n):
+                ops.append(ir.channel_op(ir.OP_UCHANNEL, q, [X, Y, Z, np.eye(2)], [p / 3, p / 3, p / 3, 1 - p]))
+                ops.append(ir.channel_op(ir.OP_KRAUS, q, [np.array([[1, 0], [0, np.sqrt(1 - g)]]),
+                                                          np.array([[0, np.sqrt(g)], [0, 0]])]))
+    terms = [(1.0, "Z", [0]), (0.5, "ZZ", [0, 1]), (0.25, "X", [n - 1])]
+    noise.simulate_noise(n, ops, 16, terms=terms)  # warm-up
+    t0 = time.perf_counter()
+    samples, expv = noise.simulate_noise(n, ops, shots, terms=terms)
+    dt = time.perf_counter() - t0
+    nch = sum(1 for o in ops if o.kind in (ir.OP_UCHANNEL, ir.OP_KRAUS))
+    res = {"workload": f"random_layers_{n}q_8layers_{nch}channels_depolarizing_amplitude_damping", "shots": shots,
+           "s_per_call": round(dt, 4), "shots_per_s": round(shots / dt, 1),
+           "mean_expectations": [round(float(v), 6) for v in expv.mean(axis=0)]}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        oracle.build()
+        k = 2
+        uni = np.random.default_rng(0).random((k, ir.noise_draws(ops)))
+        t1 = time.perf_counter()
+        oracle.simulate_noise(n, ops, uni, terms=terms)
+        cdt = (time.perf_counter() - t1) / k
+        res["cpu_baseline"] = {"value": round(1.0 / cdt, 2), "unit": "shots/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": f"{k} shots through the oracle's noisy-trajectory restatement"}
+    return res
+
+
 def measure_qnn(steps=5, warmup=3, ps_forwards=20, tune=True):
     """QNN training step: 1024 samples x 16 qubits, 12 HEA layers (384 shared
     weights), MSE of <Z_0> against sign(w . x) labels; forward and adjoint
@@ -657,7 +700,8 @@ def run_gpu(args):
         batched = {"uneven_2048": measure_uneven_batch(cpu=rank == 0 and not args.skip_cpu,
                                                        tune=not args.no_autotune),
                    "qnn_training_step": measure_qnn(tune=not args.no_autotune),
-                   "trajectories": measure_trajectories(cpu=rank == 0 and not args.skip_cpu)}
+                   "trajectories": measure_trajectories(cpu=rank == 0 and not args.skip_cpu),
+                   "noise": measure_noise(cpu=rank == 0 and not args.skip_cpu)}
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
