@@ -74,7 +74,9 @@ def fp64_ops(ops, n):
     for o in ops:
         c = 2.0 ** -o.ncontrols
         name = o.name
-        if name in ("h", "ry", "rx"):
+        if name == "h" and not o.ncontrols:
+            total += 2 * N  # sqrt(2) H: additions only, the factor folded into another gate
+        elif name in ("h", "ry", "rx"):
             total += 4 * N * c
         elif name in ("rz", "rzz"):
             total += 4 * N

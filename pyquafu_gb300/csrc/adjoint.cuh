@@ -240,8 +240,7 @@ __global__ void __launch_bounds__(1 << (T - R), MINB)
                 a[1][j] = P::s2a(sm[1][ad]);
             }
             RoundPhase<P> ph;
-            ph.f = P::one();
-            ph.on = false;
+            ph.reset();
             const KOp* op = ops + sd->op_begin;
             for (int oi = 0; oi < sd->op_count; ++oi) {
                 const KOp o = op[oi];

@@ -108,6 +108,12 @@ __device__ __forceinline__ void reg_op1(RegState<P, R, NS>& a, const KOp& op, co
                 reg_pairs<P, R, NS, TB, CTRL>(a, creg, [](A& x, A& y) { pair_y<P>(x, y); });
             });
             break;
+        case K_HAD:
+            with_bit<R>(op.t0, [&](auto tb) {
+                constexpr int TB = decltype(tb)::value;
+                reg_pairs<P, R, NS, TB, CTRL>(a, creg, [](A& x, A& y) { pair_had<P>(x, y); });
+            });
+            break;
         case K_REAL: {
             const C m0 = P::coef(coef, op.coef), m1 = P::coef(coef, op.coef + 1);
             const C m2 = P::coef(coef, op.coef + 2), m3 = P::coef(coef, op.coef + 3);
@@ -171,11 +177,25 @@ __device__ __forceinline__ void reg_swap(RegState<P, R, NS>& a, const KOp& op) {
 
 // Accumulated thread-uniform phase of a register round (the same for every
 // state of the round: all states see the same gates).
+// Quarter turns (multiples of i) are counted apart from the general phase,
+// so a round whose uniform phases are all quarter turns costs no
+// multiplication: swaps and sign flips at the end.
 template <class P>
 struct RoundPhase {
     typename P::A f;
     bool on;
+    int q4;  // accumulated i^q4
+    __device__ __forceinline__ void reset() {
+        f = P::one();
+        on = false;
+        q4 = 0;
+    }
 };
+
+// quarter turns of a special phase: -1 = i^2, i = i^1, -i = i^3
+__device__ __forceinline__ int special_quarters(int sp) { return sp == SP_NEG1 ? 2 : (sp == SP_I ? 1 : 3); }
+// the special-phase code of i^q (q = 1, 2, 3)
+__device__ __forceinline__ int quarters_special(int q) { return q == 2 ? SP_NEG1 : (q == 1 ? SP_I : SP_NEGI); }
 
 template <class P>
 __device__ __forceinline__ void phase_mul(typename P::A& f, typename P::C dr, typename P::C di) {
@@ -197,6 +217,10 @@ __device__ __forceinline__ void reg_diag(RegState<P, R, NS>& a, const KOp& op, u
     const bool d0one = (op.flags & F_D0_ONE) != 0;
     if (op.flags & F_UNIFORM) {
         if (pt == 0 && d0one) return;
+        if (pt == 1 && (op.flags & F_D1_SPEC)) {  // d0 = 1, d1 a quarter turn
+            ph.q4 += special_quarters(op.special);
+            return;
+        }
         const uint32_t o = op.coef + (pt ? 2u : 0u);
         phase_mul<P>(ph.f, P::coef(coef, o), P::coef(coef, o + 1));
         ph.on = true;
@@ -209,6 +233,15 @@ __device__ __forceinline__ void reg_diag(RegState<P, R, NS>& a, const KOp& op, u
             for (int h = 0; h < 2; ++h) {
                 const int idx = pt ^ h;
                 if (idx == 0 && d0one) continue;
+                if (idx == 1 && (op.flags & F_D1_SPEC)) {  // quarter turn: swaps and sign flips only
+#pragma unroll
+                    for (int j = 0; j < (1 << R); ++j)
+                        if (((j >> TB) & 1) == h) {
+#pragma unroll
+                            for (int s = 0; s < NS; ++s) amp_special<P>(a[s][j], op.special);
+                        }
+                    continue;
+                }
                 const uint32_t o = op.coef + (idx ? 2u : 0u);
                 const C dr = P::coef(coef, o), di = P::coef(coef, o + 1), ndi = P::cneg(di);
 #pragma unroll
@@ -258,12 +291,23 @@ __device__ __forceinline__ void reg_apply(RegState<P, R, NS>& a, const KOp& op, 
 // Applies a round's accumulated phase to every state.
 template <class P, int R, int NS>
 __device__ __forceinline__ void reg_finish_phase(RegState<P, R, NS>& a, const RoundPhase<P>& ph) {
-    if (!ph.on) return;
-    const typename P::C nfi = P::cneg(ph.f.y);
+    const int q = ph.q4 & 3;
+    if (!ph.on) {
+        if (q == 0) return;
+        const int sp = quarters_special(q);
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+#pragma unroll
+            for (int j = 0; j < (1 << R); ++j) amp_special<P>(a[s][j], sp);
+        return;
+    }
+    typename P::A f = ph.f;
+    if (q) amp_special<P>(f, quarters_special(q));  // fold i^q into the phase: once per thread
+    const typename P::C nfi = P::cneg(f.y);
 #pragma unroll
     for (int s = 0; s < NS; ++s)
 #pragma unroll
-        for (int j = 0; j < (1 << R); ++j) amp_phase<P>(a[s][j], ph.f.x, ph.f.y, nfi);
+        for (int j = 0; j < (1 << R); ++j) amp_phase<P>(a[s][j], f.x, f.y, nfi);
 }
 
 // ---------------------------------------------------------------------------
@@ -393,6 +437,7 @@ __device__ __forceinline__ void small_apply(typename P::S* sm, int n, const KOp&
                         break;
                     }
                     case K_Y: pair_y<P>(x, y); break;
+                    case K_HAD: pair_had<P>(x, y); break;
                     case K_REAL: pair_real<P>(x, y, m[0], m[1], m[2], m[3]); break;
                     case K_RX: pair_rx<P>(x, y, m[0], m[1], m[2]); break;
                     case K_DENSE: pair_dense<P>(x, y, m, nmi); break;
@@ -571,8 +616,7 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
             const KOp* op = ops + sd->op_begin;
             const int nop = sd->op_count;
             RoundPhase<P> ph;
-            ph.f = P::one();
-            ph.on = false;
+            ph.reset();
             for (int oi = 0; oi < nop; ++oi) {
                 const KOp o = op[oi];
                 reg_apply<P, R, 1>(a, o, gthr, coef, ph);

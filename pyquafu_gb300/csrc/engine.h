@@ -24,7 +24,8 @@ enum GKind : uint8_t {
     K_SWAP = 7,   // exchange qubits t0 and t1
     K_DENSE2 = 8, // 4x4 complex on (t0 = bit 0, t1 = bit 1), 32 coefs
     K_DENSEK = 9, // 2^k x 2^k complex on tk[0..k-1] (bit j = tk[j]), 2*4^k coefs
-    K_PROBE = 10  // adjoint sweep: accumulate Im<lam| Q |psi> (reads both states, changes neither)
+    K_PROBE = 10, // adjoint sweep: accumulate Im<lam| Q |psi> (reads both states, changes neither)
+    K_HAD = 11    // sqrt(2) H = [[1, 1], [1, -1]] on t0, no coefficients (see unnormalize_hadamards)
 };
 
 // DIAG flags
@@ -166,6 +167,11 @@ GOp gop_dagger(const GOp& g);
 // every value.  Returns false (with a message) for a slotted gate that
 // cannot be re-bound on the device.
 bool unfix_bound(std::vector<GOp>* gops, std::string* err);
+// Plain simulation plans: uncontrolled Hadamards become K_HAD (additions only)
+// and their 1/sqrt(2) factors, a global scalar, are folded into the
+// coefficients of other uncontrolled dense or diagonal gates of the list.
+// Hadamards whose factor finds no such gate stay as they are.
+void unnormalize_hadamards(std::vector<GOp>* gops);
 // Coefficients of a bindable gate kind at angle th (2 or 4 doubles).
 int bind_coef(int kind, double th, double* c);
 // Gate-equivalent bytes of one gop: 2 * bytes per amplitude * amplitudes it

@@ -838,4 +838,60 @@ bool unfix_bound(std::vector<GOp>* gops, std::string* err) {
     return true;
 }
 
+namespace {
+
+bool is_plain_hadamard(const GOp& g) {
+    const double h = 1. / std::sqrt(2.);
+    return g.kind == K_REAL && g.cmask == 0 && g.slot < 0 && g.bkind == 0 && g.coef.size() == 4 &&
+           g.coef[0] == h && g.coef[1] == h && g.coef[2] == h && g.coef[3] == -h;
+}
+
+// a gate that touches every amplitude through its coefficients alone, so a
+// scalar multiplies into them exactly where it would multiply the state
+bool can_absorb_scalar(const GOp& g) {
+    if (g.cmask != 0 || g.slot >= 0 || g.bkind != 0) return false;
+    if (g.kind == K_REAL || g.kind == K_RX || g.kind == K_DENSE) return !is_plain_hadamard(g);
+    if (g.kind == K_DIAG) return (g.flags & (F_D0_ONE | F_D1_SPEC)) == 0;
+    return false;
+}
+
+void scale_coefs(GOp& g, int halves) {
+    // (1/sqrt(2))^halves = 2^(-halves/2), one rounding when halves is odd
+    double f = std::ldexp(1.0, -(halves / 2));
+    if (halves & 1) f *= 1. / std::sqrt(2.);
+    for (double& c : g.coef) c *= f;
+}
+
+}  // namespace
+
+void unnormalize_hadamards(std::vector<GOp>* gops) {
+    constexpr int MAX_PENDING = 256;  // keeps |amplitudes| below 2^128 between absorptions
+    std::vector<size_t> pending;
+    int last = -1;
+    for (size_t i = 0; i < gops->size(); ++i) {
+        GOp& g = (*gops)[i];
+        if (is_plain_hadamard(g) && static_cast<int>(pending.size()) < MAX_PENDING) {
+            pending.push_back(i);
+        } else if (can_absorb_scalar(g)) {
+            if (!pending.empty()) {
+                scale_coefs(g, static_cast<int>(pending.size()));
+                for (size_t k : pending) {
+                    (*gops)[k].kind = K_HAD;
+                    (*gops)[k].coef.clear();
+                }
+                pending.clear();
+            }
+            last = static_cast<int>(i);
+        }
+    }
+    if (!pending.empty() && last >= 0) {
+        // a global scalar commutes with every gate: an earlier gate takes it
+        scale_coefs((*gops)[static_cast<size_t>(last)], static_cast<int>(pending.size()));
+        for (size_t k : pending) {
+            (*gops)[k].kind = K_HAD;
+            (*gops)[k].coef.clear();
+        }
+    }
+}
+
 }  // namespace qsv

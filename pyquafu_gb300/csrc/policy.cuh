@@ -223,6 +223,18 @@ __device__ __forceinline__ void amp_special(typename P::A& a, int sp) {
     a = na;
 }
 
+// sqrt(2) H = [[1, 1], [1, -1]]: additions only
+template <class P>
+__device__ __forceinline__ void pair_had(typename P::A& a, typename P::A& b) {
+    typename P::A na, nb;
+    na.x = P::add(a.x, b.x);
+    na.y = P::add(a.y, b.y);
+    nb.x = P::add(a.x, P::neg(b.x));
+    nb.y = P::add(a.y, P::neg(b.y));
+    a = na;
+    b = nb;
+}
+
 // Y = [[0, -i], [i, 0]]
 template <class P>
 __device__ __forceinline__ void pair_y(typename P::A& a, typename P::A& b) {

@@ -44,7 +44,7 @@ KOP_DT = np.dtype([("kind", "u1"), ("flags", "u1"), ("special", "u1"), ("k", "u1
                   align=True)
 assert PASS_DT.itemsize == 56 and STEP_DT.itemsize == 100 and KOP_DT.itemsize == 48
 
-K_DENSE, K_REAL, K_RX, K_DIAG, K_X, K_Y, K_SWAP, K_DENSE2, K_DENSEK, K_PROBE = range(1, 11)
+K_DENSE, K_REAL, K_RX, K_DIAG, K_X, K_Y, K_SWAP, K_DENSE2, K_DENSEK, K_PROBE, K_HAD = range(1, 12)
 PASS_TILE, PASS_SMALL, PASS_GLOBALOP = 0, 1, 2
 STEP_ROUND, STEP_SMEM = 0, 1
 
@@ -161,6 +161,8 @@ def apply_global(psi, kind, t, cmask, pmask, flags, special, coef, off, tk=()):
         na, nb = b, a
     elif kind == K_Y:
         na, nb = -1j * b, 1j * a
+    elif kind == K_HAD:
+        na, nb = a + b, a - b
     elif kind == K_REAL:
         m = coef[off:off + 4]
         na, nb = m[0] * a + m[1] * b, m[2] * a + m[3] * b

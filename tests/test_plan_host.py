@@ -95,3 +95,26 @@ def test_adjoint_sweep_plan(n, precision):
     ep = oracle.energy(n, [workloads.named("rzz", (0, n - 1), (0.7 + h,)) if o is ops[3] else o for o in ops], terms)
     em = oracle.energy(n, [workloads.named("rzz", (0, n - 1), (0.7 - h,)) if o is ops[3] else o for o in ops], terms)
     assert abs(got[rzz_slot] - (ep - em) / (2 * h)) < 1e-8
+
+
+def test_unnormalized_hadamards_fold_into_other_gates():
+    """Plain plans turn uncontrolled Hadamards into additions and fold their
+    1/sqrt(2) factors into other gates' coefficients: same state."""
+    from pyquafu_gb300 import ir
+
+    n = 6
+    ops = []
+    for layer in range(5):
+        ops += [workloads.named("h", (q,)) for q in range(n)]
+        ops += [ir.Op("ry", ir.OP_RY, (layer % n,), 0, (0.3 + layer,))]
+        ops += [workloads.named("cx", (q, q + 1), ncontrols=1) for q in range(n - 1)]
+    plan = helpers.host_plan(n, ops)
+    kinds = [int(k) for k in plan["ops"]["kind"]]
+    assert kinds.count(helpers.K_HAD) == 5 * n
+    psi = helpers.interpret(plan, oracle.zero_state(n))
+    assert np.max(np.abs(psi - oracle.simulate(n, ops))) < 1e-13
+    # no gate to take the factor: the Hadamards stay normalized
+    only_h = [workloads.named("h", (q,)) for q in range(n)]
+    plan = helpers.host_plan(n, only_h)
+    assert helpers.K_HAD not in [int(k) for k in plan["ops"]["kind"]]
+    assert np.max(np.abs(helpers.interpret(plan, oracle.zero_state(n)) - oracle.simulate(n, only_h))) < 1e-14
