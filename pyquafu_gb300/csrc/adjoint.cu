@@ -160,11 +160,11 @@ cudaError_t launch_small2_p(void* psi, void* lam, int n, const KOp* dops, int no
 // shapes of the two-state pass: X(T, R, NB, MINB) as for the one-state pass
 #define QSV_SHAPES_P64(X) X(11, 4, 2, 1) X(11, 3, 1, 2)
 #define QSV_SHAPES_PDS(X) X(11, 4, 2, 1)
-#define QSV_SHAPES_P32(X) X(12, 5, 2, 1) X(12, 4, 1, 2) X(11, 4, 1, 4)
+#define QSV_SHAPES_P32(X) X(12, 4, 1, 2) X(11, 4, 1, 4) X(13, 4, 1, 1)
 
 void adjoint_shape(int arith, int* T, int* R) {
     if (arith == QFVM_C64) {
-        *T = 12;
+        *T = 13;
         *R = 4;
     } else if (arith == QFVM_C128_DS) {
         *T = 11;
