@@ -83,8 +83,8 @@ __device__ __forceinline__ typename ProbeMath<P>::T reg_probe(const typename P::
                                                               const typename P::A (&lam)[1 << R], const KOp& op,
                                                               uint64_t gthr) {
     using T = typename ProbeMath<P>::T;
-    if ((gthr & op.cthr) != op.cthr) return T(0);
-    const int pt = __popcll(gthr & op.pthr) & 1;
+    if ((op.flags & F_TCTRL) && (gthr & op.cthr) != op.cthr) return T(0);
+    const int pt = (op.flags & F_TPAR) ? (__popcll(gthr & op.pthr) & 1) : 0;
     T ar = T(0), ai = T(0);
     const uint32_t x = op.xreg, z = op.preg, c = op.creg;
     if (x == 0) {
@@ -249,8 +249,16 @@ __global__ void __launch_bounds__(1 << (T - R), MINB)
                     // probe (a product of conj(lam) and psi) is unaffected by
                     // them; the warp sum runs in the probe type (FP32 for
                     // complex64), FP64 from the warp total on
-                    const double v = static_cast<double>(warp_sum(reg_probe<P, R>(a[0], a[1], o, gthr)));
-                    if (lane == 0) pacc[warp * MAX_PASS_PROBES + o.probe] += v * P::coef_d(coef, o.coef);
+                    const auto ws = warp_sum(reg_probe<P, R>(a[0], a[1], o, gthr));
+                    if constexpr (std::is_same<P, P32>::value) {
+                        // the generator scale (1 or -2) is exact in FP32: one
+                        // conversion and one FP64 add per probe and warp
+                        const float vf = ws * P::coef(coef, o.coef);
+                        if (lane == 0) pacc[warp * MAX_PASS_PROBES + o.probe] += static_cast<double>(vf);
+                    } else {
+                        const double v = static_cast<double>(ws);
+                        if (lane == 0) pacc[warp * MAX_PASS_PROBES + o.probe] += v * P::coef_d(coef, o.coef);
+                    }
                 } else {
                     reg_apply<P, R, 2>(a, o, gthr, coef, ph);
                 }

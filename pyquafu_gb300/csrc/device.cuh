@@ -213,7 +213,7 @@ template <class P, int R, int NS>
 __device__ __forceinline__ void reg_diag(RegState<P, R, NS>& a, const KOp& op, uint64_t gthr,
                                          const typename P::C* coef, RoundPhase<P>& ph) {
     using C = typename P::C;
-    const int pt = __popcll(gthr & op.pthr) & 1;
+    const int pt = (op.flags & F_TPAR) ? (__popcll(gthr & op.pthr) & 1) : 0;
     const bool d0one = (op.flags & F_D0_ONE) != 0;
     if (op.flags & F_UNIFORM) {
         if (pt == 0 && d0one) return;
@@ -274,7 +274,7 @@ __device__ __forceinline__ void reg_diag(RegState<P, R, NS>& a, const KOp& op, u
 template <class P, int R, int NS>
 __device__ __forceinline__ void reg_apply(RegState<P, R, NS>& a, const KOp& op, uint64_t gthr,
                                           const typename P::C* coef, RoundPhase<P>& ph) {
-    if ((gthr & op.cthr) != op.cthr) return;  // a control outside the registers is 0
+    if ((op.flags & F_TCTRL) && (gthr & op.cthr) != op.cthr) return;  // a control outside the registers is 0
     switch (op.kind) {
         case K_DIAG: reg_diag<P, R, NS>(a, op, gthr, coef, ph); break;
         case K_SWAP:

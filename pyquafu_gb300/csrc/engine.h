@@ -33,7 +33,9 @@ enum : uint8_t {
     F_D0_ONE = 1,  // d0 == 1 exactly: parity-0 amplitudes are untouched
     F_D1_SPEC = 2,  // d1 is exactly -1, i or -i (see SP_*), applied without arithmetic
     F_UNIFORM = 4,  // register round: no parity / control bit in the registers
-    F_ONEBIT = 8    // register round: one parity bit in the registers (t0), no register control
+    F_ONEBIT = 8,   // register round: one parity bit in the registers (t0), no register control
+    F_TCTRL = 16,   // register round: cthr != 0 (a control on a thread bit)
+    F_TPAR = 32     // register round: pthr != 0 (a parity or Z bit on a thread bit)
 };
 enum : uint8_t { SP_NEG1 = 1, SP_I = 2, SP_NEGI = 3 };
 

@@ -703,6 +703,8 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
                         else ko.pthr |= b;
                     }
                 }
+                if (ko.cthr) ko.flags |= F_TCTRL;
+                if (ko.pthr) ko.flags |= F_TPAR;
                 if (g.kind == K_PROBE) {
                     for (int q = 0; q < n; ++q)
                         if (g.xmask & (1ULL << q)) ko.xreg |= 1u << reg_of_local[local_of[q]];

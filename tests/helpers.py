@@ -286,6 +286,7 @@ def interpret(plan, psi):
             for o in ops:
                 cm = int(o["cthr"])
                 pm = int(o["pthr"])
+                assert bool(int(o["flags"]) & 16) == (cm != 0) and bool(int(o["flags"]) & 32) == (pm != 0)
                 assert all(q not in g_of_reg for q in _bits(o["cthr"])), "register qubit in thread control mask"
                 for b in _bits(o["creg"]):
                     cm |= 1 << g_of_reg[b]
