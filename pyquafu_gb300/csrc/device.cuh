@@ -115,8 +115,9 @@ __device__ __forceinline__ void reg_op1(RegState<P, R, NS>& a, const KOp& op, co
             });
             break;
         case K_REAL: {
-            const C m0 = P::coef(coef, op.coef), m1 = P::coef(coef, op.coef + 1);
-            const C m2 = P::coef(coef, op.coef + 2), m3 = P::coef(coef, op.coef + 3);
+            C mm[4];
+            P::coef4(coef, op.coef, mm);
+            const C m0 = mm[0], m1 = mm[1], m2 = mm[2], m3 = mm[3];
             with_bit<R>(op.t0, [&](auto tb) {
                 constexpr int TB = decltype(tb)::value;
                 reg_pairs<P, R, NS, TB, CTRL>(a, creg, [&](A& x, A& y) { pair_real<P>(x, y, m0, m1, m2, m3); });
@@ -133,9 +134,14 @@ __device__ __forceinline__ void reg_op1(RegState<P, R, NS>& a, const KOp& op, co
             break;
         }
         case K_DENSE: {
-            C m[8], nmi[4];
+            C m[8], nmi[4], lo[4], hi[4];
+            P::coef4(coef, op.coef, lo);
+            P::coef4(coef, op.coef + 4, hi);
 #pragma unroll
-            for (int i = 0; i < 8; ++i) m[i] = P::coef(coef, op.coef + i);
+            for (int i = 0; i < 4; ++i) {
+                m[i] = lo[i];
+                m[4 + i] = hi[i];
+            }
 #pragma unroll
             for (int i = 0; i < 4; ++i) nmi[i] = P::cneg(m[2 * i + 1]);
             with_bit<R>(op.t0, [&](auto tb) {
@@ -227,6 +233,8 @@ __device__ __forceinline__ void reg_diag(RegState<P, R, NS>& a, const KOp& op, u
         return;
     }
     if (op.flags & F_ONEBIT) {
+        C dd[4];
+        P::coef4(coef, op.coef, dd);
         with_bit<R>(op.t0, [&](auto tb) {
             constexpr int TB = decltype(tb)::value;
 #pragma unroll
@@ -242,8 +250,7 @@ __device__ __forceinline__ void reg_diag(RegState<P, R, NS>& a, const KOp& op, u
                         }
                     continue;
                 }
-                const uint32_t o = op.coef + (idx ? 2u : 0u);
-                const C dr = P::coef(coef, o), di = P::coef(coef, o + 1), ndi = P::cneg(di);
+                const C dr = idx ? dd[2] : dd[0], di = idx ? dd[3] : dd[1], ndi = P::cneg(di);
 #pragma unroll
                 for (int j = 0; j < (1 << R); ++j)
                     if (((j >> TB) & 1) == h) {
@@ -255,8 +262,9 @@ __device__ __forceinline__ void reg_diag(RegState<P, R, NS>& a, const KOp& op, u
         return;
     }
     const uint32_t creg = op.creg, preg = op.preg;
-    const C d0r = P::coef(coef, op.coef), d0i = P::coef(coef, op.coef + 1);
-    const C d1r = P::coef(coef, op.coef + 2), d1i = P::coef(coef, op.coef + 3);
+    C dd[4];
+    P::coef4(coef, op.coef, dd);
+    const C d0r = dd[0], d0i = dd[1], d1r = dd[2], d1i = dd[3];
     const C nd0i = P::cneg(d0i), nd1i = P::cneg(d1i);
 #pragma unroll
     for (int j = 0; j < (1 << R); ++j) {

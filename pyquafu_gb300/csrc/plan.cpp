@@ -405,6 +405,9 @@ void gop_targets(const GOp& g, std::vector<int>* t) {
 
 // Copy a gop's coefficients into the pool and return the offset.
 uint32_t push_coef(HostPlan* p, const GOp& g) {
+    // every block starts 4-aligned (the kernels read coefficients four at a
+    // time with 16-byte loads); the padding stays zero
+    while (p->coef.size() % 4) p->coef.push_back(0.0);
     uint32_t off = static_cast<uint32_t>(p->coef.size());
     p->coef.insert(p->coef.end(), g.coef.begin(), g.coef.end());
     if (g.bkind != 0 && g.slot >= 0 && g.kind != K_PROBE)
@@ -511,6 +514,7 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
         plan->T = n;
         plan->R = 0;
         plan->L = n;
+        while (plan->coef.size() % 4) plan->coef.push_back(0.0);  // 4-wide reads of the last block
         return true;
     }
 
@@ -734,6 +738,7 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
         st.pass_bytes += 2.0 * Sb * N;
         pending = rest;
     }
+    while (plan->coef.size() % 4) plan->coef.push_back(0.0);  // 4-wide reads of the last block
     return true;
 }
 

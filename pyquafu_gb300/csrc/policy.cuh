@@ -36,6 +36,15 @@ struct P64 {
     __device__ static __forceinline__ C coef(const C* pool, uint32_t i) { return __ldg(pool + i); }
     __device__ static __forceinline__ A one() { return make_double2(1.0, 0.0); }
     __device__ static __forceinline__ double coef_d(const C* pool, uint32_t i) { return __ldg(pool + i); }
+    // four consecutive coefficients of a 4-aligned block: two 16-byte loads
+    __device__ static __forceinline__ void coef4(const C* pool, uint32_t i, C (&m)[4]) {
+        const double2 a = __ldg(reinterpret_cast<const double2*>(pool + i));
+        const double2 b = __ldg(reinterpret_cast<const double2*>(pool + i) + 1);
+        m[0] = a.x;
+        m[1] = a.y;
+        m[2] = b.x;
+        m[3] = b.y;
+    }
     __device__ static __forceinline__ double to_d_re(A a) { return a.x; }
     __device__ static __forceinline__ double to_d_im(A a) { return a.y; }
     __device__ static __forceinline__ G make_g(double re, double im) { return make_double2(re, im); }
@@ -61,6 +70,14 @@ struct P32 {
     __device__ static __forceinline__ R add(R x, R y) { return __fadd_rn(x, y); }
     __device__ static __forceinline__ R neg(R x) { return __int_as_float(__float_as_int(x) ^ 0x80000000); }
     __device__ static __forceinline__ C cneg(C c) { return -c; }
+    // four consecutive coefficients of a 4-aligned block: one 16-byte load
+    __device__ static __forceinline__ void coef4(const C* pool, uint32_t i, C (&m)[4]) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(pool + i));
+        m[0] = v.x;
+        m[1] = v.y;
+        m[2] = v.z;
+        m[3] = v.w;
+    }
     __device__ static __forceinline__ C coef(const C* pool, uint32_t i) { return __ldg(pool + i); }
     __device__ static __forceinline__ A one() { return make_float2(1.f, 0.f); }
     __device__ static __forceinline__ double coef_d(const C* pool, uint32_t i) {
@@ -151,6 +168,15 @@ struct PDS {
     __device__ static __forceinline__ C coef(const C* pool, uint32_t i) {
         const float2 v = __ldg(reinterpret_cast<const float2*>(pool) + i);
         return {v.x, v.y};
+    }
+    // four consecutive coefficients of a 4-aligned block: two 16-byte loads
+    __device__ static __forceinline__ void coef4(const C* pool, uint32_t i, C (&m)[4]) {
+        const float4 a = __ldg(reinterpret_cast<const float4*>(pool + i));
+        const float4 b = __ldg(reinterpret_cast<const float4*>(pool + i) + 1);
+        m[0] = {a.x, a.y};
+        m[1] = {a.z, a.w};
+        m[2] = {b.x, b.y};
+        m[3] = {b.z, b.w};
     }
 };
 
