@@ -593,6 +593,20 @@ def measure_qnn(steps=5, warmup=3, ps_forwards=20, tune=True):
             "speedup_vs_param_shift": round(ps_step / dt, 1), "autotuned": tuned}
 
 
+def max_over_ranks(value: float, world: int, device: str = "cuda") -> float:
+    """The slowest rank's time: replicas run independent batches, so the
+    job's time is the maximum over ranks (all-reduce MAX; no data-path
+    collective exists)."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def autotune_all(args, n, ops):
     """Pick the fused-pass shapes for every workload of this run with the
     project autotuner (pyquafu_gb300.autotune); tuning time is reported and
@@ -651,13 +665,7 @@ def run_gpu(args):
     main = measure(args.precision, ops, n, args.steps, args.warmup)
     clk = clocks.stop()
     barrier()
-    total_ms = main["ms_per_step"] * args.steps
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(main["ms_per_step"] * args.steps, world, "cuda")
     ms_step = total_ms / args.steps
     S = S_OF[args.precision]
     gb = sum(gate_equiv_bytes(ops, n, S))
