@@ -330,6 +330,32 @@ int qfvm_plan_host_probe_slots(const qfvm_plan* plan, int32_t* slots);
 int qfvm_plan_host_counts(const qfvm_plan* plan, int64_t counts[4], int32_t shape[3]);
 int qfvm_plan_host_copy(const qfvm_plan* plan, void* passes, void* steps, void* kops, double* coef);
 
+/* ---------------------------------------------------------------------------
+ * Circuit-specialised tile passes.  Tile passes of complex128 (FP64) and
+ * complex64 plans are, by default, emitted as straight-line PTX for sm_103a
+ * (every register round unrolled with its targets, controls and coefficient
+ * offsets as constants) and compiled once per distinct pass by the driver;
+ * passes the generator does not handle, and complex128 double-single plans,
+ * run the interpreting kernels.  The environment variable QFVM_JIT=0 turns
+ * specialisation off at start-up.
+ * ------------------------------------------------------------------------- */
+/* enabled: 0/1; nb_*: tile buffers (1 or 2) of one-state / two-state passes;
+ * minb_*: minimum resident CTAs per SM the register budget is set for
+ * (0 = automatic).  Applies to plans prepared afterwards. */
+int qfvm_jit_configure(int32_t enabled, int32_t nb_one, int32_t minb_one, int32_t nb_two, int32_t minb_two);
+int qfvm_jit_get_config(int32_t config[5]);
+/* PTX the generator emits for pass `pass` of a plan (host only; nstates 1 =
+ * forward pass, 2 = reverse-sweep pass with probes).  *len receives the text
+ * length (without the terminating zero); text may be NULL to query it.
+ * QFVM_ERR_UNSUPPORTED when the pass runs interpreted. */
+int qfvm_jit_pass_ptx(const qfvm_plan* plan, int32_t pass, int32_t nstates, char* text, int64_t capacity,
+                      int64_t* len);
+/* Compiles that PTX for sm_103a on the host (no device needed) and writes the
+ * compiler's info log (registers, spills) or error to info. */
+int qfvm_jit_pass_compile(const qfvm_plan* plan, int32_t pass, int32_t nstates, char* info, int64_t capacity);
+/* Passes of a device plan that run specialised (after its first run). */
+int qfvm_jit_plan_passes(const qfvm_plan* plan, int32_t nstates, int64_t* count);
+
 #ifdef __cplusplus
 }
 #endif

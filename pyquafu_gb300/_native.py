@@ -104,6 +104,12 @@ PROTOTYPES = {
     "qfvm_plan_host_binds": (ctypes.c_int, [c_vp, ctypes.POINTER(ctypes.c_int64), c_i32p]),
     "qfvm_plan_host_probe_slots": (ctypes.c_int, [c_vp, c_i32p]),
     "qfvm_plan_host_copy": (ctypes.c_int, [c_vp, c_vp, c_vp, c_vp, c_dp]),
+    "qfvm_jit_configure": (ctypes.c_int, [ctypes.c_int32] * 5),
+    "qfvm_jit_get_config": (ctypes.c_int, [c_i32p]),
+    "qfvm_jit_pass_ptx": (ctypes.c_int, [c_vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_char_p, ctypes.c_int64,
+                                         ctypes.POINTER(ctypes.c_int64)]),
+    "qfvm_jit_plan_passes": (ctypes.c_int, [c_vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]),
+    "qfvm_jit_pass_compile": (ctypes.c_int, [c_vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_char_p, ctypes.c_int64]),
 }
 
 

@@ -21,8 +21,8 @@ LIB = os.path.join(LIBDIR, "libqfvm_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["kernels.cu", "pass_c128.cu", "pass_c64.cu", "pass_ds.cu", "adjoint.cu", "batch.cu", "shots.cu",
-              "noise.cu", "capi.cu", "batch_capi.cu", "shots_capi.cu", "noise_capi.cu", "noalloc.cu"]
-CPP_SOURCES = ["plan.cpp"]
+              "noise.cu", "capi.cu", "batch_capi.cu", "shots_capi.cu", "noise_capi.cu", "noalloc.cu", "jit.cu"]
+CPP_SOURCES = ["plan.cpp", "jit_ptx.cpp"]
 
 
 def nvcc() -> str:
@@ -30,6 +30,17 @@ def nvcc() -> str:
         if cand and os.path.exists(cand):
             return cand
     raise RuntimeError("nvcc not found")
+
+
+def ptx_compiler_lib():
+    """The toolkit's static PTX compiler library (parallel compilation of
+    circuit-specialised passes), or None: the driver then compiles them."""
+    home = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+    for sub in ("lib64", "lib", os.path.join("targets", "sbsa-linux", "lib"), os.path.join("targets", "x86_64-linux", "lib")):
+        f = os.path.join(home, sub, "libnvptxcompiler_static.a")
+        if os.path.exists(f):
+            return f
+    return None
 
 
 def _sources():
@@ -53,12 +64,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
+    ptxc = ptx_compiler_lib()
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
     jobs = []
     for src in _sources():
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         if src.endswith(".cu"):
-            cmd = [cc] + ARCH + common + ["-lineinfo", "-c", src, "-o", obj]
+            extra = ["-DQSV_PTXCOMPILER"] if ptxc and os.path.basename(src) == "jit.cu" else []
+            cmd = [cc] + ARCH + common + extra + ["-lineinfo", "-c", src, "-o", obj]
         else:
             cmd = [cc] + common + ["-x", "c++", "-c", src, "-o", obj]
         jobs.append((cmd, obj))
@@ -75,7 +88,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
         objs = list(ex.map(run, jobs))
     tmp = LIB + ".tmp"
-    link = [cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+    link = [cc] + ARCH + ["-shared", "-o", tmp] + objs + ([ptxc, "-lpthread", "-lm"] if ptxc else []) + ["-lcudart"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(link)}\n{r.stdout}\n{r.stderr}")

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "capi_internal.h"
+#include "jit.h"
 #include "kernels.h"
 
 using namespace qsv;
@@ -176,6 +177,12 @@ int add_group(qfvm_batch* b, int n, const qfvm_op* ops, int64_t n_ops, const dou
         if (rc != QFVM_OK) return bail(rc);
         g->nprobe = static_cast<int>(g->rev->hp.probe_slot.size());
     }
+    {
+        // specialised kernels now: graph captures must not compile
+        std::string jerr;
+        if (jit_prepare(g->fwd, 1, &jerr) || (grads && jit_prepare(g->rev, 2, &jerr)))
+            return bail(fail(QFVM_ERR_CUDA, jerr));
+    }
     cudaStream_t st = g->stream;
     rc = make_pool(g->fwd, arith, g->items, &g->fpool, &g->fstride, st);
     if (rc == QFVM_OK && grads) rc = make_pool(g->rev, arith, g->items, &g->rpool, &g->rstride, st);
@@ -293,6 +300,13 @@ namespace {
         if (e_ != cudaSuccess) return fail(QFVM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e_)); \
         ++*nk;                                                                                         \
     } while (0)
+// a launch that may decline (launched == false: nothing issued, not counted)
+#define QSV_LAUNCH_IF(call, launched, what)                                                             \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess) return fail(QFVM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e_)); \
+        if (launched) ++*nk;                                                                           \
+    } while (0)
 
 // One group's run on its own stream: bind, forward, expectation values; in
 // gradient mode also lam = sum_o w_o O_o psi, the reverse sweep and the slot
@@ -312,11 +326,16 @@ int enqueue_group(qfvm_batch* b, BatchGroup* g, int mode, uint64_t* nk) {
     const HostPlan& fp = g->fwd->hp;
     for (size_t i = 0; i < fp.passes.size(); ++i) {
         const PassDesc& pd = fp.passes[i];
-        if (pd.type == PASS_TILE)
-            QSV_LAUNCH(launch_tile_pass(arith, fp.T, fp.R, g->psi.p, g->fwd->dpass + i, g->fwd->dsteps, g->fwd->dops,
-                                        g->fpool.p, n, pd.H, items, g->fstride, nullptr, st),
-                       "batched pass");
-        else if (pd.type == PASS_SMALL)
+        if (pd.type == PASS_TILE) {
+            bool done = false;
+            QSV_LAUNCH_IF(jit_launch_pass(g->fwd, static_cast<int>(i), g->psi.p, nullptr, g->fpool.p, items,
+                                          g->fstride, nullptr, 0, nullptr, nullptr, st, &done),
+                          done, "batched pass");
+            if (!done)
+                QSV_LAUNCH(launch_tile_pass(arith, fp.T, fp.R, g->psi.p, g->fwd->dpass + i, g->fwd->dsteps,
+                                            g->fwd->dops, g->fpool.p, n, pd.H, items, g->fstride, nullptr, st),
+                           "batched pass");
+        } else if (pd.type == PASS_SMALL)
             QSV_LAUNCH(launch_small(arith, g->psi.p, 1ULL << n, items, n, g->fwd->dops + pd.op_begin, pd.op_count,
                                     g->fpool.p, g->fstride, nullptr, st),
                        "batched small pass");
@@ -342,9 +361,14 @@ int enqueue_group(qfvm_batch* b, BatchGroup* g, int mode, uint64_t* nk) {
         const PassDesc& pd = rp.passes[i];
         if (pd.type == PASS_TILE) {
             int grid = 0;
-            QSV_LAUNCH(launch_pass2(arith, rp.T, rp.R, g->psi.p, g->lam.p, g->rev->dpass + i, g->rev->dsteps, g->rev->dops,
-                                    g->rpool.p, n, pd.H, items, g->rstride, 1, g->partial, &grid, st),
-                       "batched adjoint pass");
+            bool done = false;
+            QSV_LAUNCH_IF(jit_launch_pass(g->rev, static_cast<int>(i), g->psi.p, g->lam.p, g->rpool.p, items,
+                                          g->rstride, nullptr, 1, g->partial, &grid, st, &done),
+                          done, "batched adjoint pass");
+            if (!done)
+                QSV_LAUNCH(launch_pass2(arith, rp.T, rp.R, g->psi.p, g->lam.p, g->rev->dpass + i, g->rev->dsteps,
+                                        g->rev->dops, g->rpool.p, n, pd.H, items, g->rstride, 1, g->partial, &grid, st),
+                           "batched adjoint pass");
             if (pd.nprobe > 0) {
                 const uint64_t tpi = 1ULL << (n - rp.T);
                 QSV_LAUNCH(launch_probe_reduce_seg(g->partial, tpi * items, static_cast<int>(tpi), items, pd.nprobe,

@@ -13,6 +13,7 @@
 #include "kernels.h"
 #include "qfvm_gb300.h"
 #include "capi_internal.h"
+#include "jit.h"
 
 using namespace qsv;
 
@@ -122,6 +123,7 @@ int make_plan_gops(int n, int precision, const std::vector<GOp>& gops, int T, in
 
 void free_plan(qfvm_plan* p) {
     if (!p) return;
+    jit_release(p);
     for (cudaEvent_t e : p->events) cudaEventDestroy(e);
     if (p->dbuf) cudaFree(p->dbuf);
     delete p;
@@ -140,8 +142,12 @@ int run_plan(qfvm_plan* p, qfvm_sv* sv, bool timed = false) {
         const PassDesc& pd = hp.passes[i];
         cudaError_t e = cudaSuccess;
         if (pd.type == PASS_TILE) {
-            e = launch_tile_pass(hp.arith, hp.T, hp.R, sv->d, p->dpass + i, p->dsteps, p->dops, p->dcoef, hp.n, pd.H,
-                                 1, 0, nullptr, sv->stream);
+            bool done = false;
+            e = jit_launch_pass(p, static_cast<int>(i), sv->d, nullptr, p->dcoef, 1, 0, nullptr, 0, nullptr, nullptr,
+                                sv->stream, &done);
+            if (e == cudaSuccess && !done)
+                e = launch_tile_pass(hp.arith, hp.T, hp.R, sv->d, p->dpass + i, p->dsteps, p->dops, p->dcoef, hp.n,
+                                     pd.H, 1, 0, nullptr, sv->stream);
         } else if (pd.type == PASS_SMALL) {
             e = launch_small(hp.arith, sv->d, 0, 1, hp.n, p->dops + pd.op_begin, pd.op_count, p->dcoef, 0, nullptr, sv->stream);
         } else {
@@ -778,8 +784,12 @@ int qfvm_adjoint(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int6
         cudaError_t ce = cudaSuccess;
         if (pd.type == PASS_TILE) {
             int grid = 0;
-            ce = launch_pass2(arith, hp.T, hp.R, psi->d, lam->d, rev->dpass + i, rev->dsteps, rev->dops, rev->dcoef, n, pd.H, 1, 0,
-                              0, dpart, &grid, st);
+            bool done = false;
+            ce = jit_launch_pass(rev, static_cast<int>(i), psi->d, lam->d, rev->dcoef, 1, 0, nullptr, 0, dpart, &grid,
+                                 st, &done);
+            if (ce == cudaSuccess && !done)
+                ce = launch_pass2(arith, hp.T, hp.R, psi->d, lam->d, rev->dpass + i, rev->dsteps, rev->dops, rev->dcoef,
+                                  n, pd.H, 1, 0, 0, dpart, &grid, st);
             g_launches.fetch_add(1, std::memory_order_relaxed);
             if (ce == cudaSuccess && pd.nprobe > 0) {
                 ce = launch_probe_reduce(dpart, grid, pd.nprobe, dvals + pd.probe_base, st);

@@ -80,6 +80,10 @@ struct qfvm_plan {
     qsv::StepDesc* dsteps = nullptr;
     qsv::KOp* dops = nullptr;
     void* dcoef = nullptr;
+    // circuit-specialised kernels of the tile passes (jit.cu), per state
+    // count (index 0: one state, 1: psi + lam); null entries run interpreted
+    std::vector<const void*> jit[2];
+    bool jit_ready[2] = {false, false};
 };
 
 namespace qsv_capi {

@@ -1,0 +1,436 @@
+// Compilation, cache and launch of the circuit-specialised tile passes.
+//
+// The PTX of a pass (jit_ptx.cpp) depends on the circuit's structure only
+// (kinds, targets, masks, coefficient offsets), not on its angles, so one
+// compiled module serves every re-run and every rebinding of a plan.  Modules
+// are cached process-wide by their PTX text and kept until exit (CUDA graphs
+// may hold their kernels).  The driver API is reached through the runtime's
+// entry-point query, so the library does not link libcuda itself.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "capi_internal.h"
+#include "jit.h"
+
+#ifdef QSV_PTXCOMPILER
+#include <nvPTXCompiler.h>
+#endif
+
+namespace qsv {
+namespace {
+
+struct Driver {
+    bool ok = false;
+    std::string err;
+    CUresult (*load)(CUmodule*, const void*, unsigned int, CUjit_option*, void**) = nullptr;
+    CUresult (*get_function)(CUfunction*, CUmodule, const char*) = nullptr;
+    CUresult (*set_attribute)(CUfunction, CUfunction_attribute, int) = nullptr;
+    CUresult (*launch)(CUfunction, unsigned int, unsigned int, unsigned int, unsigned int, unsigned int, unsigned int,
+                       unsigned int, CUstream, void**, void**) = nullptr;
+    CUresult (*occupancy)(int*, CUfunction, int, size_t) = nullptr;
+    CUresult (*error_string)(CUresult, const char**) = nullptr;
+};
+
+template <class F>
+bool entry(const char* name, F* fn, std::string* err) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || p == nullptr) {
+        *err = std::string("driver entry point not found: ") + name;
+        return false;
+    }
+    *fn = reinterpret_cast<F>(p);
+    return true;
+}
+
+Driver& driver() {
+    static Driver d = [] {
+        Driver x;
+        x.ok = entry("cuModuleLoadDataEx", &x.load, &x.err) && entry("cuModuleGetFunction", &x.get_function, &x.err) &&
+               entry("cuFuncSetAttribute", &x.set_attribute, &x.err) && entry("cuLaunchKernel", &x.launch, &x.err) &&
+               entry("cuOccupancyMaxActiveBlocksPerMultiprocessor", &x.occupancy, &x.err) &&
+               entry("cuGetErrorString", &x.error_string, &x.err);
+        return x;
+    }();
+    return d;
+}
+
+std::string cu_error(CUresult r) {
+    const char* s = nullptr;
+    if (driver().error_string) driver().error_string(r, &s);
+    return s ? s : "unknown driver error";
+}
+
+struct Kernel {
+    CUmodule mod = nullptr;
+    CUfunction fn = nullptr;
+    int threads = 0;
+    size_t smem = 0;
+    int grid_cap = 0;
+    int T = 0;
+};
+
+std::mutex g_mu;
+std::unordered_map<std::string, std::unique_ptr<Kernel>>& cache() {
+    static std::unordered_map<std::string, std::unique_ptr<Kernel>> c;
+    return c;
+}
+
+JitConfig initial_config() {
+    JitConfig c;
+    const char* e = std::getenv("QFVM_JIT");
+    if (e && e[0] == '0') c.enabled = 0;
+    return c;
+}
+JitConfig& config() {
+    static JitConfig c = initial_config();
+    return c;
+}
+
+// PTX -> cubin.  With the toolkit's PTX compiler library linked in this runs
+// on any host thread without a CUDA context, so a plan's passes compile in
+// parallel; otherwise the driver compiles the PTX when the module is loaded.
+bool to_cubin(const std::string& ptx, std::string* image, std::string* err, std::string* info = nullptr) {
+#ifdef QSV_PTXCOMPILER
+    nvPTXCompilerHandle h = nullptr;
+    if (nvPTXCompilerCreate(&h, ptx.size(), ptx.c_str()) != NVPTXCOMPILE_SUCCESS) {
+        *err = "PTX compiler: create failed";
+        return false;
+    }
+    const char* opts[] = {"--gpu-name=sm_103a", "-O3", "-v"};
+    bool ok = nvPTXCompilerCompile(h, info ? 3 : 2, opts) == NVPTXCOMPILE_SUCCESS;
+    if (info) {
+        size_t n = 0;
+        nvPTXCompilerGetInfoLogSize(h, &n);
+        std::string log(n + 1, '\0');
+        if (n) nvPTXCompilerGetInfoLog(h, &log[0]);
+        *info = log.c_str();
+    }
+    if (!ok) {
+        size_t n = 0;
+        nvPTXCompilerGetErrorLogSize(h, &n);
+        std::string log(n + 1, '\0');
+        if (n) nvPTXCompilerGetErrorLog(h, &log[0]);
+        *err = "PTX compiler: " + log;
+    } else {
+        size_t n = 0;
+        ok = nvPTXCompilerGetCompiledProgramSize(h, &n) == NVPTXCOMPILE_SUCCESS;
+        image->assign(n, '\0');
+        ok = ok && nvPTXCompilerGetCompiledProgram(h, &(*image)[0]) == NVPTXCOMPILE_SUCCESS;
+        if (!ok) *err = "PTX compiler: no program";
+    }
+    nvPTXCompilerDestroy(&h);
+    return ok;
+#else
+    *image = ptx;  // loaded as PTX: the driver compiles it
+    (void)err;
+    if (info) *info = "driver compilation";
+    return true;
+#endif
+}
+
+// load a compiled image and set the kernel up (thread with the context current)
+int load(int dev, const std::string& image, Kernel* k, std::string* err) {
+    Driver& d = driver();
+    char log[4096] = "";
+    CUjit_option opt[2] = {CU_JIT_ERROR_LOG_BUFFER, CU_JIT_ERROR_LOG_BUFFER_SIZE_BYTES};
+    void* val[2] = {log, reinterpret_cast<void*>(static_cast<uintptr_t>(sizeof log))};
+    CUresult r = d.load(&k->mod, image.c_str(), 2, opt, val);
+    if (r != CUDA_SUCCESS) {
+        *err = "specialised pass load failed: " + cu_error(r) + ": " + log;
+        return 1;
+    }
+    r = d.get_function(&k->fn, k->mod, "qsv_tile_pass");
+    if (r == CUDA_SUCCESS && k->smem > 48 * 1024)
+        r = d.set_attribute(k->fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, static_cast<int>(k->smem));
+    int per_sm = 0;
+    if (r == CUDA_SUCCESS) r = d.occupancy(&per_sm, k->fn, k->threads, k->smem);
+    if (r != CUDA_SUCCESS) {
+        *err = "specialised pass setup failed: " + cu_error(r);
+        return 1;
+    }
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    k->grid_cap = (nsm > 0 ? nsm : 1) * (per_sm > 0 ? per_sm : 1);
+    return 0;
+}
+
+JitShape shape_for(const HostPlan& hp, int nstates) {
+    const JitConfig c = config();
+    JitShape sh;
+    sh.nstates = nstates;
+    sh.nb = nstates == 1 ? c.nb1 : c.nb2;
+    int minb = nstates == 1 ? c.minb1 : c.minb2;
+    if (minb <= 0) {
+        const int nt = 1 << (hp.T - hp.R);
+        minb = 65536 / (nt * 128);
+        if (minb < 1) minb = 1;
+    }
+    sh.minb = minb;
+    return sh;
+}
+
+}  // namespace
+
+JitConfig jit_config() {
+    std::lock_guard<std::mutex> lk(g_mu);
+    return config();
+}
+void jit_set_config(const JitConfig& c) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    config() = c;
+}
+
+int jit_prepare(qfvm_plan* p, int nstates, std::string* err) {
+    const int si = nstates == 2 ? 1 : 0;
+    if (p->jit_ready[si]) return 0;
+    const HostPlan& hp = p->hp;
+    std::vector<const void*> ks(hp.passes.size(), nullptr);
+    JitShape sh;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (!config().enabled || (hp.arith != QFVM_C64 && hp.arith != QFVM_C128)) {
+            p->jit[si] = ks;
+            p->jit_ready[si] = true;
+            return 0;
+        }
+    }
+    bool any_tile = false;
+    for (const PassDesc& pd : hp.passes) any_tile |= pd.type == PASS_TILE;
+    if (!any_tile) {
+        p->jit[si] = ks;
+        p->jit_ready[si] = true;
+        return 0;
+    }
+    if (!driver().ok) {
+        *err = driver().err;
+        return 1;
+    }
+    sh = shape_for(hp, nstates);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    {
+        // double buffering only where both tiles fit in a CTA's shared memory
+        int optin = 0;
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        const size_t tile = static_cast<size_t>(hp.arith == QFVM_C128 ? 16 : 8) << hp.T;
+        const size_t pacc = static_cast<size_t>(1 << (hp.T - hp.R)) / 32 * MAX_PASS_PROBES * 8;
+        if (sh.nb == 2 && 2 * nstates * tile + pacc > static_cast<size_t>(optin)) sh.nb = 1;
+    }
+    // look the passes up by structure; generate and compile the missing ones
+    std::vector<std::string> keys(hp.passes.size());
+    std::vector<int> todo;  // first pass of each missing structure
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        for (size_t i = 0; i < hp.passes.size(); ++i) {
+            std::string why;
+            if (!jit_pass_key(hp, static_cast<int>(i), sh, &keys[i], &why)) {
+                keys[i].clear();
+                continue;
+            }
+            keys[i] += "@" + std::to_string(dev);
+            auto it = cache().find(keys[i]);
+            if (it != cache().end()) {
+                ks[i] = it->second.get();
+                continue;
+            }
+            bool dup = false;
+            for (int j : todo) dup |= keys[j] == keys[i];
+            if (!dup) todo.push_back(static_cast<int>(i));
+        }
+    }
+    std::vector<std::string> images(todo.size()), errs(todo.size());
+    std::vector<char> oks(todo.size(), 0);
+    const unsigned hw = std::thread::hardware_concurrency();
+    const size_t nthreads = std::min<size_t>(todo.size(), hw ? hw : 4);
+    std::vector<std::thread> pool;
+    std::mutex qmu;
+    size_t next = 0;
+    for (size_t t = 0; t < nthreads; ++t) {
+        pool.emplace_back([&] {
+            for (;;) {
+                size_t w;
+                {
+                    std::lock_guard<std::mutex> lk(qmu);
+                    if (next >= todo.size()) return;
+                    w = next++;
+                }
+                std::string ptx, why;
+                if (!jit_pass_ptx(hp, todo[w], sh, "qsv_tile_pass", &ptx, &why)) {
+                    errs[w] = "specialised pass: " + why;
+                    continue;
+                }
+                oks[w] = to_cubin(ptx, &images[w], &errs[w]);
+            }
+        });
+    }
+    for (auto& t : pool) t.join();
+    for (size_t w = 0; w < todo.size(); ++w)
+        if (!oks[w]) {
+            *err = errs[w];
+            return 1;
+        }
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (size_t w = 0; w < todo.size(); ++w) {
+        const int i = todo[w];
+        if (cache().count(keys[i])) continue;
+        auto k = std::make_unique<Kernel>();
+        const int nt = 1 << (hp.T - hp.R);
+        const int np = nstates == 2 ? hp.passes[i].nprobe : 0;
+        k->threads = nt;
+        k->T = hp.T;
+        k->smem = static_cast<size_t>(sh.nb) * nstates * (static_cast<size_t>(hp.arith == QFVM_C128 ? 16 : 8) << hp.T) +
+                  static_cast<size_t>(nt / 32) * np * 8;
+        if (load(dev, images[w], k.get(), err)) return 1;
+        cache().emplace(keys[i], std::move(k));
+    }
+    for (size_t i = 0; i < hp.passes.size(); ++i) {
+        if (ks[i] || keys[i].empty()) continue;
+        auto it = cache().find(keys[i]);
+        if (it != cache().end()) ks[i] = it->second.get();
+    }
+    p->jit[si] = ks;
+    p->jit_ready[si] = true;
+    return 0;
+}
+
+void jit_release(qfvm_plan* p) {
+    for (int s = 0; s < 2; ++s) {
+        p->jit[s].clear();
+        p->jit_ready[s] = false;
+    }
+}
+
+int jit_compiled_passes(const qfvm_plan* p, int nstates) {
+    const int si = nstates == 2 ? 1 : 0;
+    int c = 0;
+    for (const void* k : p->jit[si]) c += k != nullptr;
+    return c;
+}
+
+cudaError_t jit_launch_pass(qfvm_plan* p, int pi, void* psi, void* lam, const void* dcoef, int items,
+                            uint64_t cstride, const uint8_t* active, int per_tile, double* partial, int* grid_out,
+                            cudaStream_t st, bool* launched) {
+    *launched = false;
+    const int nstates = lam ? 2 : 1;
+    const int si = nstates - 1;
+    if (!p->jit_ready[si]) {
+        // never compile inside a stream capture: run interpreted instead
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return cudaSuccess;
+        std::string err;
+        if (jit_prepare(p, nstates, &err)) {
+            std::fprintf(stderr, "qfvm: %s\n", err.c_str());
+            return cudaErrorInvalidPtx;
+        }
+    }
+    if (pi < 0 || pi >= static_cast<int>(p->jit[si].size()) || !p->jit[si][pi]) return cudaSuccess;
+    const Kernel* k = static_cast<const Kernel*>(p->jit[si][pi]);
+    const HostPlan& hp = p->hp;
+    uint64_t ntiles = static_cast<uint64_t>(items) << (hp.n - hp.T);
+    const unsigned grid = static_cast<unsigned>(ntiles < static_cast<uint64_t>(k->grid_cap) ? ntiles : k->grid_cap);
+    void* a_psi = psi;
+    void* a_lam = lam;
+    const void* a_coef = dcoef;
+    uint64_t a_cs = cstride;
+    uint32_t a_ish = static_cast<uint32_t>(hp.n - hp.T);
+    const void* a_act = active;
+    int32_t a_pt = per_tile;
+    void* a_part = partial;
+    void* args[] = {&a_psi, &a_lam, &ntiles, &a_coef, &a_cs, &a_ish, &a_act, &a_pt, &a_part};
+    CUresult r = driver().launch(k->fn, grid, 1, 1, k->threads, 1, 1, static_cast<unsigned>(k->smem),
+                                 reinterpret_cast<CUstream>(st), args, nullptr);
+    if (grid_out) *grid_out = static_cast<int>(grid);
+    *launched = true;
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorLaunchFailure;
+}
+
+}  // namespace qsv
+
+using qsv_capi::fail;
+
+extern "C" {
+
+int qfvm_jit_configure(int32_t enabled, int32_t nb_one, int32_t minb_one, int32_t nb_two, int32_t minb_two) {
+    if ((nb_one != 1 && nb_one != 2) || (nb_two != 1 && nb_two != 2) || minb_one < 0 || minb_two < 0 ||
+        minb_one > 16 || minb_two > 16)
+        return fail(QFVM_ERR_INVALID, "tile buffers must be 1 or 2 and minimum CTAs 0..16");
+    qsv::JitConfig c;
+    c.enabled = enabled ? 1 : 0;
+    c.nb1 = nb_one;
+    c.minb1 = minb_one;
+    c.nb2 = nb_two;
+    c.minb2 = minb_two;
+    qsv::jit_set_config(c);
+    return QFVM_OK;
+}
+
+int qfvm_jit_get_config(int32_t config[5]) {
+    if (!config) return fail(QFVM_ERR_INVALID, "null argument");
+    const qsv::JitConfig c = qsv::jit_config();
+    config[0] = c.enabled;
+    config[1] = c.nb1;
+    config[2] = c.minb1;
+    config[3] = c.nb2;
+    config[4] = c.minb2;
+    return QFVM_OK;
+}
+
+int qfvm_jit_pass_ptx(const qfvm_plan* plan, int32_t pass, int32_t nstates, char* text, int64_t capacity,
+                      int64_t* len) {
+    if (!plan || !len || (nstates != 1 && nstates != 2)) return fail(QFVM_ERR_INVALID, "bad argument");
+    const qsv::JitConfig c = qsv::jit_config();
+    qsv::JitShape sh;
+    sh.nstates = nstates;
+    sh.nb = nstates == 1 ? c.nb1 : c.nb2;
+    sh.minb = nstates == 1 ? c.minb1 : c.minb2;
+    std::string ptx, why;
+    if (!qsv::jit_pass_ptx(plan->hp, pass, sh, "qsv_tile_pass", &ptx, &why))
+        return fail(QFVM_ERR_UNSUPPORTED, "pass runs interpreted: " + why);
+    *len = static_cast<int64_t>(ptx.size());
+    if (text) {
+        if (capacity < *len + 1) return fail(QFVM_ERR_INVALID, "text buffer too small");
+        std::memcpy(text, ptx.c_str(), ptx.size() + 1);
+    }
+    return QFVM_OK;
+}
+
+int qfvm_jit_pass_compile(const qfvm_plan* plan, int32_t pass, int32_t nstates, char* info, int64_t capacity) {
+    if (!plan || (nstates != 1 && nstates != 2)) return fail(QFVM_ERR_INVALID, "bad argument");
+    const qsv::JitConfig c = qsv::jit_config();
+    qsv::JitShape sh;
+    sh.nstates = nstates;
+    sh.nb = nstates == 1 ? c.nb1 : c.nb2;
+    sh.minb = nstates == 1 ? c.minb1 : c.minb2;
+    std::string ptx, why, image, err, log;
+    if (!qsv::jit_pass_ptx(plan->hp, pass, sh, "qsv_tile_pass", &ptx, &why))
+        return fail(QFVM_ERR_UNSUPPORTED, "pass runs interpreted: " + why);
+    const bool ok = qsv::to_cubin(ptx, &image, &err, &log);
+    if (info && capacity > 0) {
+        const std::string& m = ok ? log : err;
+        const size_t n = std::min<size_t>(m.size(), static_cast<size_t>(capacity - 1));
+        std::memcpy(info, m.data(), n);
+        info[n] = 0;
+    }
+    return ok ? QFVM_OK : fail(QFVM_ERR_INVALID, err);
+}
+
+int qfvm_jit_plan_passes(const qfvm_plan* plan, int32_t nstates, int64_t* count) {
+    if (!plan || !count) return fail(QFVM_ERR_INVALID, "null argument");
+    *count = qsv::jit_compiled_passes(plan, nstates);
+    return QFVM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,57 @@
+// Circuit-specialised tile passes: each register round of a pass is emitted
+// as straight-line PTX for sm_103a (targets, controls, coefficient offsets
+// and swizzled shared-memory offsets become constants; X/SWAP/Y become
+// register renames), compiled by the driver's JIT once per distinct pass and
+// launched instead of the interpreting kernels k_pass / k_pass2.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "engine.h"
+
+struct qfvm_plan;
+
+namespace qsv {
+
+struct JitShape {
+    int nstates = 1;  // 1: one-state pass (k_pass), 2: psi + lam with probes (k_pass2)
+    int nb = 1;       // tile buffers (2 = prefetch the next tile during this one)
+    int minb = 1;     // .minnctapersm (register budget = 64K / (threads * minb))
+};
+
+// PTX of tile pass `pi` of plan `hp` as kernel `entry`; false (with a reason)
+// when the pass has a step the generator does not handle.
+bool jit_pass_ptx(const HostPlan& hp, int pi, const JitShape& sh, const std::string& entry, std::string* ptx,
+                  std::string* why);
+
+// Everything the generator reads for pass `pi` (the module cache key);
+// false when the pass is not handled.
+bool jit_pass_key(const HostPlan& hp, int pi, const JitShape& sh, std::string* key, std::string* why);
+
+// Global switch (default on) and launch shape knobs.
+struct JitConfig {
+    int enabled = 1;
+    int nb1 = 2, minb1 = 0;  // one-state passes (minb 0 = automatic)
+    int nb2 = 1, minb2 = 0;  // two-state passes
+};
+JitConfig jit_config();
+void jit_set_config(const JitConfig& c);
+
+// Compiles every eligible tile pass of `p` for `nstates` (no-op when the
+// plan's arithmetic or the switch rules it out).  Call outside stream
+// capture.  Returns a CUDA-style error for a failed compile.
+int jit_prepare(qfvm_plan* p, int nstates, std::string* err);
+void jit_release(qfvm_plan* p);
+
+// Launches pass `pi` of `p` through its compiled kernel; *launched = false
+// (nothing issued) when the pass has none.
+cudaError_t jit_launch_pass(qfvm_plan* p, int pi, void* psi, void* lam, const void* dcoef, int items,
+                            uint64_t cstride, const uint8_t* active, int per_tile, double* partial, int* grid_out,
+                            cudaStream_t st, bool* launched);
+
+// Number of compiled passes of `p` for nstates (diagnostics).
+int jit_compiled_passes(const qfvm_plan* p, int nstates);
+
+}  // namespace qsv

@@ -1,0 +1,972 @@
+// PTX generator of circuit-specialised tile passes (see jit.h).
+//
+// The emitted kernel is the tile pass of device.cuh (k_pass) / adjoint.cuh
+// (k_pass2) with the plan's steps unrolled: the persistent tile loop, the
+// cp.async staging of a tile into swizzled shared memory, and for every
+// register round the loads, the gate arithmetic and the stores, all with
+// compile-time register indices.  The gate arithmetic follows the policy
+// primitives of policy.cuh operation for operation (mul.rn / fma.rn / add.rn,
+// no contraction), so the specialised passes compute what the interpreting
+// kernels compute.  Register permutations (X, SWAP, Y, quarter turns) are
+// renames of PTX virtual registers and cost no instruction.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "jit.h"
+#include "qfvm_gb300.h"
+
+namespace qsv {
+namespace {
+
+std::string fmt(const char* f, ...) {
+    char buf[640];
+    va_list ap;
+    va_start(ap, f);
+    vsnprintf(buf, sizeof buf, f, ap);
+    va_end(ap);
+    return buf;
+}
+
+uint32_t swz_host(uint32_t s, int gb) {
+    const uint32_t m = (1u << gb) - 1;
+    uint32_t x = s;
+    for (int k = 1; k * gb < 32; ++k) x ^= (s >> (k * gb)) & m;
+    return x;
+}
+
+struct Cx {
+    std::string x, y;
+};
+bool same(const Cx& a, const Cx& b) { return a.x == b.x && a.y == b.y; }
+
+class Gen {
+   public:
+    Gen(const HostPlan& hp, int pi, const JitShape& sh)
+        : hp_(hp), pd_(hp.passes[pi]), sh_(sh) {
+        f64_ = hp.arith == QFVM_C128;
+        ft_ = f64_ ? "f64" : "f32";
+        es_ = f64_ ? 16 : 8;
+        cb_ = f64_ ? 8 : 4;
+        gb_ = f64_ ? 3 : 4;
+        T_ = hp.T;
+        R_ = hp.R;
+        NT_ = 1 << (T_ - R_);
+        NA_ = 1 << R_;
+        NW_ = NT_ / 32;
+        PER_ = (1 << T_) / NT_;
+        NS_ = sh.nstates;
+        np_ = NS_ == 2 ? pd_.nprobe : 0;
+        tileB_ = static_cast<uint32_t>(es_) << T_;
+        slotB_ = tileB_ * NS_;
+    }
+
+    bool supported(std::string* why) const {
+        if (hp_.arith != QFVM_C64 && hp_.arith != QFVM_C128) return no(why, "arithmetic without a generator");
+        if (pd_.type != PASS_TILE) return no(why, "not a tile pass");
+        if (T_ - R_ < 6 || T_ > 13 || R_ < 1 || R_ > 5) return no(why, "tile shape out of range");
+        if (np_ > NT_ || np_ > MAX_PASS_PROBES) return no(why, "too many probes");
+        for (int si = 0; si < pd_.step_count; ++si) {
+            const StepDesc& sd = hp_.steps[pd_.step_begin + si];
+            if (sd.type != STEP_ROUND) return no(why, "shared-memory step");
+            for (int oi = 0; oi < sd.op_count; ++oi) {
+                const KOp& o = hp_.ops[sd.op_begin + oi];
+                switch (o.kind) {
+                    case K_DENSE: case K_REAL: case K_RX: case K_DIAG: case K_X: case K_Y: case K_SWAP: case K_HAD:
+                        break;
+                    case K_PROBE:
+                        if (NS_ != 2) return no(why, "probe in a one-state pass");
+                        break;
+                    default: return no(why, "operation kind without a generator");
+                }
+            }
+        }
+        return true;
+    }
+
+    std::string emit(const std::string& entry) {
+        prologue();
+        tile_loop();
+        std::string out;
+        out += "//\n// circuit-specialised tile pass\n//\n.version 9.0\n.target sm_103a\n.address_size 64\n\n";
+        out += ".extern .shared .align 16 .b8 qsv_dsm[];\n\n";
+        out += ".visible .entry " + entry + "(\n";
+        out += "\t.param .u64 p_psi,\n\t.param .u64 p_lam,\n\t.param .u64 p_ntiles,\n\t.param .u64 p_coef,\n";
+        out += "\t.param .u64 p_cstride,\n\t.param .u32 p_ishift,\n\t.param .u64 p_active,\n";
+        out += "\t.param .u32 p_per_tile,\n\t.param .u64 p_partial\n)\n";
+        out += fmt(".maxntid %d, 1, 1\n.minnctapersm %d\n{\n", NT_, sh_.minb < 1 ? 1 : sh_.minb);
+        out += fmt("\t.reg .pred %%p<%d>;\n\t.reg .b16 %%h<%d>;\n\t.reg .b32 %%r<%d>;\n\t.reg .b64 %%rd<%d>;\n",
+                   np_reg_ + 1, nh_ + 1, nr_ + 1, nrd_ + 1);
+        out += fmt("\t.reg .%s %%a<%d>;\n\t.reg .f64 %%d<%d>;\n\n", ft_, na_ + 1, nd_ + 1);
+        out += body_;
+        out += "}\n";
+        return out;
+    }
+
+   private:
+    static bool no(std::string* why, const char* m) {
+        if (why) *why = m;
+        return false;
+    }
+
+    // ---------------------------------------------------------------- emission
+    std::string R32() { return "%r" + std::to_string(nr_++); }
+    std::string R64() { return "%rd" + std::to_string(nrd_++); }
+    std::string H16() { return "%h" + std::to_string(nh_++); }
+    std::string P() { return "%p" + std::to_string(np_reg_++); }
+    std::string A() { return "%a" + std::to_string(na_++); }
+    std::string D() { return "%d" + std::to_string(nd_++); }
+    std::string L() { return "$L" + std::to_string(nl_++); }
+    void I(const std::string& s) {
+        body_ += '\t';
+        body_ += s;
+        body_ += ";\n";
+    }
+    void lab(const std::string& l) { body_ += l + ":\n"; }
+
+    // amplitude-type arithmetic (policy.cuh: mul / madd / add / neg)
+    std::string mul(const std::string& c, const std::string& x) {
+        std::string d = A();
+        I(fmt("mul.rn.%s %s, %s, %s", ft_, d.c_str(), c.c_str(), x.c_str()));
+        return d;
+    }
+    std::string fma(const std::string& c, const std::string& x, const std::string& acc) {
+        std::string d = A();
+        I(fmt("fma.rn.%s %s, %s, %s, %s", ft_, d.c_str(), c.c_str(), x.c_str(), acc.c_str()));
+        return d;
+    }
+    std::string add(const std::string& x, const std::string& y) {
+        std::string d = A();
+        I(fmt("add.rn.%s %s, %s, %s", ft_, d.c_str(), x.c_str(), y.c_str()));
+        return d;
+    }
+    std::string sub(const std::string& x, const std::string& y) {
+        std::string d = A();
+        I(fmt("sub.rn.%s %s, %s, %s", ft_, d.c_str(), x.c_str(), y.c_str()));
+        return d;
+    }
+    // exact sign flip (FP64: on the integer high word, no FP64 instruction)
+    std::string neg(const std::string& x) {
+        std::string d = A();
+        if (f64_) {
+            std::string t = R64(), u = R64();
+            I(fmt("mov.b64 %s, %s", t.c_str(), x.c_str()));
+            I(fmt("xor.b64 %s, %s, -9223372036854775808", u.c_str(), t.c_str()));
+            I(fmt("mov.b64 %s, %s", d.c_str(), u.c_str()));
+        } else {
+            I(fmt("neg.f32 %s, %s", d.c_str(), x.c_str()));
+        }
+        return d;
+    }
+    std::string sel(const std::string& a, const std::string& b, const std::string& p) {  // p ? a : b
+        std::string d = A();
+        I(fmt("selp.%s %s, %s, %s, %s", ft_, d.c_str(), a.c_str(), b.c_str(), p.c_str()));
+        return d;
+    }
+    std::string cnst(double v) {
+        auto it = consts_.find(v);
+        if (it != consts_.end()) return it->second;
+        std::string d = A();
+        if (f64_) {
+            uint64_t u;
+            std::memcpy(&u, &v, 8);
+            I(fmt("mov.f64 %s, 0d%016llX", d.c_str(), static_cast<unsigned long long>(u)));
+        } else {
+            const float f = static_cast<float>(v);
+            uint32_t u;
+            std::memcpy(&u, &f, 4);
+            I(fmt("mov.f32 %s, 0f%08X", d.c_str(), u));
+        }
+        consts_[v] = d;
+        return d;
+    }
+    // coefficients off .. off+cnt-1 of the tile's pool (widest aligned loads)
+    std::vector<std::string> coefs(uint32_t off, int cnt) {
+        std::vector<std::string> c;
+        uint32_t i = off;
+        const uint32_t end = off + cnt;
+        while (i < end) {
+            int vec = 1;
+            if (!f64_ && i % 4 == 0 && i + 4 <= end) vec = 4;
+            else if (i % 2 == 0 && i + 2 <= end) vec = 2;
+            std::string r[4];
+            for (int k = 0; k < vec; ++k) r[k] = A();
+            if (vec == 4)
+                I(fmt("ld.global.nc.v4.f32 {%s, %s, %s, %s}, [%s+%u]", r[0].c_str(), r[1].c_str(), r[2].c_str(),
+                      r[3].c_str(), coefp_.c_str(), i * cb_));
+            else if (vec == 2)
+                I(fmt("ld.global.nc.v2.%s {%s, %s}, [%s+%u]", ft_, r[0].c_str(), r[1].c_str(), coefp_.c_str(),
+                      i * cb_));
+            else
+                I(fmt("ld.global.nc.%s %s, [%s+%u]", ft_, r[0].c_str(), coefp_.c_str(), i * cb_));
+            for (int k = 0; k < vec; ++k) c.push_back(r[k]);
+            i += vec;
+        }
+        return c;
+    }
+
+    // u64 register = OR over the set bits i of `r32` (bits 0..nbits-1) of val[i]
+    std::string deposit64(const std::string& r32, int nbits, const std::vector<uint64_t>& val) {
+        std::string acc = R64();
+        I(fmt("mov.u64 %s, 0", acc.c_str()));
+        for (int i = 0; i < nbits; ++i) {
+            if (val[i] == 0) continue;
+            std::string t = R32(), p = P(), v = R64(), n = R64();
+            I(fmt("and.b32 %s, %s, %u", t.c_str(), r32.c_str(), 1u << i));
+            I(fmt("setp.ne.u32 %s, %s, 0", p.c_str(), t.c_str()));
+            I(fmt("selp.b64 %s, %llu, 0, %s", v.c_str(), static_cast<unsigned long long>(val[i]), p.c_str()));
+            I(fmt("or.b64 %s, %s, %s", n.c_str(), acc.c_str(), v.c_str()));
+            acc = n;
+        }
+        return acc;
+    }
+    // u32 register = XOR over the set bits i of `r32` of val[i]
+    std::string xor32(const std::string& r32, int nbits, const std::vector<uint32_t>& val) {
+        std::string acc = R32();
+        I(fmt("mov.u32 %s, 0", acc.c_str()));
+        for (int i = 0; i < nbits; ++i) {
+            if (val[i] == 0) continue;
+            std::string t = R32(), p = P(), v = R32(), n = R32();
+            I(fmt("and.b32 %s, %s, %u", t.c_str(), r32.c_str(), 1u << i));
+            I(fmt("setp.ne.u32 %s, %s, 0", p.c_str(), t.c_str()));
+            I(fmt("selp.b32 %s, %u, 0, %s", v.c_str(), val[i], p.c_str()));
+            I(fmt("xor.b32 %s, %s, %s", n.c_str(), acc.c_str(), v.c_str()));
+            acc = n;
+        }
+        return acc;
+    }
+
+    // ---------------------------------------------------------------- kernel
+    void prologue() {
+        tid_ = R32();
+        I(fmt("mov.u32 %s, %%tid.x", tid_.c_str()));
+        std::string bid = R32(), nbid = R32();
+        I(fmt("mov.u32 %s, %%ctaid.x", bid.c_str()));
+        I(fmt("mov.u32 %s, %%nctaid.x", nbid.c_str()));
+        bid64_ = R64();
+        nbid64_ = R64();
+        I(fmt("cvt.u64.u32 %s, %s", bid64_.c_str(), bid.c_str()));
+        I(fmt("cvt.u64.u32 %s, %s", nbid64_.c_str(), nbid.c_str()));
+        const char* pn[2] = {"p_psi", "p_lam"};
+        for (int s = 0; s < NS_; ++s) {
+            std::string g = R64();
+            stg_[s] = R64();
+            I(fmt("ld.param.u64 %s, [%s]", g.c_str(), pn[s]));
+            I(fmt("cvta.to.global.u64 %s, %s", stg_[s].c_str(), g.c_str()));
+        }
+        ntiles_ = R64();
+        I(fmt("ld.param.u64 %s, [p_ntiles]", ntiles_.c_str()));
+        std::string cg = R64();
+        coef0_ = R64();
+        I(fmt("ld.param.u64 %s, [p_coef]", cg.c_str()));
+        I(fmt("cvta.to.global.u64 %s, %s", coef0_.c_str(), cg.c_str()));
+        std::string cs = R64();
+        cstrideB_ = R64();
+        I(fmt("ld.param.u64 %s, [p_cstride]", cs.c_str()));
+        I(fmt("mul.lo.u64 %s, %s, %d", cstrideB_.c_str(), cs.c_str(), cb_));
+        ishift_ = R32();
+        I(fmt("ld.param.u32 %s, [p_ishift]", ishift_.c_str()));
+        if (NS_ == 1) {
+            std::string ag = R64();
+            active_ = R64();
+            hasact_ = P();
+            I(fmt("ld.param.u64 %s, [p_active]", ag.c_str()));
+            I(fmt("setp.ne.u64 %s, %s, 0", hasact_.c_str(), ag.c_str()));
+            I(fmt("cvta.to.global.u64 %s, %s", active_.c_str(), ag.c_str()));
+        }
+        smb_ = R32();
+        I(fmt("mov.u32 %s, qsv_dsm", smb_.c_str()));
+        // the thread's share of a tile: global element offset (bytes) and
+        // swizzled shared offset (bytes); both are XOR/OR-linear in tid
+        std::vector<uint64_t> gv(T_ - R_);
+        std::vector<uint32_t> sv(T_ - R_);
+        for (int i = 0; i < T_ - R_; ++i) {
+            gv[i] = (1ULL << pd_.tq[i]) * es_;
+            sv[i] = swz_host(1u << i, gb_) * es_;
+        }
+        gtidB_ = deposit64(tid_, T_ - R_, gv);
+        stidB_ = xor32(tid_, T_ - R_, sv);
+        if (np_ > 0) {
+            std::string lane = R32(), warp = R32();
+            lane0_ = P();
+            I(fmt("and.b32 %s, %s, 31", lane.c_str(), tid_.c_str()));
+            I(fmt("setp.eq.u32 %s, %s, 0", lane0_.c_str(), lane.c_str()));
+            I(fmt("shr.u32 %s, %s, 5", warp.c_str(), tid_.c_str()));
+            paccB_ = R32();
+            I(fmt("add.u32 %s, %s, %u", paccB_.c_str(), smb_.c_str(), slotB_ * sh_.nb));
+            paccW_ = R32();
+            I(fmt("mad.lo.u32 %s, %s, %d, %s", paccW_.c_str(), warp.c_str(), np_ * 8, paccB_.c_str()));
+            std::string pt = R64();
+            I(fmt("ld.param.u32 %s, [p_per_tile]", (perTile_ = R32()).c_str()));
+            I(fmt("ld.param.u64 %s, [p_partial]", pt.c_str()));
+            partial_ = R64();
+            I(fmt("cvta.to.global.u64 %s, %s", partial_.c_str(), pt.c_str()));
+            // zero the per-warp probe sums
+            const int tot = NW_ * np_;
+            for (int i0 = 0; i0 < tot; i0 += NT_) {
+                std::string idx = R32(), p = P(), ad = R32();
+                I(fmt("add.u32 %s, %s, %d", idx.c_str(), tid_.c_str(), i0));
+                I(fmt("setp.lt.u32 %s, %s, %d", p.c_str(), idx.c_str(), tot));
+                I(fmt("mad.lo.u32 %s, %s, 8, %s", ad.c_str(), idx.c_str(), paccB_.c_str()));
+                I(fmt("@%s st.shared.u64 [%s], 0", p.c_str(), ad.c_str()));
+            }
+            I("bar.sync 0");
+        }
+    }
+
+    // element index of the first amplitude of tile b (tile_base of device.cuh)
+    std::string tile_base(const std::string& b) {
+        std::string base = R64();
+        I(fmt("shl.b64 %s, %s, %d", base.c_str(), b.c_str(), pd_.L));
+        for (int k = 0; k < pd_.H; ++k) {
+            const int p = pd_.tq[pd_.L + k];
+            std::string hi = R64(), hi2 = R64(), lo = R64(), n = R64();
+            I(fmt("shr.u64 %s, %s, %d", hi.c_str(), base.c_str(), p));
+            I(fmt("shl.b64 %s, %s, %d", hi2.c_str(), hi.c_str(), p + 1));
+            I(fmt("and.b64 %s, %s, %llu", lo.c_str(), base.c_str(), static_cast<unsigned long long>((1ULL << p) - 1)));
+            I(fmt("or.b64 %s, %s, %s", n.c_str(), hi2.c_str(), lo.c_str()));
+            base = n;
+        }
+        return base;
+    }
+
+    uint64_t gk(int k) const {  // global byte offset of element k * NT of a tile
+        const uint32_t s = static_cast<uint32_t>(k * NT_);
+        uint64_t g = 0;
+        for (int i = 0; i < T_; ++i)
+            if ((s >> i) & 1) g |= 1ULL << pd_.tq[i];
+        return g * es_;
+    }
+    uint32_t sk(int k) const { return swz_host(static_cast<uint32_t>(k * NT_), gb_) * es_; }
+
+    // per-thread global pointer of state s for tile base `base` (element index)
+    std::string thread_gptr(int s, const std::string& base) {
+        std::string bb = R64(), t = R64(), g = R64();
+        I(fmt("mul.lo.u64 %s, %s, %d", bb.c_str(), base.c_str(), es_));
+        I(fmt("add.s64 %s, %s, %s", t.c_str(), bb.c_str(), gtidB_.c_str()));
+        I(fmt("add.s64 %s, %s, %s", g.c_str(), t.c_str(), stg_[s].c_str()));
+        return g;
+    }
+    std::string gaddr(const std::string& gp, int k) {
+        const uint64_t off = gk(k);
+        if (off < (1ULL << 31)) return gp + "+" + std::to_string(off);
+        std::string a = R64();
+        I(fmt("add.s64 %s, %s, %llu", a.c_str(), gp.c_str(), static_cast<unsigned long long>(off)));
+        return a;
+    }
+
+    void prefetch(const std::string& base, const std::string& slotbase) {
+        for (int s = 0; s < NS_; ++s) {
+            std::string gp = thread_gptr(s, base);
+            for (int k = 0; k < PER_; ++k) {
+                std::string x = R32(), d = R32();
+                I(fmt("xor.b32 %s, %s, %u", x.c_str(), stidB_.c_str(), sk(k)));
+                I(fmt("add.u32 %s, %s, %s", d.c_str(), x.c_str(), slotbase.c_str()));
+                const std::string src = gaddr(gp, k);
+                if (es_ == 16)
+                    I(fmt("cp.async.cg.shared.global [%s+%u], [%s], 16", d.c_str(), s * tileB_, src.c_str()));
+                else
+                    I(fmt("cp.async.ca.shared.global [%s+%u], [%s], 8", d.c_str(), s * tileB_, src.c_str()));
+            }
+        }
+        I("cp.async.commit_group");
+    }
+
+    void tile_loop() {
+        std::string b = R64();
+        I(fmt("mov.u64 %s, %s", b.c_str(), bid64_.c_str()));
+        const std::string lend = L(), lloop = L();
+        std::string p0 = P();
+        I(fmt("setp.ge.u64 %s, %s, %s", p0.c_str(), b.c_str(), ntiles_.c_str()));
+        I(fmt("@%s bra %s", p0.c_str(), lend.c_str()));
+        std::string slot = R32();
+        I(fmt("mov.u32 %s, 0", slot.c_str()));
+        if (sh_.nb == 2) {
+            std::string base0 = tile_base(b);
+            prefetch(base0, smb_);
+        }
+        lab(lloop);
+        // loop-carried registers are re-assigned at the end of the body
+        std::string base = tile_base(b);
+        std::string item = R64(), coff = R64();
+        I(fmt("shr.u64 %s, %s, %s", item.c_str(), b.c_str(), ishift_.c_str()));
+        I(fmt("mul.lo.u64 %s, %s, %s", coff.c_str(), item.c_str(), cstrideB_.c_str()));
+        coefp_ = R64();
+        I(fmt("add.s64 %s, %s, %s", coefp_.c_str(), coef0_.c_str(), coff.c_str()));
+        std::string sbase = R32();
+        I(fmt("add.u32 %s, %s, %s", sbase.c_str(), smb_.c_str(), slot.c_str()));
+        if (sh_.nb == 1) {
+            prefetch(base, sbase);
+            I("cp.async.wait_group 0");
+        } else {
+            std::string bn = R64(), pn = P(), nslot = R32(), nsb = R32();
+            const std::string lno = L(), ldone = L();
+            I(fmt("add.s64 %s, %s, %s", bn.c_str(), b.c_str(), nbid64_.c_str()));
+            I(fmt("setp.ge.u64 %s, %s, %s", pn.c_str(), bn.c_str(), ntiles_.c_str()));
+            I(fmt("@%s bra %s", pn.c_str(), lno.c_str()));
+            I(fmt("xor.b32 %s, %s, %u", nslot.c_str(), slot.c_str(), slotB_));
+            I(fmt("add.u32 %s, %s, %s", nsb.c_str(), smb_.c_str(), nslot.c_str()));
+            std::string nbase = tile_base(bn);
+            prefetch(nbase, nsb);
+            I("cp.async.wait_group 1");
+            I(fmt("bra.uni %s", ldone.c_str()));
+            lab(lno);
+            I("cp.async.wait_group 0");
+            lab(ldone);
+        }
+        I("bar.sync 0");
+
+        for (int si = 0; si < pd_.step_count; ++si) round(hp_.steps[pd_.step_begin + si], base, sbase);
+
+        // write the tile back (one-state passes: only active items)
+        const std::string lskip = L();
+        if (NS_ == 1) {
+            const std::string lst = L();
+            std::string nact = P();
+            I(fmt("not.pred %s, %s", nact.c_str(), hasact_.c_str()));
+            I(fmt("@%s bra %s", nact.c_str(), lst.c_str()));
+            std::string ap = R64(), av = H16(), pz = P();
+            I(fmt("add.s64 %s, %s, %s", ap.c_str(), active_.c_str(), item.c_str()));
+            I(fmt("ld.global.u8 %s, [%s]", av.c_str(), ap.c_str()));
+            I(fmt("setp.eq.u16 %s, %s, 0", pz.c_str(), av.c_str()));
+            I(fmt("@%s bra %s", pz.c_str(), lskip.c_str()));
+            lab(lst);
+        }
+        for (int s = 0; s < NS_; ++s) {
+            std::string gp = thread_gptr(s, base);
+            for (int k = 0; k < PER_; ++k) {
+                std::string x = R32(), d = R32();
+                I(fmt("xor.b32 %s, %s, %u", x.c_str(), stidB_.c_str(), sk(k)));
+                I(fmt("add.u32 %s, %s, %s", d.c_str(), x.c_str(), sbase.c_str()));
+                std::string v0 = A(), v1 = A();
+                I(fmt("ld.shared.v2.%s {%s, %s}, [%s+%u]", ft_, v0.c_str(), v1.c_str(), d.c_str(), s * tileB_));
+                const std::string dst = gaddr(gp, k);
+                I(fmt("st.global.cs.v2.%s [%s], {%s, %s}", ft_, dst.c_str(), v0.c_str(), v1.c_str()));
+            }
+        }
+        lab(lskip);
+        I("bar.sync 0");
+        if (np_ > 0) {
+            // batched runs: this tile's probe sums, then zero them
+            const std::string lnp = L();
+            std::string pp = P(), pin = P();
+            I(fmt("setp.eq.u32 %s, %s, 0", pp.c_str(), perTile_.c_str()));
+            I(fmt("@%s bra %s", pp.c_str(), lnp.c_str()));
+            I(fmt("setp.lt.u32 %s, %s, %d", pin.c_str(), tid_.c_str(), np_));
+            const std::string lno = L();
+            std::string npin = P();
+            I(fmt("not.pred %s, %s", npin.c_str(), pin.c_str()));
+            I(fmt("@%s bra %s", npin.c_str(), lno.c_str()));
+            std::string a0 = R32();
+            I(fmt("mad.lo.u32 %s, %s, 8, %s", a0.c_str(), tid_.c_str(), paccB_.c_str()));
+            std::string s = D();
+            I(fmt("mov.f64 %s, 0d0000000000000000", s.c_str()));
+            for (int w = 0; w < NW_; ++w) {
+                std::string v = D(), n = D();
+                I(fmt("ld.shared.f64 %s, [%s+%d]", v.c_str(), a0.c_str(), w * np_ * 8));
+                I(fmt("add.rn.f64 %s, %s, %s", n.c_str(), s.c_str(), v.c_str()));
+                I(fmt("st.shared.u64 [%s+%d], 0", a0.c_str(), w * np_ * 8));
+                s = n;
+            }
+            std::string t64 = R64(), ix = R64(), ad = R64();
+            I(fmt("cvt.u64.u32 %s, %s", t64.c_str(), tid_.c_str()));
+            I(fmt("mad.lo.u64 %s, %s, %s, %s", ix.c_str(), t64.c_str(), ntiles_.c_str(), b.c_str()));
+            I(fmt("mad.lo.u64 %s, %s, 8, %s", ad.c_str(), ix.c_str(), partial_.c_str()));
+            I(fmt("st.global.f64 [%s], %s", ad.c_str(), s.c_str()));
+            lab(lno);
+            I("bar.sync 0");
+            lab(lnp);
+        }
+        // next tile (PTX registers are not SSA: the loop variables are updated in place)
+        I(fmt("add.s64 %s, %s, %s", b.c_str(), b.c_str(), nbid64_.c_str()));
+        if (sh_.nb == 2) I(fmt("xor.b32 %s, %s, %u", slot.c_str(), slot.c_str(), slotB_));
+        std::string pc = P();
+        I(fmt("setp.lt.u64 %s, %s, %s", pc.c_str(), b.c_str(), ntiles_.c_str()));
+        I(fmt("@%s bra %s", pc.c_str(), lloop.c_str()));
+        lab(lend);
+        if (np_ > 0) {
+            // single state: this CTA's per-probe totals
+            const std::string lx = L();
+            std::string pp = P(), pin = P();
+            I(fmt("setp.ne.u32 %s, %s, 0", pp.c_str(), perTile_.c_str()));
+            I(fmt("@%s bra %s", pp.c_str(), lx.c_str()));
+            I("bar.sync 0");
+            I(fmt("setp.ge.u32 %s, %s, %d", pin.c_str(), tid_.c_str(), np_));
+            I(fmt("@%s bra %s", pin.c_str(), lx.c_str()));
+            std::string a0 = R32();
+            I(fmt("mad.lo.u32 %s, %s, 8, %s", a0.c_str(), tid_.c_str(), paccB_.c_str()));
+            std::string s = D();
+            I(fmt("mov.f64 %s, 0d0000000000000000", s.c_str()));
+            for (int w = 0; w < NW_; ++w) {
+                std::string v = D(), n = D();
+                I(fmt("ld.shared.f64 %s, [%s+%d]", v.c_str(), a0.c_str(), w * np_ * 8));
+                I(fmt("add.rn.f64 %s, %s, %s", n.c_str(), s.c_str(), v.c_str()));
+                s = n;
+            }
+            std::string t64 = R64(), ix = R64(), ad = R64();
+            I(fmt("cvt.u64.u32 %s, %s", t64.c_str(), tid_.c_str()));
+            I(fmt("mad.lo.u64 %s, %s, %s, %s", ix.c_str(), t64.c_str(), nbid64_.c_str(), bid64_.c_str()));
+            I(fmt("mad.lo.u64 %s, %s, 8, %s", ad.c_str(), ix.c_str(), partial_.c_str()));
+            I(fmt("st.global.f64 [%s], %s", ad.c_str(), s.c_str()));
+            lab(lx);
+        }
+        I("ret");
+    }
+
+    // ---------------------------------------------------------------- rounds
+    std::string ctl_pred(const KOp& o, const std::string& gthr) {
+        std::string t = R64(), p = P();
+        I(fmt("and.b64 %s, %s, %llu", t.c_str(), gthr.c_str(), static_cast<unsigned long long>(o.cthr)));
+        I(fmt("setp.eq.u64 %s, %s, %llu", p.c_str(), t.c_str(), static_cast<unsigned long long>(o.cthr)));
+        return p;
+    }
+    std::string par_pred(const KOp& o, const std::string& gthr) {
+        std::string t = R64(), c = R32(), c1 = R32(), p = P();
+        I(fmt("and.b64 %s, %s, %llu", t.c_str(), gthr.c_str(), static_cast<unsigned long long>(o.pthr)));
+        I(fmt("popc.b64 %s, %s", c.c_str(), t.c_str()));
+        I(fmt("and.b32 %s, %s, 1", c1.c_str(), c.c_str()));
+        I(fmt("setp.ne.u32 %s, %s, 0", p.c_str(), c1.c_str()));
+        return p;
+    }
+
+    Cx phase(const Cx& a, const std::string& dr, const std::string& di, const std::string& ndi) {
+        // amp_phase: a * (dr + i di)
+        return {fma(ndi, a.y, mul(dr, a.x)), fma(di, a.x, mul(dr, a.y))};
+    }
+    Cx special(const Cx& a, int sp) {  // amp_special: * -1, * i, * -i
+        if (sp == SP_NEG1) return {neg(a.x), neg(a.y)};
+        if (sp == SP_I) return {neg(a.y), a.x};
+        return {a.y, neg(a.x)};
+    }
+    Cx special_value(int sp) {
+        if (sp == SP_NEG1) return {cnst(-1.0), cnst(0.0)};
+        if (sp == SP_I) return {cnst(0.0), cnst(1.0)};
+        return {cnst(0.0), cnst(-1.0)};
+    }
+    Cx rot_q(const Cx& a, const std::string& s1, const std::string& s2) {  // a * i^q, q = s1 + 2 s2
+        Cx t{sel(neg(a.y), a.x, s1), sel(a.x, a.y, s1)};
+        return {sel(neg(t.x), t.x, s2), sel(neg(t.y), t.y, s2)};
+    }
+
+    std::vector<int> pairs(int t, uint32_t creg) const {
+        std::vector<int> v;
+        for (int j = 0; j < NA_; ++j)
+            if (!((j >> t) & 1) && (static_cast<uint32_t>(j) & creg) == creg) v.push_back(j);
+        return v;
+    }
+
+    // the two diagonal entries of a DIAG op (constants where the flags fix them)
+    void diag_entries(const KOp& o, Cx* d0, Cx* d1) {
+        std::vector<std::string> c;
+        const bool need_load = !(o.flags & F_D0_ONE) || !(o.flags & F_D1_SPEC);
+        if (need_load) c = coefs(o.coef, 4);
+        *d0 = (o.flags & F_D0_ONE) ? Cx{cnst(1.0), cnst(0.0)} : Cx{c[0], c[1]};
+        *d1 = (o.flags & F_D1_SPEC) ? special_value(o.special) : Cx{c[2], c[3]};
+    }
+
+    void op_diag(const KOp& o, const std::string& gthr, const std::string& ctl) {
+        const bool tpar = (o.flags & F_TPAR) != 0;
+        std::string pt = tpar ? par_pred(o, gthr) : "";
+        if (o.flags & F_UNIFORM) {
+            if (!tpar) {
+                if (o.flags & F_D0_ONE) return;
+                std::vector<std::string> c = coefs(o.coef, 2);
+                phase_mul({c[0], c[1]}, ctl);
+                return;
+            }
+            if ((o.flags & F_D0_ONE) && (o.flags & F_D1_SPEC)) {
+                const int qa = o.special == SP_NEG1 ? 2 : (o.special == SP_I ? 1 : 3);
+                std::string pa = pt;
+                if (!ctl.empty()) {
+                    pa = P();
+                    I(fmt("and.pred %s, %s, %s", pa.c_str(), pt.c_str(), ctl.c_str()));
+                }
+                std::string v = R32(), nq = R32();
+                I(fmt("selp.b32 %s, %d, 0, %s", v.c_str(), qa, pa.c_str()));
+                if (q_.empty()) {
+                    q_ = v;
+                } else {
+                    I(fmt("add.u32 %s, %s, %s", nq.c_str(), q_.c_str(), v.c_str()));
+                    q_ = nq;
+                }
+                return;
+            }
+            Cx d0, d1;
+            diag_entries(o, &d0, &d1);
+            phase_mul({sel(d1.x, d0.x, pt), sel(d1.y, d0.y, pt)}, ctl);
+            return;
+        }
+        auto old = A_;
+        if (o.flags & F_ONEBIT) {
+            const int t = o.t0;
+            if (!tpar) {
+                std::vector<std::string> c;
+                if (!(o.flags & F_D0_ONE) || !(o.flags & F_D1_SPEC)) c = coefs(o.coef, 4);
+                for (int j = 0; j < NA_; ++j) {
+                    const int h = (j >> t) & 1;
+                    for (int s = 0; s < NS_; ++s) {
+                        if (h == 0) {
+                            if (o.flags & F_D0_ONE) continue;
+                            A_[s][j] = phase(A_[s][j], c[0], c[1], neg(c[1]));
+                        } else if (o.flags & F_D1_SPEC) {
+                            A_[s][j] = special(A_[s][j], o.special);
+                        } else {
+                            A_[s][j] = phase(A_[s][j], c[2], c[3], neg(c[3]));
+                        }
+                    }
+                }
+            } else {
+                Cx d0, d1;
+                diag_entries(o, &d0, &d1);
+                Cx f[2] = {{sel(d1.x, d0.x, pt), sel(d1.y, d0.y, pt)}, {sel(d0.x, d1.x, pt), sel(d0.y, d1.y, pt)}};
+                std::string nf[2] = {neg(f[0].y), neg(f[1].y)};
+                for (int j = 0; j < NA_; ++j) {
+                    const int h = (j >> t) & 1;
+                    for (int s = 0; s < NS_; ++s) A_[s][j] = phase(A_[s][j], f[h].x, f[h].y, nf[h]);
+                }
+            }
+        } else {
+            // parity over register bits (and the thread's), register controls
+            Cx d0, d1;
+            std::vector<std::string> c = coefs(o.coef, 4);
+            d0 = {c[0], c[1]};
+            d1 = {c[2], c[3]};
+            Cx f[2] = {d0, d1};
+            if (tpar) {
+                f[0] = {sel(d1.x, d0.x, pt), sel(d1.y, d0.y, pt)};
+                f[1] = {sel(d0.x, d1.x, pt), sel(d0.y, d1.y, pt)};
+            }
+            std::string nf[2] = {neg(f[0].y), neg(f[1].y)};
+            for (int j = 0; j < NA_; ++j) {
+                if ((static_cast<uint32_t>(j) & o.creg) != o.creg) continue;
+                const int par = __builtin_popcount(static_cast<uint32_t>(j) & o.preg) & 1;
+                for (int s = 0; s < NS_; ++s) A_[s][j] = phase(A_[s][j], f[par].x, f[par].y, nf[par]);
+            }
+        }
+        guard(old, ctl);
+    }
+
+    // round phase *= f (only where ctl holds, when given)
+    void phase_mul(const Cx& f, const std::string& ctl) {
+        Cx n;
+        if (!ph_on_) {
+            n = f;
+            if (!ctl.empty()) n = {sel(f.x, cnst(1.0), ctl), sel(f.y, cnst(0.0), ctl)};
+        } else {
+            n = phase(ph_, f.x, f.y, neg(f.y));
+            if (!ctl.empty()) n = {sel(n.x, ph_.x, ctl), sel(n.y, ph_.y, ctl)};
+        }
+        ph_ = n;
+        ph_on_ = true;
+    }
+
+    // thread-controlled op: keep the old values where the control is 0
+    void guard(const std::vector<std::vector<Cx>>& old, const std::string& ctl) {
+        if (ctl.empty()) return;
+        for (int s = 0; s < NS_; ++s)
+            for (int j = 0; j < NA_; ++j)
+                if (!same(A_[s][j], old[s][j]))
+                    A_[s][j] = {sel(A_[s][j].x, old[s][j].x, ctl), sel(A_[s][j].y, old[s][j].y, ctl)};
+    }
+
+    void op_gate(const KOp& o, const std::string& ctl) {
+        auto old = A_;
+        const int t = o.t0;
+        switch (o.kind) {
+            case K_X:
+                for (int j : pairs(t, o.creg))
+                    for (int s = 0; s < NS_; ++s) std::swap(A_[s][j], A_[s][j | (1 << t)]);
+                break;
+            case K_Y:
+                for (int j : pairs(t, o.creg))
+                    for (int s = 0; s < NS_; ++s) {
+                        const Cx a = A_[s][j], b = A_[s][j | (1 << t)];
+                        A_[s][j] = {b.y, neg(b.x)};
+                        A_[s][j | (1 << t)] = {neg(a.y), a.x};
+                    }
+                break;
+            case K_HAD:
+                for (int j : pairs(t, o.creg))
+                    for (int s = 0; s < NS_; ++s) {
+                        const Cx a = A_[s][j], b = A_[s][j | (1 << t)];
+                        A_[s][j] = {add(a.x, b.x), add(a.y, b.y)};
+                        A_[s][j | (1 << t)] = {sub(a.x, b.x), sub(a.y, b.y)};
+                    }
+                break;
+            case K_REAL: {
+                std::vector<std::string> m = coefs(o.coef, 4);
+                for (int j : pairs(t, o.creg))
+                    for (int s = 0; s < NS_; ++s) {
+                        const Cx a = A_[s][j], b = A_[s][j | (1 << t)];
+                        A_[s][j] = {fma(m[1], b.x, mul(m[0], a.x)), fma(m[1], b.y, mul(m[0], a.y))};
+                        A_[s][j | (1 << t)] = {fma(m[3], b.x, mul(m[2], a.x)), fma(m[3], b.y, mul(m[2], a.y))};
+                    }
+                break;
+            }
+            case K_RX: {
+                std::vector<std::string> m = coefs(o.coef, 2);
+                const std::string c = m[0], sn = m[1], ns = neg(m[1]);
+                for (int j : pairs(t, o.creg))
+                    for (int s = 0; s < NS_; ++s) {
+                        const Cx a = A_[s][j], b = A_[s][j | (1 << t)];
+                        A_[s][j] = {fma(sn, b.y, mul(c, a.x)), fma(ns, b.x, mul(c, a.y))};
+                        A_[s][j | (1 << t)] = {fma(sn, a.y, mul(c, b.x)), fma(ns, a.x, mul(c, b.y))};
+                    }
+                break;
+            }
+            case K_DENSE: {
+                std::vector<std::string> m = coefs(o.coef, 8);
+                std::string nmi[4];
+                for (int i = 0; i < 4; ++i) nmi[i] = neg(m[2 * i + 1]);
+                for (int j : pairs(t, o.creg))
+                    for (int s = 0; s < NS_; ++s) {
+                        const Cx a = A_[s][j], b = A_[s][j | (1 << t)];
+                        A_[s][j] = {fma(nmi[1], b.y, fma(m[2], b.x, fma(nmi[0], a.y, mul(m[0], a.x)))),
+                                    fma(m[3], b.x, fma(m[2], b.y, fma(m[1], a.x, mul(m[0], a.y))))};
+                        A_[s][j | (1 << t)] = {fma(nmi[3], b.y, fma(m[6], b.x, fma(nmi[2], a.y, mul(m[4], a.x)))),
+                                               fma(m[7], b.x, fma(m[6], b.y, fma(m[5], a.x, mul(m[4], a.y))))};
+                    }
+                break;
+            }
+            case K_SWAP: {
+                const int lo = o.t0 < o.t1 ? o.t0 : o.t1, hi = o.t0 < o.t1 ? o.t1 : o.t0;
+                for (int j = 0; j < NA_; ++j) {
+                    if (j & ((1 << lo) | (1 << hi))) continue;
+                    if ((static_cast<uint32_t>(j) & o.creg) != o.creg) continue;
+                    for (int s = 0; s < NS_; ++s) std::swap(A_[s][j | (1 << lo)], A_[s][j | (1 << hi)]);
+                }
+                break;
+            }
+            default: break;
+        }
+        guard(old, ctl);
+    }
+
+    // Im<lam| Q |psi> share of the thread, warp-summed, added to this warp's
+    // slot of the probe (probe_sum / reg_probe of adjoint.cuh)
+    void op_probe(const KOp& o, const std::string& gthr, const std::string& ctl) {
+        std::string ar, ai;
+        for (int j = 0; j < NA_; ++j) {
+            if ((static_cast<uint32_t>(j) & o.creg) != o.creg) continue;
+            const int jx = j ^ static_cast<int>(o.xreg);
+            const bool ng = (__builtin_popcount(static_cast<uint32_t>(jx) & o.preg) & 1) != 0;
+            const Cx l = A_[1][j], w = A_[0][jx];
+            const std::string zr = fma(l.x, w.x, mul(l.y, w.y));
+            const std::string zi = fma(l.x, w.y, neg(mul(l.y, w.x)));
+            if (ar.empty()) {
+                ar = ng ? neg(zr) : zr;
+                ai = ng ? neg(zi) : zi;
+            } else {
+                ar = ng ? sub(ar, zr) : add(ar, zr);
+                ai = ng ? sub(ai, zi) : add(ai, zi);
+            }
+        }
+        if (ar.empty()) ar = ai = cnst(0.0);
+        std::string v;
+        switch (o.special & 3) {
+            case 0: v = ai; break;
+            case 1: v = ar; break;
+            case 2: v = neg(ai); break;
+            default: v = neg(ar); break;
+        }
+        if (o.flags & F_TPAR) {
+            std::string pt = par_pred(o, gthr);
+            v = sel(neg(v), v, pt);
+        }
+        if (!ctl.empty()) v = sel(v, cnst(0.0), ctl);
+        for (int sh = 16; sh > 0; sh >>= 1) v = add(v, shfl(v, sh));
+        const int slot = o.probe;
+        std::string cur = D(), nxt = D();
+        if (f64_) {
+            std::string c = coefs(o.coef, 1)[0];
+            I(fmt("@%s ld.shared.f64 %s, [%s+%d]", lane0_.c_str(), cur.c_str(), paccW_.c_str(), slot * 8));
+            I(fmt("@%s fma.rn.f64 %s, %s, %s, %s", lane0_.c_str(), nxt.c_str(), v.c_str(), c.c_str(), cur.c_str()));
+        } else {
+            std::string c = coefs(o.coef, 1)[0];
+            std::string vf = mul(v, c), dv = D();
+            I(fmt("cvt.f64.f32 %s, %s", dv.c_str(), vf.c_str()));
+            I(fmt("@%s ld.shared.f64 %s, [%s+%d]", lane0_.c_str(), cur.c_str(), paccW_.c_str(), slot * 8));
+            I(fmt("@%s add.rn.f64 %s, %s, %s", lane0_.c_str(), nxt.c_str(), cur.c_str(), dv.c_str()));
+        }
+        I(fmt("@%s st.shared.f64 [%s+%d], %s", lane0_.c_str(), paccW_.c_str(), slot * 8, nxt.c_str()));
+    }
+    std::string shfl(const std::string& v, int lanemask) {
+        std::string d = A();
+        if (f64_) {
+            std::string lo = R32(), hi = R32(), lo2 = R32(), hi2 = R32();
+            I(fmt("mov.b64 {%s, %s}, %s", lo.c_str(), hi.c_str(), v.c_str()));
+            I(fmt("shfl.sync.bfly.b32 %s, %s, %d, 31, -1", lo2.c_str(), lo.c_str(), lanemask));
+            I(fmt("shfl.sync.bfly.b32 %s, %s, %d, 31, -1", hi2.c_str(), hi.c_str(), lanemask));
+            I(fmt("mov.b64 %s, {%s, %s}", d.c_str(), lo2.c_str(), hi2.c_str()));
+        } else {
+            std::string r = R32(), r2 = R32();
+            I(fmt("mov.b32 %s, %s", r.c_str(), v.c_str()));
+            I(fmt("shfl.sync.bfly.b32 %s, %s, %d, 31, -1", r2.c_str(), r.c_str(), lanemask));
+            I(fmt("mov.b32 %s, %s", d.c_str(), r2.c_str()));
+        }
+        return d;
+    }
+
+    void round(const StepDesc& sd, const std::string& base, const std::string& sbase) {
+        bool need_g = false;
+        for (int oi = 0; oi < sd.op_count; ++oi)
+            if (hp_.ops[sd.op_begin + oi].flags & (F_TCTRL | F_TPAR)) need_g = true;
+        std::vector<uint32_t> tsw(T_ - R_);
+        for (int k = 0; k < T_ - R_; ++k) tsw[k] = static_cast<uint32_t>(sd.tsw[k]) * es_;
+        std::string psb = xor32(tid_, T_ - R_, tsw);
+        std::string gthr;
+        if (need_g) {
+            std::vector<uint64_t> tg(T_ - R_);
+            for (int k = 0; k < T_ - R_; ++k) tg[k] = 1ULL << sd.tglob[k];
+            std::string td = deposit64(tid_, T_ - R_, tg);
+            gthr = R64();
+            I(fmt("or.b64 %s, %s, %s", gthr.c_str(), base.c_str(), td.c_str()));
+        }
+        auto offb = [&](int j) {
+            uint32_t o = 0;
+            for (int k = 0; k < R_; ++k)
+                if ((j >> k) & 1) o ^= static_cast<uint32_t>(sd.rsw[k]) * es_;
+            return o;
+        };
+        A_.assign(NS_, std::vector<Cx>(NA_));
+        for (int j = 0; j < NA_; ++j) {
+            std::string x = R32(), ad = R32();
+            I(fmt("xor.b32 %s, %s, %u", x.c_str(), psb.c_str(), offb(j)));
+            I(fmt("add.u32 %s, %s, %s", ad.c_str(), x.c_str(), sbase.c_str()));
+            for (int s = 0; s < NS_; ++s) {
+                Cx c{A(), A()};
+                I(fmt("ld.shared.v2.%s {%s, %s}, [%s+%u]", ft_, c.x.c_str(), c.y.c_str(), ad.c_str(), s * tileB_));
+                A_[s][j] = c;
+            }
+        }
+        ph_on_ = false;
+        q_.clear();
+        for (int oi = 0; oi < sd.op_count; ++oi) {
+            const KOp& o = hp_.ops[sd.op_begin + oi];
+            const std::string ctl = (o.flags & F_TCTRL) ? ctl_pred(o, gthr) : "";
+            if (o.kind == K_PROBE) op_probe(o, gthr, ctl);
+            else if (o.kind == K_DIAG) op_diag(o, gthr, ctl);
+            else op_gate(o, ctl);
+        }
+        // the round's uniform phase (reg_finish_phase)
+        if (!q_.empty()) {
+            std::string q1 = R32(), q2 = R32(), s1 = P(), s2 = P();
+            I(fmt("and.b32 %s, %s, 1", q1.c_str(), q_.c_str()));
+            I(fmt("and.b32 %s, %s, 2", q2.c_str(), q_.c_str()));
+            I(fmt("setp.ne.u32 %s, %s, 0", s1.c_str(), q1.c_str()));
+            I(fmt("setp.ne.u32 %s, %s, 0", s2.c_str(), q2.c_str()));
+            if (ph_on_) {
+                ph_ = rot_q(ph_, s1, s2);
+            } else {
+                for (int s = 0; s < NS_; ++s)
+                    for (int j = 0; j < NA_; ++j) A_[s][j] = rot_q(A_[s][j], s1, s2);
+            }
+        }
+        if (ph_on_) {
+            const std::string nfi = neg(ph_.y);
+            for (int s = 0; s < NS_; ++s)
+                for (int j = 0; j < NA_; ++j) A_[s][j] = phase(A_[s][j], ph_.x, ph_.y, nfi);
+        }
+        for (int j = 0; j < NA_; ++j) {
+            std::string x = R32(), ad = R32();
+            I(fmt("xor.b32 %s, %s, %u", x.c_str(), psb.c_str(), offb(j)));
+            I(fmt("add.u32 %s, %s, %s", ad.c_str(), x.c_str(), sbase.c_str()));
+            for (int s = 0; s < NS_; ++s)
+                I(fmt("st.shared.v2.%s [%s+%u], {%s, %s}", ft_, ad.c_str(), s * tileB_, A_[s][j].x.c_str(),
+                      A_[s][j].y.c_str()));
+        }
+        I("bar.sync 0");
+    }
+
+    // ---------------------------------------------------------------- state
+    const HostPlan& hp_;
+    const PassDesc& pd_;
+    JitShape sh_;
+    bool f64_;
+    const char* ft_;
+    int es_, cb_, gb_, T_, R_, NT_, NA_, NW_, PER_, NS_, np_;
+    uint32_t tileB_, slotB_;
+    std::string body_;
+    int nr_ = 0, nrd_ = 0, nh_ = 0, np_reg_ = 0, na_ = 0, nd_ = 0, nl_ = 0;
+    std::map<double, std::string> consts_;
+    std::string tid_, bid64_, nbid64_, stg_[2], ntiles_, coef0_, cstrideB_, ishift_, active_, hasact_, smb_;
+    std::string gtidB_, stidB_, lane0_, paccB_, paccW_, perTile_, partial_, coefp_;
+    std::vector<std::vector<Cx>> A_;
+    bool ph_on_ = false;
+    Cx ph_;
+    std::string q_;
+};
+
+}  // namespace
+
+namespace {
+template <class T>
+void put(std::string* k, const T& v) {
+    k->append(reinterpret_cast<const char*>(&v), sizeof(T));
+}
+}  // namespace
+
+bool jit_pass_key(const HostPlan& hp, int pi, const JitShape& sh, std::string* key, std::string* why) {
+    if (pi < 0 || pi >= static_cast<int>(hp.passes.size())) {
+        if (why) *why = "pass index out of range";
+        return false;
+    }
+    Gen g(hp, pi, sh);
+    if (!g.supported(why)) return false;
+    // every field the generator reads, explicitly (no struct padding)
+    const PassDesc& pd = hp.passes[pi];
+    std::string& k = *key;
+    k.clear();
+    put(&k, hp.arith);
+    put(&k, hp.T);
+    put(&k, hp.R);
+    put(&k, sh.nstates);
+    put(&k, sh.nb);
+    put(&k, sh.minb);
+    put(&k, pd.L);
+    put(&k, pd.H);
+    put(&k, pd.step_count);
+    put(&k, sh.nstates == 2 ? pd.nprobe : 0);
+    k.append(reinterpret_cast<const char*>(pd.tq), sizeof pd.tq);
+    for (int si = 0; si < pd.step_count; ++si) {
+        const StepDesc& sd = hp.steps[pd.step_begin + si];
+        put(&k, sd.type);
+        put(&k, sd.op_count);
+        k.append(reinterpret_cast<const char*>(sd.tglob), sizeof sd.tglob);
+        k.append(reinterpret_cast<const char*>(sd.rsw), sizeof sd.rsw);
+        k.append(reinterpret_cast<const char*>(sd.tsw), sizeof sd.tsw);
+        for (int oi = 0; oi < sd.op_count; ++oi) {
+            const KOp& o = hp.ops[sd.op_begin + oi];
+            put(&k, o.kind);
+            put(&k, o.flags);
+            put(&k, o.special);
+            put(&k, o.t0);
+            put(&k, o.t1);
+            put(&k, o.probe);
+            put(&k, o.creg);
+            put(&k, o.preg);
+            put(&k, o.cthr);
+            put(&k, o.pthr);
+            put(&k, o.coef);
+            put(&k, o.xreg);
+        }
+    }
+    return true;
+}
+
+bool jit_pass_ptx(const HostPlan& hp, int pi, const JitShape& sh, const std::string& entry, std::string* ptx,
+                  std::string* why) {
+    if (pi < 0 || pi >= static_cast<int>(hp.passes.size())) {
+        if (why) *why = "pass index out of range";
+        return false;
+    }
+    Gen g(hp, pi, sh);
+    if (!g.supported(why)) return false;
+    *ptx = g.emit(entry);
+    return true;
+}
+
+}  // namespace qsv

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "capi_internal.h"
+#include "jit.h"
 #include "kernels.h"
 
 using namespace qsv;
@@ -122,10 +123,14 @@ int run_plan_items(qfvm_plan* p, void* state, int items, const uint8_t* active, 
     for (size_t i = 0; i < hp.passes.size(); ++i) {
         const PassDesc& pd = hp.passes[i];
         cudaError_t e;
-        if (pd.type == PASS_TILE)
-            e = launch_tile_pass(hp.arith, hp.T, hp.R, state, p->dpass + i, p->dsteps, p->dops, p->dcoef, hp.n, pd.H,
-                                 items, 0, active, st);
-        else if (pd.type == PASS_SMALL)
+        if (pd.type == PASS_TILE) {
+            bool done = false;
+            e = qsv::jit_launch_pass(p, static_cast<int>(i), state, nullptr, p->dcoef, items, 0, active, 0, nullptr,
+                                     nullptr, st, &done);
+            if (e == cudaSuccess && !done)
+                e = launch_tile_pass(hp.arith, hp.T, hp.R, state, p->dpass + i, p->dsteps, p->dops, p->dcoef, hp.n,
+                                     pd.H, items, 0, active, st);
+        } else if (pd.type == PASS_SMALL)
             e = launch_small(hp.arith, state, 1ULL << hp.n, items, hp.n, p->dops + pd.op_begin, pd.op_count, p->dcoef,
                              0, active, st);
         else

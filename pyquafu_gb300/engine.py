@@ -175,6 +175,13 @@ class Plan:
                                                 nat.i32ptr(ty)), "plan run (timed)")
         return ms, ty
 
+    def jit_passes(self, nstates: int = 1) -> int:
+        """Passes of this plan that run as circuit-specialised kernels (known
+        after the first run)."""
+        c = ctypes.c_int64()
+        nat.check(self._lib.qfvm_jit_plan_passes(self._h, int(nstates), ctypes.byref(c)), "plan jit passes")
+        return c.value
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.qfvm_plan_destroy(self._h)
@@ -185,3 +192,17 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def jit_configure(enabled: bool = True, nb_one: int = 2, minb_one: int = 0, nb_two: int = 1, minb_two: int = 0):
+    """Circuit-specialised tile passes: on/off, and the tile buffers / minimum
+    resident CTAs per SM of one-state and two-state passes (0 = automatic).
+    Applies to plans prepared afterwards."""
+    nat.check(nat.load().qfvm_jit_configure(int(bool(enabled)), int(nb_one), int(minb_one), int(nb_two),
+                                            int(minb_two)), "jit configure")
+
+
+def jit_config() -> dict:
+    c = (ctypes.c_int32 * 5)()
+    nat.check(nat.load().qfvm_jit_get_config(c), "jit config")
+    return {"enabled": bool(c[0]), "nb_one": c[1], "minb_one": c[2], "nb_two": c[3], "minb_two": c[4]}

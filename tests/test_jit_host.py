@@ -1,0 +1,110 @@
+"""The PTX generator of circuit-specialised tile passes, on the CPU: every
+tile pass of representative plans (complex128 and complex64 one-state
+passes, reverse sweeps with probes, batched plans) is emitted, and where the
+toolkit's ptxas is on the PATH it must assemble for sm_103a (and compile
+through the library's own PTX compiler path); passes the
+generator does not handle are reported as unsupported, not emitted."""
+
+import ctypes
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import helpers
+from pyquafu_gb300 import _native as nat
+from pyquafu_gb300 import ir, workloads
+
+
+def plan_handle(n, ops, precision, T=0, R=0, batched=False, adjoint=False):
+    lib = nat.load()
+    arr, pool = ir.pack(ops)
+    h = ctypes.c_void_p()
+    if batched:
+        nat.check(lib.qfvm_plan_host_build_batched(n, precision, nat.vptr(arr), arr.size,
+                                                   nat.dptr(pool.view(np.float64)), pool.size, int(adjoint),
+                                                   ctypes.byref(h)))
+    else:
+        nat.check(lib.qfvm_plan_host_build(n, precision, nat.vptr(arr), arr.size, nat.dptr(pool.view(np.float64)),
+                                           pool.size, T, R, ctypes.byref(h)))
+    return h
+
+
+def pass_ptx(h, i, nstates):
+    lib = nat.load()
+    ln = ctypes.c_int64()
+    rc = lib.qfvm_jit_pass_ptx(h, i, nstates, None, 0, ctypes.byref(ln))
+    if rc != 0:
+        return None
+    buf = ctypes.create_string_buffer(ln.value + 1)
+    nat.check(lib.qfvm_jit_pass_ptx(h, i, nstates, buf, ln.value + 1, ctypes.byref(ln)))
+    return buf.value.decode()
+
+
+def assemble(tmp_path, src, tag):
+    exe = shutil.which("ptxas")
+    if exe is None:
+        return
+    f = tmp_path / f"{tag}.ptx"
+    f.write_text(src)
+    r = subprocess.run([exe, "-arch=sm_103a", "-O1", "-o", str(tmp_path / f"{tag}.cubin"), str(f)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+
+
+CASES = [
+    ("c128_11_3", 16, 0, 11, 3, False, False, 1),
+    ("c128_12_5", 16, 0, 12, 5, False, False, 1),
+    ("c64_13_4", 16, 1, 13, 4, False, False, 1),
+    ("c64_rev_batched", 16, 1, 0, 0, True, True, 2),
+    ("c128_rev_batched", 15, 0, 0, 0, True, True, 2),
+    ("c64_fwd_batched", 16, 1, 0, 0, True, False, 1),
+]
+
+
+@pytest.mark.parametrize("tag,n,precision,T,R,batched,adjoint,nstates", CASES)
+def test_passes_assemble(tmp_path, tag, n, precision, T, R, batched, adjoint, nstates):
+    if batched:
+        ops, _, _, _ = workloads.qnn_batch(batch=2, n=n, layers=2, seed=1)
+    else:
+        ops = workloads.random_layers(n, 4, seed=n + T, extras=True)
+    h = plan_handle(n, ops, precision, T, R, batched, adjoint)
+    counts = (ctypes.c_int64 * 4)()
+    shape = (ctypes.c_int32 * 3)()
+    nat.check(nat.load().qfvm_plan_host_counts(h, counts, shape))
+    passes = np.zeros(counts[0], helpers.PASS_DT)
+    nat.check(nat.load().qfvm_plan_host_copy(h, nat.vptr(passes), None, None, None))
+    emitted = 0
+    for i in range(counts[0]):
+        src = pass_ptx(h, i, nstates)
+        if int(passes[i]["type"]) != helpers.PASS_TILE:
+            assert src is None
+            continue
+        assert src is not None and ".target sm_103a" in src
+        emitted += 1
+        if i in (0, counts[0] - 1):
+            assemble(tmp_path, src, f"{tag}_{i}")
+            info = ctypes.create_string_buffer(4096)
+            rc = nat.load().qfvm_jit_pass_compile(h, i, nstates, info, 4096)
+            assert rc == 0, info.value.decode()
+    nat.load().qfvm_plan_destroy(h)
+    assert emitted > 0
+
+
+def test_probe_pass_needs_two_states():
+    ops, _, _, _ = workloads.qnn_batch(batch=2, n=16, layers=2, seed=1)
+    h = plan_handle(16, ops, 1, batched=True, adjoint=True)
+    assert pass_ptx(h, 0, 1) is None  # probes read lam
+    assert pass_ptx(h, 0, 2) is not None
+    nat.load().qfvm_plan_destroy(h)
+
+
+def test_jit_config_roundtrip():
+    from pyquafu_gb300 import engine
+
+    engine.jit_configure(True, 2, 1, 1, 2)
+    assert engine.jit_config() == {"enabled": True, "nb_one": 2, "minb_one": 1, "nb_two": 1, "minb_two": 2}
+    with pytest.raises(nat.QfvmError):
+        engine.jit_configure(True, 3, 0, 1, 0)
+    engine.jit_configure(True)
