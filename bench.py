@@ -233,12 +233,16 @@ S_OF = {"c128": 16, "c128_ds": 16, "c64": 8}
 POLICY_OF = {"c128": "P64", "c128_ds": "PDS", "c64": "P32"}
 
 
-def kernel_name(precision, n):
+def kernel_name(precision, n, specialised=False):
     """The one-state pass kernel a plan of n qubits runs (shape as resolved
-    by the engine: tuned or built-in)."""
+    by the engine: tuned or built-in): the circuit-specialised PTX kernel
+    `qsv_tile_pass` when the plan's passes were specialised, else the
+    interpreting k_pass instance."""
     from pyquafu_gb300 import autotune
 
     t, r = autotune.current(precision, 0, n)
+    if specialised:
+        return f"qsv_tile_pass<{POLICY_OF[precision]},{t},{r}> (specialised PTX)"
     return f"k_pass<{POLICY_OF[precision]},{t},{r}>"
 
 
@@ -254,9 +258,12 @@ def measure(precision, ops, n, steps, warmup, per_pass=True):
     st_plan = plan.stats()
     state = engine.DeviceState(n, precision).set_zero()
     stream = torch.cuda.ExternalStream(state.stream())
+    t_first = time.perf_counter()
     for _ in range(warmup):
         plan.run(state)
     torch.cuda.synchronize()
+    warm_s = time.perf_counter() - t_first  # includes compiling specialised passes
+    specialised = plan.jit_passes(1)
     l0 = nat.launch_count()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
@@ -276,7 +283,8 @@ def measure(precision, ops, n, steps, warmup, per_pass=True):
     gb = sum(gate_equiv_bytes(ops, n, S))
     out = {"precision": precision, "ms_per_step": ms_step, "gbps": gb / (ms_step * 1e-3) / 1e9,
            "passes": st_plan["passes"], "rounds": st_plan["rounds"], "gates": st_plan["gates"],
-           "pass_bytes": st_plan["pass_bytes"], "launches": int(launches)}
+           "pass_bytes": st_plan["pass_bytes"], "launches": int(launches),
+           "specialised_passes": int(specialised), "warmup_s": round(warm_s, 2)}
     if per_pass:
         pm = np.concatenate(pass_ms)
         pt = np.concatenate(pass_ty)
@@ -677,7 +685,8 @@ def run_gpu(args):
     for v in [x for x in args.variants.split(",") if x and x != args.precision]:
         r = measure(v, ops, n, args.steps, max(1, min(args.warmup, 3)))
         variants[v] = {"value": round(r["gbps"], 2), "unit": "GB/s", "ms_per_step": round(r["ms_per_step"], 3),
-                       "passes": r["passes"], "tile_kernel": kernel_name(v, n), "tile_pass_gbps": round(r["tile_gbps"], 1),
+                       "passes": r["passes"], "tile_kernel": kernel_name(v, n, r["specialised_passes"] > 0),
+                       "specialised_passes": r["specialised_passes"], "tile_pass_gbps": round(r["tile_gbps"], 1),
                        "tile_pass_frac_hbm": round(r["tile_gbps"] / peak, 4)}
 
     # --- end to end through the reference-shaped API (host buffers) ---
@@ -731,7 +740,8 @@ def run_gpu(args):
                        "seed": SEED, "gates": len(ops), "precision": args.precision, "passes": main["passes"],
                        "rounds": main["rounds"], "parallelism": "replicas" if world > 1 else "single",
                        "l2": "state >> L2 (no flush needed)"},
-            "roofline": {"bound": "hbm", "kernel": kernel_name(args.precision, n), "achieved": round(achieved, 1),
+            "roofline": {"bound": "hbm", "kernel": kernel_name(args.precision, n, main["specialised_passes"] > 0),
+                         "achieved": round(achieved, 1),
                          "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                          "traffic": None, "bytes_per_launch": main["tile_bytes"],
                          "avg_launch_ms": round(main["avg_tile_ms"], 3)},
@@ -744,6 +754,8 @@ def run_gpu(args):
             "autotune": tuning,
             "clocks": clk,
             "gpu_launches": int(main["launches"]),
+            "specialised": {"passes": main["specialised_passes"], "of": main["passes"],
+                            "first_runs_s": main["warmup_s"]},
         }
         if args.precision == "c128":
             line["fp64"] = {"instr_per_s": fp64 / (ms_step * 1e-3),
