@@ -331,12 +331,12 @@ int qfvm_plan_host_counts(const qfvm_plan* plan, int64_t counts[4], int32_t shap
 int qfvm_plan_host_copy(const qfvm_plan* plan, void* passes, void* steps, void* kops, double* coef);
 
 /* ---------------------------------------------------------------------------
- * Circuit-specialised tile passes.  Tile passes of complex128 (FP64) and
- * complex64 plans are, by default, emitted as straight-line PTX for sm_103a
- * (every register round unrolled with its targets, controls and coefficient
- * offsets as constants) and compiled once per distinct pass by the driver;
- * passes the generator does not handle, and complex128 double-single plans,
- * run the interpreting kernels.  The environment variable QFVM_JIT=0 turns
+ * Circuit-specialised tile passes.  Tile passes of complex128 (FP64 and
+ * double-single) and complex64 plans are, by default, emitted as
+ * straight-line PTX for sm_103a (every register round unrolled with its
+ * targets, controls and coefficient offsets as constants) and compiled once
+ * per distinct pass; passes the generator does not handle (shared-memory
+ * steps, double-single reverse sweeps) run the interpreting kernels.  The environment variable QFVM_JIT=0 turns
  * specialisation off at start-up.
  * ------------------------------------------------------------------------- */
 /* enabled: 0/1; nb_*: tile buffers (1 or 2) of one-state / two-state passes;

@@ -201,7 +201,7 @@ int jit_prepare(qfvm_plan* p, int nstates, std::string* err) {
     JitShape sh;
     {
         std::lock_guard<std::mutex> lk(g_mu);
-        if (!config().enabled || (hp.arith != QFVM_C64 && hp.arith != QFVM_C128)) {
+        if (!config().enabled || (hp.arith != QFVM_C64 && hp.arith != QFVM_C128 && hp.arith != QFVM_C128_DS)) {
             p->jit[si] = ks;
             p->jit_ready[si] = true;
             return 0;
@@ -225,7 +225,7 @@ int jit_prepare(qfvm_plan* p, int nstates, std::string* err) {
         // double buffering only where both tiles fit in a CTA's shared memory
         int optin = 0;
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        const size_t tile = static_cast<size_t>(hp.arith == QFVM_C128 ? 16 : 8) << hp.T;
+        const size_t tile = static_cast<size_t>(hp.arith == QFVM_C64 ? 8 : 16) << hp.T;
         const size_t pacc = static_cast<size_t>(1 << (hp.T - hp.R)) / 32 * MAX_PASS_PROBES * 8;
         if (sh.nb == 2 && 2 * nstates * tile + pacc > static_cast<size_t>(optin)) sh.nb = 1;
     }
@@ -291,7 +291,7 @@ int jit_prepare(qfvm_plan* p, int nstates, std::string* err) {
         const int np = nstates == 2 ? hp.passes[i].nprobe : 0;
         k->threads = nt;
         k->T = hp.T;
-        k->smem = static_cast<size_t>(sh.nb) * nstates * (static_cast<size_t>(hp.arith == QFVM_C128 ? 16 : 8) << hp.T) +
+        k->smem = static_cast<size_t>(sh.nb) * nstates * (static_cast<size_t>(hp.arith == QFVM_C64 ? 8 : 16) << hp.T) +
                   static_cast<size_t>(nt / 32) * np * 8;
         if (load(dev, images[w], k.get(), err)) return 1;
         cache().emplace(keys[i], std::move(k));

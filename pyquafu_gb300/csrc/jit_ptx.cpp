@@ -48,10 +48,11 @@ class Gen {
     Gen(const HostPlan& hp, int pi, const JitShape& sh)
         : hp_(hp), pd_(hp.passes[pi]), sh_(sh) {
         f64_ = hp.arith == QFVM_C128;
+        ds_ = hp.arith == QFVM_C128_DS;
         ft_ = f64_ ? "f64" : "f32";
-        es_ = f64_ ? 16 : 8;
-        cb_ = f64_ ? 8 : 4;
-        gb_ = f64_ ? 3 : 4;
+        es_ = (f64_ || ds_) ? 16 : 8;
+        cb_ = (f64_ || ds_) ? 8 : 4;
+        gb_ = (f64_ || ds_) ? 3 : 4;
         T_ = hp.T;
         R_ = hp.R;
         NT_ = 1 << (T_ - R_);
@@ -65,7 +66,9 @@ class Gen {
     }
 
     bool supported(std::string* why) const {
-        if (hp_.arith != QFVM_C64 && hp_.arith != QFVM_C128) return no(why, "arithmetic without a generator");
+        if (hp_.arith != QFVM_C64 && hp_.arith != QFVM_C128 && hp_.arith != QFVM_C128_DS)
+            return no(why, "arithmetic without a generator");
+        if (ds_ && NS_ != 1) return no(why, "double-single reverse sweeps run interpreted");
         if (pd_.type != PASS_TILE) return no(why, "not a tile pass");
         if (T_ - R_ < 6 || T_ > 13 || R_ < 1 || R_ > 5) return no(why, "tile shape out of range");
         if (np_ > NT_ || np_ > MAX_PASS_PROBES) return no(why, "too many probes");
@@ -127,29 +130,81 @@ class Gen {
     }
     void lab(const std::string& l) { body_ += l + ":\n"; }
 
-    // amplitude-type arithmetic (policy.cuh: mul / madd / add / neg)
+    // Amplitude-type arithmetic (policy.cuh: mul / madd / add / neg).  A real
+    // value is a register name, or for double-single "high|low" (two f32).
+    static std::pair<std::string, std::string> hl(const std::string& v) {
+        const size_t k = v.find('|');
+        return {v.substr(0, k), v.substr(k + 1)};
+    }
+    std::string f32op(const char* op, const std::string& a, const std::string& b) {
+        std::string d = A();
+        I(fmt("%s.rn.f32 %s, %s, %s", op, d.c_str(), a.c_str(), b.c_str()));
+        return d;
+    }
+    std::string f32fma(const std::string& a, const std::string& b, const std::string& c) {
+        std::string d = A();
+        I(fmt("fma.rn.f32 %s, %s, %s, %s", d.c_str(), a.c_str(), b.c_str(), c.c_str()));
+        return d;
+    }
+    std::string f32neg(const std::string& a) {
+        std::string d = A();
+        I(fmt("neg.f32 %s, %s", d.c_str(), a.c_str()));
+        return d;
+    }
+    // double-single: a + b (TwoSum on the high parts), c * x unnormalised
+    std::string ds_add(const std::string& a, const std::string& b) {
+        auto [ah, al] = hl(a);
+        auto [bh, bl] = hl(b);
+        const std::string sh = f32op("add", ah, bh);
+        const std::string v = f32op("sub", sh, ah);
+        std::string e = f32op("add", f32op("sub", ah, f32op("sub", sh, v)), f32op("sub", bh, v));
+        e = f32op("add", e, f32op("add", al, bl));
+        const std::string h = f32op("add", sh, e);
+        return h + "|" + f32op("sub", e, f32op("sub", h, sh));
+    }
+    std::string ds_mul_raw(const std::string& c, const std::string& x) {
+        auto [ch, cl] = hl(c);
+        auto [xh, xl] = hl(x);
+        const std::string p = f32op("mul", ch, xh);
+        std::string e = f32fma(ch, xh, f32neg(p));
+        e = f32fma(ch, xl, e);
+        e = f32fma(cl, xh, e);
+        return p + "|" + e;
+    }
     std::string mul(const std::string& c, const std::string& x) {
+        if (ds_) {
+            auto [ph, pl] = hl(ds_mul_raw(c, x));
+            const std::string h = f32op("add", ph, pl);
+            return h + "|" + f32op("sub", pl, f32op("sub", h, ph));
+        }
         std::string d = A();
         I(fmt("mul.rn.%s %s, %s, %s", ft_, d.c_str(), c.c_str(), x.c_str()));
         return d;
     }
     std::string fma(const std::string& c, const std::string& x, const std::string& acc) {
+        if (ds_) return ds_add(acc, ds_mul_raw(c, x));
         std::string d = A();
         I(fmt("fma.rn.%s %s, %s, %s, %s", ft_, d.c_str(), c.c_str(), x.c_str(), acc.c_str()));
         return d;
     }
     std::string add(const std::string& x, const std::string& y) {
+        if (ds_) return ds_add(x, y);
         std::string d = A();
         I(fmt("add.rn.%s %s, %s, %s", ft_, d.c_str(), x.c_str(), y.c_str()));
         return d;
     }
     std::string sub(const std::string& x, const std::string& y) {
+        if (ds_) return ds_add(x, neg(y));
         std::string d = A();
         I(fmt("sub.rn.%s %s, %s, %s", ft_, d.c_str(), x.c_str(), y.c_str()));
         return d;
     }
     // exact sign flip (FP64: on the integer high word, no FP64 instruction)
     std::string neg(const std::string& x) {
+        if (ds_) {
+            auto [h, l] = hl(x);
+            return f32neg(h) + "|" + f32neg(l);
+        }
         std::string d = A();
         if (f64_) {
             std::string t = R64(), u = R64();
@@ -162,25 +217,81 @@ class Gen {
         return d;
     }
     std::string sel(const std::string& a, const std::string& b, const std::string& p) {  // p ? a : b
+        if (ds_) {
+            auto [ah, al] = hl(a);
+            auto [bh, bl] = hl(b);
+            std::string h = A(), l = A();
+            I(fmt("selp.f32 %s, %s, %s, %s", h.c_str(), ah.c_str(), bh.c_str(), p.c_str()));
+            I(fmt("selp.f32 %s, %s, %s, %s", l.c_str(), al.c_str(), bl.c_str(), p.c_str()));
+            return h + "|" + l;
+        }
         std::string d = A();
         I(fmt("selp.%s %s, %s, %s, %s", ft_, d.c_str(), a.c_str(), b.c_str(), p.c_str()));
+        return d;
+    }
+    std::string f32const(float f) {
+        uint32_t u;
+        std::memcpy(&u, &f, 4);
+        std::string d = A();
+        I(fmt("mov.f32 %s, 0f%08X", d.c_str(), u));
         return d;
     }
     std::string cnst(double v) {
         auto it = consts_.find(v);
         if (it != consts_.end()) return it->second;
-        std::string d = A();
-        if (f64_) {
+        std::string d;
+        if (ds_) {
+            const float h = static_cast<float>(v);
+            const float l = static_cast<float>(v - static_cast<double>(h));
+            d = f32const(h) + "|" + f32const(l);
+        } else if (f64_) {
+            d = A();
             uint64_t u;
             std::memcpy(&u, &v, 8);
             I(fmt("mov.f64 %s, 0d%016llX", d.c_str(), static_cast<unsigned long long>(u)));
         } else {
-            const float f = static_cast<float>(v);
-            uint32_t u;
-            std::memcpy(&u, &f, 4);
-            I(fmt("mov.f32 %s, 0f%08X", d.c_str(), u));
+            d = f32const(static_cast<float>(v));
         }
         consts_[v] = d;
+        return d;
+    }
+    // complex amplitude <-> shared memory (double-single: (re.h, re.l, im.h, im.l))
+    Cx load_amp(const std::string& addr, uint32_t off) {
+        if (ds_) {
+            std::string r[4] = {A(), A(), A(), A()};
+            I(fmt("ld.shared.v4.f32 {%s, %s, %s, %s}, [%s+%u]", r[0].c_str(), r[1].c_str(), r[2].c_str(),
+                  r[3].c_str(), addr.c_str(), off));
+            return {r[0] + "|" + r[1], r[2] + "|" + r[3]};
+        }
+        Cx c{A(), A()};
+        I(fmt("ld.shared.v2.%s {%s, %s}, [%s+%u]", ft_, c.x.c_str(), c.y.c_str(), addr.c_str(), off));
+        return c;
+    }
+    void store_amp(const std::string& addr, uint32_t off, const Cx& c) {
+        if (ds_) {
+            auto [xh, xl] = hl(c.x);
+            auto [yh, yl] = hl(c.y);
+            I(fmt("st.shared.v4.f32 [%s+%u], {%s, %s, %s, %s}", addr.c_str(), off, xh.c_str(), xl.c_str(),
+                  yh.c_str(), yl.c_str()));
+            return;
+        }
+        I(fmt("st.shared.v2.%s [%s+%u], {%s, %s}", ft_, addr.c_str(), off, c.x.c_str(), c.y.c_str()));
+    }
+    // double-single <-> FP64 (ds_from_double / ds_to_double of policy.cuh)
+    std::string ds_from(const std::string& v) {
+        std::string h = A(), l = A(), hd = D(), r = D();
+        I(fmt("cvt.rn.f32.f64 %s, %s", h.c_str(), v.c_str()));
+        I(fmt("cvt.f64.f32 %s, %s", hd.c_str(), h.c_str()));
+        I(fmt("sub.rn.f64 %s, %s, %s", r.c_str(), v.c_str(), hd.c_str()));
+        I(fmt("cvt.rn.f32.f64 %s, %s", l.c_str(), r.c_str()));
+        return h + "|" + l;
+    }
+    std::string ds_to(const std::string& v) {
+        auto [h, l] = hl(v);
+        std::string a = D(), b = D(), d = D();
+        I(fmt("cvt.f64.f32 %s, %s", a.c_str(), h.c_str()));
+        I(fmt("cvt.f64.f32 %s, %s", b.c_str(), l.c_str()));
+        I(fmt("add.rn.f64 %s, %s, %s", d.c_str(), a.c_str(), b.c_str()));
         return d;
     }
     // coefficients off .. off+cnt-1 of the tile's pool (widest aligned loads)
@@ -189,6 +300,22 @@ class Gen {
         uint32_t i = off;
         const uint32_t end = off + cnt;
         while (i < end) {
+            if (ds_) {  // (high, low) float pairs, two per 16-byte load
+                if (i % 2 == 0 && i + 2 <= end) {
+                    std::string r[4] = {A(), A(), A(), A()};
+                    I(fmt("ld.global.nc.v4.f32 {%s, %s, %s, %s}, [%s+%u]", r[0].c_str(), r[1].c_str(),
+                          r[2].c_str(), r[3].c_str(), coefp_.c_str(), i * cb_));
+                    c.push_back(r[0] + "|" + r[1]);
+                    c.push_back(r[2] + "|" + r[3]);
+                    i += 2;
+                } else {
+                    std::string h = A(), l = A();
+                    I(fmt("ld.global.nc.v2.f32 {%s, %s}, [%s+%u]", h.c_str(), l.c_str(), coefp_.c_str(), i * cb_));
+                    c.push_back(h + "|" + l);
+                    ++i;
+                }
+                continue;
+            }
             int vec = 1;
             if (!f64_ && i % 4 == 0 && i + 4 <= end) vec = 4;
             else if (i % 2 == 0 && i + 2 <= end) vec = 2;
@@ -418,6 +545,16 @@ class Gen {
             lab(ldone);
         }
         I("bar.sync 0");
+        if (ds_) {
+            for (int k = 0; k < PER_; ++k) {
+                std::string x = R32(), d = R32(), re = D(), im = D();
+                I(fmt("xor.b32 %s, %s, %u", x.c_str(), stidB_.c_str(), sk(k)));
+                I(fmt("add.u32 %s, %s, %s", d.c_str(), x.c_str(), sbase.c_str()));
+                I(fmt("ld.shared.v2.f64 {%s, %s}, [%s]", re.c_str(), im.c_str(), d.c_str()));
+                store_amp(d, 0, {ds_from(re), ds_from(im)});
+            }
+            I("bar.sync 0");
+        }
 
         for (int si = 0; si < pd_.step_count; ++si) round(hp_.steps[pd_.step_begin + si], base, sbase);
 
@@ -441,10 +578,16 @@ class Gen {
                 std::string x = R32(), d = R32();
                 I(fmt("xor.b32 %s, %s, %u", x.c_str(), stidB_.c_str(), sk(k)));
                 I(fmt("add.u32 %s, %s, %s", d.c_str(), x.c_str(), sbase.c_str()));
-                std::string v0 = A(), v1 = A();
-                I(fmt("ld.shared.v2.%s {%s, %s}, [%s+%u]", ft_, v0.c_str(), v1.c_str(), d.c_str(), s * tileB_));
                 const std::string dst = gaddr(gp, k);
-                I(fmt("st.global.cs.v2.%s [%s], {%s, %s}", ft_, dst.c_str(), v0.c_str(), v1.c_str()));
+                if (ds_) {
+                    const Cx c = load_amp(d, s * tileB_);
+                    const std::string re = ds_to(c.x), im = ds_to(c.y);
+                    I(fmt("st.global.cs.v2.f64 [%s], {%s, %s}", dst.c_str(), re.c_str(), im.c_str()));
+                } else {
+                    std::string v0 = A(), v1 = A();
+                    I(fmt("ld.shared.v2.%s {%s, %s}, [%s+%u]", ft_, v0.c_str(), v1.c_str(), d.c_str(), s * tileB_));
+                    I(fmt("st.global.cs.v2.%s [%s], {%s, %s}", ft_, dst.c_str(), v0.c_str(), v1.c_str()));
+                }
             }
         }
         lab(lskip);
@@ -836,11 +979,7 @@ class Gen {
             std::string x = R32(), ad = R32();
             I(fmt("xor.b32 %s, %s, %u", x.c_str(), psb.c_str(), offb(j)));
             I(fmt("add.u32 %s, %s, %s", ad.c_str(), x.c_str(), sbase.c_str()));
-            for (int s = 0; s < NS_; ++s) {
-                Cx c{A(), A()};
-                I(fmt("ld.shared.v2.%s {%s, %s}, [%s+%u]", ft_, c.x.c_str(), c.y.c_str(), ad.c_str(), s * tileB_));
-                A_[s][j] = c;
-            }
+            for (int s = 0; s < NS_; ++s) A_[s][j] = load_amp(ad, s * tileB_);
         }
         ph_on_ = false;
         q_.clear();
@@ -874,9 +1013,7 @@ class Gen {
             std::string x = R32(), ad = R32();
             I(fmt("xor.b32 %s, %s, %u", x.c_str(), psb.c_str(), offb(j)));
             I(fmt("add.u32 %s, %s, %s", ad.c_str(), x.c_str(), sbase.c_str()));
-            for (int s = 0; s < NS_; ++s)
-                I(fmt("st.shared.v2.%s [%s+%u], {%s, %s}", ft_, ad.c_str(), s * tileB_, A_[s][j].x.c_str(),
-                      A_[s][j].y.c_str()));
+            for (int s = 0; s < NS_; ++s) store_amp(ad, s * tileB_, A_[s][j]);
         }
         I("bar.sync 0");
     }
@@ -885,7 +1022,7 @@ class Gen {
     const HostPlan& hp_;
     const PassDesc& pd_;
     JitShape sh_;
-    bool f64_;
+    bool f64_, ds_;
     const char* ft_;
     int es_, cb_, gb_, T_, R_, NT_, NA_, NW_, PER_, NS_, np_;
     uint32_t tileB_, slotB_;

@@ -1,6 +1,7 @@
 """Circuit-specialised tile passes (PTX generated per pass and compiled by the
 driver) against the interpreting kernels and the oracle, on the same inputs:
-one-state passes in complex128 and complex64 for several tile shapes and
+one-state passes in complex128 (FP64 and double-single arithmetic) and
+complex64 for several tile shapes and
 both buffering modes, reverse sweeps with probes (adjoint gradients), batched
 groups (per-item coefficients, per-tile probe sums) and per-shot
 trajectories whose classically controlled blocks use the active-item mask.
@@ -16,7 +17,7 @@ from pyquafu_gb300.batch import BatchSession
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"c128": 1e-12, "c64": 1e-5}
+TOL = {"c128": 1e-12, "c128_ds": 1e-12, "c64": 1e-5}
 
 
 @pytest.fixture(autouse=True)
@@ -39,7 +40,8 @@ def run_state(n, ops, precision, T, R, jit, nb=1, minb=0):
 
 
 @pytest.mark.parametrize("precision,T,R", [("c128", 11, 3), ("c128", 11, 4), ("c128", 12, 5),
-                                           ("c64", 13, 4), ("c64", 12, 5), ("c64", 12, 4)])
+                                           ("c64", 13, 4), ("c64", 12, 5), ("c64", 12, 4),
+                                           ("c128_ds", 12, 3), ("c128_ds", 11, 4)])
 @pytest.mark.parametrize("nb", [1, 2])
 def test_one_state_passes(precision, T, R, nb):
     n = 17

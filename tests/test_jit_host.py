@@ -1,6 +1,7 @@
 """The PTX generator of circuit-specialised tile passes, on the CPU: every
 tile pass of representative plans (complex128 and complex64 one-state
-passes, reverse sweeps with probes, batched plans) is emitted, and where the
+passes, double-single passes, reverse sweeps with probes, batched plans)
+is emitted, and where the
 toolkit's ptxas is on the PATH it must assemble for sm_103a (and compile
 through the library's own PTX compiler path); passes the
 generator does not handle are reported as unsupported, not emitted."""
@@ -57,6 +58,7 @@ CASES = [
     ("c128_11_3", 16, 0, 11, 3, False, False, 1),
     ("c128_12_5", 16, 0, 12, 5, False, False, 1),
     ("c64_13_4", 16, 1, 13, 4, False, False, 1),
+    ("ds_12_3", 16, 2, 12, 3, False, False, 1),
     ("c64_rev_batched", 16, 1, 0, 0, True, True, 2),
     ("c128_rev_batched", 15, 0, 0, 0, True, True, 2),
     ("c64_fwd_batched", 16, 1, 0, 0, True, False, 1),
