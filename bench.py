@@ -236,13 +236,14 @@ POLICY_OF = {"c128": "P64", "c128_ds": "PDS", "c64": "P32"}
 def kernel_name(precision, n, specialised=False):
     """The one-state pass kernel a plan of n qubits runs (shape as resolved
     by the engine: tuned or built-in): the circuit-specialised PTX kernel
-    `qsv_tile_pass` when the plan's passes were specialised, else the
+    `qsv_tile_pass_*` when the plan's passes were specialised, else the
     interpreting k_pass instance."""
     from pyquafu_gb300 import autotune
 
     t, r = autotune.current(precision, 0, n)
     if specialised:
-        return f"qsv_tile_pass<{POLICY_OF[precision]},{t},{r}> (specialised PTX)"
+        name = {"c128": "qsv_tile_pass_c128", "c128_ds": "qsv_tile_pass_ds", "c64": "qsv_tile_pass_c64"}[precision]
+        return f"{name} (specialised PTX, tile {t}, registers {r})"
     return f"k_pass<{POLICY_OF[precision]},{t},{r}>"
 
 

@@ -164,14 +164,11 @@ cudaError_t launch_small2_p(void* psi, void* lam, int n, const KOp* dops, int no
 
 void adjoint_shape(int arith, int* T, int* R) {
     if (arith == QFVM_C64) {
-        *T = 13;
-        *R = 4;
-    } else if (arith == QFVM_C128_DS) {
-        *T = 11;
+        *T = 12;
         *R = 4;
     } else {
         *T = 11;
-        *R = 3;
+        *R = 4;
     }
 }
 

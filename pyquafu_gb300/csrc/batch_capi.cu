@@ -180,8 +180,8 @@ int add_group(qfvm_batch* b, int n, const qfvm_op* ops, int64_t n_ops, const dou
     {
         // specialised kernels now: graph captures must not compile
         std::string jerr;
-        if (jit_prepare(g->fwd, 1, &jerr) || (grads && jit_prepare(g->rev, 2, &jerr)))
-            return bail(fail(QFVM_ERR_CUDA, jerr));
+        jit_prepare(g->fwd, 1, &jerr);
+        if (grads) jit_prepare(g->rev, 2, &jerr);
     }
     cudaStream_t st = g->stream;
     rc = make_pool(g->fwd, arith, g->items, &g->fpool, &g->fstride, st);

@@ -74,6 +74,7 @@ std::string cu_error(CUresult r) {
 }
 
 struct Kernel {
+    std::string entry;
     CUmodule mod = nullptr;
     CUfunction fn = nullptr;
     int threads = 0;
@@ -152,7 +153,7 @@ int load(int dev, const std::string& image, Kernel* k, std::string* err) {
         *err = "specialised pass load failed: " + cu_error(r) + ": " + log;
         return 1;
     }
-    r = d.get_function(&k->fn, k->mod, "qsv_tile_pass");
+    r = d.get_function(&k->fn, k->mod, k->entry.c_str());
     if (r == CUDA_SUCCESS && k->smem > 48 * 1024)
         r = d.set_attribute(k->fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, static_cast<int>(k->smem));
     int per_sm = 0;
@@ -184,6 +185,11 @@ JitShape shape_for(const HostPlan& hp, int nstates) {
 
 }  // namespace
 
+std::string jit_entry_name(int arith, int nstates) {
+    const char* a = arith == QFVM_C64 ? "c64" : (arith == QFVM_C128_DS ? "ds" : "c128");
+    return std::string(nstates == 2 ? "qsv_tile_sweep_" : "qsv_tile_pass_") + a;
+}
+
 JitConfig jit_config() {
     std::lock_guard<std::mutex> lk(g_mu);
     return config();
@@ -193,9 +199,30 @@ void jit_set_config(const JitConfig& c) {
     config() = c;
 }
 
+namespace {
+int prepare_impl(qfvm_plan* p, int nstates, std::string* err);
+}
+
+// A pass that cannot be compiled runs on the interpreting kernel: the
+// failure is reported once on stderr and the plan continues without
+// specialised passes for that state count.
 int jit_prepare(qfvm_plan* p, int nstates, std::string* err) {
     const int si = nstates == 2 ? 1 : 0;
     if (p->jit_ready[si]) return 0;
+    if (prepare_impl(p, nstates, err) == 0) return 0;
+    static bool warned = false;
+    if (!warned) {
+        warned = true;
+        std::fprintf(stderr, "qfvm: specialised passes unavailable, interpreting kernels used: %s\n", err->c_str());
+    }
+    p->jit[si].assign(p->hp.passes.size(), nullptr);
+    p->jit_ready[si] = true;
+    return 0;
+}
+
+namespace {
+int prepare_impl(qfvm_plan* p, int nstates, std::string* err) {
+    const int si = nstates == 2 ? 1 : 0;
     const HostPlan& hp = p->hp;
     std::vector<const void*> ks(hp.passes.size(), nullptr);
     JitShape sh;
@@ -268,7 +295,7 @@ int jit_prepare(qfvm_plan* p, int nstates, std::string* err) {
                     w = next++;
                 }
                 std::string ptx, why;
-                if (!jit_pass_ptx(hp, todo[w], sh, "qsv_tile_pass", &ptx, &why)) {
+                if (!jit_pass_ptx(hp, todo[w], sh, jit_entry_name(hp.arith, nstates), &ptx, &why)) {
                     errs[w] = "specialised pass: " + why;
                     continue;
                 }
@@ -291,6 +318,7 @@ int jit_prepare(qfvm_plan* p, int nstates, std::string* err) {
         const int np = nstates == 2 ? hp.passes[i].nprobe : 0;
         k->threads = nt;
         k->T = hp.T;
+        k->entry = jit_entry_name(hp.arith, nstates);
         k->smem = static_cast<size_t>(sh.nb) * nstates * (static_cast<size_t>(hp.arith == QFVM_C64 ? 8 : 16) << hp.T) +
                   static_cast<size_t>(nt / 32) * np * 8;
         if (load(dev, images[w], k.get(), err)) return 1;
@@ -305,6 +333,7 @@ int jit_prepare(qfvm_plan* p, int nstates, std::string* err) {
     p->jit_ready[si] = true;
     return 0;
 }
+}  // namespace
 
 void jit_release(qfvm_plan* p) {
     for (int s = 0; s < 2; ++s) {
@@ -331,10 +360,7 @@ cudaError_t jit_launch_pass(qfvm_plan* p, int pi, void* psi, void* lam, const vo
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return cudaSuccess;
         std::string err;
-        if (jit_prepare(p, nstates, &err)) {
-            std::fprintf(stderr, "qfvm: %s\n", err.c_str());
-            return cudaErrorInvalidPtx;
-        }
+        jit_prepare(p, nstates, &err);
     }
     if (pi < 0 || pi >= static_cast<int>(p->jit[si].size()) || !p->jit[si][pi]) return cudaSuccess;
     const Kernel* k = static_cast<const Kernel*>(p->jit[si][pi]);
@@ -397,7 +423,7 @@ int qfvm_jit_pass_ptx(const qfvm_plan* plan, int32_t pass, int32_t nstates, char
     sh.nb = nstates == 1 ? c.nb1 : c.nb2;
     sh.minb = nstates == 1 ? c.minb1 : c.minb2;
     std::string ptx, why;
-    if (!qsv::jit_pass_ptx(plan->hp, pass, sh, "qsv_tile_pass", &ptx, &why))
+    if (!qsv::jit_pass_ptx(plan->hp, pass, sh, qsv::jit_entry_name(plan->hp.arith, nstates), &ptx, &why))
         return fail(QFVM_ERR_UNSUPPORTED, "pass runs interpreted: " + why);
     *len = static_cast<int64_t>(ptx.size());
     if (text) {
@@ -415,7 +441,7 @@ int qfvm_jit_pass_compile(const qfvm_plan* plan, int32_t pass, int32_t nstates, 
     sh.nb = nstates == 1 ? c.nb1 : c.nb2;
     sh.minb = nstates == 1 ? c.minb1 : c.minb2;
     std::string ptx, why, image, err, log;
-    if (!qsv::jit_pass_ptx(plan->hp, pass, sh, "qsv_tile_pass", &ptx, &why))
+    if (!qsv::jit_pass_ptx(plan->hp, pass, sh, qsv::jit_entry_name(plan->hp.arith, nstates), &ptx, &why))
         return fail(QFVM_ERR_UNSUPPORTED, "pass runs interpreted: " + why);
     const bool ok = qsv::to_cubin(ptx, &image, &err, &log);
     if (info && capacity > 0) {

@@ -26,6 +26,10 @@ struct JitShape {
 bool jit_pass_ptx(const HostPlan& hp, int pi, const JitShape& sh, const std::string& entry, std::string* ptx,
                   std::string* why);
 
+// Kernel name of a specialised pass: qsv_tile_pass_<c128|ds|c64> (one
+// state) or qsv_tile_sweep_<c128|c64> (reverse sweep with probes).
+std::string jit_entry_name(int arith, int nstates);
+
 // Everything the generator reads for pass `pi` (the module cache key);
 // false when the pass is not handled.
 bool jit_pass_key(const HostPlan& hp, int pi, const JitShape& sh, std::string* key, std::string* why);
@@ -41,7 +45,8 @@ void jit_set_config(const JitConfig& c);
 
 // Compiles every eligible tile pass of `p` for `nstates` (no-op when the
 // plan's arithmetic or the switch rules it out).  Call outside stream
-// capture.  Returns a CUDA-style error for a failed compile.
+// capture.  A failed compile leaves the plan on the interpreting kernels
+// (reported once on stderr, message in *err); the return value is 0.
 int jit_prepare(qfvm_plan* p, int nstates, std::string* err);
 void jit_release(qfvm_plan* p);
 

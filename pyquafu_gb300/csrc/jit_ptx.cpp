@@ -417,10 +417,9 @@ class Gen {
         gtidB_ = deposit64(tid_, T_ - R_, gv);
         stidB_ = xor32(tid_, T_ - R_, sv);
         if (np_ > 0) {
-            std::string lane = R32(), warp = R32();
-            lane0_ = P();
-            I(fmt("and.b32 %s, %s, 31", lane.c_str(), tid_.c_str()));
-            I(fmt("setp.eq.u32 %s, %s, 0", lane0_.c_str(), lane.c_str()));
+            std::string warp = R32();
+            lane_ = R32();
+            I(fmt("and.b32 %s, %s, 31", lane_.c_str(), tid_.c_str()));
             I(fmt("shr.u32 %s, %s, 5", warp.c_str(), tid_.c_str()));
             paccB_ = R32();
             I(fmt("add.u32 %s, %s, %u", paccB_.c_str(), smb_.c_str(), slotB_ * sh_.nb));
@@ -888,26 +887,41 @@ class Gen {
         guard(old, ctl);
     }
 
-    // Im<lam| Q |psi> share of the thread, warp-summed, added to this warp's
-    // slot of the probe (probe_sum / reg_probe of adjoint.cuh)
+    // Im<lam| Q |psi> share of the thread (probe_sum / reg_probe of
+    // adjoint.cuh, the register terms summed as a balanced tree).  The
+    // thread values of up to 8 probes wait in registers and are warp-summed
+    // together (flush_probes).
     void op_probe(const KOp& o, const std::string& gthr, const std::string& ctl) {
-        std::string ar, ai;
+        struct Term {
+            std::string r;
+            bool neg;
+        };
+        std::vector<Term> tr, ti;
         for (int j = 0; j < NA_; ++j) {
             if ((static_cast<uint32_t>(j) & o.creg) != o.creg) continue;
             const int jx = j ^ static_cast<int>(o.xreg);
             const bool ng = (__builtin_popcount(static_cast<uint32_t>(jx) & o.preg) & 1) != 0;
             const Cx l = A_[1][j], w = A_[0][jx];
-            const std::string zr = fma(l.x, w.x, mul(l.y, w.y));
-            const std::string zi = fma(l.x, w.y, neg(mul(l.y, w.x)));
-            if (ar.empty()) {
-                ar = ng ? neg(zr) : zr;
-                ai = ng ? neg(zi) : zi;
-            } else {
-                ar = ng ? sub(ar, zr) : add(ar, zr);
-                ai = ng ? sub(ai, zi) : add(ai, zi);
-            }
+            tr.push_back({fma(l.x, w.x, mul(l.y, w.y)), ng});
+            ti.push_back({fma(l.x, w.y, neg(mul(l.y, w.x))), ng});
         }
-        if (ar.empty()) ar = ai = cnst(0.0);
+        auto tree = [&](std::vector<Term> t) -> std::string {
+            if (t.empty()) return cnst(0.0);
+            while (t.size() > 1) {
+                std::vector<Term> n;
+                for (size_t i = 0; i + 1 < t.size(); i += 2) {
+                    const Term& a = t[i];
+                    const Term& b = t[i + 1];
+                    if (a.neg == b.neg) n.push_back({add(a.r, b.r), a.neg});
+                    else if (a.neg) n.push_back({sub(b.r, a.r), false});
+                    else n.push_back({sub(a.r, b.r), false});
+                }
+                if (t.size() & 1) n.push_back(t.back());
+                t.swap(n);
+            }
+            return t[0].neg ? neg(t[0].r) : t[0].r;
+        };
+        const std::string ar = tree(tr), ai = tree(ti);
         std::string v;
         switch (o.special & 3) {
             case 0: v = ai; break;
@@ -920,21 +934,69 @@ class Gen {
             v = sel(neg(v), v, pt);
         }
         if (!ctl.empty()) v = sel(v, cnst(0.0), ctl);
-        for (int sh = 16; sh > 0; sh >>= 1) v = add(v, shfl(v, sh));
-        const int slot = o.probe;
-        std::string cur = D(), nxt = D();
+        pending_.push_back({v, static_cast<int>(o.probe), o.coef});
+        if (static_cast<int>(pending_.size()) == (f64_ ? 4 : 8)) flush_probes();
+    }
+
+    // Warp sums of the pending probes with one butterfly: at each of the
+    // first log2(P) exchanges a lane keeps half of its values and sends the
+    // other half, so P values cost about P shuffles instead of 5 P.  Lane L
+    // ends with probe L >> (5 - log2 P); the first lane of each group adds
+    // the warp total (times the generator scale) to this warp's slot.
+    void flush_probes() {
+        const int n = static_cast<int>(pending_.size());
+        if (n == 0) return;
+        int k = 0;
+        while ((1 << k) < n) ++k;
+        std::vector<std::string> vals;
+        for (const auto& q : pending_) vals.push_back(q.v);
+        while (static_cast<int>(vals.size()) < (1 << k)) vals.push_back(cnst(0.0));
+        for (int st = 0; st < k; ++st) {
+            const int m = 16 >> st;
+            std::string t = R32(), b = P();
+            I(fmt("and.b32 %s, %s, %d", t.c_str(), lane_.c_str(), m));
+            I(fmt("setp.ne.u32 %s, %s, 0", b.c_str(), t.c_str()));
+            const size_t half = vals.size() / 2;
+            std::vector<std::string> nv;
+            for (size_t i = 0; i < half; ++i) {
+                const std::string keep = sel(vals[half + i], vals[i], b);
+                const std::string send = sel(vals[i], vals[half + i], b);
+                nv.push_back(add(keep, shfl(send, m)));
+            }
+            vals.swap(nv);
+        }
+        std::string v = vals[0];
+        for (int st = k; st < 5; ++st) v = add(v, shfl(v, 16 >> st));
+        // writer lanes and their probe
+        const int lowbits = 5 - k;
+        std::string pl = R32(), lo = R32(), w = P(), pin = P();
+        I(fmt("shr.u32 %s, %s, %d", pl.c_str(), lane_.c_str(), lowbits));
+        I(fmt("and.b32 %s, %s, %d", lo.c_str(), lane_.c_str(), (1 << lowbits) - 1));
+        I(fmt("setp.eq.u32 %s, %s, 0", w.c_str(), lo.c_str()));
+        I(fmt("setp.lt.and.u32 %s, %s, %d, %s", pin.c_str(), pl.c_str(), n, w.c_str()));
+        std::string c = coefs(pending_[0].coef, 1)[0];
+        std::string off = R32();
+        I(fmt("mov.u32 %s, %d", off.c_str(), pending_[0].slot * 8));
+        for (int i = 1; i < n; ++i) {
+            std::string pi = P(), no = R32();
+            I(fmt("setp.eq.u32 %s, %s, %d", pi.c_str(), pl.c_str(), i));
+            c = sel(coefs(pending_[i].coef, 1)[0], c, pi);
+            I(fmt("selp.b32 %s, %d, %s, %s", no.c_str(), pending_[i].slot * 8, off.c_str(), pi.c_str()));
+            off = no;
+        }
+        std::string ad = R32(), cur = D(), nxt = D();
+        I(fmt("add.u32 %s, %s, %s", ad.c_str(), paccW_.c_str(), off.c_str()));
         if (f64_) {
-            std::string c = coefs(o.coef, 1)[0];
-            I(fmt("@%s ld.shared.f64 %s, [%s+%d]", lane0_.c_str(), cur.c_str(), paccW_.c_str(), slot * 8));
-            I(fmt("@%s fma.rn.f64 %s, %s, %s, %s", lane0_.c_str(), nxt.c_str(), v.c_str(), c.c_str(), cur.c_str()));
+            I(fmt("@%s ld.shared.f64 %s, [%s]", pin.c_str(), cur.c_str(), ad.c_str()));
+            I(fmt("@%s fma.rn.f64 %s, %s, %s, %s", pin.c_str(), nxt.c_str(), v.c_str(), c.c_str(), cur.c_str()));
         } else {
-            std::string c = coefs(o.coef, 1)[0];
             std::string vf = mul(v, c), dv = D();
             I(fmt("cvt.f64.f32 %s, %s", dv.c_str(), vf.c_str()));
-            I(fmt("@%s ld.shared.f64 %s, [%s+%d]", lane0_.c_str(), cur.c_str(), paccW_.c_str(), slot * 8));
-            I(fmt("@%s add.rn.f64 %s, %s, %s", lane0_.c_str(), nxt.c_str(), cur.c_str(), dv.c_str()));
+            I(fmt("@%s ld.shared.f64 %s, [%s]", pin.c_str(), cur.c_str(), ad.c_str()));
+            I(fmt("@%s add.rn.f64 %s, %s, %s", pin.c_str(), nxt.c_str(), cur.c_str(), dv.c_str()));
         }
-        I(fmt("@%s st.shared.f64 [%s+%d], %s", lane0_.c_str(), paccW_.c_str(), slot * 8, nxt.c_str()));
+        I(fmt("@%s st.shared.f64 [%s], %s", pin.c_str(), ad.c_str(), nxt.c_str()));
+        pending_.clear();
     }
     std::string shfl(const std::string& v, int lanemask) {
         std::string d = A();
@@ -990,6 +1052,7 @@ class Gen {
             else if (o.kind == K_DIAG) op_diag(o, gthr, ctl);
             else op_gate(o, ctl);
         }
+        flush_probes();
         // the round's uniform phase (reg_finish_phase)
         if (!q_.empty()) {
             std::string q1 = R32(), q2 = R32(), s1 = P(), s2 = P();
@@ -1030,7 +1093,13 @@ class Gen {
     int nr_ = 0, nrd_ = 0, nh_ = 0, np_reg_ = 0, na_ = 0, nd_ = 0, nl_ = 0;
     std::map<double, std::string> consts_;
     std::string tid_, bid64_, nbid64_, stg_[2], ntiles_, coef0_, cstrideB_, ishift_, active_, hasact_, smb_;
-    std::string gtidB_, stidB_, lane0_, paccB_, paccW_, perTile_, partial_, coefp_;
+    std::string gtidB_, stidB_, lane_, paccB_, paccW_, perTile_, partial_, coefp_;
+    struct Pending {
+        std::string v;
+        int slot;
+        uint32_t coef;
+    };
+    std::vector<Pending> pending_;
     std::vector<std::vector<Cx>> A_;
     bool ph_on_ = false;
     Cx ph_;
