@@ -13,6 +13,40 @@
 
 namespace qsv {
 
+// Bits of the nonzero entries of a row-major 2x2 complex matrix k[8]
+// (bit j <-> k[j]).  Products with exact zeros are skipped below: they add
+// exact zeros, so the skipped forms compute the same sums.
+__device__ __forceinline__ uint32_t nonzero_mask(const double* k) {
+    uint32_t nz = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if (k[j] != 0.0) nz |= 1u << j;
+    return nz;
+}
+
+// One output row of K (a, c)^T: (k0 + i k1) a + (k2 + i k3) c, zero terms
+// skipped (nz: the row's 4 mask bits).
+__device__ __forceinline__ double2 row_apply(const double* k, uint32_t nz, double2 a, double2 c) {
+    double re = 0.0, im = 0.0;
+    if (nz & 1) {
+        re = __fma_rn(k[0], a.x, re);
+        im = __fma_rn(k[0], a.y, im);
+    }
+    if (nz & 2) {
+        re = __fma_rn(-k[1], a.y, re);
+        im = __fma_rn(k[1], a.x, im);
+    }
+    if (nz & 4) {
+        re = __fma_rn(k[2], c.x, re);
+        im = __fma_rn(k[2], c.y, im);
+    }
+    if (nz & 8) {
+        re = __fma_rn(-k[3], c.y, re);
+        im = __fma_rn(k[3], c.x, im);
+    }
+    return make_double2(re, im);
+}
+
 // part[(item * bpi + b) * (m + 1) + i] = block b's sum of ||K_i (a_g0, a_g1)||^2
 // for i < m, and of |a_g0|^2 + |a_g1|^2 at i = m; groups g = the pairs on qubit q
 __global__ void __launch_bounds__(256) k_channel_norms(const double2* __restrict__ state, int n, int q, int m,
@@ -25,8 +59,11 @@ __global__ void __launch_bounds__(256) k_channel_norms(const double2* __restrict
     const uint64_t g0 = b * groups_per_block;
     const uint64_t g1 = g0 + groups_per_block < ng ? g0 + groups_per_block : ng;
     double acc[MAX_CHANNEL_OPS + 1];
+    uint32_t nz[MAX_CHANNEL_OPS];
 #pragma unroll
     for (int i = 0; i <= MAX_CHANNEL_OPS; ++i) acc[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < MAX_CHANNEL_OPS; ++i) nz[i] = i < m ? nonzero_mask(mats + 8 * i) : 0u;
     for (uint64_t g = g0 + threadIdx.x; g < g1; g += 256) {
         const uint64_t i0 = insert0(g, q), i1 = i0 | (1ULL << q);
         const double2 a = st[i0], c = st[i1];
@@ -35,11 +72,16 @@ __global__ void __launch_bounds__(256) k_channel_norms(const double2* __restrict
         for (int i = 0; i < MAX_CHANNEL_OPS; ++i) {
             if (i >= m) break;
             const double* k = mats + 8 * i;  // row-major 2x2, (re, im) pairs
-            const double v0r = k[0] * a.x - k[1] * a.y + k[2] * c.x - k[3] * c.y;
-            const double v0i = k[0] * a.y + k[1] * a.x + k[2] * c.y + k[3] * c.x;
-            const double v1r = k[4] * a.x - k[5] * a.y + k[6] * c.x - k[7] * c.y;
-            const double v1i = k[4] * a.y + k[5] * a.x + k[6] * c.y + k[7] * c.x;
-            acc[i] += v0r * v0r + v0i * v0i + v1r * v1r + v1i * v1i;
+            double s = 0.0;
+            if (nz[i] & 0x0f) {
+                const double2 v = row_apply(k, nz[i] & 0x0f, a, c);
+                s = __fma_rn(v.x, v.x, __dmul_rn(v.y, v.y));
+            }
+            if (nz[i] & 0xf0) {
+                const double2 v = row_apply(k + 4, nz[i] >> 4, a, c);
+                s = __fma_rn(v.x, v.x, __fma_rn(v.y, v.y, s));
+            }
+            acc[i] += s;
         }
     }
     for (int i = 0; i <= m; ++i) {
@@ -99,24 +141,31 @@ __global__ void k_channel_choose(const double* __restrict__ part, int bpi, int m
     }
 }
 
-// Every item's own 2x2 matrix on qubit q: one thread per (item, pair).
+// Every item's own 2x2 matrix on qubit q: one thread per (item, pair).  An
+// item whose matrix is exactly the identity (the common pick of a unitary
+// channel) is not touched; zero entries are skipped.
 __global__ void __launch_bounds__(256) k_item_gate1(double2* __restrict__ state, int n, int q, int items,
                                                     const double* __restrict__ imat) {
     const uint64_t ng = 1ULL << (n - 1);
     const uint64_t total = ng * static_cast<uint64_t>(items);
+    uint64_t cur = ~0ULL;
+    uint32_t nz = 0;
+    bool ident = false;
+    const double* k = imat;
     for (uint64_t t = blockIdx.x * 256ULL + threadIdx.x; t < total; t += gridDim.x * 256ULL) {
         const uint64_t item = t / ng, g = t - item * ng;
+        if (item != cur) {
+            cur = item;
+            k = imat + 8 * item;
+            nz = nonzero_mask(k);
+            ident = nz == 0x41u && k[0] == 1.0 && k[6] == 1.0;
+        }
+        if (ident) continue;
         double2* st = state + (item << n);
-        const double* k = imat + 8 * item;
         const uint64_t i0 = insert0(g, q), i1 = i0 | (1ULL << q);
         const double2 a = st[i0], c = st[i1];
-        double2 v0, v1;
-        v0.x = k[0] * a.x - k[1] * a.y + k[2] * c.x - k[3] * c.y;
-        v0.y = k[0] * a.y + k[1] * a.x + k[2] * c.y + k[3] * c.x;
-        v1.x = k[4] * a.x - k[5] * a.y + k[6] * c.x - k[7] * c.y;
-        v1.y = k[4] * a.y + k[5] * a.x + k[6] * c.y + k[7] * c.x;
-        st[i0] = v0;
-        st[i1] = v1;
+        st[i0] = row_apply(k, nz & 0x0f, a, c);
+        st[i1] = row_apply(k + 4, nz >> 4, a, c);
     }
 }
 
