@@ -111,9 +111,12 @@ cudaError_t launch_items_copy(void* state, int n, int items, const void* psi0, c
 namespace qsv {
 // noise.cu: per-shot noise channels on one qubit, per-item final sample
 constexpr int MAX_CHANNEL_OPS = 8;
-cudaError_t launch_channel(void* state, int n, int q, int m, int kraus, const double* dmats, const double* dprobs,
-                           int items, const double* duni, int draw, int ndraws, double* dpart, double* dimat,
-                           cudaStream_t st);
+int channel_blocks_per_item(int n);  // CTAs per item of the Kraus-norm reduction
+// cross: some Kraus operator's Gram matrix K^dagger K has a nonzero
+// off-diagonal entry (the norms then need sum conj(a) c as well)
+cudaError_t launch_channel(void* state, int n, int q, int m, int kraus, int cross, const double* dmats,
+                           const double* dprobs, int items, const double* duni, int draw, int ndraws, double* dpart,
+                           double* dimat, cudaStream_t st);
 cudaError_t launch_item_sample(const void* state, int n, int items, const double* duni, int draw, int ndraws,
                                uint64_t* dout, cudaStream_t st);
 }  // namespace qsv

@@ -14,13 +14,14 @@
 namespace qsv {
 
 // Bits of the nonzero entries of a row-major 2x2 complex matrix k[8]
-// (bit j <-> k[j]).  Products with exact zeros are skipped below: they add
-// exact zeros, so the skipped forms compute the same sums.
+// (bit j <-> k[j]), from the bit patterns (integer work only).  Products
+// with exact zeros are skipped below: they add exact zeros, so the skipped
+// forms compute the same sums.
 __device__ __forceinline__ uint32_t nonzero_mask(const double* k) {
     uint32_t nz = 0;
 #pragma unroll
     for (int j = 0; j < 8; ++j)
-        if (k[j] != 0.0) nz |= 1u << j;
+        if (static_cast<uint64_t>(__double_as_longlong(k[j])) << 1) nz |= 1u << j;
     return nz;
 }
 
@@ -47,46 +48,50 @@ __device__ __forceinline__ double2 row_apply(const double* k, uint32_t nz, doubl
     return make_double2(re, im);
 }
 
-// part[(item * bpi + b) * (m + 1) + i] = block b's sum of ||K_i (a_g0, a_g1)||^2
-// for i < m, and of |a_g0|^2 + |a_g1|^2 at i = m; groups g = the pairs on qubit q
-__global__ void __launch_bounds__(256) k_channel_norms(const double2* __restrict__ state, int n, int q, int m,
-                                                       const double* __restrict__ mats, uint64_t groups_per_block,
-                                                       int bpi, double* __restrict__ part) {
+// Kraus norms through the Gram matrices M_i = K_i^dagger K_i: summed over
+// the pairs (a, c) of qubit q,
+//   sum ||K_i (a, c)||^2 = m00 sum|a|^2 + m11 sum|c|^2 + 2 Re(m01 sum conj(a) c),
+// so the state is reduced once to four sums, whatever the number of
+// operators.  part[(item * bpi + b) * 4 + {0,1,2,3}] = block b's
+// sum |a|^2, sum |c|^2, Re and Im of sum conj(a) c (CROSS: the last two are
+// needed only when some m01 is nonzero).
+constexpr int NORM_PAIRS = 8;
+template <bool CROSS>
+__global__ void __launch_bounds__(256) k_channel_norms(const double2* __restrict__ state, int n, int q, int bpi,
+                                                       double* __restrict__ part) {
     __shared__ double red[8];
     const int item = blockIdx.x / bpi, b = blockIdx.x - item * bpi;
     const double2* st = state + (static_cast<uint64_t>(item) << n);
     const uint64_t ng = 1ULL << (n - 1);
-    const uint64_t g0 = b * groups_per_block;
-    const uint64_t g1 = g0 + groups_per_block < ng ? g0 + groups_per_block : ng;
-    double acc[MAX_CHANNEL_OPS + 1];
-    uint32_t nz[MAX_CHANNEL_OPS];
+    const uint64_t g0 = static_cast<uint64_t>(b) * 256 * NORM_PAIRS + threadIdx.x;
+    double sa = 0.0, sc = 0.0, xr = 0.0, xi = 0.0;
 #pragma unroll
-    for (int i = 0; i <= MAX_CHANNEL_OPS; ++i) acc[i] = 0.0;
-#pragma unroll
-    for (int i = 0; i < MAX_CHANNEL_OPS; ++i) nz[i] = i < m ? nonzero_mask(mats + 8 * i) : 0u;
-    for (uint64_t g = g0 + threadIdx.x; g < g1; g += 256) {
-        const uint64_t i0 = insert0(g, q), i1 = i0 | (1ULL << q);
-        const double2 a = st[i0], c = st[i1];
-        acc[MAX_CHANNEL_OPS] += a.x * a.x + a.y * a.y + c.x * c.x + c.y * c.y;
-#pragma unroll
-        for (int i = 0; i < MAX_CHANNEL_OPS; ++i) {
-            if (i >= m) break;
-            const double* k = mats + 8 * i;  // row-major 2x2, (re, im) pairs
-            double s = 0.0;
-            if (nz[i] & 0x0f) {
-                const double2 v = row_apply(k, nz[i] & 0x0f, a, c);
-                s = __fma_rn(v.x, v.x, __dmul_rn(v.y, v.y));
+    for (int r = 0; r < NORM_PAIRS; ++r) {
+        const uint64_t g = g0 + static_cast<uint64_t>(r) * 256;
+        if (g < ng) {
+            const uint64_t i0 = insert0(g, q), i1 = i0 | (1ULL << q);
+            const double2 a = st[i0], c = st[i1];
+            sa = __fma_rn(a.x, a.x, __fma_rn(a.y, a.y, sa));
+            sc = __fma_rn(c.x, c.x, __fma_rn(c.y, c.y, sc));
+            if (CROSS) {
+                xr = __fma_rn(a.x, c.x, __fma_rn(a.y, c.y, xr));
+                xi = __fma_rn(a.x, c.y, __fma_rn(-a.y, c.x, xi));
             }
-            if (nz[i] & 0xf0) {
-                const double2 v = row_apply(k + 4, nz[i] >> 4, a, c);
-                s = __fma_rn(v.x, v.x, __fma_rn(v.y, v.y, s));
-            }
-            acc[i] += s;
         }
     }
-    for (int i = 0; i <= m; ++i) {
-        const double s = block_sum<256>(acc[i == m ? MAX_CHANNEL_OPS : i], red);
-        if (threadIdx.x == 0) part[(static_cast<size_t>(blockIdx.x)) * (m + 1) + i] = s;
+    double* out = part + static_cast<size_t>(blockIdx.x) * 4;
+    double v = block_sum<256>(sa, red);
+    if (threadIdx.x == 0) out[0] = v;
+    v = block_sum<256>(sc, red);
+    if (threadIdx.x == 0) out[1] = v;
+    if (CROSS) {
+        v = block_sum<256>(xr, red);
+        if (threadIdx.x == 0) out[2] = v;
+        v = block_sum<256>(xi, red);
+        if (threadIdx.x == 0) out[3] = v;
+    } else if (threadIdx.x == 0) {
+        out[2] = 0.0;
+        out[3] = 0.0;
     }
 }
 
@@ -115,16 +120,22 @@ __global__ void k_channel_choose(const double* __restrict__ part, int bpi, int m
         }
         if (pick < 0) pick = m - 1;
     } else {
-        double nrm[MAX_CHANNEL_OPS + 1];
-        for (int i = 0; i <= m; ++i) {
-            double s = 0.0;
-            for (int b = 0; b < bpi; ++b) s += part[(static_cast<size_t>(item) * bpi + b) * (m + 1) + i];
-            nrm[i] = s;
-        }
-        const double norm0 = sqrt(nrm[m]);
+        double sum[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int b = 0; b < bpi; ++b)
+            for (int j = 0; j < 4; ++j) sum[j] += part[(static_cast<size_t>(item) * bpi + b) * 4 + j];
+        const double norm0 = sqrt(sum[0] + sum[1]);
         double s = 0.0;
         for (int i = 0; i < m; ++i) {
-            const double norm1 = sqrt(nrm[i]);
+            // M = K^dagger K: m00 = |k00|^2 + |k10|^2, m11 = |k01|^2 + |k11|^2,
+            // m01 = conj(k00) k01 + conj(k10) k11
+            const double* k = mats + 8 * i;
+            const double m00 = k[0] * k[0] + k[1] * k[1] + k[4] * k[4] + k[5] * k[5];
+            const double m11 = k[2] * k[2] + k[3] * k[3] + k[6] * k[6] + k[7] * k[7];
+            const double m01r = k[0] * k[2] + k[1] * k[3] + k[4] * k[6] + k[5] * k[7];
+            const double m01i = k[0] * k[3] - k[1] * k[2] + k[4] * k[7] - k[5] * k[6];
+            double nrm = m00 * sum[0] + m11 * sum[1] + 2.0 * (m01r * sum[2] - m01i * sum[3]);
+            if (nrm < 0.0) nrm = 0.0;  // rounding of a vanishing norm
+            const double norm1 = sqrt(nrm);
             s += norm1 / norm0;
             if (u < s) {
                 pick = i;
@@ -141,27 +152,25 @@ __global__ void k_channel_choose(const double* __restrict__ part, int bpi, int m
     }
 }
 
-// Every item's own 2x2 matrix on qubit q: one thread per (item, pair).  An
-// item whose matrix is exactly the identity (the common pick of a unitary
-// channel) is not touched; zero entries are skipped.
-__global__ void __launch_bounds__(256) k_item_gate1(double2* __restrict__ state, int n, int q, int items,
+// Every item's own 2x2 matrix on qubit q: a run of CTAs per item, each
+// thread a few pairs.  An item whose matrix is exactly the identity (the
+// usual pick of a unitary channel) is not touched; zero entries are skipped.
+constexpr int GATE1_PAIRS = 8;  // pairs per thread
+__global__ void __launch_bounds__(256) k_item_gate1(double2* __restrict__ state, int n, int q, int bpi,
                                                     const double* __restrict__ imat) {
+    const int item = blockIdx.x / bpi, b = blockIdx.x - item * bpi;
+    const double* k = imat + 8 * static_cast<size_t>(item);
+    const uint32_t nz = nonzero_mask(k);
+    if (nz == 0x41u && __double_as_longlong(k[0]) == 0x3FF0000000000000LL &&
+        __double_as_longlong(k[6]) == 0x3FF0000000000000LL)
+        return;
+    double2* st = state + (static_cast<uint64_t>(item) << n);
     const uint64_t ng = 1ULL << (n - 1);
-    const uint64_t total = ng * static_cast<uint64_t>(items);
-    uint64_t cur = ~0ULL;
-    uint32_t nz = 0;
-    bool ident = false;
-    const double* k = imat;
-    for (uint64_t t = blockIdx.x * 256ULL + threadIdx.x; t < total; t += gridDim.x * 256ULL) {
-        const uint64_t item = t / ng, g = t - item * ng;
-        if (item != cur) {
-            cur = item;
-            k = imat + 8 * item;
-            nz = nonzero_mask(k);
-            ident = nz == 0x41u && k[0] == 1.0 && k[6] == 1.0;
-        }
-        if (ident) continue;
-        double2* st = state + (item << n);
+    const uint64_t g0 = static_cast<uint64_t>(b) * 256 * GATE1_PAIRS + threadIdx.x;
+#pragma unroll
+    for (int r = 0; r < GATE1_PAIRS; ++r) {
+        const uint64_t g = g0 + static_cast<uint64_t>(r) * 256;
+        if (g >= ng) break;
         const uint64_t i0 = insert0(g, q), i1 = i0 | (1ULL << q);
         const double2 a = st[i0], c = st[i1];
         st[i0] = row_apply(k, nz & 0x0f, a, c);
@@ -226,19 +235,22 @@ __global__ void __launch_bounds__(256) k_item_sample(const double2* __restrict__
     }
 }
 
-static unsigned grid_for_items(uint64_t work) {
-    const uint64_t b = (work + 255) / 256;
-    return static_cast<unsigned>(b < 1 ? 1 : (b < 152 * 16 ? b : 152 * 16));
+int channel_blocks_per_item(int n) {
+    const uint64_t per = 256ULL * NORM_PAIRS;
+    return static_cast<int>(((1ULL << (n - 1)) + per - 1) / per);
 }
 
-cudaError_t launch_channel(void* state, int n, int q, int m, int kraus, const double* dmats, const double* dprobs,
-                           int items, const double* duni, int draw, int ndraws, double* dpart, double* dimat,
-                           cudaStream_t st) {
+cudaError_t launch_channel(void* state, int n, int q, int m, int kraus, int cross, const double* dmats,
+                           const double* dprobs, int items, const double* duni, int draw, int ndraws, double* dpart,
+                           double* dimat, cudaStream_t st) {
     if (m < 1 || m > MAX_CHANNEL_OPS) return cudaErrorInvalidValue;
-    const int bpi = outcome_blocks_per_item(n, 1);
+    const int bpi = channel_blocks_per_item(n);
     if (kraus) {
-        k_channel_norms<<<static_cast<unsigned>(bpi) * items, 256, 0, st>>>(static_cast<const double2*>(state), n, q,
-                                                                          m, dmats, 256ULL * 16, bpi, dpart);
+        const unsigned grid = static_cast<unsigned>(bpi) * items;
+        if (cross)
+            k_channel_norms<true><<<grid, 256, 0, st>>>(static_cast<const double2*>(state), n, q, bpi, dpart);
+        else
+            k_channel_norms<false><<<grid, 256, 0, st>>>(static_cast<const double2*>(state), n, q, bpi, dpart);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
@@ -246,8 +258,10 @@ cudaError_t launch_channel(void* state, int n, int q, int m, int kraus, const do
                                                           ndraws, dimat);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_item_gate1<<<grid_for_items((1ULL << (n - 1)) * items), 256, 0, st>>>(static_cast<double2*>(state), n, q,
-                                                                           items, dimat);
+    const uint64_t per_block = 256ULL * GATE1_PAIRS;
+    const int gbpi = static_cast<int>(((1ULL << (n - 1)) + per_block - 1) / per_block);
+    k_item_gate1<<<static_cast<unsigned>(gbpi) * items, 256, 0, st>>>(static_cast<double2*>(state), n, q, gbpi,
+                                                                     dimat);
     return cudaGetLastError();
 }
 

@@ -24,6 +24,7 @@ struct NoiseSegment {
     int type = 0;  // 0 gates, 1 channel
     qfvm_plan* plan = nullptr;
     int q = 0, m = 0, kraus = 0, draw = -1;
+    int cross = 0;  // Kraus: some K^dagger K has a nonzero off-diagonal entry
     size_t mat_off = 0, prob_off = 0;  // into the channel data (doubles)
 };
 
@@ -69,6 +70,12 @@ int parse_noise(int n, const qfvm_op* ops, int64_t n_ops, const double* matpool,
             s.mat_off = data->size();
             const double* src = matpool + 2 * o.mat_offset;  // complex128 pool
             data->insert(data->end(), src, src + 8 * m);
+            for (int j = 0; kraus && j < m; ++j) {
+                const double* k = src + 8 * j;  // row-major 2x2, (re, im) pairs
+                const double m01r = k[0] * k[2] + k[1] * k[3] + k[4] * k[6] + k[5] * k[7];
+                const double m01i = k[0] * k[3] - k[1] * k[2] + k[4] * k[7] - k[5] * k[6];
+                if (m01r != 0.0 || m01i != 0.0) s.cross = 1;
+            }
             s.prob_off = data->size();
             double tot = 0.0;
             for (int j = 0; j < m; ++j) {
@@ -126,7 +133,7 @@ int qfvm_simulate_noise(int32_t num_qubits, const qfvm_op* ops, int64_t n_ops, c
         return fail(QFVM_ERR_INVALID, "expected " + std::to_string(ndraws) + " uniforms per shot");
     }
     const size_t N = 1ULL << n;
-    const int bpi = outcome_blocks_per_item(n, 1);
+    const int bpi = channel_blocks_per_item(n);
     const uint64_t chunk_amps = hamiltonian_chunk(n);
     const uint64_t epi = N / chunk_amps;  // expectation chunks per item
     size_t free_b = 0, total_b = 0;
@@ -227,7 +234,8 @@ int qfvm_simulate_noise(int32_t num_qubits, const qfvm_op* ops, int64_t n_ops, c
             if (sg.type == 0) {
                 NZ_TRY(run_plan_items(sg.plan, dstate.p, items, nullptr, st));
             } else {
-                NZ_CUDA(launch_channel(dstate.p, n, sg.q, sg.m, sg.kraus, dcd + sg.mat_off, dcd + sg.prob_off, items,
+                NZ_CUDA(launch_channel(dstate.p, n, sg.q, sg.m, sg.kraus, sg.cross, dcd + sg.mat_off, dcd + sg.prob_off,
+                                       items,
                                        duni.as<double>(), sg.draw, ndraws, dpart, dimat, st),
                         "channel");
                 g_launches.fetch_add(sg.kraus ? 3 : 2, std::memory_order_relaxed);

@@ -1,7 +1,8 @@
 """Noisy trajectories on the GPU (qfvm_simulate_noise, the NoiseSVSimulator
 drop-in): the reference's seeded runs (golden averaged expectations and
 counts), random circuits with unitary and Kraus channels against the oracle
-shot by shot, and the drop-in class on protocol objects."""
+shot by shot (Kraus sets whose Gram matrices are diagonal and ones that are
+not), and the drop-in class on protocol objects."""
 
 import numpy as np
 import pytest
@@ -56,6 +57,34 @@ def test_random_noisy_circuits_match_oracle(n):
     shots = 12
     uni = np.random.default_rng(n).random((shots, ir.noise_draws(ops)))
     terms = [(1.0, "Z", [0]), (0.5, "XY", [1, 2]), (-0.7, "ZZ", [0, n - 1])]
+    samples, expv = noise.simulate_noise(n, ops, shots, terms=terms, uniforms=uni)
+    ref_s, ref_e = oracle.simulate_noise(n, ops, uni, terms=terms)
+    assert samples.tolist() == ref_s
+    np.testing.assert_allclose(expv, ref_e, atol=1e-12)
+
+
+def rotated_kraus(theta, seed):
+    """Amplitude damping followed by a random unitary V: K_i V.  Its Gram
+    matrices V^dagger K_i^dagger K_i V have off-diagonal entries, so the
+    kernels' norm sums need the cross term sum conj(a) c."""
+    rng = np.random.default_rng(seed)
+    z = rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2))
+    v, _ = np.linalg.qr(z)
+    return [k @ v for k in amp_damp(theta)]
+
+
+@pytest.mark.parametrize("n", [6, 15])
+def test_kraus_channels_with_cross_terms(n):
+    rng = np.random.default_rng(40 + n)
+    ops = []
+    for layer in range(3):
+        ops += workloads.random_layers(n, 1, seed=500 + layer)
+        for _ in range(3):
+            ops.append(ir.channel_op(ir.OP_KRAUS, int(rng.integers(n)),
+                                     rotated_kraus(float(rng.uniform(0.1, 0.7)), int(rng.integers(1 << 30)))))
+    shots = 16
+    uni = np.random.default_rng(n).random((shots, ir.noise_draws(ops)))
+    terms = [(1.0, "Z", [0]), (0.5, "XX", [1, 2])]
     samples, expv = noise.simulate_noise(n, ops, shots, terms=terms, uniforms=uni)
     ref_s, ref_e = oracle.simulate_noise(n, ops, uni, terms=terms)
     assert samples.tolist() == ref_s
