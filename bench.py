@@ -42,6 +42,11 @@ S128 = 16
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM = 6800.0
 FP64_PEAK_INSTR = 0.596e12  # measured FP64 FMA instructions/s on this GPU model (profiles/gb300_arith_peaks.md)
+# DRAM bytes per launch of the complex128 tile pass: ncu capture of the
+# 26-qubit case (dram__bytes_read + dram__bytes_write = 2.086e9 for 2^26
+# amplitudes), scaled by the amplitudes a launch processes (traffic grows in
+# proportion: each pass reads and writes every amplitude once)
+TRAFFIC_PER_AMP_C128 = 2.086e9 / 2 ** 26
 
 
 def env_int(name, default):
@@ -744,8 +749,17 @@ def run_gpu(args):
             "roofline": {"bound": "hbm", "kernel": kernel_name(args.precision, n, main["specialised_passes"] > 0),
                          "achieved": round(achieved, 1),
                          "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                         "traffic": None, "bytes_per_launch": main["tile_bytes"],
-                         "avg_launch_ms": round(main["avg_tile_ms"], 3)},
+                         "traffic": (round(TRAFFIC_PER_AMP_C128 * 2 ** n) if args.precision == "c128" else None),
+                         "traffic_source": ("ncu dram bytes of a 26-qubit launch, scaled by 2^(n-26) "
+                                            "(profiles/qsv_tile_pass_c128_random_layers.md)"
+                                            if args.precision == "c128" else None),
+                         "bytes_per_launch": main["tile_bytes"],
+                         "avg_launch_ms": round(main["avg_tile_ms"], 3),
+                         "compute": ({"pipe": "fp64", "frac": round(fp64 / (ms_step * 1e-3) / FP64_PEAK_INSTR, 3),
+                                      "achieved_instr_per_s": round(fp64 / (ms_step * 1e-3)),
+                                      "peak_instr_per_s": FP64_PEAK_INSTR,
+                                      "peak_kind": "measured (profiles/gb300_arith_peaks.md)"}
+                                     if args.precision == "c128" else None)},
             "pass_gbps": round(main["pass_bytes"] / (ms_step * 1e-3) / 1e9, 1),
             "e2e": e2e,
             "cpu_baseline": cpu,
