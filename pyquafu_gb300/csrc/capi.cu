@@ -3,6 +3,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -622,15 +625,41 @@ int qfvm_simulate_circuit(int32_t num_qubits, const qfvm_op* ops, int64_t n_ops,
     std::lock_guard<std::mutex> lk(g_boundary_mu);
     if (!state) return fail(QFVM_ERR_INVALID, "null state buffer");
     QSV_TRY(check_device());
+    // QFVM_TRACE=1: wall time of every stage on stderr (stages synchronised)
+    static const bool trace = [] {
+        const char* e = std::getenv("QFVM_TRACE");
+        return e && e[0] == '1';
+    }();
+    using clk = std::chrono::steady_clock;
+    auto t0 = clk::now();
+    double ms[6] = {0, 0, 0, 0, 0, 0};
+    auto stage = [&](int k, qfvm_sv* s) {
+        if (!trace) return;
+        if (s) cudaStreamSynchronize(s->stream);
+        const auto t1 = clk::now();
+        ms[k] = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        t0 = t1;
+    };
     qfvm_plan* p = nullptr;
     QSV_TRY(make_plan(num_qubits, QFVM_C128, ops, n_ops, matpool, matpool_len, 0, 0, &p));
+    stage(0, nullptr);
     qfvm_sv* sv = nullptr;
     int rc = cached_state(num_qubits, QFVM_C128, &sv);
+    stage(1, nullptr);
     if (rc == QFVM_OK) rc = state_given ? sv_upload(sv, state, sv->N) : sv_set_zero(sv);
+    stage(2, sv);
     if (rc == QFVM_OK) rc = run_plan(p, sv);
+    stage(3, sv);
     if (rc == QFVM_OK && shots > 0) rc = sv_sample(sv, uniforms, shots, out_indices);
     if (rc == QFVM_OK) rc = sv_download(sv, state, sv->N);
+    stage(4, sv);
     free_plan(p);
+    stage(5, nullptr);
+    if (trace)
+        std::fprintf(stderr,
+                     "qfvm trace simulate_circuit: plan %.1f ms, state %.1f ms, upload %.1f ms, run %.1f ms, "
+                     "sample+download %.1f ms, release %.1f ms\n",
+                     ms[0], ms[1], ms[2], ms[3], ms[4], ms[5]);
     return rc;
 }
 
