@@ -92,6 +92,7 @@ int make_plan(int n, int precision, const qfvm_op* ops, int64_t n_ops, const dou
     std::vector<GOp> gops;
     std::string err;
     if (!classify(n, ops, n_ops, matpool, matpool_len, &gops, &err)) return fail(QFVM_ERR_INVALID, err);
+    fuse_single_qubit(&gops);
     unnormalize_hadamards(&gops);
     const int sp = store_precision(precision);
     if (T > 0 || R > 0) {
@@ -514,6 +515,7 @@ int qfvm_plan_host_build(int32_t num_qubits, int32_t precision, const qfvm_op* o
     std::vector<GOp> gops;
     std::string err;
     if (!classify(num_qubits, ops, n_ops, matpool, matpool_len, &gops, &err)) return fail(QFVM_ERR_INVALID, err);
+    fuse_single_qubit(&gops);
     unnormalize_hadamards(&gops);
     if (tile_qubits > 0 || reg_qubits > 0) {
         int dT, dR;

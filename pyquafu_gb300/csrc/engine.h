@@ -174,6 +174,12 @@ bool unfix_bound(std::vector<GOp>* gops, std::string* err);
 // coefficients of other uncontrolled dense or diagonal gates of the list.
 // Hadamards whose factor finds no such gate stay as they are.
 void unnormalize_hadamards(std::vector<GOp>* gops);
+// Plain simulation plans: an uncontrolled one-qubit diagonal, RX or X gate
+// is merged into the previous gate of the same class on its qubit when every
+// gate between commutes with it (diagonals pass diagonals and gates that use
+// the qubit only as a control; X-type gates pass X / RX on the same target):
+// d.d' -> one diagonal, rx(a) rx(b) -> rx(a + b), X X -> nothing.
+void fuse_single_qubit(std::vector<GOp>* gops);
 // Coefficients of a bindable gate kind at angle th (2 or 4 doubles).
 int bind_coef(int kind, double th, double* c);
 // Gate-equivalent bytes of one gop: 2 * bytes per amplitude * amplitudes it

@@ -871,6 +871,75 @@ void scale_coefs(GOp& g, int halves) {
 
 }  // namespace
 
+namespace {
+
+uint64_t targets_of(const GOp& g) {
+    uint64_t m = 0;
+    if (g.t0 >= 0) m |= 1ULL << g.t0;
+    if (g.t1 >= 0) m |= 1ULL << g.t1;
+    if (g.kind == K_DENSEK)
+        for (int j = 0; j < g.k; ++j) m |= 1ULL << g.tk[j];
+    return m;
+}
+uint64_t touches(const GOp& g) { return g.cmask | g.pmask | targets_of(g); }
+
+enum MergeClass { M_NONE, M_DIAG, M_RX, M_X };
+MergeClass merge_class(const GOp& g) {
+    if (g.cmask != 0 || g.slot >= 0 || g.bkind != 0) return M_NONE;
+    if (g.kind == K_DIAG && g.pmask != 0 && (g.pmask & (g.pmask - 1)) == 0 && g.coef.size() == 4) return M_DIAG;
+    if (g.kind == K_RX && g.coef.size() == 2) return M_RX;
+    if (g.kind == K_X) return M_X;
+    return M_NONE;
+}
+
+// whether a one-qubit gate of class c on qubit bit qb commutes with p (which
+// touches qb): diagonals commute with diagonals and with gates that use qb
+// only as a control; X-type gates commute with X / RX on the same target
+bool commutes(MergeClass c, uint64_t qb, const GOp& p) {
+    if (c == M_DIAG) return p.kind == K_DIAG || ((p.cmask & qb) && !(p.pmask & qb) && !(targets_of(p) & qb));
+    return (p.kind == K_X || p.kind == K_RX) && p.t0 >= 0 && (1ULL << p.t0) == qb && !(p.cmask & qb);
+}
+
+}  // namespace
+
+void fuse_single_qubit(std::vector<GOp>* gops) {
+    constexpr int MAX_SCAN = 512;
+    std::vector<GOp>& g = *gops;
+    std::vector<char> dead(g.size(), 0);
+    for (size_t j = 0; j < g.size(); ++j) {
+        const MergeClass c = merge_class(g[j]);
+        if (c == M_NONE) continue;
+        const uint64_t qb = c == M_DIAG ? g[j].pmask : (1ULL << g[j].t0);
+        int scanned = 0;
+        for (size_t i = j; i-- > 0 && scanned < MAX_SCAN; ++scanned) {
+            if (dead[i] || !(touches(g[i]) & qb)) continue;
+            GOp& a = g[i];
+            if (merge_class(a) == c && (c == M_DIAG ? a.pmask == qb : (1ULL << a.t0) == qb)) {
+                if (c == M_DIAG) {
+                    const cd d0 = cd(a.coef[0], a.coef[1]) * cd(g[j].coef[0], g[j].coef[1]);
+                    const cd d1 = cd(a.coef[2], a.coef[3]) * cd(g[j].coef[2], g[j].coef[3]);
+                    a.flags &= static_cast<uint8_t>(~(F_D0_ONE | F_D1_SPEC));
+                    a.special = 0;
+                    set_diag(a, d0, d1);
+                } else if (c == M_RX) {
+                    // rx(a) rx(b) = rx(a + b): [[c, -is], [-is, c]]
+                    const double c1 = a.coef[0], s1 = a.coef[1], c2 = g[j].coef[0], s2 = g[j].coef[1];
+                    a.coef = {c1 * c2 - s1 * s2, s1 * c2 + c1 * s2};
+                } else {
+                    dead[i] = 1;  // X X = I
+                }
+                dead[j] = 1;
+                break;
+            }
+            if (!commutes(c, qb, a)) break;
+        }
+    }
+    size_t w = 0;
+    for (size_t i = 0; i < g.size(); ++i)
+        if (!dead[i]) g[w++] = g[i];
+    g.resize(w);
+}
+
 void unnormalize_hadamards(std::vector<GOp>* gops) {
     constexpr int MAX_PENDING = 256;  // keeps |amplitudes| below 2^128 between absorptions
     std::vector<size_t> pending;
