@@ -175,8 +175,11 @@ JitShape shape_for(const HostPlan& hp, int nstates) {
     sh.nb = nstates == 1 ? c.nb1 : c.nb2;
     int minb = nstates == 1 ? c.minb1 : c.minb2;
     if (minb <= 0) {
+        // 128 registers per thread; double-single sweeps hold two states of
+        // float pairs (4 registers per amplitude) and get the full 255
         const int nt = 1 << (hp.T - hp.R);
-        minb = 65536 / (nt * 128);
+        const int budget = (hp.arith == QFVM_C128_DS && nstates == 2) ? 255 : 128;
+        minb = 65536 / (nt * budget);
         if (minb < 1) minb = 1;
     }
     sh.minb = minb;

@@ -68,7 +68,6 @@ class Gen {
     bool supported(std::string* why) const {
         if (hp_.arith != QFVM_C64 && hp_.arith != QFVM_C128 && hp_.arith != QFVM_C128_DS)
             return no(why, "arithmetic without a generator");
-        if (ds_ && NS_ != 1) return no(why, "double-single reverse sweeps run interpreted");
         if (pd_.type != PASS_TILE) return no(why, "not a tile pass");
         if (T_ - R_ < 6 || T_ > 13 || R_ < 1 || R_ > 5) return no(why, "tile shape out of range");
         if (np_ > NT_ || np_ > MAX_PASS_PROBES) return no(why, "too many probes");
@@ -546,11 +545,14 @@ class Gen {
         I("bar.sync 0");
         if (ds_) {
             for (int k = 0; k < PER_; ++k) {
-                std::string x = R32(), d = R32(), re = D(), im = D();
+                std::string x = R32(), d = R32();
                 I(fmt("xor.b32 %s, %s, %u", x.c_str(), stidB_.c_str(), sk(k)));
                 I(fmt("add.u32 %s, %s, %s", d.c_str(), x.c_str(), sbase.c_str()));
-                I(fmt("ld.shared.v2.f64 {%s, %s}, [%s]", re.c_str(), im.c_str(), d.c_str()));
-                store_amp(d, 0, {ds_from(re), ds_from(im)});
+                for (int st = 0; st < NS_; ++st) {
+                    std::string re = D(), im = D();
+                    I(fmt("ld.shared.v2.f64 {%s, %s}, [%s+%u]", re.c_str(), im.c_str(), d.c_str(), st * tileB_));
+                    store_amp(d, st * tileB_, {ds_from(re), ds_from(im)});
+                }
             }
             I("bar.sync 0");
         }
@@ -934,6 +936,7 @@ class Gen {
             v = sel(neg(v), v, pt);
         }
         if (!ctl.empty()) v = sel(v, cnst(0.0), ctl);
+        if (ds_) v = ds_to(v);  // warp sums in FP64
         pending_.push_back({v, static_cast<int>(o.probe), o.coef});
         if (static_cast<int>(pending_.size()) == (f64_ ? 4 : 8)) flush_probes();
     }
@@ -943,6 +946,39 @@ class Gen {
     // other half, so P values cost about P shuffles instead of 5 P.  Lane L
     // ends with probe L >> (5 - log2 P); the first lane of each group adds
     // the warp total (times the generator scale) to this warp's slot.
+    // probe-value arithmetic: the amplitude type, or FP64 for double-single
+    std::string pzero() {
+        if (!ds_) return cnst(0.0);
+        std::string d = D();
+        I(fmt("mov.f64 %s, 0d0000000000000000", d.c_str()));
+        return d;
+    }
+    std::string psel(const std::string& a, const std::string& b, const std::string& p) {
+        if (!ds_) return sel(a, b, p);
+        std::string d = D();
+        I(fmt("selp.f64 %s, %s, %s, %s", d.c_str(), a.c_str(), b.c_str(), p.c_str()));
+        return d;
+    }
+    std::string padd(const std::string& a, const std::string& b) {
+        if (!ds_) return add(a, b);
+        std::string d = D();
+        I(fmt("add.rn.f64 %s, %s, %s", d.c_str(), a.c_str(), b.c_str()));
+        return d;
+    }
+    std::string pshfl(const std::string& v, int lanemask) {
+        if (!ds_) return shfl(v, lanemask);
+        std::string lo = R32(), hi = R32(), lo2 = R32(), hi2 = R32(), d = D();
+        I(fmt("mov.b64 {%s, %s}, %s", lo.c_str(), hi.c_str(), v.c_str()));
+        I(fmt("shfl.sync.bfly.b32 %s, %s, %d, 31, -1", lo2.c_str(), lo.c_str(), lanemask));
+        I(fmt("shfl.sync.bfly.b32 %s, %s, %d, 31, -1", hi2.c_str(), hi.c_str(), lanemask));
+        I(fmt("mov.b64 %s, {%s, %s}", d.c_str(), lo2.c_str(), hi2.c_str()));
+        return d;
+    }
+    std::string pcoef(uint32_t off) {
+        const std::string c = coefs(off, 1)[0];
+        return ds_ ? ds_to(c) : c;
+    }
+
     void flush_probes() {
         const int n = static_cast<int>(pending_.size());
         if (n == 0) return;
@@ -950,7 +986,7 @@ class Gen {
         while ((1 << k) < n) ++k;
         std::vector<std::string> vals;
         for (const auto& q : pending_) vals.push_back(q.v);
-        while (static_cast<int>(vals.size()) < (1 << k)) vals.push_back(cnst(0.0));
+        while (static_cast<int>(vals.size()) < (1 << k)) vals.push_back(pzero());
         for (int st = 0; st < k; ++st) {
             const int m = 16 >> st;
             std::string t = R32(), b = P();
@@ -959,14 +995,14 @@ class Gen {
             const size_t half = vals.size() / 2;
             std::vector<std::string> nv;
             for (size_t i = 0; i < half; ++i) {
-                const std::string keep = sel(vals[half + i], vals[i], b);
-                const std::string send = sel(vals[i], vals[half + i], b);
-                nv.push_back(add(keep, shfl(send, m)));
+                const std::string keep = psel(vals[half + i], vals[i], b);
+                const std::string send = psel(vals[i], vals[half + i], b);
+                nv.push_back(padd(keep, pshfl(send, m)));
             }
             vals.swap(nv);
         }
         std::string v = vals[0];
-        for (int st = k; st < 5; ++st) v = add(v, shfl(v, 16 >> st));
+        for (int st = k; st < 5; ++st) v = padd(v, pshfl(v, 16 >> st));
         // writer lanes and their probe
         const int lowbits = 5 - k;
         std::string pl = R32(), lo = R32(), w = P(), pin = P();
@@ -974,19 +1010,19 @@ class Gen {
         I(fmt("and.b32 %s, %s, %d", lo.c_str(), lane_.c_str(), (1 << lowbits) - 1));
         I(fmt("setp.eq.u32 %s, %s, 0", w.c_str(), lo.c_str()));
         I(fmt("setp.lt.and.u32 %s, %s, %d, %s", pin.c_str(), pl.c_str(), n, w.c_str()));
-        std::string c = coefs(pending_[0].coef, 1)[0];
+        std::string c = pcoef(pending_[0].coef);
         std::string off = R32();
         I(fmt("mov.u32 %s, %d", off.c_str(), pending_[0].slot * 8));
         for (int i = 1; i < n; ++i) {
             std::string pi = P(), no = R32();
             I(fmt("setp.eq.u32 %s, %s, %d", pi.c_str(), pl.c_str(), i));
-            c = sel(coefs(pending_[i].coef, 1)[0], c, pi);
+            c = psel(pcoef(pending_[i].coef), c, pi);
             I(fmt("selp.b32 %s, %d, %s, %s", no.c_str(), pending_[i].slot * 8, off.c_str(), pi.c_str()));
             off = no;
         }
         std::string ad = R32(), cur = D(), nxt = D();
         I(fmt("add.u32 %s, %s, %s", ad.c_str(), paccW_.c_str(), off.c_str()));
-        if (f64_) {
+        if (f64_ || ds_) {
             I(fmt("@%s ld.shared.f64 %s, [%s]", pin.c_str(), cur.c_str(), ad.c_str()));
             I(fmt("@%s fma.rn.f64 %s, %s, %s, %s", pin.c_str(), nxt.c_str(), v.c_str(), c.c_str(), cur.c_str()));
         } else {

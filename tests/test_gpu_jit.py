@@ -80,7 +80,7 @@ def test_thread_controls_and_phases():
     assert np.abs(got - ref).max() < 1e-12
 
 
-@pytest.mark.parametrize("precision", ["c128", "c64"])
+@pytest.mark.parametrize("precision", ["c128", "c128_ds", "c64"])
 def test_adjoint_reverse_sweep(precision):
     n = 16
     enc = np.random.default_rng(1).uniform(-np.pi, np.pi, n)
@@ -90,10 +90,10 @@ def test_adjoint_reverse_sweep(precision):
     e1, g1 = gradients.adjoint(n, ops, terms, precision)
     engine.jit_configure(False)
     e0, g0 = gradients.adjoint(n, ops, terms, precision)
-    gtol = 1e-10 if precision == "c128" else 1e-4
-    assert abs(e1 - e0) < (1e-12 if precision == "c128" else 1e-5)
+    gtol = 1e-4 if precision == "c64" else 1e-10
+    assert abs(e1 - e0) < (1e-5 if precision == "c64" else 1e-12)
     np.testing.assert_allclose(g1, g0, atol=gtol)
-    if precision == "c128":
+    if precision != "c64":
         ref = oracle.grad_adjoint(n, ops, [o.slot for o in ops], terms)
         np.testing.assert_allclose(g1[: len(ref)], ref, atol=1e-10)
 
