@@ -219,14 +219,15 @@ def run_reference(args):
         tot += step()
     dt = time.perf_counter() - t0
     v = tot / dt / 1e9
-    sample = (f"{per_step} consecutive gates of the 30-qubit circuit per step on a 16 GiB complex128 state "
-              f"(oracle/qsv_oracle.c, OpenMP {cores} threads)")
+    sample = (f"{per_step} consecutive gates of the {n}-qubit circuit per step on a {16 * 2 ** n / 2 ** 30:g} GiB "
+              f"complex128 state (oracle/qsv_oracle.c, OpenMP {cores} threads)")
     line = {"impl": "reference", "metric": "statevector_gbps", "value": round(v, 3), "unit": "GB/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "random_layers_30q_c128_depth40_extras", "qubits": n, "depth": DEPTH,
-                       "seed": SEED, "l2": "state 16 GiB >> L2 (no flush needed)"},
+            "config": {"workload": f"random_layers_{n}q_c128_depth40_extras", "qubits": n, "depth": DEPTH,
+                       "seed": SEED, "l2": f"state {16 * 2 ** n / 2 ** 30:g} GiB"
+                                          + (" >> L2 (no flush needed)" if 16 * 2 ** n > 4 * 129e6 else "")},
             "cpu_baseline": {"value": round(v, 3), "unit": "GB/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(v, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

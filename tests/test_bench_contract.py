@@ -1,0 +1,49 @@
+"""The bench.py JSON contract: the reference arm on the CPU (host cores,
+oracle port) and, on a GPU, the engine arm's line with every key the
+contract names (roofline, e2e, cpu_baseline, clocks, gpu_launches), on a
+20-qubit instance of the benchmark circuit."""
+
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BASE_KEYS = {"metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+             "vs_baseline", "dtype", "data", "config", "e2e", "cpu_baseline"}
+
+
+def run_bench(args, qubits):
+    env = dict(os.environ, QFVM_BENCH_QUBITS=str(qubits))
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py")] + args, capture_output=True, text=True,
+                       cwd=ROOT, env=env, timeout=1200)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, r.stdout[-2000:]
+    return json.loads(lines[0])
+
+
+def test_reference_arm_line():
+    d = run_bench(["--impl", "reference", "--steps", "2", "--warmup", "1"], 16)
+    assert BASE_KEYS <= set(d)
+    assert d["impl"] == "reference" and d["metric"] == "statevector_gbps" and d["value"] > 0
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["config"]["qubits"] == 16
+
+
+@pytest.mark.gpu
+def test_engine_arm_line():
+    d = run_bench(["--steps", "2", "--warmup", "3", "--no-autotune", "--skip-batch", "--skip-adjoint",
+                   "--skip-variants", "--cpu-seconds", "1"], 20)
+    assert BASE_KEYS | {"roofline", "clocks", "gpu_launches"} <= set(d)
+    rf = d["roofline"]
+    assert {"bound", "achieved", "peak", "unit", "frac", "traffic"} <= set(rf)
+    assert abs(rf["frac"] - rf["achieved"] / rf["peak"]) < 1e-3
+    assert rf["compute"]["pipe"] == "fp64" and rf["compute"]["frac"] > 0
+    e2e = d["e2e"]
+    assert e2e["h2d_bytes_per_step"] == 16 * 2 ** 20 and e2e["d2h_bytes_per_step"] == 16 * 2 ** 20
+    assert d["gpu_launches"] > 0 and d["specialised"]["passes"] == d["specialised"]["of"]
+    assert {"sm_mhz", "sm_max_mhz", "reasons"} <= set(d["clocks"])
