@@ -252,12 +252,19 @@ int prepare_impl(qfvm_plan* p, int nstates, std::string* err) {
     int dev = 0;
     cudaGetDevice(&dev);
     {
-        // double buffering only where both tiles fit in a CTA's shared memory
-        int optin = 0;
+        // double buffering only where the register budget's resident CTAs
+        // (minb) still fit in the SM's shared memory with two tiles each:
+        // otherwise the second buffer costs a resident CTA (measured 1.5x
+        // slower for double-single (12,4))
+        int optin = 0, per_sm = 0;
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
         const size_t tile = static_cast<size_t>(hp.arith == QFVM_C64 ? 8 : 16) << hp.T;
         const size_t pacc = static_cast<size_t>(1 << (hp.T - hp.R)) / 32 * MAX_PASS_PROBES * 8;
-        if (sh.nb == 2 && 2 * nstates * tile + pacc > static_cast<size_t>(optin)) sh.nb = 1;
+        const size_t two = 2 * nstates * tile + pacc;
+        if (sh.nb == 2 && (two > static_cast<size_t>(optin) ||
+                           static_cast<size_t>(sh.minb) * (two + 1024) > static_cast<size_t>(per_sm)))
+            sh.nb = 1;
     }
     // look the passes up by structure; generate and compile the missing ones
     std::vector<std::string> keys(hp.passes.size());

@@ -842,6 +842,10 @@ class Gen {
                 break;
             case K_REAL: {
                 std::vector<std::string> m = coefs(o.coef, 4);
+                if (!flip_[t].empty()) {  // X U X = [[m3, m2], [m1, m0]] where the thread's bit t is flipped
+                    const std::string& p = flip_[t];
+                    m = {sel(m[3], m[0], p), sel(m[2], m[1], p), sel(m[1], m[2], p), sel(m[0], m[3], p)};
+                }
                 for (int j : pairs(t, o.creg))
                     for (int s = 0; s < NS_; ++s) {
                         const Cx a = A_[s][j], b = A_[s][j | (1 << t)];
@@ -863,6 +867,13 @@ class Gen {
             }
             case K_DENSE: {
                 std::vector<std::string> m = coefs(o.coef, 8);
+                if (!flip_[t].empty()) {  // X U X: (m00, m01, m10, m11) -> (m11, m10, m01, m00)
+                    const std::string& p = flip_[t];
+                    std::vector<std::string> f(8);
+                    for (int e = 0; e < 4; ++e)
+                        for (int c = 0; c < 2; ++c) f[2 * e + c] = sel(m[2 * (3 - e) + c], m[2 * e + c], p);
+                    m = f;
+                }
                 std::string nmi[4];
                 for (int i = 0; i < 4; ++i) nmi[i] = neg(m[2 * i + 1]);
                 for (int j : pairs(t, o.creg))
@@ -877,6 +888,7 @@ class Gen {
             }
             case K_SWAP: {
                 const int lo = o.t0 < o.t1 ? o.t0 : o.t1, hi = o.t0 < o.t1 ? o.t1 : o.t0;
+                std::swap(flip_[lo], flip_[hi]);
                 for (int j = 0; j < NA_; ++j) {
                     if (j & ((1 << lo) | (1 << hi))) continue;
                     if ((static_cast<uint32_t>(j) & o.creg) != o.creg) continue;
@@ -1081,9 +1093,22 @@ class Gen {
         }
         ph_on_ = false;
         q_.clear();
+        flip_.assign(R_, std::string());
         for (int oi = 0; oi < sd.op_count; ++oi) {
             const KOp& o = hp_.ops[sd.op_begin + oi];
             const std::string ctl = (o.flags & F_TCTRL) ? ctl_pred(o, gthr) : "";
+            if (o.kind == K_X && !ctl.empty() && o.creg == 0) {
+                add_flip(o.t0, ctl);  // thread-controlled X: a pending flip of the thread's bit t0
+                continue;
+            }
+            // register controls, parities and targets whose meaning a flip changes
+            uint32_t need = o.creg;
+            if (o.kind == K_DIAG) need |= o.preg | ((o.flags & F_ONEBIT) ? (1u << o.t0) : 0u);
+            if (o.kind == K_Y || o.kind == K_HAD) need |= 1u << o.t0;
+            if (o.kind == K_SWAP && o.creg) need |= (1u << o.t0) | (1u << o.t1);
+            if (o.kind == K_PROBE) need |= o.xreg | o.preg;
+            for (int t = 0; t < R_; ++t)
+                if ((need >> t) & 1) materialize(t);
             if (o.kind == K_PROBE) op_probe(o, gthr, ctl);
             else if (o.kind == K_DIAG) op_diag(o, gthr, ctl);
             else op_gate(o, ctl);
@@ -1108,13 +1133,45 @@ class Gen {
             for (int s = 0; s < NS_; ++s)
                 for (int j = 0; j < NA_; ++j) A_[s][j] = phase(A_[s][j], ph_.x, ph_.y, nfi);
         }
+        // a pending flip of bit t: register r holds logical r ^ (1 << t), whose
+        // (XOR-linear) address is the thread's base XOR rsw[t]
+        std::string psbs = psb;
+        for (int t = 0; t < R_; ++t) {
+            if (flip_[t].empty()) continue;
+            std::string v = R32(), n = R32();
+            I(fmt("selp.b32 %s, %u, 0, %s", v.c_str(), static_cast<uint32_t>(sd.rsw[t]) * es_, flip_[t].c_str()));
+            I(fmt("xor.b32 %s, %s, %s", n.c_str(), psbs.c_str(), v.c_str()));
+            psbs = n;
+        }
         for (int j = 0; j < NA_; ++j) {
             std::string x = R32(), ad = R32();
-            I(fmt("xor.b32 %s, %s, %u", x.c_str(), psb.c_str(), offb(j)));
+            I(fmt("xor.b32 %s, %s, %u", x.c_str(), psbs.c_str(), offb(j)));
             I(fmt("add.u32 %s, %s, %s", ad.c_str(), x.c_str(), sbase.c_str()));
             for (int s = 0; s < NS_; ++s) store_amp(ad, s * tileB_, A_[s][j]);
         }
         I("bar.sync 0");
+    }
+
+    // pending per-thread flips of register bits (thread-controlled X)
+    void add_flip(int t, const std::string& p) {
+        if (flip_[t].empty()) {
+            flip_[t] = p;
+            return;
+        }
+        std::string q = P();
+        I(fmt("xor.pred %s, %s, %s", q.c_str(), flip_[t].c_str(), p.c_str()));
+        flip_[t] = q;
+    }
+    void materialize(int t) {
+        if (flip_[t].empty()) return;
+        const std::string p = flip_[t];
+        flip_[t].clear();
+        for (int j : pairs(t, 0))
+            for (int s = 0; s < NS_; ++s) {
+                const Cx a = A_[s][j], b = A_[s][j | (1 << t)];
+                A_[s][j] = {sel(b.x, a.x, p), sel(b.y, a.y, p)};
+                A_[s][j | (1 << t)] = {sel(a.x, b.x, p), sel(a.y, b.y, p)};
+            }
     }
 
     // ---------------------------------------------------------------- state
@@ -1137,6 +1194,7 @@ class Gen {
     };
     std::vector<Pending> pending_;
     std::vector<std::vector<Cx>> A_;
+    std::vector<std::string> flip_;
     bool ph_on_ = false;
     Cx ph_;
     std::string q_;
