@@ -97,7 +97,7 @@ def apply_cached() -> int:
                     set_shape(prec, int(kind), int(n), tuple(ent["shape"]))
                     count += 1
                 except nat.QfvmError:
-                    pass  # a shape this build no longer compiles
+                    pass  # a shape the library no longer compiles
     return count
 
 
