@@ -2,7 +2,9 @@
 driver) against the interpreting kernels and the oracle, on the same inputs:
 one-state passes in complex128 (FP64 and double-single arithmetic) and
 complex64 for several tile shapes and
-both buffering modes, reverse sweeps with probes (adjoint gradients), batched
+both buffering modes, dense / Y / Hadamard / SWAP gates on the targets of
+thread-controlled cx (pending per-thread flips), reverse sweeps with probes
+(adjoint gradients), batched
 groups (per-item coefficients, per-tile probe sums) and per-shot
 trajectories whose classically controlled blocks use the active-item mask.
 Tolerances: complex128 1e-12 per amplitude, gradients 1e-10; complex64
@@ -78,6 +80,37 @@ def test_thread_controls_and_phases():
     assert used > 0
     ref = oracle.simulate(n, ops)
     assert np.abs(got - ref).max() < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["c128", "c64", "c128_ds"])
+def test_dense_gates_after_thread_controlled_flips(precision):
+    """Random one-qubit unitaries (dense 2x2), Y, Hadamards and SWAPs on the
+    targets of cx gates whose controls are thread bits: the pending flips are
+    conjugated into dense coefficients, moved by SWAP or materialised."""
+    n = 17
+    rng = np.random.default_rng(11)
+    ops = []
+    for layer in range(8):
+        for q in range(n):
+            z = rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2))
+            u, _ = np.linalg.qr(z)
+            kind = int(rng.integers(4))
+            if kind == 0:
+                ops.append(workloads.matrix_gate("u", (q,), u))
+            elif kind == 1:
+                ops.append(workloads.named(["y", "h"][int(rng.integers(2))], (q,)))
+            elif kind == 2:
+                ops.append(workloads.named(["rx", "ry"][int(rng.integers(2))], (q,), (float(rng.uniform(0, 6.3)),)))
+        perm = rng.permutation(n)
+        for i in range(0, n - 1, 2):
+            ops.append(workloads.named("cx", (int(perm[i]), int(perm[i + 1])), ncontrols=1))
+        a, b = (int(v) for v in rng.choice(n, 2, replace=False))
+        ops.append(workloads.matrix_gate("swap", (a, b), workloads.SWAP))
+    T, R = (12, 4) if precision == "c64" else (11, 4)
+    got, used = run_state(n, ops, precision, T, R, True)
+    assert used > 0
+    ref = oracle.simulate(n, ops)
+    assert np.abs(got - ref).max() < TOL[precision]
 
 
 @pytest.mark.parametrize("precision", ["c128", "c128_ds", "c64"])
