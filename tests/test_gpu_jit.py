@@ -1,11 +1,10 @@
-"""Circuit-specialised tile passes (PTX generated per pass and compiled by the
-driver) against the interpreting kernels and the oracle, on the same inputs:
-one-state passes in complex128 (FP64 and double-single arithmetic) and
-complex64 for several tile shapes and
-both buffering modes, dense / Y / Hadamard / SWAP gates on the targets of
-thread-controlled cx (pending per-thread flips), reverse sweeps with probes
-(adjoint gradients), batched
-groups (per-item coefficients, per-tile probe sums) and per-shot
+"""Circuit-specialised tile passes (PTX generated per pass and compiled on
+the host) against the interpreting kernels and the oracle, on the same
+inputs: one-state passes in complex128 (FP64 and double-single arithmetic)
+and complex64 for several tile shapes and both buffering modes; dense, Y,
+Hadamard and SWAP gates on the targets of thread-controlled cx (pending
+per-thread flips); reverse sweeps with probes (adjoint gradients); batched
+groups (per-item coefficients, per-tile probe sums); and per-shot
 trajectories whose classically controlled blocks use the active-item mask.
 Tolerances: complex128 1e-12 per amplitude, gradients 1e-10; complex64
 1e-5."""
