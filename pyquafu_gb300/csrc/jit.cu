@@ -175,10 +175,13 @@ JitShape shape_for(const HostPlan& hp, int nstates) {
     sh.nb = nstates == 1 ? c.nb1 : c.nb2;
     int minb = nstates == 1 ? c.minb1 : c.minb2;
     if (minb <= 0) {
-        // 128 registers per thread; double-single sweeps hold two states of
-        // float pairs (4 registers per amplitude) and get the full 255
+        // 128 registers per thread, or the full 255 when the round's
+        // amplitudes alone need more than 64 (two states of FP64 or float-pair
+        // amplitudes at R = 4: 128 registers; at 128 the sweep spilled and
+        // wrote 5x its algorithmic bytes to DRAM)
         const int nt = 1 << (hp.T - hp.R);
-        const int budget = (hp.arith == QFVM_C128_DS && nstates == 2) ? 255 : 128;
+        const int per_amp = hp.arith == QFVM_C64 ? 2 : 4;
+        const int budget = nstates * (1 << hp.R) * per_amp > 64 ? 255 : 128;
         minb = 65536 / (nt * budget);
         if (minb < 1) minb = 1;
     }
