@@ -335,9 +335,9 @@ int qfvm_plan_host_copy(const qfvm_plan* plan, void* passes, void* steps, void* 
  * double-single) and complex64 plans are, by default, emitted as
  * straight-line PTX for sm_103a (every register round unrolled with its
  * targets, controls and coefficient offsets as constants) and compiled once
- * per distinct pass; passes the generator does not handle (shared-memory
- * steps of two-target dense gates) run the interpreting kernels.  The
- * environment variable QFVM_JIT=0 turns specialisation off at start-up.
+ * per distinct pass (two-target dense gates as shared-memory steps of the
+ * pass); whole-state passes and k-target gates run the hand-written kernels.
+ * The environment variable QFVM_JIT=0 turns specialisation off at start-up.
  * ------------------------------------------------------------------------- */
 /* enabled: 0/1; nb_*: tile buffers (1 or 2) of one-state / two-state passes;
  * minb_*: minimum resident CTAs per SM the register budget is set for

@@ -73,9 +73,12 @@ class Gen {
         if (np_ > NT_ || np_ > MAX_PASS_PROBES) return no(why, "too many probes");
         for (int si = 0; si < pd_.step_count; ++si) {
             const StepDesc& sd = hp_.steps[pd_.step_begin + si];
-            if (sd.type != STEP_ROUND) return no(why, "shared-memory step");
             for (int oi = 0; oi < sd.op_count; ++oi) {
                 const KOp& o = hp_.ops[sd.op_begin + oi];
+                if (sd.type == STEP_SMEM) {
+                    if (o.kind != K_DENSE2) return no(why, "shared-memory step kind without a generator");
+                    continue;
+                }
                 switch (o.kind) {
                     case K_DENSE: case K_REAL: case K_RX: case K_DIAG: case K_X: case K_Y: case K_SWAP: case K_HAD:
                         break;
@@ -266,15 +269,16 @@ class Gen {
         I(fmt("ld.shared.v2.%s {%s, %s}, [%s+%u]", ft_, c.x.c_str(), c.y.c_str(), addr.c_str(), off));
         return c;
     }
-    void store_amp(const std::string& addr, uint32_t off, const Cx& c) {
+    void store_amp(const std::string& addr, uint32_t off, const Cx& c, const std::string& pred = "") {
+        const std::string g = pred.empty() ? "" : "@" + pred + " ";
         if (ds_) {
             auto [xh, xl] = hl(c.x);
             auto [yh, yl] = hl(c.y);
-            I(fmt("st.shared.v4.f32 [%s+%u], {%s, %s, %s, %s}", addr.c_str(), off, xh.c_str(), xl.c_str(),
-                  yh.c_str(), yl.c_str()));
+            I(fmt("%sst.shared.v4.f32 [%s+%u], {%s, %s, %s, %s}", g.c_str(), addr.c_str(), off, xh.c_str(),
+                  xl.c_str(), yh.c_str(), yl.c_str()));
             return;
         }
-        I(fmt("st.shared.v2.%s [%s+%u], {%s, %s}", ft_, addr.c_str(), off, c.x.c_str(), c.y.c_str()));
+        I(fmt("%sst.shared.v2.%s [%s+%u], {%s, %s}", g.c_str(), ft_, addr.c_str(), off, c.x.c_str(), c.y.c_str()));
     }
     // double-single <-> FP64 (ds_from_double / ds_to_double of policy.cuh)
     std::string ds_from(const std::string& v) {
@@ -557,7 +561,11 @@ class Gen {
             I("bar.sync 0");
         }
 
-        for (int si = 0; si < pd_.step_count; ++si) round(hp_.steps[pd_.step_begin + si], base, sbase);
+        for (int si = 0; si < pd_.step_count; ++si) {
+            const StepDesc& sd = hp_.steps[pd_.step_begin + si];
+            if (sd.type == STEP_SMEM) smem_step(sd, base, sbase);
+            else round(sd, base, sbase);
+        }
 
         // write the tile back (one-state passes: only active items)
         const std::string lskip = L();
@@ -1061,6 +1069,95 @@ class Gen {
             I(fmt("mov.b32 %s, %s", d.c_str(), r2.c_str()));
         }
         return d;
+    }
+
+    // Two-target dense gate over the whole tile in shared memory
+    // (tile_smem_op / small_apply of device.cuh): quads of amplitudes that
+    // differ in tile positions t0 and t1, register controls as a store
+    // predicate, controls outside the tile as a uniform skip.
+    void smem_step(const StepDesc& sd, const std::string& base, const std::string& sbase) {
+        for (int oi = 0; oi < sd.op_count; ++oi) {
+            const KOp& o = hp_.ops[sd.op_begin + oi];
+            const std::string lskip = L();
+            if (o.cthr) {
+                std::string t = R64(), p = P();
+                I(fmt("and.b64 %s, %s, %llu", t.c_str(), base.c_str(), static_cast<unsigned long long>(o.cthr)));
+                I(fmt("setp.ne.u64 %s, %s, %llu", p.c_str(), t.c_str(), static_cast<unsigned long long>(o.cthr)));
+                I(fmt("@%s bra %s", p.c_str(), lskip.c_str()));
+            }
+            const std::vector<std::string> m = coefs(o.coef, 32);
+            std::vector<std::string> nm(16);
+            for (int e = 0; e < 16; ++e) nm[e] = neg(m[2 * e + 1]);
+            const int lo = o.t0 < o.t1 ? o.t0 : o.t1, hi = o.t0 < o.t1 ? o.t1 : o.t0;
+            const uint32_t d0 = swz_host(1u << o.t0, gb_) * es_, d1 = swz_host(1u << o.t1, gb_) * es_;
+            const uint32_t d01 = swz_host((1u << o.t0) | (1u << o.t1), gb_) * es_;
+            const int iters = (1 << (T_ - 2)) / NT_;
+            for (int k = 0; k < iters; ++k) {
+                // i = the quad's index with zeros at lo and hi
+                std::string qd = R32();
+                I(fmt("add.u32 %s, %s, %d", qd.c_str(), tid_.c_str(), k * NT_));
+                std::string i = qd;
+                for (int pos : {lo, hi}) {
+                    std::string h = R32(), h2 = R32(), l = R32(), n = R32();
+                    I(fmt("shr.b32 %s, %s, %d", h.c_str(), i.c_str(), pos));
+                    I(fmt("shl.b32 %s, %s, %d", h2.c_str(), h.c_str(), pos + 1));
+                    I(fmt("and.b32 %s, %s, %u", l.c_str(), i.c_str(), (1u << pos) - 1));
+                    I(fmt("or.b32 %s, %s, %s", n.c_str(), h2.c_str(), l.c_str()));
+                    i = n;
+                }
+                std::string pc;
+                if (o.creg) {
+                    std::string t = R32();
+                    pc = P();
+                    I(fmt("and.b32 %s, %s, %u", t.c_str(), i.c_str(), o.creg));
+                    I(fmt("setp.eq.u32 %s, %s, %u", pc.c_str(), t.c_str(), o.creg));
+                }
+                // swizzled byte offset of i (XOR-fold of the higher bit groups)
+                std::string sw = i;
+                for (int g = 1; g * gb_ < T_; ++g) {
+                    std::string t = R32(), t2 = R32(), n = R32();
+                    I(fmt("shr.b32 %s, %s, %d", t.c_str(), i.c_str(), g * gb_));
+                    I(fmt("and.b32 %s, %s, %u", t2.c_str(), t.c_str(), (1u << gb_) - 1));
+                    I(fmt("xor.b32 %s, %s, %s", n.c_str(), sw.c_str(), t2.c_str()));
+                    sw = n;
+                }
+                std::string ab = R32(), ad = R32();
+                I(fmt("mul.lo.u32 %s, %s, %d", ab.c_str(), sw.c_str(), es_));
+                I(fmt("add.u32 %s, %s, %s", ad.c_str(), ab.c_str(), sbase.c_str()));
+                const uint32_t dx[4] = {0u, d0, d1, d01};
+                std::string addr[4];
+                addr[0] = ad;
+                for (int v = 1; v < 4; ++v) {
+                    std::string x = R32(), a = R32();
+                    I(fmt("xor.b32 %s, %s, %u", x.c_str(), ab.c_str(), dx[v]));
+                    I(fmt("add.u32 %s, %s, %s", a.c_str(), x.c_str(), sbase.c_str()));
+                    addr[v] = a;
+                }
+                for (int st = 0; st < NS_; ++st) {
+                    Cx in[4];
+                    for (int v = 0; v < 4; ++v) in[v] = load_amp(addr[v], st * tileB_);
+                    Cx out[4];
+                    for (int r = 0; r < 4; ++r) {  // quad_dense of policy.cuh
+                        const int b0 = 8 * r;
+                        std::string xr = mul(m[b0], in[0].x), xi = mul(m[b0], in[0].y);
+                        xr = fma(nm[4 * r], in[0].y, xr);
+                        xi = fma(m[b0 + 1], in[0].x, xi);
+                        for (int c = 1; c < 4; ++c) {
+                            const std::string& mr = m[b0 + 2 * c];
+                            const std::string& mi = m[b0 + 2 * c + 1];
+                            xr = fma(mr, in[c].x, xr);
+                            xr = fma(nm[4 * r + c], in[c].y, xr);
+                            xi = fma(mr, in[c].y, xi);
+                            xi = fma(mi, in[c].x, xi);
+                        }
+                        out[r] = {xr, xi};
+                    }
+                    for (int v = 0; v < 4; ++v) store_amp(addr[v], st * tileB_, out[v], pc);
+                }
+            }
+            lab(lskip);
+            I("bar.sync 0");
+        }
     }
 
     void round(const StepDesc& sd, const std::string& base, const std::string& sbase) {

@@ -3,7 +3,7 @@ the host) against the interpreting kernels and the oracle, on the same
 inputs: one-state passes in complex128 (FP64 and double-single arithmetic)
 and complex64 for several tile shapes and both buffering modes; dense, Y,
 Hadamard and SWAP gates on the targets of thread-controlled cx (pending
-per-thread flips); reverse sweeps with probes (adjoint gradients); batched
+per-thread flips); two-qubit unitaries as shared-memory steps; reverse sweeps with probes (adjoint gradients); batched
 groups (per-item coefficients, per-tile probe sums); and per-shot
 trajectories whose classically controlled blocks use the active-item mask.
 Tolerances: complex128 1e-12 per amplitude, gradients 1e-10; complex64
@@ -110,6 +110,43 @@ def test_dense_gates_after_thread_controlled_flips(precision):
     assert used > 0
     ref = oracle.simulate(n, ops)
     assert np.abs(got - ref).max() < TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["c128", "c64", "c128_ds"])
+def test_shared_memory_steps(precision):
+    """Random two-qubit unitaries run as shared-memory steps inside the
+    specialised passes (no pass falls back to the interpreting kernel)."""
+    from test_jit_host import dense2_circuit
+
+    n = 17
+    ops = dense2_circuit(n, 5)
+    T, R = (12, 4) if precision == "c64" else (11, 4)
+    engine.jit_configure(True)
+    st = engine.DeviceState(n, precision)
+    st.set_zero()
+    plan = engine.Plan(n, ops, precision, T, R)
+    plan.run(st)
+    got = st.download()
+    assert plan.jit_passes(1) == plan.stats()["passes"]
+    plan.close()
+    st.close()
+    assert np.abs(got - oracle.simulate(n, ops)).max() < TOL[precision]
+
+
+def test_shared_memory_steps_in_reverse_sweeps():
+    from test_jit_host import dense2_circuit
+
+    n = 15
+    enc = np.random.default_rng(2).uniform(-np.pi, np.pi, n)
+    ops, _ = workloads.hea(n, 2, seed=4, encode=enc)
+    ops = dense2_circuit(n, 6)[: 3 * n] + ops
+    terms = workloads.zz_x_hamiltonian(n, seed=5)
+    engine.jit_configure(True)
+    e1, g1 = gradients.adjoint(n, ops, terms, "c128")
+    engine.jit_configure(False)
+    e0, g0 = gradients.adjoint(n, ops, terms, "c128")
+    assert abs(e1 - e0) < 1e-12
+    np.testing.assert_allclose(g1, g0, atol=1e-10)
 
 
 @pytest.mark.parametrize("precision", ["c128", "c128_ds", "c64"])

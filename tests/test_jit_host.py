@@ -95,6 +95,40 @@ def test_passes_assemble(tmp_path, tag, n, precision, T, R, batched, adjoint, ns
     assert emitted > 0
 
 
+def dense2_circuit(n, seed):
+    """Random two-qubit unitaries (shared-memory steps of tile passes) between
+    layers of one-qubit gates and cx."""
+    rng = np.random.default_rng(seed)
+    ops = []
+    for layer in range(4):
+        ops += workloads.random_layers(n, 1, seed=seed * 10 + layer)
+        for _ in range(3):
+            a, b = (int(v) for v in rng.choice(n, 2, replace=False))
+            z = rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4))
+            u, _ = np.linalg.qr(z)
+            ops.append(workloads.matrix_gate("u2", (a, b), u))
+    return ops
+
+
+@pytest.mark.parametrize("precision", [0, 1, 2])
+def test_shared_memory_steps_assemble(tmp_path, precision):
+    n = 16
+    T, R = (12, 4) if precision == 1 else (11, 4)
+    h = plan_handle(n, dense2_circuit(n, 3), precision, T, R)
+    counts = (ctypes.c_int64 * 4)()
+    shape = (ctypes.c_int32 * 3)()
+    nat.check(nat.load().qfvm_plan_host_counts(h, counts, shape))
+    steps = np.zeros(counts[1], helpers.STEP_DT)
+    nat.check(nat.load().qfvm_plan_host_copy(h, None, nat.vptr(steps), None, None))
+    assert (steps["type"] == helpers.STEP_SMEM).any()
+    for i in range(counts[0]):
+        src = pass_ptx(h, i, 1)
+        assert src is not None
+        if i == 0:
+            assemble(tmp_path, src, f"smem_{precision}")
+    nat.load().qfvm_plan_destroy(h)
+
+
 def test_probe_pass_needs_two_states():
     ops, _, _, _ = workloads.qnn_batch(batch=2, n=16, layers=2, seed=1)
     h = plan_handle(16, ops, 1, batched=True, adjoint=True)
