@@ -1,8 +1,9 @@
 // Circuit-specialised tile passes: each register round of a pass is emitted
 // as straight-line PTX for sm_103a (targets, controls, coefficient offsets
 // and swizzled shared-memory offsets become constants; X/SWAP/Y become
-// register renames), compiled by the driver's JIT once per distinct pass and
-// launched instead of the interpreting kernels k_pass / k_pass2.
+// register renames), two-target dense gates as shared-memory steps; the PTX
+// is compiled once per distinct pass and launched instead of the
+// interpreting kernels k_pass / k_pass2.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>

@@ -2,9 +2,10 @@
 //
 // The emitted kernel is the tile pass of device.cuh (k_pass) / adjoint.cuh
 // (k_pass2) with the plan's steps unrolled: the persistent tile loop, the
-// cp.async staging of a tile into swizzled shared memory, and for every
+// cp.async staging of a tile into swizzled shared memory, for every
 // register round the loads, the gate arithmetic and the stores, all with
-// compile-time register indices.  The gate arithmetic follows the policy
+// compile-time register indices, and two-target dense gates as
+// shared-memory steps over the tile.  The gate arithmetic follows the policy
 // primitives of policy.cuh operation for operation (mul.rn / fma.rn / add.rn,
 // no contraction), so the specialised passes compute what the interpreting
 // kernels compute.  Register permutations (X, SWAP, Y, quarter turns) are
