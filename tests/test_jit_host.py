@@ -145,3 +145,21 @@ def test_jit_config_roundtrip():
     with pytest.raises(nat.QfvmError):
         engine.jit_configure(True, 3, 0, 1, 0)
     engine.jit_configure(True)
+
+
+def test_pass_text_depends_on_structure_only():
+    """The module cache keys passes by structure: the same circuit with other
+    rotation angles emits identical PTX (coefficients are loaded, not baked
+    in); moving a gate to another qubit changes it."""
+    n = 16
+    a = workloads.hea(n, 2, seed=1)[0]
+    b = workloads.hea(n, 2, seed=2)[0]  # same structure, other angles
+    c = list(a)
+    c[0] = workloads.named("ry", ((c[0].qubits[0] + 1) % n,), c[0].params)
+    texts = []
+    for ops in (a, b, c):
+        h = plan_handle(n, ops, 1, 12, 4)
+        texts.append(pass_ptx(h, 0, 1))
+        nat.load().qfvm_plan_destroy(h)
+    assert texts[0] == texts[1]
+    assert texts[0] != texts[2]

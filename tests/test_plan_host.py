@@ -143,3 +143,41 @@ def test_unnormalized_hadamards_fold_into_other_gates():
     plan = helpers.host_plan(n, only_h)
     assert helpers.K_HAD not in [int(k) for k in plan["ops"]["kind"]]
     assert np.max(np.abs(helpers.interpret(plan, oracle.zero_state(n)) - oracle.simulate(n, only_h))) < 1e-14
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_commuting_merges(seed):
+    """Dense random mixes of diagonals, RX, X, cx, cz, ccx and Hadamards on few
+    qubits (many merge opportunities) against the oracle."""
+    rng = np.random.default_rng(seed)
+    n = 6
+    named = workloads.named
+    ops = []
+    for _ in range(120):
+        k = int(rng.integers(9))
+        q = int(rng.integers(n))
+        if k == 0:
+            ops.append(named("rz", (q,), (float(rng.uniform(0, 6.3)),)))
+        elif k == 1:
+            ops.append(named(["t", "s", "z", "sdg", "tdg"][int(rng.integers(5))], (q,)))
+        elif k == 2:
+            ops.append(named("rx", (q,), (float(rng.uniform(0, 6.3)),)))
+        elif k == 3:
+            ops.append(named("x", (q,)))
+        elif k == 4:
+            a, b = (int(v) for v in rng.choice(n, 2, replace=False))
+            ops.append(named("cx", (a, b), ncontrols=1))
+        elif k == 5:
+            a, b = (int(v) for v in rng.choice(n, 2, replace=False))
+            ops.append(named("cz", (a, b), ncontrols=1))
+        elif k == 6:
+            a, b, c = (int(v) for v in rng.choice(n, 3, replace=False))
+            ops.append(named("ccx", (a, b, c), ncontrols=2))
+        elif k == 7:
+            ops.append(named("h", (q,)))
+        else:
+            ops.append(named("p", (q,), (float(rng.uniform(0, 6.3)),)))
+    plan = helpers.host_plan(n, ops, 0, 0, 0)
+    got = helpers.interpret(plan, oracle.zero_state(n))
+    assert np.abs(got - oracle.simulate(n, ops)).max() < 1e-12
+    assert plan_op_count(plan) < len(ops)
