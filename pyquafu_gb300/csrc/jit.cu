@@ -169,7 +169,11 @@ int load(int dev, const std::string& image, Kernel* k, std::string* err) {
 }
 
 JitShape shape_for(const HostPlan& hp, int nstates) {
-    const JitConfig c = config();
+    JitConfig c;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        c = config();
+    }
     JitShape sh;
     sh.nstates = nstates;
     sh.nb = nstates == 1 ? c.nb1 : c.nb2;
