@@ -150,8 +150,12 @@ int qfvm_adjoint(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int6
  * terms per call (larger requests are rejected).  All calls on a device share
  * that scratch, so calls that overlap on the GPU race and must be serialised
  * by the caller.  The first call on each device resolves the scratch address
- * (with that device current); make it before any stream capture.  On failure
- * the message is in qfvm_noalloc_last_error(). */
+ * (with that device current).  A call synchronises its stream and copies
+ * through pageable host memory, so it cannot be used inside a stream capture:
+ * on a capturing stream it returns QFVM_ERR_UNSUPPORTED.  `dev_state` must be
+ * device (or managed) memory of the current device, else QFVM_ERR_INVALID.
+ * On failure the message is in qfvm_noalloc_last_error() (kept per calling
+ * thread). */
 #define QFVM_NOALLOC_MAX_TERMS 1024
 int qfvm_expect_device_noalloc(const void* dev_state, uint64_t state_len, int32_t precision,
                                const uint64_t* x_masks, const uint64_t* z_masks, const int32_t* y_counts,

@@ -17,6 +17,13 @@ case "$(uname -m)" in
   *) SIMD="" ;;
 esac
 mkdir -p "$HERE/_ref"
+# where the sources were read from, for oracle/refload.py
+echo "$REF" > "$HERE/_ref/reference_root"
+OUT="$HERE/_ref/qfvm$EXT"
+if [ -f "$OUT" ] && [ "$OUT" -nt "$REF/src/qfvm/qfvm.cpp" ] && [ "${1:-}" != "--force" ]; then
+  echo "$OUT"
+  exit 0
+fi
 g++ -std=c++20 -O3 -shared -fPIC -fvisibility=hidden -fopenmp -DENABLE_OPENMP $SIMD \
     -I"$HERE/shim" -I"$PYBIND" -I"$PYINC" -I"$REF/src/qfvm" -I"$REF/src/qfvm_clifford" \
     "$REF/src/qfvm/qfvm.cpp" -o "$HERE/_ref/qfvm$EXT"

@@ -12,7 +12,21 @@ import os
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_ROOT = os.environ.get("QFVM_REFERENCE_ROOT", "/root/reference")
+
+
+def _reference_root() -> str:
+    """$QFVM_REFERENCE_ROOT, else the tree oracle/build_ref.sh last built from."""
+    root = os.environ.get("QFVM_REFERENCE_ROOT")
+    if root:
+        return root
+    try:
+        with open(os.path.join(HERE, "_ref", "reference_root")) as f:
+            return f.read().strip()
+    except OSError:
+        return ""
+
+
+REFERENCE_ROOT = _reference_root()
 
 
 def ref_qfvm_path():
@@ -21,7 +35,8 @@ def ref_qfvm_path():
 
 
 def available() -> bool:
-    return os.path.isdir(os.path.join(REFERENCE_ROOT, "quafu")) and ref_qfvm_path() is not None
+    return bool(REFERENCE_ROOT) and os.path.isdir(os.path.join(REFERENCE_ROOT, "quafu")) and \
+        ref_qfvm_path() is not None
 
 
 def load_ref_qfvm():

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -396,8 +397,23 @@ cudaError_t jit_launch_pass(qfvm_plan* p, int pi, void* psi, void* lam, const vo
     CUresult r = driver().launch(k->fn, grid, 1, 1, k->threads, 1, 1, static_cast<unsigned>(k->smem),
                                  reinterpret_cast<CUstream>(st), args, nullptr);
     if (grid_out) *grid_out = static_cast<int>(grid);
+    if (r == CUDA_SUCCESS) {
+        *launched = true;
+        return cudaSuccess;
+    }
+    if (r == CUDA_ERROR_INVALID_VALUE || r == CUDA_ERROR_LAUNCH_OUT_OF_RESOURCES || r == CUDA_ERROR_INVALID_HANDLE) {
+        // a launch-configuration error leaves the context usable: the caller
+        // runs the interpreting kernel for this pass instead
+        static std::atomic<int> reported{0};
+        if (reported.fetch_add(1) == 0)
+            std::fprintf(stderr, "qfvm: specialised pass launch refused (%s); running the interpreting kernel\n",
+                         cu_error(r).c_str());
+        return cudaSuccess;
+    }
+    // anything else is reported with the driver's own code (the runtime and
+    // driver APIs share the numbering of these errors)
     *launched = true;
-    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorLaunchFailure;
+    return static_cast<cudaError_t>(r);
 }
 
 }  // namespace qsv

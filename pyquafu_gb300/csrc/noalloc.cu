@@ -17,8 +17,14 @@
 //     several host threads or streams) race on it and must be serialised by
 //     the caller;
 //   * the first call on each device looks the array's device address up with
-//     cudaGetSymbolAddress (with that device current) and caches it; make this
-//     first call before any stream capture.
+//     cudaGetSymbolAddress (with that device current) and caches it;
+//   * a call waits for its own results (cudaStreamSynchronize) and copies
+//     through pageable host memory, so it cannot be recorded into a stream
+//     capture: on a capturing stream it returns QFVM_ERR_UNSUPPORTED before
+//     touching the stream;
+//   * the state must be device (or managed) memory of the current device;
+//     anything else (a host pointer, another GPU's memory) is refused with
+//     QFVM_ERR_INVALID before any launch.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -48,10 +54,10 @@ constexpr int MAX_DEVICES = 64;
 std::mutex g_mu;
 void* g_scratch_ptr[MAX_DEVICES] = {nullptr};
 
-char g_noalloc_err[256] = "";  // last error message (fixed buffer: no allocation)
+// last error message of the calling thread (fixed buffer: no allocation)
+thread_local char g_noalloc_err[256] = "";
 
 int nfail(int code, const char* what, const char* detail = "") {
-    std::lock_guard<std::mutex> lk(g_mu);
     std::snprintf(g_noalloc_err, sizeof(g_noalloc_err), "%s%s%s", what, detail[0] ? ": " : "", detail);
     return code;
 }
@@ -104,6 +110,25 @@ extern "C" int qfvm_expect_device_noalloc(const void* dev_state, uint64_t state_
     for (int64_t t = 0; t < n_terms; ++t)
         if ((x_masks[t] | z_masks[t]) & ~lim) return nfail(QFVM_ERR_INVALID, "Pauli term acts outside the state");
 
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    NA_CUDA(cudaStreamIsCapturing(st, &cs), "cudaStreamIsCapturing");
+    if (cs != cudaStreamCaptureStatusNone)
+        return nfail(QFVM_ERR_UNSUPPORTED, "the allocation-free expectation cannot run inside a stream capture");
+    int dev = 0;
+    NA_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    cudaPointerAttributes attr;
+    std::memset(&attr, 0, sizeof(attr));
+    if (cudaPointerGetAttributes(&attr, dev_state) != cudaSuccess) {
+        cudaGetLastError();  // the lookup's error is not sticky: clear it for the caller
+        return nfail(QFVM_ERR_INVALID, "dev_state is not a pointer the CUDA runtime knows");
+    }
+    if ((attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged) || attr.device != dev)
+        return nfail(QFVM_ERR_INVALID, "dev_state is not device memory of the current device");
+    const size_t elem = precision == QFVM_C64 ? 8 : 16;
+    if (reinterpret_cast<uintptr_t>(dev_state) % elem != 0)
+        return nfail(QFVM_ERR_INVALID, "dev_state is not aligned to one amplitude");
+
     unsigned char* scratch = nullptr;
     int rc = scratch_for_current_device(&scratch);
     if (rc != QFVM_OK) return rc;
@@ -111,7 +136,6 @@ extern "C" int qfvm_expect_device_noalloc(const void* dev_state, uint64_t state_
     uint64_t* d_zm = reinterpret_cast<uint64_t*>(scratch + ZM_OFF);
     int32_t* d_ny = reinterpret_cast<int32_t*>(scratch + NY_OFF);
     double* d_out = reinterpret_cast<double*>(scratch + OUT_OFF);
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
 
     // group the terms by flip mask (fixed-size stack arrays: no allocation)
     int32_t order[MAXT];

@@ -6,11 +6,13 @@ cudaMalloc/cudaFree would synchronise the device): the caller passes a state
 already in its own device memory, and the library uses a fixed 64 KiB scratch
 array instead of allocating.  This file is collected last on purpose.
 
-The check: through the C ABI, the allocation-free call gives the same values
-as the existing qfvm_sv_expect entry point on the same device state, within
-the tests' complex128 tolerance, on two calls in a row (the second with a
-different, smaller term set, so stale scratch contents would show), and it
-rejects a request above its stated limit.
+The checks: through the C ABI, the allocation-free call gives the same values
+as the existing qfvm_sv_expect entry point and as the oracle's expect_pauli
+on the same state, within the tests' tolerances, on two calls in a row (the
+second with a different, smaller term set, so stale scratch contents would
+show); the device's free memory does not move across repeated calls; and it
+rejects a request above its stated limit and a state pointer that is not
+device memory, before launching anything.
 """
 
 import ctypes
@@ -19,6 +21,7 @@ import numpy as np
 import pytest
 
 import helpers
+import oracle
 from pyquafu_gb300 import _native as nat
 from pyquafu_gb300 import engine
 
@@ -56,15 +59,51 @@ def test_noalloc_matches_existing_entry_point(precision, tol):
     build()
     lib = nat.load()
     n = 16
+    psi = helpers.random_state(n, 42)
     st = engine.DeviceState(n, "c64" if precision == nat.QFVM_C64 else "c128")
-    st.upload(helpers.random_state(n, 42))
+    st.upload(psi)
+    if precision == nat.QFVM_C64:
+        psi = psi.astype(np.complex64).astype(np.complex128)  # what the complex64 state holds
     first = _terms(n, 1, 30)
     second = _terms(n, 2, 7)
     for terms in (first, second):  # two calls in a row
         got = _noalloc(lib, st, terms, precision)
         ref = st.expect(terms)
         np.testing.assert_allclose(got, ref, atol=tol, rtol=0)
+        exact = [oracle.expect_pauli(psi, p, pos) for p, pos in terms]
+        np.testing.assert_allclose(got, exact, atol=tol, rtol=0)
     st.close()
+
+
+def test_noalloc_leaves_device_memory_untouched():
+    import torch
+
+    lib = nat.load()
+    n = 18
+    st = engine.DeviceState(n, "c128")
+    st.upload(helpers.random_state(n, 7))
+    terms = _terms(n, 3, 40)
+    _noalloc(lib, st, terms, nat.QFVM_C128)  # first call: module and scratch address set up
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(5):
+        _noalloc(lib, st, terms, nat.QFVM_C128)
+    free1 = torch.cuda.mem_get_info()[0]
+    st.close()
+    assert free1 == free0
+
+
+def test_noalloc_rejects_host_pointer():
+    lib = nat.load()
+    host = np.zeros(2 * 16, dtype=np.float64)  # 16 complex128 amplitudes in host memory
+    x = np.zeros(1, dtype=np.uint64)
+    z = np.ones(1, dtype=np.uint64)
+    y = np.zeros(1, dtype=np.int32)
+    out = np.zeros(1)
+    rc = lib.qfvm_expect_device_noalloc(ctypes.c_void_p(host.ctypes.data), 16, nat.QFVM_C128, nat.u64ptr(x),
+                                        nat.u64ptr(z), nat.i32ptr(y), 1, nat.dptr(out), None)
+    assert rc == 1
+    assert b"device memory" in lib.qfvm_noalloc_last_error()
 
 
 def test_noalloc_rejects_oversize_request():
