@@ -172,6 +172,7 @@ int sv_create(int n, int precision, qfvm_sv** out) {
     qfvm_sv* sv = new qfvm_sv();
     sv->n = n;
     sv->precision = store_precision(precision);
+    sv->arith = precision;
     sv->N = 1ULL << n;
     cudaError_t e = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -376,6 +377,7 @@ qfvm_sv* g_cached[2] = {nullptr, nullptr};
 int cached_state(int n, int precision, qfvm_sv** out) {
     const int k = store_precision(precision) == QFVM_C64 ? 1 : 0;
     if (g_cached[k] && g_cached[k]->n == n) {
+        g_cached[k]->arith = precision;
         *out = g_cached[k];
         return QFVM_OK;
     }
@@ -430,7 +432,7 @@ int qfvm_sv_download(qfvm_sv* sv, double* host, uint64_t n_amps) {
 int qfvm_sv_apply(qfvm_sv* sv, const qfvm_op* ops, int64_t n_ops, const double* matpool, int64_t matpool_len) {
     if (!sv) return fail(QFVM_ERR_INVALID, "null state");
     qfvm_plan* p = nullptr;
-    QSV_TRY(make_plan(sv->n, sv->precision, ops, n_ops, matpool, matpool_len, 0, 0, &p));
+    QSV_TRY(make_plan(sv->n, sv->arith, ops, n_ops, matpool, matpool_len, 0, 0, &p));
     int rc = run_plan(p, sv);
     cudaError_t e = cudaStreamSynchronize(sv->stream);
     free_plan(p);

@@ -65,7 +65,8 @@ inline size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255);
 }  // namespace qsv_capi
 
 struct qfvm_sv {
-    int n = 0, precision = QFVM_C128;
+    int n = 0, precision = QFVM_C128;  // storage: QFVM_C128 or QFVM_C64
+    int arith = QFVM_C128;             // arithmetic of qfvm_sv_apply: QFVM_C128, QFVM_C128_DS or QFVM_C64
     uint64_t N = 0;
     void* d = nullptr;
     cudaStream_t stream = nullptr;

@@ -190,6 +190,28 @@ class Gen {
         I(fmt("fma.rn.%s %s, %s, %s, %s", ft_, d.c_str(), c.c_str(), x.c_str(), acc.c_str()));
         return d;
     }
+    // sum of c_i * x_i.  FP64 / FP32: mul then fma in order (the same
+    // roundings as the nested mul / fma form).  Double-single: every product
+    // split exactly (FMA TwoProd), the products' high parts summed with
+    // TwoSum, all error terms summed in FP32, one renormalisation at the end.
+    std::string dot(const std::vector<std::pair<std::string, std::string>>& t) {
+        if (!ds_) {
+            std::string acc = mul(t[0].first, t[0].second);
+            for (size_t i = 1; i < t.size(); ++i) acc = fma(t[i].first, t[i].second, acc);
+            return acc;
+        }
+        auto [s, err] = hl(ds_mul_raw(t[0].first, t[0].second));
+        for (size_t i = 1; i < t.size(); ++i) {
+            auto [p, e] = hl(ds_mul_raw(t[i].first, t[i].second));
+            const std::string sn = f32op("add", s, p);
+            const std::string v = f32op("sub", sn, s);
+            const std::string r = f32op("add", f32op("sub", s, f32op("sub", sn, v)), f32op("sub", p, v));
+            err = f32op("add", f32op("add", err, e), r);
+            s = sn;
+        }
+        const std::string h = f32op("add", s, err);
+        return h + "|" + f32op("sub", err, f32op("sub", h, s));
+    }
     std::string add(const std::string& x, const std::string& y) {
         if (ds_) return ds_add(x, y);
         std::string d = A();
@@ -281,22 +303,83 @@ class Gen {
         }
         I(fmt("%sst.shared.v2.%s [%s+%u], {%s, %s}", g.c_str(), ft_, addr.c_str(), off, c.x.c_str(), c.y.c_str()));
     }
-    // double-single <-> FP64 (ds_from_double / ds_to_double of policy.cuh)
+    // double-single <-> FP64 on the integer and FP32 pipes, no FP64
+    // instruction (ds_from_double / ds_to_double of policy.cuh, step for step)
     std::string ds_from(const std::string& v) {
-        std::string h = A(), l = A(), hd = D(), r = D();
-        I(fmt("cvt.rn.f32.f64 %s, %s", h.c_str(), v.c_str()));
-        I(fmt("cvt.f64.f32 %s, %s", hd.c_str(), h.c_str()));
-        I(fmt("sub.rn.f64 %s, %s, %s", r.c_str(), v.c_str(), hd.c_str()));
-        I(fmt("cvt.rn.f32.f64 %s, %s", l.c_str(), r.c_str()));
+        std::string lw = R32(), hw = R32(), ah = R32(), f = R32(), sg = R32(), t = R32(), hb = R32();
+        std::string ef = R32(), e2 = R32(), e3 = R32(), r23 = R32(), lb = R32(), lo = R32(), hz = R32(),
+                    lz = R32();
+        std::string tiny = P();
+        std::string fl = A(), fe = A(), fd = A(), h = A(), l = A();
+        I(fmt("mov.b64 {%s, %s}, %s", lw.c_str(), hw.c_str(), v.c_str()));
+        I(fmt("and.b32 %s, %s, 0x7FFFFFFF", ah.c_str(), hw.c_str()));
+        I(fmt("setp.lt.u32 %s, %s, 0x39800000", tiny.c_str(), ah.c_str()));  // |v| < 2^-103
+        I(fmt("shf.l.clamp.b32 %s, %s, %s, 3", f.c_str(), lw.c_str(), hw.c_str()));
+        I(fmt("and.b32 %s, %s, 0x80000000", sg.c_str(), hw.c_str()));
+        I(fmt("xor.b32 %s, %s, 0x40000000", t.c_str(), f.c_str()));
+        I(fmt("and.b32 %s, %s, 0x7FFFFFFF", t.c_str(), t.c_str()));
+        I(fmt("or.b32 %s, %s, %s", hb.c_str(), t.c_str(), sg.c_str()));
+        I(fmt("and.b32 %s, %s, 0x7F800000", ef.c_str(), f.c_str()));
+        I(fmt("add.u32 %s, %s, 0x34800000", e2.c_str(), ef.c_str()));
+        I(fmt("and.b32 %s, %s, 0x7F800000", e3.c_str(), e2.c_str()));
+        I(fmt("bfe.u32 %s, %s, 6, 23", r23.c_str(), lw.c_str()));
+        I(fmt("or.b32 %s, %s, %s", lb.c_str(), e3.c_str(), r23.c_str()));
+        I(fmt("mov.b32 %s, %s", fl.c_str(), lb.c_str()));
+        I(fmt("mov.b32 %s, %s", fe.c_str(), e3.c_str()));
+        I(fmt("sub.rn.f32 %s, %s, %s", fd.c_str(), fl.c_str(), fe.c_str()));
+        I(fmt("mov.b32 %s, %s", lo.c_str(), fd.c_str()));
+        I(fmt("or.b32 %s, %s, %s", lo.c_str(), lo.c_str(), sg.c_str()));
+        I(fmt("selp.b32 %s, %s, %s, %s", hz.c_str(), sg.c_str(), hb.c_str(), tiny.c_str()));
+        I(fmt("selp.b32 %s, %s, %s, %s", lz.c_str(), sg.c_str(), lo.c_str(), tiny.c_str()));
+        I(fmt("mov.b32 %s, %s", h.c_str(), hz.c_str()));
+        I(fmt("mov.b32 %s, %s", l.c_str(), lz.c_str()));
         return h + "|" + l;
     }
     std::string ds_to(const std::string& v) {
         auto [h, l] = hl(v);
-        std::string a = D(), b = D(), d = D();
-        I(fmt("cvt.f64.f32 %s, %s", a.c_str(), h.c_str()));
-        I(fmt("cvt.f64.f32 %s, %s", b.c_str(), l.c_str()));
-        I(fmt("add.rn.f64 %s, %s, %s", d.c_str(), a.c_str(), b.c_str()));
-        return d;
+        std::string H = R32(), Lb = R32(), sh = R32(), eh = R32(), el = R32(), mh = R32(), ml = R32(), x = R32(),
+                    d = R32(), z = R32(), ex = R32(), hi = R32(), lo = R32(), hw = R32(), hw2 = R32(), lw2 = R32();
+        std::string MH = R64(), ML = R64(), MLs = R64(), Ms = R64(), Ma = R64(), M = R64(), Mn = R64(), mant = R64();
+        std::string pel = P(), pneg = P(), pz = P();
+        std::string out = D();
+        I(fmt("mov.b32 %s, %s", H.c_str(), h.c_str()));
+        I(fmt("mov.b32 %s, %s", Lb.c_str(), l.c_str()));
+        I(fmt("and.b32 %s, %s, 0x80000000", sh.c_str(), H.c_str()));
+        I(fmt("bfe.u32 %s, %s, 23, 8", eh.c_str(), H.c_str()));
+        I(fmt("bfe.u32 %s, %s, 23, 8", el.c_str(), Lb.c_str()));
+        I(fmt("and.b32 %s, %s, 0x007FFFFF", mh.c_str(), H.c_str()));
+        I(fmt("or.b32 %s, %s, 0x00800000", mh.c_str(), mh.c_str()));
+        I(fmt("and.b32 %s, %s, 0x007FFFFF", ml.c_str(), Lb.c_str()));
+        I(fmt("or.b32 %s, %s, 0x00800000", ml.c_str(), ml.c_str()));
+        I(fmt("xor.b32 %s, %s, %s", x.c_str(), H.c_str(), Lb.c_str()));
+        I(fmt("setp.lt.s32 %s, %s, 0", pneg.c_str(), x.c_str()));  // opposite signs
+        I(fmt("setp.eq.u32 %s, %s, 0", pel.c_str(), el.c_str()));
+        I(fmt("sub.u32 %s, %s, %s", d.c_str(), eh.c_str(), el.c_str()));
+        I(fmt("selp.b32 %s, 64, %s, %s", d.c_str(), d.c_str(), pel.c_str()));
+        I(fmt("cvt.u64.u32 %s, %s", MH.c_str(), mh.c_str()));
+        I(fmt("shl.b64 %s, %s, 39", MH.c_str(), MH.c_str()));
+        I(fmt("cvt.u64.u32 %s, %s", ML.c_str(), ml.c_str()));
+        I(fmt("shl.b64 %s, %s, 39", ML.c_str(), ML.c_str()));
+        I(fmt("shr.b64 %s, %s, %s", MLs.c_str(), ML.c_str(), d.c_str()));
+        I(fmt("sub.s64 %s, %s, %s", Ms.c_str(), MH.c_str(), MLs.c_str()));
+        I(fmt("add.s64 %s, %s, %s", Ma.c_str(), MH.c_str(), MLs.c_str()));
+        I(fmt("selp.b64 %s, %s, %s, %s", M.c_str(), Ms.c_str(), Ma.c_str(), pneg.c_str()));
+        I(fmt("clz.b64 %s, %s", z.c_str(), M.c_str()));
+        I(fmt("shl.b64 %s, %s, %s", Mn.c_str(), M.c_str(), z.c_str()));
+        I(fmt("shr.b64 %s, %s, 11", mant.c_str(), Mn.c_str()));
+        I(fmt("mov.b64 {%s, %s}, %s", lo.c_str(), hi.c_str(), mant.c_str()));
+        I(fmt("sub.u32 %s, %s, %s", ex.c_str(), eh.c_str(), z.c_str()));
+        I(fmt("add.u32 %s, %s, 896", ex.c_str(), ex.c_str()));
+        I(fmt("shl.b32 %s, %s, 20", ex.c_str(), ex.c_str()));
+        I(fmt("add.u32 %s, %s, %s", hw.c_str(), ex.c_str(), hi.c_str()));
+        I(fmt("or.b32 %s, %s, %s", hw.c_str(), hw.c_str(), sh.c_str()));
+        // h zero or below the FP32 normal range, or a cancelled pair: zero
+        I(fmt("setp.eq.u32 %s, %s, 0", pz.c_str(), eh.c_str()));
+        I(fmt("setp.eq.or.u32 %s, %s, 64, %s", pz.c_str(), z.c_str(), pz.c_str()));
+        I(fmt("selp.b32 %s, %s, %s, %s", hw2.c_str(), sh.c_str(), hw.c_str(), pz.c_str()));
+        I(fmt("selp.b32 %s, 0, %s, %s", lw2.c_str(), lo.c_str(), pz.c_str()));
+        I(fmt("mov.b64 %s, {%s, %s}", out.c_str(), lw2.c_str(), hw2.c_str()));
+        return out;
     }
     // coefficients off .. off+cnt-1 of the tile's pool (widest aligned loads)
     std::vector<std::string> coefs(uint32_t off, int cnt) {
@@ -687,7 +770,7 @@ class Gen {
 
     Cx phase(const Cx& a, const std::string& dr, const std::string& di, const std::string& ndi) {
         // amp_phase: a * (dr + i di)
-        return {fma(ndi, a.y, mul(dr, a.x)), fma(di, a.x, mul(dr, a.y))};
+        return {dot({{dr, a.x}, {ndi, a.y}}), dot({{dr, a.y}, {di, a.x}})};
     }
     Cx special(const Cx& a, int sp) {  // amp_special: * -1, * i, * -i
         if (sp == SP_NEG1) return {neg(a.x), neg(a.y)};
@@ -858,8 +941,8 @@ class Gen {
                 for (int j : pairs(t, o.creg))
                     for (int s = 0; s < NS_; ++s) {
                         const Cx a = A_[s][j], b = A_[s][j | (1 << t)];
-                        A_[s][j] = {fma(m[1], b.x, mul(m[0], a.x)), fma(m[1], b.y, mul(m[0], a.y))};
-                        A_[s][j | (1 << t)] = {fma(m[3], b.x, mul(m[2], a.x)), fma(m[3], b.y, mul(m[2], a.y))};
+                        A_[s][j] = {dot({{m[0], a.x}, {m[1], b.x}}), dot({{m[0], a.y}, {m[1], b.y}})};
+                        A_[s][j | (1 << t)] = {dot({{m[2], a.x}, {m[3], b.x}}), dot({{m[2], a.y}, {m[3], b.y}})};
                     }
                 break;
             }
@@ -869,8 +952,8 @@ class Gen {
                 for (int j : pairs(t, o.creg))
                     for (int s = 0; s < NS_; ++s) {
                         const Cx a = A_[s][j], b = A_[s][j | (1 << t)];
-                        A_[s][j] = {fma(sn, b.y, mul(c, a.x)), fma(ns, b.x, mul(c, a.y))};
-                        A_[s][j | (1 << t)] = {fma(sn, a.y, mul(c, b.x)), fma(ns, a.x, mul(c, b.y))};
+                        A_[s][j] = {dot({{c, a.x}, {sn, b.y}}), dot({{c, a.y}, {ns, b.x}})};
+                        A_[s][j | (1 << t)] = {dot({{c, b.x}, {sn, a.y}}), dot({{c, b.y}, {ns, a.x}})};
                     }
                 break;
             }
@@ -888,10 +971,10 @@ class Gen {
                 for (int j : pairs(t, o.creg))
                     for (int s = 0; s < NS_; ++s) {
                         const Cx a = A_[s][j], b = A_[s][j | (1 << t)];
-                        A_[s][j] = {fma(nmi[1], b.y, fma(m[2], b.x, fma(nmi[0], a.y, mul(m[0], a.x)))),
-                                    fma(m[3], b.x, fma(m[2], b.y, fma(m[1], a.x, mul(m[0], a.y))))};
-                        A_[s][j | (1 << t)] = {fma(nmi[3], b.y, fma(m[6], b.x, fma(nmi[2], a.y, mul(m[4], a.x)))),
-                                               fma(m[7], b.x, fma(m[6], b.y, fma(m[5], a.x, mul(m[4], a.y))))};
+                        A_[s][j] = {dot({{m[0], a.x}, {nmi[0], a.y}, {m[2], b.x}, {nmi[1], b.y}}),
+                                    dot({{m[0], a.y}, {m[1], a.x}, {m[2], b.y}, {m[3], b.x}})};
+                        A_[s][j | (1 << t)] = {dot({{m[4], a.x}, {nmi[2], a.y}, {m[6], b.x}, {nmi[3], b.y}}),
+                                               dot({{m[4], a.y}, {m[5], a.x}, {m[6], b.y}, {m[7], b.x}})};
                     }
                 break;
             }
@@ -1140,18 +1223,16 @@ class Gen {
                     Cx out[4];
                     for (int r = 0; r < 4; ++r) {  // quad_dense of policy.cuh
                         const int b0 = 8 * r;
-                        std::string xr = mul(m[b0], in[0].x), xi = mul(m[b0], in[0].y);
-                        xr = fma(nm[4 * r], in[0].y, xr);
-                        xi = fma(m[b0 + 1], in[0].x, xi);
-                        for (int c = 1; c < 4; ++c) {
+                        std::vector<std::pair<std::string, std::string>> tr, ti;
+                        for (int c = 0; c < 4; ++c) {
                             const std::string& mr = m[b0 + 2 * c];
                             const std::string& mi = m[b0 + 2 * c + 1];
-                            xr = fma(mr, in[c].x, xr);
-                            xr = fma(nm[4 * r + c], in[c].y, xr);
-                            xi = fma(mr, in[c].y, xi);
-                            xi = fma(mi, in[c].x, xi);
+                            tr.push_back({mr, in[c].x});
+                            tr.push_back({nm[4 * r + c], in[c].y});
+                            ti.push_back({mr, in[c].y});
+                            ti.push_back({mi, in[c].x});
                         }
-                        out[r] = {xr, xi};
+                        out[r] = {dot(tr), dot(ti)};
                     }
                     for (int v = 0; v < 4; ++v) store_amp(addr[v], st * tileB_, out[v], pc);
                 }

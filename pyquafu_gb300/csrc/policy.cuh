@@ -105,13 +105,42 @@ struct ds2 {
     ds x, y;
 };
 
+// FP64 -> float pair with integer and FP32 instructions only (the FP64 pipe
+// of GB300 issues about 2 instructions per clock per SM).  The high float is
+// v truncated to 24 significant bits (v's own exponent and top mantissa
+// bits, re-biased), the low float the next 23 mantissa bits, exactly.
+// |v| < 2^-103 becomes (0, 0); |v| must stay below 2^127.
 __device__ __forceinline__ ds ds_from_double(double v) {
-    const float h = __double2float_rn(v);
-    const float l = __double2float_rn(__dsub_rn(v, static_cast<double>(h)));
-    return {h, l};
+    const uint32_t hw = static_cast<uint32_t>(__double2hiint(v));
+    const uint32_t lw = static_cast<uint32_t>(__double2loint(v));
+    const uint32_t sg = hw & 0x80000000u;
+    const bool tiny = (hw & 0x7FFFFFFFu) < 0x39800000u;  // exponent field < 920
+    const uint32_t f = __funnelshift_l(lw, hw, 3);       // exponent low 8 bits | 23 mantissa bits
+    const uint32_t hb = ((f ^ 0x40000000u) & 0x7FFFFFFFu) | sg;  // FP32 exponent = FP64 exponent - 896
+    const uint32_t e = ((f & 0x7F800000u) + 0x34800000u) & 0x7F800000u;  // FP64 exponent - 919
+    const float lo = __fsub_rn(__uint_as_float(e | ((lw >> 6) & 0x7FFFFFu)), __uint_as_float(e));
+    const uint32_t lb = __float_as_uint(lo) | sg;
+    return {__uint_as_float(tiny ? sg : hb), __uint_as_float(tiny ? sg : lb)};
 }
+// Float pair -> FP64, again without FP64 instructions: both significands
+// are aligned in a 64-bit integer (h's at bits 62..39), added or subtracted,
+// normalised with a leading-zero count and truncated to 53 bits.  Needs
+// |l| <= |h| (every float pair the arithmetic below produces is normalised);
+// h zero or below the FP32 normal range gives zero.
 __device__ __forceinline__ double ds_to_double(ds a) {
-    return __dadd_rn(static_cast<double>(a.h), static_cast<double>(a.l));
+    const uint32_t H = __float_as_uint(a.h), Lb = __float_as_uint(a.l);
+    const uint32_t sh = H & 0x80000000u;
+    const uint32_t eh = (H >> 23) & 0xFFu, el = (Lb >> 23) & 0xFFu;
+    const uint64_t mh = static_cast<uint64_t>((H & 0x7FFFFFu) | 0x800000u) << 39;
+    const uint64_t ml = static_cast<uint64_t>((Lb & 0x7FFFFFu) | 0x800000u) << 39;
+    const uint32_t d = el == 0 ? 64u : eh - el;
+    const uint64_t mls = d < 64u ? (ml >> d) : 0ull;
+    const uint64_t m = (static_cast<int32_t>(H ^ Lb) < 0) ? mh - mls : mh + mls;
+    const int z = __clzll(static_cast<long long>(m));
+    const uint64_t mant = z < 64 ? ((m << z) >> 11) : 0ull;
+    const uint32_t hw = (((eh - static_cast<uint32_t>(z) + 896u) << 20) + static_cast<uint32_t>(mant >> 32)) | sh;
+    const bool zero = eh == 0 || z == 64;
+    return __hiloint2double(static_cast<int>(zero ? sh : hw), static_cast<int>(zero ? 0u : static_cast<uint32_t>(mant)));
 }
 // a + b with TwoSum on the high parts
 __device__ __forceinline__ ds ds_add(ds a, ds b) {
