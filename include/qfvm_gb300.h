@@ -162,6 +162,17 @@ int qfvm_expect_device_noalloc(const void* dev_state, uint64_t state_len, int32_
                                int64_t n_terms, double* out, void* stream);
 const char* qfvm_noalloc_last_error(void);
 
+/* Failure-path test hook (no counterpart in the reference).  kind 1: the
+ * countdown-th device allocation from now on fails (QFVM_ERR_NOMEM) without
+ * calling cudaMalloc; kind 2: the countdown-th pass of a plan run fails
+ * (QFVM_ERR_CUDA, "injected kernel-stage failure") before its launch; kind
+ * 0 disarms.  One fault fires, then the hook disarms itself.  Nothing
+ * touches the GPU, so the context stays usable. */
+#define QFVM_FAULT_NONE 0
+#define QFVM_FAULT_ALLOC 1
+#define QFVM_FAULT_STAGE 2
+int qfvm_test_fault(int32_t kind, int64_t countdown);
+
 /* ------------------------------------------------------------------ */
 /* Device-resident statevector (engine-owned HBM buffer)               */
 /* ------------------------------------------------------------------ */

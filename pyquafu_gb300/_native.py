@@ -19,6 +19,8 @@ QFVM_C128, QFVM_C64, QFVM_C128_DS = 0, 1, 2
 PRECISIONS = {"c128": QFVM_C128, "complex128": QFVM_C128, "c64": QFVM_C64, "complex64": QFVM_C64,
               "c128_ds": QFVM_C128_DS}
 
+QFVM_ERR_INVALID, QFVM_ERR_CUDA, QFVM_ERR_NOMEM, QFVM_ERR_UNSUPPORTED, QFVM_ERR_TIMEOUT, QFVM_ERR_NODEVICE = range(1, 7)
+
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory",
     4: "unsupported", 5: "device wait timed out", 6: "no CUDA device",
@@ -54,6 +56,7 @@ PROTOTYPES = {
     "qfvm_expect_device_noalloc": (ctypes.c_int, [c_vp, ctypes.c_uint64, ctypes.c_int32, c_u64p, c_u64p, c_i32p,
                                                   ctypes.c_int64, c_dp, c_vp]),
     "qfvm_noalloc_last_error": (ctypes.c_char_p, []),
+    "qfvm_test_fault": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64]),
     "qfvm_simulate_shots": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int64, c_dp,
                                            ctypes.c_int64, c_dp, ctypes.c_int64, c_dp, ctypes.c_int64, c_u64p, c_dp]),
     "qfvm_simulate_noise": (ctypes.c_int, [ctypes.c_int32, c_vp, ctypes.c_int64, c_dp, ctypes.c_int64, c_dp,

@@ -340,7 +340,7 @@ int enqueue_group(qfvm_batch* b, BatchGroup* g, int mode, uint64_t* nk) {
                                     g->fpool.p, g->fstride, nullptr, st),
                        "batched small pass");
         else
-            QSV_LAUNCH(launch_globalop(arith, g->psi.p, n, g->fwd->dops + pd.op_begin, g->fpool.p, items, g->fstride,
+            QSV_LAUNCH(launch_globalop(arith, g->psi.p, n, g->fwd->hp.ops[pd.op_begin].k, g->fwd->dops + pd.op_begin, g->fpool.p, items, g->fstride,
                                        nullptr, st),
                        "batched global op");
     }
@@ -380,10 +380,10 @@ int enqueue_group(qfvm_batch* b, BatchGroup* g, int mode, uint64_t* nk) {
                                      items, g->rstride, g->pvals, static_cast<uint64_t>(g->nprobe), st),
                        "batched adjoint small pass");
         } else {
-            QSV_LAUNCH(launch_globalop(arith, g->psi.p, n, g->rev->dops + pd.op_begin, g->rpool.p, items, g->rstride,
+            QSV_LAUNCH(launch_globalop(arith, g->psi.p, n, g->rev->hp.ops[pd.op_begin].k, g->rev->dops + pd.op_begin, g->rpool.p, items, g->rstride,
                                        nullptr, st),
                        "batched global op");
-            QSV_LAUNCH(launch_globalop(arith, g->lam.p, n, g->rev->dops + pd.op_begin, g->rpool.p, items, g->rstride,
+            QSV_LAUNCH(launch_globalop(arith, g->lam.p, n, g->rev->hp.ops[pd.op_begin].k, g->rev->dops + pd.op_begin, g->rpool.p, items, g->rstride,
                                        nullptr, st),
                        "batched global op");
         }

@@ -24,6 +24,26 @@ namespace qsv_capi {
 
 thread_local std::string g_err;
 std::atomic<uint64_t> g_launches{0};
+
+namespace {
+std::atomic<int> g_fault_kind{FAULT_NONE};
+std::atomic<int64_t> g_fault_count{0};
+}  // namespace
+
+bool fault_hit(int kind) {
+    if (g_fault_kind.load(std::memory_order_relaxed) != kind) return false;
+    if (g_fault_count.fetch_sub(1) != 1) return false;
+    g_fault_kind.store(FAULT_NONE);
+    return true;
+}
+
+cudaError_t dev_malloc(void** p, size_t bytes) {
+    if (fault_hit(FAULT_ALLOC)) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
 std::mutex g_boundary_mu;
 
 int fail(int code, const std::string& msg) {
@@ -73,7 +93,7 @@ int upload_plan(qfvm_plan* p) {
     } else if (!hp.coef.empty()) {
         std::memcpy(cdst, hp.coef.data(), hp.coef.size() * sizeof(double));
     }
-    QSV_CUDA(cudaMalloc(&p->dbuf, total), "plan allocation");
+    QSV_CUDA(dev_malloc(&p->dbuf, total), "plan allocation");
     QSV_CUDA(cudaMemcpy(p->dbuf, host.data(), total, cudaMemcpyHostToDevice), "plan upload");
     unsigned char* b = static_cast<unsigned char*>(p->dbuf);
     p->dpass = reinterpret_cast<PassDesc*>(b);
@@ -144,6 +164,7 @@ int run_plan(qfvm_plan* p, qfvm_sv* sv, bool timed = false) {
     if (timed) QSV_CUDA(cudaEventRecord(p->events[0], sv->stream), "event record");
     for (size_t i = 0; i < hp.passes.size(); ++i) {
         const PassDesc& pd = hp.passes[i];
+        if (fault_hit(FAULT_STAGE)) return fail(QFVM_ERR_CUDA, "pass launch: injected kernel-stage failure");
         cudaError_t e = cudaSuccess;
         if (pd.type == PASS_TILE) {
             bool done = false;
@@ -155,7 +176,7 @@ int run_plan(qfvm_plan* p, qfvm_sv* sv, bool timed = false) {
         } else if (pd.type == PASS_SMALL) {
             e = launch_small(hp.arith, sv->d, 0, 1, hp.n, p->dops + pd.op_begin, pd.op_count, p->dcoef, 0, nullptr, sv->stream);
         } else {
-            e = launch_globalop(hp.arith, sv->d, hp.n, p->dops + pd.op_begin, p->dcoef, 1, 0, nullptr, sv->stream);
+            e = launch_globalop(hp.arith, sv->d, hp.n, hp.ops[pd.op_begin].k, p->dops + pd.op_begin, p->dcoef, 1, 0, nullptr, sv->stream);
         }
         g_launches.fetch_add(1, std::memory_order_relaxed);
         if (e != cudaSuccess) return fail(QFVM_ERR_CUDA, std::string("pass launch: ") + cudaGetErrorString(e));
@@ -179,7 +200,7 @@ int sv_create(int n, int precision, qfvm_sv** out) {
         delete sv;
         return fail(QFVM_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e));
     }
-    e = cudaMalloc(&sv->d, sv->N * amp_bytes(sv->precision));
+    e = dev_malloc(&sv->d, sv->N * amp_bytes(sv->precision));
     if (e != cudaSuccess) {
         cudaStreamDestroy(sv->stream);
         delete sv;
@@ -406,6 +427,15 @@ extern "C" {
 const char* qfvm_last_error(void) { return g_err.c_str(); }
 int32_t qfvm_abi_version(void) { return QFVM_ABI_VERSION; }
 uint64_t qfvm_launch_count(void) { return g_launches.load(); }
+
+int qfvm_test_fault(int32_t kind, int64_t countdown) {
+    if (kind < FAULT_NONE || kind > FAULT_STAGE) return fail(QFVM_ERR_INVALID, "fault kind must be 0, 1 or 2");
+    if (kind != FAULT_NONE && countdown < 1) return fail(QFVM_ERR_INVALID, "fault countdown must be >= 1");
+    g_fault_kind.store(FAULT_NONE);
+    g_fault_count.store(countdown);
+    g_fault_kind.store(kind);
+    return QFVM_OK;
+}
 
 int qfvm_sv_create(int32_t num_qubits, int32_t precision, qfvm_sv** out) {
     if (!out) return fail(QFVM_ERR_INVALID, "null output");
@@ -833,8 +863,8 @@ int qfvm_adjoint(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int6
                                dvals, 0, st);
             g_launches.fetch_add(1, std::memory_order_relaxed);
         } else {
-            ce = launch_globalop(arith, psi->d, n, rev->dops + pd.op_begin, rev->dcoef, 1, 0, nullptr, st);
-            if (ce == cudaSuccess) ce = launch_globalop(arith, lam->d, n, rev->dops + pd.op_begin, rev->dcoef, 1, 0, nullptr, st);
+            ce = launch_globalop(arith, psi->d, n, rev->hp.ops[pd.op_begin].k, rev->dops + pd.op_begin, rev->dcoef, 1, 0, nullptr, st);
+            if (ce == cudaSuccess) ce = launch_globalop(arith, lam->d, n, rev->hp.ops[pd.op_begin].k, rev->dops + pd.op_begin, rev->dcoef, 1, 0, nullptr, st);
             g_launches.fetch_add(2, std::memory_order_relaxed);
         }
         if (ce != cudaSuccess) return done(fail(QFVM_ERR_CUDA, std::string("adjoint pass: ") + cudaGetErrorString(ce)));

@@ -34,6 +34,15 @@ int check_device();
         if (rc_ != QFVM_OK) return rc_; \
     } while (0)
 
+// Host-side fault injection (qfvm_test_fault): once armed, the countdown-th
+// device allocation or kernel stage from then on fails on the host without
+// calling CUDA, so failure paths are exercised with no GPU fault.
+enum { FAULT_NONE = 0, FAULT_ALLOC = 1, FAULT_STAGE = 2 };
+bool fault_hit(int kind);
+// cudaMalloc, unless an armed allocation fault fires (then
+// cudaErrorMemoryAllocation with *p = nullptr)
+cudaError_t dev_malloc(void** p, size_t bytes);
+
 // Growable device scratch buffer.
 struct DevBuf {
     void* p = nullptr;
@@ -44,7 +53,7 @@ struct DevBuf {
         p = nullptr;
         cap = 0;
         size_t want = std::max<size_t>(bytes, 256);
-        QSV_CUDA(cudaMalloc(&p, want), "scratch allocation");
+        QSV_CUDA(dev_malloc(&p, want), "scratch allocation");
         cap = want;
         return QFVM_OK;
     }

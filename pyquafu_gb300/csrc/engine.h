@@ -39,14 +39,19 @@ enum : uint8_t {
 };
 enum : uint8_t { SP_NEG1 = 1, SP_I = 2, SP_NEGI = 3 };
 
-constexpr int MAXK = 6;  // largest dense target count handled by the global-op kernel
+constexpr int MAXK = 6;  // largest dense target count held in a thread's registers (k_globalop, k_small)
+// Dense gates on MAXK+1 .. MAX_DENSE_TARGETS targets run one CTA per group of
+// 2^k amplitudes in shared memory (k_globalop_wide); their targets are
+// ascending (the matrix is relabelled on the host) and travel as the mask
+// KOp::pthr.
+constexpr int MAX_DENSE_TARGETS = 12;
 
 struct GOp {
     GKind kind;
     uint8_t flags = 0, special = 0;
     int t0 = -1, t1 = -1;
     int k = 0;
-    int tk[MAXK] = {0};
+    int tk[MAX_DENSE_TARGETS] = {0};
     uint64_t cmask = 0;  // control qubits (all must be 1)
     uint64_t pmask = 0;  // DIAG parity qubits
     std::vector<double> coef;

@@ -93,6 +93,68 @@ __global__ void __launch_bounds__(256) k_globalop(typename P::G* __restrict__ st
 }
 
 // ---------------------------------------------------------------------------
+// Dense gate on MAXK+1 .. MAX_DENSE_TARGETS targets (statevector.hpp:945-995
+// applies any target count): one CTA per group of 2^k amplitudes, the group
+// staged in shared memory, each thread computing output rows.  The targets
+// are ascending (op.pthr is their mask; the host relabelled the matrix), so
+// group member m sits at base | deposit(m, mask).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t deposit_bits(uint32_t m, uint64_t mask) {
+    uint64_t r = 0;
+    for (int j = 0; mask; ++j) {
+        const uint64_t low = mask & (~mask + 1);
+        if ((m >> j) & 1u) r |= low;
+        mask &= mask - 1;
+    }
+    return r;
+}
+
+template <class P>
+__global__ void __launch_bounds__(256) k_globalop_wide(typename P::G* __restrict__ state, int n, int items,
+                                                       const KOp* __restrict__ opp,
+                                                       const typename P::C* __restrict__ coef0, uint64_t cstride,
+                                                       const uint8_t* __restrict__ active) {
+    using A = typename P::A;
+    using C = typename P::C;
+    extern __shared__ __align__(16) unsigned char wide_smem[];
+    A* in = reinterpret_cast<A*>(wide_smem);
+    const KOp op = *opp;
+    const int k = op.k;
+    const uint32_t dim = 1u << k;
+    const uint64_t tmask = op.pthr;
+    const uint64_t groups = static_cast<uint64_t>(items) << (n - k);
+    for (uint64_t g = blockIdx.x; g < groups; g += gridDim.x) {
+        uint64_t i = g;
+        for (uint64_t mm = tmask; mm; mm &= mm - 1) i = insert0(i, __ffsll(static_cast<long long>(mm)) - 1);
+        if ((i & op.cthr) != op.cthr) continue;  // the same for the whole CTA
+        if (active && !active[i >> n]) continue;
+        const C* coef = coef0 + (i >> n) * cstride;
+        for (uint32_t m = threadIdx.x; m < dim; m += blockDim.x) in[m] = P::s2a(P::g2s(state[i | deposit_bits(m, tmask)]));
+        __syncthreads();
+        for (uint32_t r = threadIdx.x; r < dim; r += blockDim.x) {
+            const uint32_t row = op.coef + 2 * (r * dim);
+            typename P::R xr = P::mul(P::coef(coef, row), in[0].x);
+            typename P::R xi = P::mul(P::coef(coef, row), in[0].y);
+            xr = P::madd(P::cneg(P::coef(coef, row + 1)), in[0].y, xr);
+            xi = P::madd(P::coef(coef, row + 1), in[0].x, xi);
+            for (uint32_t c = 1; c < dim; ++c) {
+                const C mr = P::coef(coef, row + 2 * c);
+                const C mi = P::coef(coef, row + 2 * c + 1);
+                xr = P::madd(mr, in[c].x, xr);
+                xr = P::madd(P::cneg(mi), in[c].y, xr);
+                xi = P::madd(mr, in[c].y, xi);
+                xi = P::madd(mi, in[c].x, xi);
+            }
+            A o;
+            o.x = xr;
+            o.y = xi;
+            state[i | deposit_bits(r, tmask)] = P::s2g(P::a2s(o));
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Utility kernels
 // ---------------------------------------------------------------------------
 template <class P>
@@ -338,8 +400,30 @@ cudaError_t launch_small(int precision, void* state, uint64_t stride, int batch,
     return launch_small_p<P64>(state, stride, batch, n, dops, nops, dcoef, cstride, active, st);
 }
 
-cudaError_t launch_globalop(int precision, void* state, int n, const KOp* dop, const void* dcoef, int items,
+template <class P>
+static cudaError_t launch_wide(void* state, int n, int k, const KOp* dop, const void* dcoef, int items,
+                               uint64_t cstride, const uint8_t* active, cudaStream_t st) {
+    const size_t smem = sizeof(typename P::A) << k;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_globalop_wide<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+    }
+    const uint64_t groups = static_cast<uint64_t>(items) << (n - k);
+    const unsigned blocks = static_cast<unsigned>(groups < 152 * 8 ? groups : 152 * 8);
+    k_globalop_wide<P><<<blocks, 256, smem, st>>>(static_cast<typename P::G*>(state), n, items, dop,
+                                                  static_cast<const typename P::C*>(dcoef), cstride, active);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_globalop(int precision, void* state, int n, int k, const KOp* dop, const void* dcoef, int items,
                             uint64_t cstride, const uint8_t* active, cudaStream_t st) {
+    if (k > MAXK) {
+        if (k > MAX_DENSE_TARGETS || k > n) return cudaErrorInvalidValue;
+        if (precision == QFVM_C64) return launch_wide<P32>(state, n, k, dop, dcoef, items, cstride, active, st);
+        if (precision == QFVM_C128_DS) return launch_wide<PDS>(state, n, k, dop, dcoef, items, cstride, active, st);
+        return launch_wide<P64>(state, n, k, dop, dcoef, items, cstride, active, st);
+    }
     const uint64_t groups = static_cast<uint64_t>(items) << (n - 1);
     const unsigned blocks = static_cast<unsigned>(groups / 256 < 152 * 16 ? (groups + 255) / 256 : 152 * 16);
     if (precision == QFVM_C64)

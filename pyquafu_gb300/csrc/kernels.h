@@ -33,7 +33,8 @@ cudaError_t launch_tile_pass(int precision, int T, int R, void* state, const Pas
                              int items, uint64_t cstride, const uint8_t* active, cudaStream_t st);
 cudaError_t launch_small(int precision, void* state, uint64_t stride, int batch, int n, const KOp* dops, int nops,
                          const void* dcoef, uint64_t cstride, const uint8_t* active, cudaStream_t st);
-cudaError_t launch_globalop(int precision, void* state, int n, const KOp* dop, const void* dcoef, int items,
+// k: the op's dense target count (host copy of dop->k; selects the wide kernel)
+cudaError_t launch_globalop(int precision, void* state, int n, int k, const KOp* dop, const void* dcoef, int items,
                             uint64_t cstride, const uint8_t* active, cudaStream_t st);
 cudaError_t launch_set_basis(int precision, void* state, uint64_t N, uint64_t index, cudaStream_t st);
 cudaError_t launch_convert(bool to64, const void* in, void* out, uint64_t n, cudaStream_t st);

@@ -209,8 +209,10 @@ bool classify(int n, const qfvm_op* ops, int64_t n_ops, const double* matpool, i
                     *err = "op " + std::to_string(i) + ": matrix gate without a target";
                     return false;
                 }
-                if (k > MAXK) {
-                    *err = "op " + std::to_string(i) + ": " + std::to_string(k) + "-target matrix gates are not supported";
+                if (k > MAX_DENSE_TARGETS) {
+                    *err = "op " + std::to_string(i) + ": " + std::to_string(k) +
+                           "-target matrix gates are not supported (at most " + std::to_string(MAX_DENSE_TARGETS) +
+                           " targets)";
                     return false;
                 }
                 const int64_t dim = 1LL << k;
@@ -268,7 +270,7 @@ bool classify(int n, const qfvm_op* ops, int64_t n_ops, const double* matpool, i
                             g.coef[2 * j + 1] = m[j].imag();
                         }
                     }
-                } else {
+                } else if (k <= MAXK) {
                     g.kind = K_DENSEK;
                     g.k = k;
                     for (int j = 0; j < k; ++j) g.tk[j] = q[nc + j];
@@ -277,6 +279,29 @@ bool classify(int n, const qfvm_op* ops, int64_t n_ops, const double* matpool, i
                         g.coef[2 * j] = m[j].real();
                         g.coef[2 * j + 1] = m[j].imag();
                     }
+                } else {
+                    // wide gate: targets in ascending order, the matrix's index
+                    // bits relabelled to match (a permutation of entries, exact)
+                    g.kind = K_DENSEK;
+                    g.k = k;
+                    int ord[MAX_DENSE_TARGETS];
+                    for (int j = 0; j < k; ++j) ord[j] = j;
+                    std::sort(ord, ord + k, [&](int a, int b) { return q[nc + a] < q[nc + b]; });
+                    for (int j = 0; j < k; ++j) g.tk[j] = q[nc + ord[j]];
+                    std::vector<int64_t> old_of(static_cast<size_t>(dim));
+                    for (int64_t v = 0; v < dim; ++v) {
+                        int64_t o2 = 0;
+                        for (int j = 0; j < k; ++j)
+                            if ((v >> j) & 1) o2 |= int64_t{1} << ord[j];
+                        old_of[static_cast<size_t>(v)] = o2;
+                    }
+                    g.coef.resize(static_cast<size_t>(2 * dim * dim));
+                    for (int64_t r = 0; r < dim; ++r)
+                        for (int64_t c = 0; c < dim; ++c) {
+                            const cd e = m[old_of[static_cast<size_t>(r)] * dim + old_of[static_cast<size_t>(c)]];
+                            g.coef[static_cast<size_t>(2 * (r * dim + c))] = e.real();
+                            g.coef[static_cast<size_t>(2 * (r * dim + c) + 1)] = e.imag();
+                        }
                 }
                 break;
             }
@@ -425,9 +450,13 @@ KOp global_kop(HostPlan* p, const GOp& g) {
     k.t0 = static_cast<uint8_t>(g.t0 < 0 ? 0 : g.t0);
     k.t1 = static_cast<uint8_t>(g.t1 < 0 ? 0 : g.t1);
     k.k = static_cast<uint8_t>(g.k);
-    for (int j = 0; j < g.k; ++j) k.tk[j] = static_cast<uint8_t>(g.tk[j]);
+    for (int j = 0; j < g.k && j < MAXK; ++j) k.tk[j] = static_cast<uint8_t>(g.tk[j]);
     k.cthr = g.cmask;
     k.pthr = g.pmask;
+    if (g.kind == K_DENSEK && g.k > MAXK) {
+        k.pthr = 0;
+        for (int j = 0; j < g.k; ++j) k.pthr |= 1ULL << g.tk[j];  // ascending targets as a mask
+    }
     if (g.kind == K_PROBE) {
         k.xreg = static_cast<uint32_t>(g.xmask);  // whole-state kernels: global flip bits (n <= 14)
         k.probe = static_cast<uint16_t>(p->probe_slot.size());
@@ -498,19 +527,32 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
             *err = "state too large for the whole-state kernel";
             return false;
         }
-        PassDesc pd;
-        std::memset(&pd, 0, sizeof(pd));
-        pd.type = PASS_SMALL;
-        pd.T = n;
-        pd.op_begin = 0;
-        for (const auto& g : gops) plan->ops.push_back(global_kop(plan, g));
-        pd.op_count = static_cast<int32_t>(plan->ops.size());
-        pd.probe_base = 0;
-        pd.nprobe = static_cast<int32_t>(plan->probe_slot.size());
-        plan->passes.push_back(pd);
-        st.passes = 1;
+        // runs of gates become whole-state passes; a dense gate on more than
+        // MAXK targets (beyond the whole-state kernel's registers) runs as its
+        // own global pass between them
+        size_t gi = 0;
+        while (gi < gops.size()) {
+            PassDesc pd;
+            std::memset(&pd, 0, sizeof(pd));
+            pd.T = n;
+            pd.op_begin = static_cast<int32_t>(plan->ops.size());
+            pd.probe_base = static_cast<int32_t>(plan->probe_slot.size());
+            if (gops[gi].kind == K_DENSEK && gops[gi].k > MAXK) {
+                pd.type = PASS_GLOBALOP;
+                plan->ops.push_back(global_kop(plan, gops[gi]));
+                ++gi;
+            } else {
+                pd.type = PASS_SMALL;
+                while (gi < gops.size() && !(gops[gi].kind == K_DENSEK && gops[gi].k > MAXK))
+                    plan->ops.push_back(global_kop(plan, gops[gi++]));
+            }
+            pd.op_count = static_cast<int32_t>(plan->ops.size()) - pd.op_begin;
+            pd.nprobe = static_cast<int32_t>(plan->probe_slot.size()) - pd.probe_base;
+            plan->passes.push_back(pd);
+            st.passes += 1;
+            st.pass_bytes += 2.0 * Sb * N;
+        }
         st.rounds = 0;
-        st.pass_bytes = 2.0 * Sb * N;
         plan->T = n;
         plan->R = 0;
         plan->L = n;

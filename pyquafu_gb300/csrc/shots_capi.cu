@@ -134,7 +134,7 @@ int run_plan_items(qfvm_plan* p, void* state, int items, const uint8_t* active, 
             e = launch_small(hp.arith, state, 1ULL << hp.n, items, hp.n, p->dops + pd.op_begin, pd.op_count, p->dcoef,
                              0, active, st);
         else
-            e = launch_globalop(hp.arith, state, hp.n, p->dops + pd.op_begin, p->dcoef, items, 0, active, st);
+            e = launch_globalop(hp.arith, state, hp.n, hp.ops[pd.op_begin].k, p->dops + pd.op_begin, p->dcoef, items, 0, active, st);
         g_launches.fetch_add(1, std::memory_order_relaxed);
         if (e != cudaSuccess) return fail(QFVM_ERR_CUDA, std::string("pass launch: ") + cudaGetErrorString(e));
     }

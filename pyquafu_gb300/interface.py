@@ -17,9 +17,10 @@ two more evaluations per parameter, sample and observable
   directly (no Jacobian of size B x n_obs x P is ever formed).
 
 ``TorchTransformer.execute`` mirrors the reference's entry point of the same
-name (torch.py:39-62) for circuits whose parameterised gates take plain
-``Parameter`` objects; ``QuantumLayer`` is a module with shared weights and
-per-sample angle-encoded inputs (the QNN training workload).
+name (torch.py:39-62) for circuits whose parameterised gates take
+``Parameter`` objects or ``ParameterExpression`` objects built from them
+(quafu/elements/parameters.py); ``QuantumLayer`` is a module with shared
+weights and per-sample angle-encoded inputs (the QNN training workload).
 """
 
 from __future__ import annotations
@@ -117,8 +118,14 @@ def _z_observables(n):
 
 
 class _CircuitBinding:
-    """Gate slots of a circuit: gate i of ``circ.gates`` whose angle is a
-    ``Parameter`` reads variable ``var_of_slot[slot]``."""
+    """Gate slots of a circuit.  Gate i of ``circ.gates`` whose angle is a
+    ``Parameter`` gets a slot that reads variable ``var_of_slot[slot]``; one
+    whose angle is a ``ParameterExpression`` gets a slot whose value is the
+    expression of its variables (``exprs``: (slot, expression, indices of the
+    expression's variables among the circuit's)), evaluated per sample with
+    the expression's own ``_func`` and differentiated with its own ``grad``,
+    as the reference's chain rule does (``_calc_parameter_grads``,
+    quafu/circuits/quantum_circuit.py:285-297)."""
 
     def __init__(self, circ):
         parsed = ir.read_circuit(circ)
@@ -127,20 +134,71 @@ class _CircuitBinding:
             raise ValueError("circuits with wrapped sub-circuits are not supported here: unwrap them first")
         variables = list(circ.variables)
         index = {id(v): k for k, v in enumerate(variables)}
-        var_of_slot = []
+        var_of_slot, plain, exprs = [], [], []
         for i, g in enumerate(circ.gates):
             paras = list(getattr(g, "paras", []) or [])
             kinds = [type(p).__name__ for p in paras]
-            if "ParameterExpression" in kinds:
-                raise NotImplementedError("gate angles given as ParameterExpression are not batched: use "
-                                          "Parameter objects")
+            if any(k in ("Parameter", "ParameterExpression") for k in kinds[1:]):
+                raise NotImplementedError("only a gate's first angle can be a trainable parameter here")
             if kinds and kinds[0] == "Parameter":
                 gates[i].slot = len(var_of_slot)
+                plain.append(len(var_of_slot))
                 var_of_slot.append(index[id(paras[0])])
+            elif kinds and kinds[0] == "ParameterExpression":
+                gates[i].slot = len(var_of_slot)
+                exprs.append((len(var_of_slot), paras[0], [index[id(v)] for v in paras[0]._variables]))
+                var_of_slot.append(-1)
         self.n = parsed.num_qubits
         self.gates = gates
         self.num_vars = len(variables)
+        self.num_slots = len(var_of_slot)
         self.var_of_slot = torch.as_tensor(var_of_slot, dtype=torch.long)
+        self.plain_slots = torch.as_tensor(plain, dtype=torch.long)
+        self.plain_vars = torch.as_tensor([var_of_slot[k] for k in plain], dtype=torch.long)
+        self.exprs = exprs
+
+    def values(self, params: torch.Tensor) -> torch.Tensor:
+        """(batch, variables) -> (batch, slots) gate angles, differentiable."""
+        b = params.shape[0]
+        p64 = params.to(torch.float64)
+        out = torch.zeros(b, self.num_slots, dtype=torch.float64, device=params.device)
+        if self.plain_slots.numel():
+            dev = params.device
+            out = out.index_copy(1, self.plain_slots.to(dev), p64.index_select(1, self.plain_vars.to(dev)))
+        if self.exprs:
+            ev = _ExpressionSlots.apply(p64, self)
+            out = out.index_copy(1, torch.as_tensor([e[0] for e in self.exprs], device=params.device), ev)
+        return out
+
+
+class _ExpressionSlots(torch.autograd.Function):
+    """Angles of ParameterExpression slots per sample, and their chain rule:
+    d angle / d variable from the expression's own ``grad`` at the sample's
+    values."""
+
+    @staticmethod
+    def forward(ctx, params, bind):  # pylint: disable=arguments-differ
+        x = params.detach().to("cpu", torch.float64).numpy()
+        vals = np.empty((x.shape[0], len(bind.exprs)))
+        grads = []
+        for e, (_, expr, vidx) in enumerate(bind.exprs):
+            g = np.empty((x.shape[0], len(vidx)))
+            for b in range(x.shape[0]):
+                xv = np.array(x[b, vidx], dtype=np.float64)
+                vals[b, e] = float(np.real(expr._func(xv)))
+                g[b] = np.real(np.asarray(expr.grad(xv), dtype=np.complex128))
+            grads.append(g)
+        ctx.bind, ctx.grads, ctx.nvars = bind, grads, x.shape[1]
+        return torch.from_numpy(vals).to(device=params.device)
+
+    @staticmethod
+    def backward(ctx, grad_out):  # pylint: disable=arguments-differ
+        go = grad_out.detach().to("cpu", torch.float64).numpy()
+        gp = np.zeros((go.shape[0], ctx.nvars))
+        for e, (_, _, vidx) in enumerate(ctx.bind.exprs):
+            for j, v in enumerate(vidx):
+                gp[:, v] += go[:, e] * ctx.grads[e][:, j]
+        return torch.from_numpy(gp).to(device=grad_out.device, dtype=grad_out.dtype), None
 
 
 class TorchTransformer:
@@ -176,12 +234,12 @@ class TorchTransformer:
         if params.shape[1] != bind.num_vars:
             raise ValueError(f"expected {bind.num_vars} parameters per sample, got {params.shape[1]}")
         b = params.shape[0]
-        values = params.to(torch.float64).index_select(1, bind.var_of_slot.to(params.device))
+        values = bind.values(params)
         if method == "param_shift":
             return ParamShiftExpval.apply(values, bind, precision)
         runner = runners.get(b)
         if runner is None:
-            runner = BatchRunner(bind.n, bind.gates, _z_observables(bind.n), b, len(bind.var_of_slot), precision)
+            runner = BatchRunner(bind.n, bind.gates, _z_observables(bind.n), b, bind.num_slots, precision)
             runners[b] = runner
         return BatchedExpval.apply(values, runner)
 

@@ -148,6 +148,34 @@ class Parameter:
         return self.value
 
 
+class ParameterExpression:
+    """Stand-in with the reference ParameterExpression's protocol
+    (quafu/elements/parameters.py:24-107): ``_variables`` maps its
+    Parameters to positions, ``_func(x)`` is its value at variable values x,
+    ``grad(x)`` its gradient there.  Here built from a function and its
+    gradient over the listed Parameters."""
+
+    def __init__(self, variables, func, grad):
+        self._vars = list(variables)
+        self._f, self._g = func, grad
+
+    @property
+    def _variables(self):
+        return {v: i for i, v in enumerate(self._vars)}
+
+    @property
+    def _func(self):
+        return self._f
+
+    def grad(self, input_value=None):
+        if input_value is None or len(input_value) == 0:
+            input_value = np.array([v.value for v in self._vars])
+        return np.asarray(self._g(np.asarray(input_value, dtype=np.float64)))
+
+    def __float__(self):
+        return float(self._f(np.array([v.value for v in self._vars])))
+
+
 class _ProtoGate:
     def __init__(self, op: ir.Op, variables=None):
         self.name = op.name.upper()
@@ -198,7 +226,22 @@ class ProtoCircuit:
             for j, p in enumerate(getattr(g, "paras", [])):
                 if isinstance(p, Parameter):
                     out.setdefault(p, []).append([(i, j), 1.0])
+                elif isinstance(p, ParameterExpression):
+                    for v in p._variables:
+                        out.setdefault(v, []).append([(i, j), 0.0])
         return out
+
+    def _calc_parameter_grads(self):
+        """quantum_circuit.py:285-297: d angle / d variable at the current
+        values (expressions through their own grad)."""
+        grads = self.get_parameter_grads()
+        for var, items in grads.items():
+            for item in items:
+                i, j = item[0]
+                p = self.gates[i].paras[j]
+                if isinstance(p, ParameterExpression):
+                    item[1] = float(p.grad()[p._variables[var]])
+        return grads
 
     @property
     def variables(self):

@@ -189,6 +189,14 @@ def probe_value(psi, lam, xmask, zmask, cmask, ny, scale):
     return float(scale * np.sum(np.where(ok, np.conj(lam) * w, 0)).imag)
 
 
+def kop_targets(o):
+    """Targets and parity mask of a whole-state op record: a dense gate on
+    more than 6 targets carries its ascending targets as the mask pthr."""
+    if int(o["kind"]) == K_DENSEK and int(o["k"]) > 6:
+        return [q for q in range(64) if (int(o["pthr"]) >> q) & 1], 0
+    return [int(x) for x in o["tk"][: o["k"]]], int(o["pthr"])
+
+
 def interpret2(plan, psi, lam):
     """Execute an adjoint sweep plan on (psi, lam); returns the probe values."""
     states = [psi.copy(), lam.copy()]
@@ -206,9 +214,9 @@ def interpret2(plan, psi, lam):
                     vals[o["probe"]] = probe_value(states[0], states[1], int(o["xreg"]), int(o["pthr"]),
                                                    int(o["cthr"]), int(o["special"]), coef[o["coef"]])
                     continue
-                tk = [int(x) for x in o["tk"][: o["k"]]]
+                tk, pm = kop_targets(o)
                 t = (int(o["t0"]), int(o["t1"])) if o["kind"] in (K_SWAP, K_DENSE2) else int(o["t0"])
-                apply_both(int(o["kind"]), t, int(o["cthr"]), int(o["pthr"]), int(o["flags"]), int(o["special"]),
+                apply_both(int(o["kind"]), t, int(o["cthr"]), pm, int(o["flags"]), int(o["special"]),
                            int(o["coef"]), tk)
             continue
         T = int(pd["T"])
@@ -256,9 +264,9 @@ def interpret(plan, psi):
     for pd in plan["passes"]:
         if pd["type"] in (PASS_SMALL, PASS_GLOBALOP):
             for o in plan["ops"][pd["op_begin"]: pd["op_begin"] + pd["op_count"]]:
-                tk = [int(x) for x in o["tk"][: o["k"]]]
+                tk, pm = kop_targets(o)
                 t = (int(o["t0"]), int(o["t1"])) if o["kind"] in (K_SWAP, K_DENSE2) else int(o["t0"])
-                apply_global(psi, int(o["kind"]), t, int(o["cthr"]), int(o["pthr"]), int(o["flags"]),
+                apply_global(psi, int(o["kind"]), t, int(o["cthr"]), pm, int(o["flags"]),
                              int(o["special"]), coef, int(o["coef"]), tk)
             continue
         T, L = int(pd["T"]), int(pd["L"])

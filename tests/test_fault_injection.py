@@ -1,0 +1,80 @@
+"""Failure paths exercised by host-side injection (qfvm_test_fault): an
+allocation that fails, and a kernel stage that reports an error before its
+launch.  Nothing faults the GPU: the hook makes the host wrapper return the
+error without calling CUDA.  The engine must report the status with its
+message, leave no half-made object behind, and keep working afterwards
+(checked against the oracle)."""
+
+import numpy as np
+import pytest
+
+import oracle
+from pyquafu_gb300 import _native as nat
+from pyquafu_gb300 import engine, workloads
+
+FAULT_NONE, FAULT_ALLOC, FAULT_STAGE = 0, 1, 2
+
+
+@pytest.fixture(autouse=True)
+def disarm():
+    yield
+    nat.load().qfvm_test_fault(FAULT_NONE, 0)
+
+
+def test_fault_hook_argument_checks():
+    lib = nat.load()
+    assert lib.qfvm_test_fault(7, 1) == nat.QFVM_ERR_INVALID
+    assert b"fault kind" in lib.qfvm_last_error()
+    assert lib.qfvm_test_fault(FAULT_ALLOC, 0) == nat.QFVM_ERR_INVALID
+    assert lib.qfvm_test_fault(FAULT_NONE, 0) == 0
+
+
+@pytest.mark.gpu
+def test_injected_allocation_failure_then_recovery():
+    from pyquafu_gb300.builder import build
+
+    build()
+    lib = nat.load()
+    n = 14
+    ops = workloads.random_layers(n, 4, seed=21, extras=True)
+    assert lib.qfvm_test_fault(FAULT_ALLOC, 1) == 0
+    with pytest.raises(nat.QfvmError) as err:
+        engine.DeviceState(n, "c128")
+    assert err.value.status == nat.QFVM_ERR_NOMEM
+    assert "state allocation" in str(err.value)
+    # the hook disarmed itself: the same request now succeeds and computes
+    st = engine.DeviceState(n, "c128").set_zero()
+    st.apply(ops)
+    assert np.abs(st.download() - oracle.simulate(n, ops)).max() <= 1e-12
+    # a failing plan allocation (its device records)
+    assert lib.qfvm_test_fault(FAULT_ALLOC, 1) == 0
+    with pytest.raises(nat.QfvmError) as err:
+        engine.Plan(n, ops, "c128")
+    assert err.value.status == nat.QFVM_ERR_NOMEM
+    plan = engine.Plan(n, ops, "c128")
+    st.set_zero()
+    plan.run(st)
+    assert np.abs(st.download() - oracle.simulate(n, ops)).max() <= 1e-12
+    plan.close()
+    st.close()
+
+
+@pytest.mark.gpu
+def test_injected_stage_failure_then_recovery():
+    lib = nat.load()
+    n = 16
+    ops = workloads.random_layers(n, 6, seed=22, extras=True)
+    plan = engine.Plan(n, ops, "c128")
+    assert plan.stats()["passes"] >= 2
+    st = engine.DeviceState(n, "c128").set_zero()
+    assert lib.qfvm_test_fault(FAULT_STAGE, 2) == 0  # the second pass of the next run
+    with pytest.raises(nat.QfvmError) as err:
+        plan.run(st)
+    assert err.value.status == nat.QFVM_ERR_CUDA
+    assert "injected kernel-stage failure" in str(err.value)
+    # the context is intact: a fresh run gives the oracle's state
+    st.set_zero()
+    plan.run(st)
+    assert np.abs(st.download() - oracle.simulate(n, ops)).max() <= 1e-12
+    plan.close()
+    st.close()

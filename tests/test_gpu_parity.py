@@ -124,6 +124,31 @@ def test_dense_multi_target_large_state():
     assert np.abs(got - oracle.simulate(15, ops)).max() <= TOL128
 
 
+def _unitary(k, seed):
+    rng = np.random.default_rng(seed)
+    d = 1 << k
+    return np.linalg.qr(rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d)))[0]
+
+
+@pytest.mark.parametrize("precision,tol", [("c128", TOL128), ("c128_ds", TOL128), ("c64", TOL64)])
+@pytest.mark.parametrize("n", [10, 16])
+def test_dense_gates_on_7_to_12_targets(precision, tol, n):
+    """Matrix gates on 7, 8 and 12 targets in any order, some controlled
+    (the reference's apply_multi_targe_gate_general takes any count,
+    statevector.hpp:945-995), in a small state and a tiled one."""
+    rng = np.random.default_rng(n)
+    ops = [workloads.named("h", (q,)) for q in range(n)]
+    for k, nc in ((7, 0), (8, 1), (7, 2)):
+        qs = [int(q) for q in rng.permutation(n)[: k + nc]]
+        ops.append(workloads.matrix_gate(f"u{k}", qs, _unitary(k, k + nc), ncontrols=nc))
+        ops += [workloads.named("ry", (q,), (0.1 + 0.2 * q,)) for q in range(n)]
+    if n >= 12:
+        qs = [int(q) for q in rng.permutation(n)[:12]]
+        ops.append(workloads.matrix_gate("u12", qs, _unitary(12, 3)))
+    got = run(n, ops, precision)
+    assert np.abs(got - oracle.simulate(n, ops)).max() <= tol
+
+
 def test_input_state_and_controls_outside_tile():
     n = 16
     psi = helpers.random_state(n, 5)

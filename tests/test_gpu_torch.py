@@ -1,7 +1,8 @@
 """The torch binding of the batched engine on the GPU: QuantumLayer (shared
 weights + per-sample inputs, one observable: Jacobian from the forward run)
 and the TorchTransformer.execute drop-in (<Z_i> of every qubit: weighted
-adjoint run in backward), both against the oracle."""
+adjoint run in backward, Parameter and ParameterExpression angles), both
+against the oracle."""
 
 import numpy as np
 import pytest
@@ -83,3 +84,32 @@ def test_batched_param_shift_matches_adjoint():
     params.grad = None
     (TorchTransformer.execute(circ, params, method="adjoint", precision="c128") * go).sum().backward()
     np.testing.assert_allclose(g_ps.numpy(), params.grad.numpy(), atol=1e-10)
+
+
+def test_transformer_execute_parameter_expressions():
+    """Angles given as ParameterExpressions of the circuit's variables
+    (quantum_circuit.py:285-297 chain rule): outputs and the vector-Jacobian
+    product against the oracle's adjoint per gate slot, chained by hand."""
+    import test_interface_host as tih
+
+    circ, ops = tih.expression_circuit()
+    rng = np.random.default_rng(11)
+    batch = 4
+    params = torch.tensor(rng.uniform(-2, 2, (batch, 2)), requires_grad=True)
+    out = TorchTransformer.execute(circ, params, method="adjoint", precision="c128")
+    go = torch.tensor(rng.normal(size=(batch, 2)))
+    (out * go).sum().backward()
+    for b in range(batch):
+        t0, t1 = params[b].detach().numpy()
+        angles = [t0, 2 * t1 + np.sin(t0), t1, t0 * t1]
+        gates = [o for o in ops]
+        for gi, sl in ((0, 0), (2, 1), (3, 2), (4, 3)):
+            gates[gi] = type(ops[gi])(ops[gi].name, ops[gi].kind, ops[gi].qubits, 0, (angles[sl],), slot=sl)
+        psi = oracle.simulate(2, gates)
+        for q in range(2):
+            assert abs(out[b, q].item() - oracle.expect_pauli(psi, "Z", [q])) < 1e-12
+        terms = [(float(go[b, q]), "Z", [q]) for q in range(2)]
+        gs = oracle.grad_adjoint(2, gates, [o.slot for o in gates], terms)
+        d0 = gs[0] + gs[1] * np.cos(t0) + gs[3] * t1
+        d1 = 2 * gs[1] + gs[2] + gs[3] * t0
+        np.testing.assert_allclose(params.grad[b].numpy(), [d0, d1], atol=1e-10)

@@ -84,6 +84,54 @@ def test_dense_k_gate_becomes_global_pass():
     assert np.abs(got - oracle.simulate(13, ops)).max() < 1e-13
 
 
+def _unitary(k, seed):
+    rng = np.random.default_rng(seed)
+    d = 1 << k
+    return np.linalg.qr(rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d)))[0]
+
+
+@pytest.mark.parametrize("n,T", [(10, 11), (15, 12)])
+def test_wide_dense_gates_plans(n, T):
+    """Dense gates on 7, 8 and 12 targets (the reference applies any count,
+    statevector.hpp:945-995): given in any target order, with and without
+    controls, in small states (split whole-state passes) and tiled ones."""
+    rng = np.random.default_rng(n)
+    ops = [workloads.named("h", (q,)) for q in range(n)]
+    for k, nc in ((7, 0), (8, 1), (7, 2)):
+        qs = [int(q) for q in rng.permutation(n)[: k + nc]]
+        ops.append(workloads.matrix_gate(f"u{k}", qs, _unitary(k, k + nc), ncontrols=nc))
+        ops += [workloads.named("ry", (q,), (0.1 + 0.2 * q,)) for q in range(n)]
+    if n >= 12:
+        qs = [int(q) for q in rng.permutation(n)[:12]]
+        ops.append(workloads.matrix_gate("u12", qs, _unitary(12, 3)))
+    plan = helpers.host_plan(n, ops, 0, T, 4)
+    got = helpers.interpret(plan, oracle.zero_state(n))
+    assert np.abs(got - oracle.simulate(n, ops)).max() < 1e-12
+
+
+def test_dense_gate_beyond_twelve_targets_rejected():
+    from pyquafu_gb300 import _native as nat
+
+    with pytest.raises(nat.QfvmError, match="at most 12"):
+        helpers.host_plan(14, [workloads.matrix_gate("u13", list(range(13)), np.eye(1 << 13))])
+
+
+def test_wide_dense_gate_in_adjoint_sweep():
+    n = 9
+    ops, _ = workloads.hea(n, 2, seed=1)
+    ops.insert(10, workloads.matrix_gate("u7", [8, 0, 3, 5, 1, 7, 2], _unitary(7, 5)))
+    terms = workloads.zz_x_hamiltonian(n, seed=2)
+    plan = helpers.host_plan(n, ops, 0, adjoint=True)
+    psi = oracle.simulate(n, ops)
+    lam = oracle.apply_hamiltonian(psi, terms)
+    vals = helpers.interpret2(plan, psi, lam)
+    grads = np.zeros(max(o.slot for o in ops) + 1)
+    for slot, v in zip(plan["probe_slots"], vals):
+        grads[slot] += v
+    ref = oracle.grad_adjoint(n, ops, [o.slot for o in ops], terms)
+    np.testing.assert_allclose(grads, ref, atol=1e-12)
+
+
 def test_invalid_ops_rejected():
     from pyquafu_gb300 import _native as nat
 
