@@ -3,19 +3,33 @@
 Workload (seeded, synthetic): 30 qubits, complex128 (16 GiB state), 40 random
 layers (one of h/x/s/t/rx/ry/rz per qubit, angles U[0, 2pi), then cx on a
 random perfect matching), plus cz/swap/rzz on random pairs and ccx on a
-random triple in ~5% of layers; seed 0.  One step = one full circuit on the
-device-resident state.  The state (16 GiB) is far larger than L2, so no L2
-flush is needed between steps.
+random triple in ~5% of layers; seed 0 (1808 gates).  One step = one full
+circuit on the device-resident state.  The state (16 GiB) is far larger than
+L2, so no L2 flush is needed between steps.
 
-metric  statevector_gbps: effective bandwidth = sum over gates of
-        2 * 16 B * (amplitudes the gate must touch) / circuit time
+metric  statevector_gbps: circuit throughput as gate-equivalent bytes, i.e.
+        sum over the circuit's gates of 2 * 16 B * (amplitudes the gate must
+        touch), divided by the circuit time.  Both arms use the same
+        numerator, so the ratio of two lines is a speed ratio.  It is not an
+        HBM figure: the engine fuses many gates per pass over the state; the
+        HBM figures are `roofline` (the dominant kernel) and `hbm_gbps`
+        (every pass's read + write of the state over the circuit time).
 e2e     the same metric through pyquafu_gb300.qfvm.simulate_circuit (the
         reference's API) with the input state in pinned host memory: H2D of
         the state, the run, and D2H of the result are inside the timed region.
 
+The default arithmetic is complex128 storage with float-pair arithmetic
+(`c128_ds`, the engine's default for complex128 work); IEEE FP64 (`c128`)
+and complex64 (`c64`) are reported as variants.  After the timed rows, the
+final state of every variant is compared with the oracle (the CPU
+restatement of the reference's FP64 path, run on the host cores), and the
+24-qubit adjoint gradients with the oracle's adjoint (--skip-oracle-check
+skips both).
+
 --impl reference times the reference algorithm on the host cores instead (the
 CPU restatement in oracle/, OpenMP over all cores) on a bounded sample of the
-same circuit and state size.
+same circuit and state size: each step applies a stride of the circuit's
+gates, so the sample covers the whole gate mix.
 """
 
 from __future__ import annotations
@@ -41,12 +55,14 @@ SEED = 0
 S128 = 16
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM = 6800.0
-FP64_PEAK_INSTR = 0.596e12  # measured FP64 FMA instructions/s on this GPU model (profiles/gb300_arith_peaks.md)
-# DRAM bytes per launch of the complex128 tile pass: ncu capture of the
-# 26-qubit case (dram__bytes_read + dram__bytes_write = 2.086e9 for 2^26
-# amplitudes), scaled by the amplitudes a launch processes (traffic grows in
-# proportion: each pass reads and writes every amplitude once)
-TRAFFIC_PER_AMP_C128 = 2.086e9 / 2 ** 26
+# DRAM bytes per launch of the one-state tile pass, from ncu captures of the
+# 26-qubit case of this generator (dram__bytes_read + dram__bytes_write for
+# 2^26 amplitudes), scaled by the amplitudes a launch processes (traffic grows
+# in proportion: each pass reads and writes every amplitude once)
+TRAFFIC_PER_AMP = {"c128": 2.086e9 / 2 ** 26, "c128_ds": 2.087e9 / 2 ** 26}
+# the C2 random circuit with the arithmetic the engine defaults to
+DEFAULT_PRECISION = "c128_ds"
+ORACLE_FLAGS = "gcc -O2 -fopenmp -ffp-contract=off (oracle/qsv_oracle.c)"
 
 
 def env_int(name, default):
@@ -71,25 +87,31 @@ def workload(n=N_QUBITS, depth=DEPTH, seed=SEED):
     return workloads.random_layers(n, depth, seed, extras=True)
 
 
-def fp64_ops(ops, n):
-    """FP64 arithmetic instructions of one circuit under the engine's kernels
-    (mul/fma/add per touched amplitude component)."""
-    N = float(2 ** n)
-    total = 0.0
-    for o in ops:
-        c = 2.0 ** -o.ncontrols
-        name = o.name
-        if name == "h" and not o.ncontrols:
-            total += 2 * N  # sqrt(2) H: additions only, the factor folded into another gate
-        elif name in ("h", "ry", "rx"):
-            total += 4 * N * c
-        elif name in ("rz", "rzz"):
-            total += 4 * N
-        elif name in ("t", "tdg", "p", "cp"):
-            total += 2 * N * c
-        elif o.matrix is not None and name not in ("swap",):
-            total += 8 * N * c
-    return total
+def cpu_info():
+    """Model name and logical CPU count of the host (for the CPU baselines)."""
+    model = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                model = ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"model": model or "unknown", "cores": os.cpu_count() or 1, "build": ORACLE_FLAGS}
+
+
+def config_of(n, ops):
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": f"random_layers_{n}q_c128_depth40_extras", "qubits": n, "depth": DEPTH, "seed": SEED,
+            "gates": len(ops), "l2": f"state {16 * 2 ** n / 2 ** 30:g} GiB"
+                                      + (" >> L2 (no flush needed)" if 16 * 2 ** n > 4 * 129e6 else "")}
+
+
+def max_abs_diff(a, b, chunk=1 << 24):
+    m = 0.0
+    for i in range(0, a.size, chunk):
+        m = max(m, float(np.abs(a[i:i + chunk] - b[i:i + chunk]).max()))
+    return m
 
 
 class ClockSampler:
@@ -142,32 +164,36 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample(ops, n, seconds=12.0, threads=None):
+STRIDE = 301  # coprime with the gate count: t -> (t * STRIDE) mod gates visits every gate
+
+
+def strided_gates(ops, start, count):
+    """Gate indices start .. start+count-1 of the circuit's strided order: a
+    bounded sample that covers the whole gate mix."""
+    return [(t * STRIDE) % len(ops) for t in range(start, start + count)]
+
+
+def cpu_sample(ops, n, seconds=12.0):
     """Time the CPU restatement of the reference (oracle/) on the host cores:
-    apply the circuit's gates in order to a 2^n complex128 state until
-    `seconds` have elapsed; returns (gbps, gates applied, cores)."""
+    apply the circuit's gates in strided order to a 2^n complex128 state
+    until `seconds` have elapsed; returns (gbps, gates applied, seconds)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
-    cores = threads or os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
     oracle.build()
     psi = np.zeros(1 << n, dtype=np.complex128)
     psi[0] = 1.0
-    from pyquafu_gb300 import workloads  # noqa: F401
-
     gate_bytes = gate_equiv_bytes(ops, n)
-    done = 0
-    bytes_done = 0.0
+    done, bytes_done = 0, 0.0
     t0 = time.perf_counter()
-    for i, o in enumerate(ops):
-        oracle.apply_op(psi, o)
-        done += 1
+    while time.perf_counter() - t0 <= seconds:
+        i = strided_gates(ops, done, 1)[0]
+        oracle.apply_op(psi, ops[i])
         bytes_done += gate_bytes[i]
-        if time.perf_counter() - t0 > seconds:
-            break
+        done += 1
     dt = time.perf_counter() - t0
-    return bytes_done / dt / 1e9, done, dt, cores
+    return bytes_done / dt / 1e9, done, dt
 
 
 def gate_equiv_bytes(ops, n, S=S128):
@@ -205,10 +231,10 @@ def run_reference(args):
     def step():
         nonlocal pos
         b = 0.0
-        for _ in range(per_step):
-            oracle.apply_op(psi, ops[pos])
-            b += gb[pos]
-            pos = (pos + 1) % len(ops)
+        for i in strided_gates(ops, pos, per_step):
+            oracle.apply_op(psi, ops[i])
+            b += gb[i]
+        pos += per_step
         return b
 
     for _ in range(args.warmup):
@@ -219,17 +245,16 @@ def run_reference(args):
         tot += step()
     dt = time.perf_counter() - t0
     v = tot / dt / 1e9
-    sample = (f"{per_step} consecutive gates of the {n}-qubit circuit per step on a {16 * 2 ** n / 2 ** 30:g} GiB "
-              f"complex128 state (oracle/qsv_oracle.c, OpenMP {cores} threads)")
+    info = cpu_info()
+    sample = (f"{per_step} gates per step in strided order (gate t*{STRIDE} mod {len(ops)}), {args.steps} steps "
+              f"after {args.warmup} warm-up steps, on a {16 * 2 ** n / 2 ** 30:g} GiB complex128 state "
+              f"(oracle/qsv_oracle.c, OpenMP {cores} threads, {info['model']})")
     line = {"impl": "reference", "metric": "statevector_gbps", "value": round(v, 3), "unit": "GB/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"random_layers_{n}q_c128_depth40_extras", "qubits": n, "depth": DEPTH,
-                       "seed": SEED, "l2": f"state {16 * 2 ** n / 2 ** 30:g} GiB"
-                                          + (" >> L2 (no flush needed)" if 16 * 2 ** n > 4 * 129e6 else "")},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_of(n, ops),
             "cpu_baseline": {"value": round(v, 3), "unit": "GB/s", "cores": cores, "kind": "port",
-                             "sample": sample},
+                             "sample": sample, "cpu": info},
             "e2e": {"value": round(v, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -304,22 +329,55 @@ def measure(precision, ops, n, steps, warmup, per_pass=True):
     return out
 
 
-def measure_adjoint(n=24, layers=20, ps_params=6):
+def plain_passes(n, ops, precision):
+    """(forward passes, reverse-sweep passes) of the single-state adjoint
+    plans (host planning only)."""
+    import ctypes
+
+    from pyquafu_gb300 import _native as nat
+    from pyquafu_gb300 import ir
+
+    lib = nat.load()
+    arr, pool = ir.pack([o for o in ops if o.is_gate])
+    prec = nat.PRECISIONS[precision]
+    out = []
+    for adjoint in (0, 1):
+        h = ctypes.c_void_p()
+        if adjoint:
+            nat.check(lib.qfvm_plan_host_build_adjoint(n, prec, nat.vptr(arr), arr.size,
+                                                       nat.dptr(pool.view(np.float64)), pool.size, ctypes.byref(h)))
+        else:
+            nat.check(lib.qfvm_plan_host_build(n, prec, nat.vptr(arr), arr.size, nat.dptr(pool.view(np.float64)),
+                                               pool.size, 0, 0, ctypes.byref(h)))
+        counts = (ctypes.c_int64 * 4)()
+        shape = (ctypes.c_int32 * 3)()
+        nat.check(lib.qfvm_plan_host_counts(h, counts, shape))
+        lib.qfvm_plan_destroy(h)
+        out.append(int(counts[0]))
+    return out[0], out[1]
+
+
+def measure_adjoint(n=24, layers=20, ps_params=6, peak=FALLBACK_HBM, cpu=True, cpu_seconds=10.0):
     """Adjoint gradients of a hardware-efficient ansatz (ry, rz on every qubit
     then a cx ladder, 2 * n * layers parameters; observable sum a_i Z_i Z_i+1 +
-    sum b_i X_i): time per full gradient for each precision, the same GPU's
-    parameter-shift rate (timed on `ps_params` parameters, 2 forward runs each,
-    extrapolated), and each precision's gradient error against complex128."""
+    sum b_i X_i): time per full gradient for each precision, its HBM rate
+    (algorithmic bytes of the forward and reverse passes over the time), the
+    same GPU's parameter-shift rate (timed on `ps_params` parameters, 2
+    forward runs each, extrapolated), and the CPU baseline (the oracle's
+    restatement of grad_adjoint, gradiant.py:144-173, its reverse sweep timed
+    for `cpu_seconds` and extrapolated).  Gradients are returned for the
+    oracle comparison."""
     import torch
 
+    from pyquafu_gb300 import batch as bmod
     from pyquafu_gb300 import gradients, workloads
 
     ops, _ = workloads.hea(n, layers, seed=0)
     terms = workloads.zz_x_hamiltonian(n, seed=0)
     nparam = 2 * n * layers
     out = {"workload": f"hea_{n}q_{layers}layers_{nparam}params_{len(terms)}terms"}
-    ref = None
-    for prec in ("c128", "c128_ds", "c64"):
+    grads = {}
+    for prec in ("c128_ds", "c128", "c64"):
         gradients.adjoint(n, ops, terms, prec)  # warm-up (plans, allocation)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -328,14 +386,13 @@ def measure_adjoint(n=24, layers=20, ps_params=6):
             e, g = gradients.adjoint(n, ops, terms, prec)
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) / reps
-        item = {"s_per_gradient": round(dt, 4), "grads_per_s": round(nparam / dt, 1), "energy": e}
-        if ref is None:
-            ref = g
-        else:
-            item["max_abs_err_vs_c128"] = float(np.abs(g - ref).max())
-        out[prec] = item
-    # parameter shift on the plain GPU path (complex128), a subset of parameters
-    sub = [o for o in ops]
+        fp, rp = plain_passes(n, ops, prec)
+        nbytes = bmod.algorithmic_bytes(n, 1, fp, rp, S_OF[prec])
+        out[prec] = {"s_per_gradient": round(dt, 4), "grads_per_s": round(nparam / dt, 1), "energy": e,
+                     "passes": [fp, rp], "hbm_gbps": round(nbytes / dt / 1e9, 1),
+                     "frac_hbm": round(nbytes / dt / 1e9 / peak, 4)}
+        grads[prec] = g
+    # parameter shift on the plain GPU path (complex128 FP64), a subset of parameters
     keep = set(range(ps_params))
     sub = [o if (o.slot in keep or o.slot < 0) else workloads.named(o.name, o.qubits, o.params) for o in ops]
     t0 = time.perf_counter()
@@ -345,13 +402,24 @@ def measure_adjoint(n=24, layers=20, ps_params=6):
     out["param_shift_c128"] = {"s_per_parameter": round(per_param, 4),
                                "s_per_gradient_extrapolated": round(per_param * nparam, 2),
                                "params_timed": len(keep),
-                               "max_abs_diff_vs_adjoint": float(np.abs(ps[: len(keep)] - ref[: len(keep)]).max())}
+                               "max_abs_diff_vs_adjoint": float(np.abs(ps[: len(keep)] - grads["c128"][: len(keep)]).max())}
     out["adjoint_speedup_vs_param_shift"] = {
-        p: round(per_param * nparam / out[p]["s_per_gradient"], 1) for p in ("c128", "c128_ds", "c64")}
-    return out
+        p: round(per_param * nparam / out[p]["s_per_gradient"], 1) for p in ("c128_ds", "c128", "c64")}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        oracle.build()
+        fwd_s, lam_s, done, rev_s = oracle.grad_adjoint_timing(n, ops, [o.slot for o in ops], terms, cpu_seconds)
+        total = fwd_s + lam_s + rev_s * len(ops) / max(done, 1)
+        out["cpu_baseline"] = {"value": round(nparam / total, 2), "unit": "grads/s", "cores": os.cpu_count(),
+                               "kind": "port", "s_per_gradient": round(total, 2),
+                               "sample": f"oracle grad_adjoint: forward {fwd_s:.1f} s and lam {lam_s:.1f} s in full, "
+                                         f"reverse sweep {done} of {len(ops)} gates in {rev_s:.1f} s, extrapolated"}
+    return out, (ops, terms, grads)
 
 
-def measure_uneven_batch(reps=5, check_items=8, cpu=True, cpu_seconds=8.0, tune=True):
+def measure_uneven_batch(reps=5, check_items=8, cpu=True, cpu_seconds=8.0, tune=True, peak=FALLBACK_HBM):
     """2048 circuits of 10..18 qubits (ry encoding + 6 HEA layers), complex64
     with FP64 reductions: per-circuit <Z_0> and full gradient in one CUDA-graph
     launch.  Device time of the graph launch (uploads and downloads
@@ -409,6 +477,7 @@ def measure_uneven_batch(reps=5, check_items=8, cpu=True, cpu_seconds=8.0, tune=
            "circuits_per_s": round(ncirc / dev_s, 1), "grads_per_s": round(ngrad / dev_s, 1),
            "e2e_circuits_per_s": round(ncirc / wall, 1),
            "algorithmic_gb": round(nbytes / 1e9, 3), "achieved_gbps": round(nbytes / dev_s / 1e9, 1),
+           "frac_hbm": round(nbytes / dev_s / 1e9 / peak, 4),
            "max_abs_err_vs_c128": {"expval": err_e, "grad": err_g, "items_checked": check_items * len(keys)},
            "autotuned_shapes": tuned}
     if cpu:
@@ -527,7 +596,7 @@ def measure_noise(n=16, shots=2048, cpu=True):
     return res
 
 
-def measure_qnn(steps=5, warmup=3, ps_forwards=20, tune=True):
+def measure_qnn(steps=5, warmup=3, ps_forwards=20, tune=True, peak=FALLBACK_HBM, cpu=True, cpu_forwards=6):
     """QNN training step: 1024 samples x 16 qubits, 12 HEA layers (384 shared
     weights), MSE of <Z_0> against sign(w . x) labels; forward and adjoint
     backward through the torch binding (complex64, FP64 reductions), SGD
@@ -595,7 +664,28 @@ def measure_qnn(steps=5, warmup=3, ps_forwards=20, tune=True):
     t2 = time.perf_counter()
     gradients.jacobian_param_shift(n, ops, [(1.0, "Z", [0])], vals[:sub], "c64")
     psb = (time.perf_counter() - t2) / sub * B
-    return {"workload": "qnn_1024x16q_12hea_layers_384_weights_mse_z0_c64",
+    cpu_base = None
+    if cpu:
+        # the reference's ExecuteCircuits step on the host: B forward
+        # evaluations, then B * 2 * 384 shifted evaluations for the
+        # parameter-shift Jacobian (torch.py:65-89, vjp.py:60-103), each a
+        # simulation of the circuit and <Z_0> through the oracle
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        oracle.build()
+        t3 = time.perf_counter()
+        for k in range(cpu_forwards):
+            b_ops = gradients.bind(ops, vals[k])
+            oracle.expect_pauli(oracle.simulate(n, b_ops), "Z", [0])
+        cfw = (time.perf_counter() - t3) / cpu_forwards
+        cstep = B * (1 + 2 * nw) * cfw
+        cpu_base = {"value": round(1.0 / cstep, 9), "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+                    "s_per_step": round(cstep, 1),
+                    "sample": f"{cpu_forwards} oracle forward evaluations ({cfw * 1e3:.1f} ms each) extrapolated to "
+                              f"{B} x (1 + 2 x {nw}) evaluations per step"}
+    return {"workload": "qnn_1024x16q_12hea_layers_384_weights_mse_z0_c64", "cpu_baseline": cpu_base,
+            "frac_hbm": round(nbytes / dev_s / 1e9 / peak, 4),
             "param_shift_batched": {"samples_timed": sub, "evaluations_per_sample": 1 + 2 * nw,
                                     "s_per_step_extrapolated": round(psb, 2),
                                     "adjoint_speedup": round(psb / dt, 1)},
@@ -606,6 +696,106 @@ def measure_qnn(steps=5, warmup=3, ps_forwards=20, tune=True):
             "param_shift_plain_path": {"s_per_forward": round(fwd_s, 6), "forwards_per_step": B * (1 + 2 * nw),
                                        "s_per_step_extrapolated": round(ps_step, 1)},
             "speedup_vs_param_shift": round(ps_step / dt, 1), "autotuned": tuned}
+
+
+def measure_c1(steps=20, shots=4096, cpu=True, peak=FALLBACK_HBM):
+    """The 20-qubit random circuit (depth 20, seed 0, complex128) with 4096
+    shots: gate time on the device (the 16 MiB state stays in L2 between
+    steps, so its GB/s are L2-resident figures), sampling time (one call:
+    uniforms up, block sums, block prefix, per-shot locate, exact fallback,
+    indices down), shots the exact scan resolved, and the oracle's gate and
+    sequential-scan times on the host cores (statevector.hpp:1380-1412 is
+    serial).  Errors: final state against the oracle per amplitude, sampled
+    indices against the oracle's scan with the same seeded uniforms."""
+    import torch
+
+    from pyquafu_gb300 import engine, workloads
+
+    n = 20
+    ops = workloads.random_layers(n, 20, seed=0)
+    out = {"workload": f"random_layers_{n}q_c128_depth20_{shots}shots", "gates": len(ops)}
+    u = np.random.Generator(np.random.MT19937(0)).random(shots)
+    states = {}
+    for prec in ("c128_ds", "c128"):
+        plan = engine.Plan(n, ops, prec)
+        st = engine.DeviceState(n, prec).set_zero()
+        for _ in range(3):
+            st.set_zero()
+            plan.run(st)
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(steps):
+            st.set_zero()
+            p_ms, _ = plan.run_timed(st)
+            ms.append(float(np.sum(p_ms)))
+        st.set_zero()
+        plan.run(st)
+        torch.cuda.synchronize()
+        gms = float(np.median(ms))
+        gb = sum(gate_equiv_bytes(ops, n, 16))
+        row = {"gates_ms": round(gms, 3), "gbps_gate_equiv_l2_resident": round(gb / (gms * 1e-3) / 1e9, 1),
+               "passes": plan.stats()["passes"]}
+        if prec == "c128_ds":
+            st.sample(u)  # warm-up
+            t0 = time.perf_counter()
+            reps = 5
+            for _ in range(reps):
+                idx = st.sample(u)
+            row["sample_ms"] = round((time.perf_counter() - t0) / reps * 1e3, 3)
+            row["exact_scan_shots"] = st.exact_sampled_shots()
+            out["indices"] = idx
+        states[prec] = st.download()
+        st.close()
+        plan.close()
+        out[prec] = row
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        oracle.build()
+        t0 = time.perf_counter()
+        ref = oracle.simulate(n, ops)
+        t1 = time.perf_counter()
+        ref_idx = oracle.sample_indices(ref, u)
+        t2 = time.perf_counter()
+        out["cpu_baseline"] = {"gates_s": round(t1 - t0, 3), "scan_s": round(t2 - t1, 3), "kind": "port",
+                               "cores": os.cpu_count(), "cpu": cpu_info(),
+                               "sample": "the full circuit and all 4096 shots (sequential scan, one core)"}
+        for prec in ("c128_ds", "c128"):
+            out[prec]["max_abs_err_vs_oracle"] = max_abs_diff(states[prec], ref)
+        out["sample_mismatches_vs_oracle"] = int(np.sum(out["indices"] != ref_idx))
+    del out["indices"]
+    return out
+
+
+def oracle_check_c2(n, ops, precisions):
+    """Final state of every arithmetic against the oracle (its full run on
+    the host cores, timed), per amplitude, and <Z0 Z1>."""
+    import torch
+
+    from pyquafu_gb300 import engine
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    oracle.build()
+    t0 = time.perf_counter()
+    ref = oracle.simulate(n, ops)
+    oracle_s = time.perf_counter() - t0
+    zz_ref = oracle.expect_pauli(ref, "ZZ", [0, 1])
+    out = {"oracle_full_circuit_s": round(oracle_s, 1), "oracle_cores": os.cpu_count()}
+    buf = np.empty(1 << n, dtype=np.complex128)
+    for prec in precisions:
+        plan = engine.Plan(n, ops, prec)
+        st = engine.DeviceState(n, prec).set_zero()
+        plan.run(st)
+        torch.cuda.synchronize()
+        zz = float(st.expect([("ZZ", [0, 1])])[0])
+        st.download(buf)
+        st.close()
+        plan.close()
+        out[prec] = {"max_abs_err": max_abs_diff(buf, ref), "zz_abs_err": abs(zz - zz_ref)}
+    return out
 
 
 def max_over_ranks(value: float, world: int, device: str = "cuda") -> float:
@@ -665,6 +855,7 @@ def run_gpu(args):
     n = N_QUBITS
     ops = workload()
     peak, peak_kind = hbm_peak()
+    cpu_here = rank == 0 and not args.skip_cpu
 
     def barrier():
         torch.cuda.synchronize()
@@ -686,19 +877,20 @@ def run_gpu(args):
     gb = sum(gate_equiv_bytes(ops, n, S))
     value = world * gb / (ms_step * 1e-3) / 1e9
     achieved = main["tile_gbps"]
-    fp64 = fp64_ops(ops, n)
 
     variants = {}
     for v in [x for x in args.variants.split(",") if x and x != args.precision]:
-        r = measure(v, ops, n, args.steps, max(1, min(args.warmup, 3)))
+        r = measure(v, ops, n, min(args.steps, 3), max(1, min(args.warmup, 3)))
         variants[v] = {"value": round(r["gbps"], 2), "unit": "GB/s", "ms_per_step": round(r["ms_per_step"], 3),
                        "passes": r["passes"], "tile_kernel": kernel_name(v, n, r["specialised_passes"] > 0),
                        "specialised_passes": r["specialised_passes"], "tile_pass_gbps": round(r["tile_gbps"], 1),
-                       "tile_pass_frac_hbm": round(r["tile_gbps"] / peak, 4)}
+                       "tile_pass_frac_hbm": round(r["tile_gbps"] / peak, 4),
+                       "hbm_gbps": round(r["pass_bytes"] / (r["ms_per_step"] * 1e-3) / 1e9, 1)}
 
     # --- end to end through the reference-shaped API (host buffers) ---
     e2e = None
     if not args.skip_e2e:
+        qfvm.set_arithmetic("ds" if args.precision == "c128_ds" else "fp64")
         host = torch.empty(2 * 2 ** n, dtype=torch.float64, pin_memory=True)
         psi = host.numpy().view(np.complex128)
         psi[:] = 0
@@ -714,68 +906,82 @@ def run_gpu(args):
         gb128 = sum(gate_equiv_bytes(ops, n, 16))
         e2e = {"value": round(world * gb128 / e2e_s / 1e9, 2), "unit": "GB/s",
                "h2d_bytes_per_step": int(16 * 2 ** n), "d2h_bytes_per_step": int(16 * 2 ** n),
-               "ms_per_step": round(e2e_s * 1e3, 2),
+               "ms_per_step": round(e2e_s * 1e3, 2), "arithmetic": qfvm.get_arithmetic(),
                "api": "pyquafu_gb300.qfvm.simulate_circuit(circuit, pinned complex128 state, shots=0)"}
         del psi, host
+        qfvm.set_arithmetic("ds")
 
-    adj = None
+    c1 = None if args.skip_c1 else measure_c1(cpu=cpu_here, peak=peak)
+    adj = adj_data = None
     if not args.skip_adjoint:
-        adj = measure_adjoint(args.adjoint_qubits)
+        adj, adj_data = measure_adjoint(args.adjoint_qubits, peak=peak, cpu=cpu_here)
     batched = None
     if not args.skip_batch:
-        batched = {"uneven_2048": measure_uneven_batch(cpu=rank == 0 and not args.skip_cpu,
-                                                       tune=not args.no_autotune),
-                   "qnn_training_step": measure_qnn(tune=not args.no_autotune),
-                   "trajectories": measure_trajectories(cpu=rank == 0 and not args.skip_cpu),
-                   "noise": measure_noise(cpu=rank == 0 and not args.skip_cpu)}
+        batched = {"uneven_2048": measure_uneven_batch(cpu=cpu_here, tune=not args.no_autotune, peak=peak),
+                   "qnn_training_step": measure_qnn(tune=not args.no_autotune, peak=peak, cpu=cpu_here),
+                   "trajectories": measure_trajectories(cpu=cpu_here),
+                   "noise": measure_noise(cpu=cpu_here)}
 
     cpu = None
-    if rank == 0 and not args.skip_cpu:
-        cgbps, gates_done, cdt, cores = cpu_sample(ops, n, seconds=args.cpu_seconds)
-        cpu = {"value": round(cgbps, 3), "unit": "GB/s", "cores": cores, "kind": "port",
-               "sample": f"first {gates_done} gates of the circuit on the {n}-qubit complex128 state "
-                         f"({cdt:.1f} s, oracle/qsv_oracle.c with OpenMP)"}
+    if cpu_here:
+        cgbps, gates_done, cdt = cpu_sample(ops, n, seconds=args.cpu_seconds)
+        info = cpu_info()
+        cpu = {"value": round(cgbps, 3), "unit": "GB/s", "cores": info["cores"], "kind": "port",
+               "sample": f"{gates_done} gates of the circuit in strided order on the {n}-qubit complex128 state "
+                         f"({cdt:.1f} s, OpenMP over all cores)", "cpu": info}
+
+    # --- the error of every result against the oracle (after all timing) ---
+    check = None
+    if rank == 0 and not args.skip_oracle_check:
+        precs = [args.precision] + [v for v in args.variants.split(",") if v and v != args.precision]
+        check = oracle_check_c2(n, ops, precs)
+        if adj_data is not None:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+
+            aops, aterms, grads = adj_data
+            t0 = time.perf_counter()
+            gref = oracle.grad_adjoint(args.adjoint_qubits, aops, [o.slot for o in aops], aterms)
+            adj["oracle_s"] = round(time.perf_counter() - t0, 1)
+            for prec, g in grads.items():
+                adj[prec]["max_abs_err_vs_oracle"] = float(np.abs(g - gref).max())
 
     if rank == 0:
+        err = (check or {}).get(args.precision, {})
         line = {
             "metric": "statevector_gbps", "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": {"c128": "f64", "c128_ds": "f32x2", "c64": "f32"}[args.precision],
             "data": "synthetic",
-            "config": {"workload": f"random_layers_{n}q_c128_depth40_extras", "qubits": n, "depth": DEPTH,
-                       "seed": SEED, "gates": len(ops), "precision": args.precision, "passes": main["passes"],
-                       "rounds": main["rounds"], "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "state >> L2 (no flush needed)"},
+            "config": config_of(n, ops),
+            "engine": {"precision": args.precision, "storage": "c64" if args.precision == "c64" else "c128",
+                       "passes": main["passes"], "rounds": main["rounds"],
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "max_abs_err_vs_oracle": err.get("max_abs_err"),
             "roofline": {"bound": "hbm", "kernel": kernel_name(args.precision, n, main["specialised_passes"] > 0),
-                         "achieved": round(achieved, 1),
-                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                         "traffic": (round(TRAFFIC_PER_AMP_C128 * 2 ** n) if args.precision == "c128" else None),
-                         "traffic_source": ("ncu dram bytes of a 26-qubit launch, scaled by 2^(n-26) "
-                                            "(profiles/qsv_tile_pass_c128_random_layers.md)"
-                                            if args.precision == "c128" else None),
-                         "bytes_per_launch": main["tile_bytes"],
-                         "avg_launch_ms": round(main["avg_tile_ms"], 3),
-                         "compute": ({"pipe": "fp64", "frac": round(fp64 / (ms_step * 1e-3) / FP64_PEAK_INSTR, 3),
-                                      "achieved_instr_per_s": round(fp64 / (ms_step * 1e-3)),
-                                      "peak_instr_per_s": FP64_PEAK_INSTR,
-                                      "peak_kind": "measured (profiles/gb300_arith_peaks.md)"}
-                                     if args.precision == "c128" else None)},
-            "pass_gbps": round(main["pass_bytes"] / (ms_step * 1e-3) / 1e9, 1),
+                         "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                         "traffic": (round(TRAFFIC_PER_AMP[args.precision] * 2 ** n)
+                                     if args.precision in TRAFFIC_PER_AMP else None),
+                         "traffic_source": ("ncu dram bytes of a 26-qubit launch, scaled by 2^(n-26)"
+                                            if args.precision in TRAFFIC_PER_AMP else None),
+                         "bytes_per_launch": main["tile_bytes"], "avg_launch_ms": round(main["avg_tile_ms"], 3)},
+            "hbm_gbps": round(main["pass_bytes"] / (ms_step * 1e-3) / 1e9, 1),
             "e2e": e2e,
             "cpu_baseline": cpu,
-            "variants": variants,
-            "adjoint": adj,
-            "batched": batched,
-            "autotune": tuning,
             "clocks": clk,
             "gpu_launches": int(main["launches"]),
             "specialised": {"passes": main["specialised_passes"], "of": main["passes"],
                             "first_runs_s": main["warmup_s"]},
+            "autotune": tuning,
+            "variants": variants,
+            "oracle_check": check,
+            "c1_sampling": c1,
+            "adjoint": adj,
+            "batched": batched,
         }
-        if args.precision == "c128":
-            line["fp64"] = {"instr_per_s": fp64 / (ms_step * 1e-3),
-                            "frac_of_measured_peak": round(fp64 / (ms_step * 1e-3) / FP64_PEAK_INSTR, 3)}
+        line["rows"] = summary_rows(line)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -784,14 +990,57 @@ def run_gpu(args):
     return 0
 
 
+def _r(x, nd=4):
+    return None if x is None else (round(x, nd) if isinstance(x, float) else x)
+
+
+def summary_rows(line):
+    """Compact per-configuration figures, printed last on the line."""
+    rows = {}
+    chk = line.get("oracle_check") or {}
+    c2 = {line["engine"]["precision"]: {"ms": line["ms_per_step"], "frac": line["roofline"]["frac"],
+                                        "err": chk.get(line["engine"]["precision"], {}).get("max_abs_err")}}
+    for v, r in (line.get("variants") or {}).items():
+        c2[v] = {"ms": r["ms_per_step"], "frac": r["tile_pass_frac_hbm"], "err": chk.get(v, {}).get("max_abs_err")}
+    rows["C2_30q"] = c2
+    c1 = line.get("c1_sampling")
+    if c1:
+        cb = c1.get("cpu_baseline") or {}
+        rows["C1_20q_4096shots"] = {"gates_ms": c1["c128_ds"]["gates_ms"], "sample_ms": c1["c128_ds"]["sample_ms"],
+                                    "exact_scan_shots": c1["c128_ds"]["exact_scan_shots"],
+                                    "err": c1["c128_ds"].get("max_abs_err_vs_oracle"),
+                                    "sample_mismatches": c1.get("sample_mismatches_vs_oracle"),
+                                    "cpu_gates_s": cb.get("gates_s"), "cpu_scan_s": cb.get("scan_s")}
+    a = line.get("adjoint")
+    if a:
+        rows["C3_24q_adjoint"] = {p: {"s": a[p]["s_per_gradient"], "frac": a[p]["frac_hbm"],
+                                      "err": a[p].get("max_abs_err_vs_oracle")} for p in ("c128_ds", "c128", "c64")}
+        rows["C3_24q_adjoint"]["vs_param_shift"] = a["adjoint_speedup_vs_param_shift"]
+        rows["C3_24q_adjoint"]["cpu_s"] = (a.get("cpu_baseline") or {}).get("s_per_gradient")
+    b = line.get("batched") or {}
+    if "uneven_2048" in b:
+        u = b["uneven_2048"]
+        rows["C4_2048_circuits"] = {"circuits_per_s": u["circuits_per_s"], "frac": u["frac_hbm"],
+                                    "err_vs_c128": u["max_abs_err_vs_c128"]["grad"],
+                                    "cpu_circuits_per_s": (u.get("cpu_baseline") or {}).get("value")}
+    if "qnn_training_step" in b:
+        q = b["qnn_training_step"]
+        rows["C5_qnn_step"] = {"steps_per_s": q["steps_per_s"], "frac": q["frac_hbm"],
+                               "vs_param_shift": q["speedup_vs_param_shift"],
+                               "cpu_s_per_step": (q.get("cpu_baseline") or {}).get("s_per_step")}
+    return rows
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="c128", choices=["c128", "c128_ds", "c64"])
-    ap.add_argument("--variants", default="c128_ds,c64")
+    ap.add_argument("--precision", default=DEFAULT_PRECISION, choices=["c128", "c128_ds", "c64"])
+    ap.add_argument("--variants", default="c128,c64")
+    ap.add_argument("--skip-c1", action="store_true")
+    ap.add_argument("--skip-oracle-check", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-variants", action="store_true")

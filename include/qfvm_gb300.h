@@ -162,6 +162,15 @@ int qfvm_expect_device_noalloc(const void* dev_state, uint64_t state_len, int32_
                                int64_t n_terms, double* out, void* stream);
 const char* qfvm_noalloc_last_error(void);
 
+/* Arithmetic of the complex128 work the host-buffer entry points issue
+ * (qfvm_simulate_circuit, qfvm_applyop_statevec, qfvm_simulate_shots,
+ * qfvm_simulate_noise): QFVM_C128_DS (the default; float-pair arithmetic on
+ * the FP32 pipes, per-amplitude error below 1e-12 against FP64) or QFVM_C128
+ * (IEEE FP64).  Storage is complex128 either way.  No counterpart in the
+ * reference, whose CPU path is FP64. */
+int qfvm_set_c128_arithmetic(int32_t arith);
+int32_t qfvm_get_c128_arithmetic(void);
+
 /* Failure-path test hook (no counterpart in the reference).  kind 1: the
  * countdown-th device allocation from now on fails (QFVM_ERR_NOMEM) without
  * calling cudaMalloc; kind 2: the countdown-th pass of a plan run fails
@@ -189,6 +198,9 @@ int qfvm_sv_expect(qfvm_sv* sv, const uint64_t* x_masks, const uint64_t* z_masks
                    int64_t n_terms, double* out);
 int qfvm_sv_sample(qfvm_sv* sv, const double* uniforms, int64_t shots, uint64_t* out_indices);
 int qfvm_sv_norm2(qfvm_sv* sv, double* out);                           /* FP64 sum |a|^2 */
+/* Shots of the last qfvm_sv_sample on this state that the certified parallel
+ * scan could not decide and the exact sequential scan resolved. */
+int qfvm_sv_sample_stats(qfvm_sv* sv, int64_t* exact_shots);
 /* Raw device pointer and byte size of the state (for host-side interop). */
 int qfvm_sv_device_ptr(qfvm_sv* sv, void** dev_ptr, uint64_t* nbytes);
 /* Stream the engine issues this state's work on (cudaStream_t as void*). */

@@ -11,6 +11,7 @@ Each function cites the reference lines it follows:
   * ``sample_indices``      statevector.hpp:1380-1412 (host-supplied uniforms)
   * ``measure_counts``      statevector.hpp:1398-1409 (bitstring per cbit)
   * ``grad_adjoint``        quafu/algorithms/gradients/gradiant.py:144-173
+  * ``grad_adjoint_timing`` the same, timed on a bounded reverse sweep (CPU baseline)
   * ``grad_param_shift``    quafu/algorithms/gradients/gradiant.py:38-73
 """
 
@@ -447,6 +448,33 @@ def grad_adjoint(n, ops, param_index, terms, psi_in=None):
             grads[param_index[i]] += np.real(2.0 * np.vdot(lam, mu))
         apply_op(lam, _dagger(op))
     return grads
+
+
+def grad_adjoint_timing(n, ops, param_index, terms, seconds):
+    """grad_adjoint above, timed for the CPU baseline: the forward
+    simulation and lam = H psi in full, then the reverse sweep until
+    `seconds` have elapsed.  Returns (forward s, lam s, reverse gates done,
+    reverse s)."""
+    import time
+
+    t0 = time.perf_counter()
+    phi = simulate(n, ops)
+    t1 = time.perf_counter()
+    lam = apply_hamiltonian(phi, terms)
+    t2 = time.perf_counter()
+    done = 0
+    for i in range(len(ops) - 1, -1, -1):
+        op = ops[i]
+        apply_op(phi, _dagger(op))
+        if param_index[i] >= 0 and not op.ncontrols:
+            mu = phi.copy()
+            apply_op(mu, _grad_gate(op))
+            np.real(2.0 * np.vdot(lam, mu))
+        apply_op(lam, _dagger(op))
+        done += 1
+        if time.perf_counter() - t2 > seconds:
+            break
+    return t1 - t0, t2 - t1, done, time.perf_counter() - t2
 
 
 def energy(n, ops, terms, psi_in=None) -> float:

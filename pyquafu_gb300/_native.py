@@ -57,6 +57,8 @@ PROTOTYPES = {
                                                   ctypes.c_int64, c_dp, c_vp]),
     "qfvm_noalloc_last_error": (ctypes.c_char_p, []),
     "qfvm_test_fault": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64]),
+    "qfvm_set_c128_arithmetic": (ctypes.c_int, [ctypes.c_int32]),
+    "qfvm_get_c128_arithmetic": (ctypes.c_int32, []),
     "qfvm_simulate_shots": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int64, c_dp,
                                            ctypes.c_int64, c_dp, ctypes.c_int64, c_dp, ctypes.c_int64, c_u64p, c_dp]),
     "qfvm_simulate_noise": (ctypes.c_int, [ctypes.c_int32, c_vp, ctypes.c_int64, c_dp, ctypes.c_int64, c_dp,
@@ -73,6 +75,7 @@ PROTOTYPES = {
     "qfvm_sv_expect": (ctypes.c_int, [c_vp, c_u64p, c_u64p, c_i32p, ctypes.c_int64, c_dp]),
     "qfvm_sv_sample": (ctypes.c_int, [c_vp, c_dp, ctypes.c_int64, c_u64p]),
     "qfvm_sv_norm2": (ctypes.c_int, [c_vp, c_dp]),
+    "qfvm_sv_sample_stats": (ctypes.c_int, [c_vp, ctypes.POINTER(ctypes.c_int64)]),
     "qfvm_sv_device_ptr": (ctypes.c_int, [c_vp, ctypes.POINTER(c_vp), c_u64p]),
     "qfvm_sv_stream": (ctypes.c_int, [c_vp, ctypes.POINTER(c_vp)]),
     "qfvm_plan_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, c_vp, ctypes.c_int64, c_dp, ctypes.c_int64,

@@ -26,9 +26,12 @@ thread_local std::string g_err;
 std::atomic<uint64_t> g_launches{0};
 
 namespace {
+std::atomic<int> g_c128_arith{QFVM_C128_DS};
 std::atomic<int> g_fault_kind{FAULT_NONE};
 std::atomic<int64_t> g_fault_count{0};
 }  // namespace
+
+int c128_arith() { return g_c128_arith.load(std::memory_order_relaxed); }
 
 bool fault_hit(int kind) {
     if (g_fault_kind.load(std::memory_order_relaxed) != kind) return false;
@@ -377,6 +380,7 @@ int sv_sample(qfvm_sv* sv, const double* uni, int64_t shots, uint64_t* out) {
     std::vector<int64_t> ord;
     for (size_t i = 0; i < s; ++i)
         if (unsure[i]) ord.push_back(static_cast<int64_t>(i));
+    sv->last_exact = static_cast<int64_t>(ord.size());
     if (!ord.empty()) {
         std::stable_sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return uni[a] < uni[b]; });
         QSV_CUDA(cudaMemcpyAsync(dord, ord.data(), ord.size() * 8, cudaMemcpyHostToDevice, sv->stream),
@@ -411,6 +415,53 @@ int cached_state(int n, int precision, qfvm_sv** out) {
     return QFVM_OK;
 }
 
+// Plans of the last few circuits simulate_circuit saw, keyed by the raw op
+// records and matrix pool (callers that re-run one circuit, as a sampling or
+// parameter loop does, skip classification, fusion, the plan upload and the
+// specialised-kernel lookup).  Guarded by g_boundary_mu.
+struct CachedPlan {
+    int n = 0, arith = 0;
+    std::vector<unsigned char> key;
+    qfvm_plan* plan = nullptr;
+};
+std::vector<CachedPlan> g_plan_cache;
+constexpr size_t PLAN_CACHE_SIZE = 4;
+
+int cached_plan(int n, int arith, const qfvm_op* ops, int64_t n_ops, const double* matpool, int64_t matpool_len,
+                qfvm_plan** out) {
+    if (n_ops < 0 || (n_ops > 0 && !ops) || matpool_len < 0 || (matpool_len > 0 && !matpool))
+        return fail(QFVM_ERR_INVALID, "bad op list");
+    std::vector<unsigned char> key(static_cast<size_t>(n_ops) * sizeof(qfvm_op) +
+                                   static_cast<size_t>(matpool_len) * sizeof(double));
+    if (n_ops) std::memcpy(key.data(), ops, static_cast<size_t>(n_ops) * sizeof(qfvm_op));
+    if (matpool_len)
+        std::memcpy(key.data() + static_cast<size_t>(n_ops) * sizeof(qfvm_op), matpool,
+                    static_cast<size_t>(matpool_len) * sizeof(double));
+    for (size_t i = 0; i < g_plan_cache.size(); ++i) {
+        CachedPlan& c = g_plan_cache[i];
+        if (c.n == n && c.arith == arith && c.key == key) {
+            std::rotate(g_plan_cache.begin(), g_plan_cache.begin() + static_cast<std::ptrdiff_t>(i),
+                        g_plan_cache.begin() + static_cast<std::ptrdiff_t>(i) + 1);
+            *out = g_plan_cache.front().plan;
+            return QFVM_OK;
+        }
+    }
+    qfvm_plan* p = nullptr;
+    QSV_TRY(make_plan(n, arith, ops, n_ops, matpool, matpool_len, 0, 0, &p));
+    CachedPlan c;
+    c.n = n;
+    c.arith = arith;
+    c.key = std::move(key);
+    c.plan = p;
+    g_plan_cache.insert(g_plan_cache.begin(), std::move(c));
+    if (g_plan_cache.size() > PLAN_CACHE_SIZE) {
+        free_plan(g_plan_cache.back().plan);
+        g_plan_cache.pop_back();
+    }
+    *out = p;
+    return QFVM_OK;
+}
+
 int log2_len(uint64_t len, int* n) {
     if (len < 2 || (len & (len - 1)) != 0) return fail(QFVM_ERR_INVALID, "state length must be a power of two >= 2");
     int k = 0;
@@ -427,6 +478,14 @@ extern "C" {
 const char* qfvm_last_error(void) { return g_err.c_str(); }
 int32_t qfvm_abi_version(void) { return QFVM_ABI_VERSION; }
 uint64_t qfvm_launch_count(void) { return g_launches.load(); }
+
+int qfvm_set_c128_arithmetic(int32_t arith) {
+    if (arith != QFVM_C128 && arith != QFVM_C128_DS)
+        return fail(QFVM_ERR_INVALID, "complex128 arithmetic must be QFVM_C128 or QFVM_C128_DS");
+    g_c128_arith.store(arith);
+    return QFVM_OK;
+}
+int32_t qfvm_get_c128_arithmetic(void) { return c128_arith(); }
 
 int qfvm_test_fault(int32_t kind, int64_t countdown) {
     if (kind < FAULT_NONE || kind > FAULT_STAGE) return fail(QFVM_ERR_INVALID, "fault kind must be 0, 1 or 2");
@@ -478,6 +537,11 @@ int qfvm_sv_expect(qfvm_sv* sv, const uint64_t* x_masks, const uint64_t* z_masks
 int qfvm_sv_sample(qfvm_sv* sv, const double* uniforms, int64_t shots, uint64_t* out_indices) {
     if (!sv) return fail(QFVM_ERR_INVALID, "null state");
     return sv_sample(sv, uniforms, shots, out_indices);
+}
+int qfvm_sv_sample_stats(qfvm_sv* sv, int64_t* exact_shots) {
+    if (!sv || !exact_shots) return fail(QFVM_ERR_INVALID, "null argument");
+    *exact_shots = sv->last_exact;
+    return QFVM_OK;
 }
 int qfvm_sv_norm2(qfvm_sv* sv, double* out) {
     if (!sv || !out) return fail(QFVM_ERR_INVALID, "null argument");
@@ -675,7 +739,7 @@ int qfvm_simulate_circuit(int32_t num_qubits, const qfvm_op* ops, int64_t n_ops,
         t0 = t1;
     };
     qfvm_plan* p = nullptr;
-    QSV_TRY(make_plan(num_qubits, QFVM_C128, ops, n_ops, matpool, matpool_len, 0, 0, &p));
+    QSV_TRY(cached_plan(num_qubits, c128_arith(), ops, n_ops, matpool, matpool_len, &p));
     stage(0, nullptr);
     qfvm_sv* sv = nullptr;
     int rc = cached_state(num_qubits, QFVM_C128, &sv);
@@ -687,7 +751,6 @@ int qfvm_simulate_circuit(int32_t num_qubits, const qfvm_op* ops, int64_t n_ops,
     if (rc == QFVM_OK && shots > 0) rc = sv_sample(sv, uniforms, shots, out_indices);
     if (rc == QFVM_OK) rc = sv_download(sv, state, sv->N);
     stage(4, sv);
-    free_plan(p);
     stage(5, nullptr);
     if (trace)
         std::fprintf(stderr,
@@ -705,7 +768,7 @@ int qfvm_applyop_statevec(const qfvm_op* op, const double* matpool, int64_t matp
     QSV_TRY(log2_len(state_len, &n));
     QSV_TRY(check_device());
     qfvm_plan* p = nullptr;
-    QSV_TRY(make_plan(n, QFVM_C128, op, 1, matpool, matpool_len, 0, 0, &p));
+    QSV_TRY(make_plan(n, c128_arith(), op, 1, matpool, matpool_len, 0, 0, &p));
     qfvm_sv* sv = nullptr;
     int rc = cached_state(n, QFVM_C128, &sv);
     if (rc == QFVM_OK) rc = sv_upload(sv, state, sv->N);

@@ -34,6 +34,11 @@ int check_device();
         if (rc_ != QFVM_OK) return rc_; \
     } while (0)
 
+// Arithmetic of complex128 work issued by the host-buffer entry points
+// (simulate_circuit, applyop_statevec, per-shot and noisy trajectories):
+// QFVM_C128_DS (float pairs, the default) or QFVM_C128 (IEEE FP64).
+int c128_arith();
+
 // Host-side fault injection (qfvm_test_fault): once armed, the countdown-th
 // device allocation or kernel stage from then on fails on the host without
 // calling CUDA, so failure paths are exercised with no GPU fault.
@@ -76,6 +81,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255);
 struct qfvm_sv {
     int n = 0, precision = QFVM_C128;  // storage: QFVM_C128 or QFVM_C64
     int arith = QFVM_C128;             // arithmetic of qfvm_sv_apply: QFVM_C128, QFVM_C128_DS or QFVM_C64
+    int64_t last_exact = 0;            // shots the last qfvm_sv_sample resolved by the exact sequential scan
     uint64_t N = 0;
     void* d = nullptr;
     cudaStream_t stream = nullptr;

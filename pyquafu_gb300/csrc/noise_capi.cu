@@ -41,7 +41,7 @@ int parse_noise(int n, const qfvm_op* ops, int64_t n_ops, const double* matpool,
     auto flush = [&]() -> int {
         if (pending.empty()) return QFVM_OK;
         NoiseSegment s;
-        QSV_TRY(make_plan(n, QFVM_C128, pending.data(), static_cast<int64_t>(pending.size()), matpool, matpool_len, 0,
+        QSV_TRY(make_plan(n, c128_arith(), pending.data(), static_cast<int64_t>(pending.size()), matpool, matpool_len, 0,
                           0, &s.plan));
         segs->push_back(s);
         pending.clear();

@@ -44,7 +44,7 @@ int parse_program(int n, int ncb, const qfvm_op* ops, int64_t n_ops, const doubl
         if (pending.empty()) return QFVM_OK;
         Segment s;
         s.type = 0;
-        QSV_TRY(make_plan(n, QFVM_C128, pending.data(), static_cast<int64_t>(pending.size()), matpool, matpool_len, 0,
+        QSV_TRY(make_plan(n, c128_arith(), pending.data(), static_cast<int64_t>(pending.size()), matpool, matpool_len, 0,
                           0, &s.plan));
         segs->push_back(s);
         pending.clear();
@@ -100,7 +100,7 @@ int parse_program(int n, int ncb, const qfvm_op* ops, int64_t n_ops, const doubl
                 if (!is_gate_kind(ops[i + b].kind))
                     return fail(QFVM_ERR_UNSUPPORTED, "a cif body holds gates only");
             if (nb > 0) {
-                QSV_TRY(make_plan(n, QFVM_C128, ops + i + 1, nb, matpool, matpool_len, 0, 0, &s.plan));
+                QSV_TRY(make_plan(n, c128_arith(), ops + i + 1, nb, matpool, matpool_len, 0, 0, &s.plan));
                 segs->push_back(s);
             }
             i += nb;

@@ -122,6 +122,13 @@ class DeviceState:
         nat.check(self._lib.qfvm_sv_sample(self._h, nat.dptr(u), u.size, nat.u64ptr(out)), "sample")
         return out
 
+    def exact_sampled_shots(self) -> int:
+        """Shots of the last sample() that needed the exact sequential scan
+        (the parallel scan could not certify them)."""
+        v = ctypes.c_int64()
+        nat.check(self._lib.qfvm_sv_sample_stats(self._h, ctypes.byref(v)), "sample stats")
+        return v.value
+
     def norm2(self) -> float:
         v = ctypes.c_double()
         nat.check(self._lib.qfvm_sv_norm2(self._h, ctypes.byref(v)), "norm2")

@@ -37,6 +37,21 @@ def set_seed(seed) -> None:
     _rng = np.random.default_rng(seed)
 
 
+def set_arithmetic(kind: str) -> None:
+    """Arithmetic of this module's complex128 work (no counterpart in the
+    reference): "ds" (float pairs on the FP32 pipes, the default;
+    per-amplitude error below 1e-12 against FP64) or "fp64" (IEEE FP64).
+    The state stays complex128 either way."""
+    codes = {"ds": nat.QFVM_C128_DS, "fp64": nat.QFVM_C128}
+    if kind not in codes:
+        raise ValueError(f"arithmetic must be 'ds' or 'fp64', not {kind!r}")
+    nat.check(nat.load().qfvm_set_c128_arithmetic(codes[kind]), "set_arithmetic")
+
+
+def get_arithmetic() -> str:
+    return "ds" if nat.load().qfvm_get_c128_arithmetic() == nat.QFVM_C128_DS else "fp64"
+
+
 def _uniforms(shots: int) -> np.ndarray:
     global last_uniforms
     last_uniforms = _rng.random(int(shots))

@@ -42,8 +42,16 @@ def test_engine_arm_line():
     rf = d["roofline"]
     assert {"bound", "achieved", "peak", "unit", "frac", "traffic"} <= set(rf)
     assert abs(rf["frac"] - rf["achieved"] / rf["peak"]) < 1e-3
-    assert rf["compute"]["pipe"] == "fp64" and rf["compute"]["frac"] > 0
     e2e = d["e2e"]
     assert e2e["h2d_bytes_per_step"] == 16 * 2 ** 20 and e2e["d2h_bytes_per_step"] == 16 * 2 ** 20
     assert d["gpu_launches"] > 0 and d["specialised"]["passes"] == d["specialised"]["of"]
     assert {"sm_mhz", "sm_max_mhz", "reasons"} <= set(d["clocks"])
+    # the same workload description as the reference arm, and the error of
+    # the result against the oracle
+    ref = run_bench(["--impl", "reference", "--steps", "1", "--warmup", "1"], 20)
+    assert d["config"] == ref["config"]
+    assert d["max_abs_err_vs_oracle"] <= 1e-12
+    rows = d["rows"]
+    assert rows["C2_30q"][d["engine"]["precision"]]["err"] <= 1e-12
+    c1 = rows["C1_20q_4096shots"]
+    assert c1["sample_mismatches"] == 0 and c1["err"] <= 1e-12
