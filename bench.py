@@ -742,7 +742,7 @@ def measure_c1(steps=20, shots=4096, cpu=True, peak=FALLBACK_HBM):
             for _ in range(reps):
                 idx = st.sample(u)
             row["sample_ms"] = round((time.perf_counter() - t0) / reps * 1e3, 3)
-            row["exact_scan_shots"] = st.exact_sampled_shots()
+            row["sequential_blocks"] = st.sequential_blocks()
             out["indices"] = idx
         states[prec] = st.download()
         st.close()
@@ -1007,7 +1007,7 @@ def summary_rows(line):
     if c1:
         cb = c1.get("cpu_baseline") or {}
         rows["C1_20q_4096shots"] = {"gates_ms": c1["c128_ds"]["gates_ms"], "sample_ms": c1["c128_ds"]["sample_ms"],
-                                    "exact_scan_shots": c1["c128_ds"]["exact_scan_shots"],
+                                    "sequential_blocks": c1["c128_ds"]["sequential_blocks"],
                                     "err": c1["c128_ds"].get("max_abs_err_vs_oracle"),
                                     "sample_mismatches": c1.get("sample_mismatches_vs_oracle"),
                                     "cpu_gates_s": cb.get("gates_s"), "cpu_scan_s": cb.get("scan_s")}

@@ -198,9 +198,11 @@ int qfvm_sv_expect(qfvm_sv* sv, const uint64_t* x_masks, const uint64_t* z_masks
                    int64_t n_terms, double* out);
 int qfvm_sv_sample(qfvm_sv* sv, const double* uniforms, int64_t shots, uint64_t* out_indices);
 int qfvm_sv_norm2(qfvm_sv* sv, double* out);                           /* FP64 sum |a|^2 */
-/* Shots of the last qfvm_sv_sample on this state that the certified parallel
- * scan could not decide and the exact sequential scan resolved. */
-int qfvm_sv_sample_stats(qfvm_sv* sv, int64_t* exact_shots);
+/* Blocks of 4096 amplitudes that the last qfvm_sv_sample on this state summed
+ * element by element (the exact running sum crossed a binade or met a
+ * rounding tie there); every other block advanced the sum by one integer
+ * addition.  Sampling is exact either way. */
+int qfvm_sv_sample_stats(qfvm_sv* sv, int64_t* sequential_blocks);
 /* Raw device pointer and byte size of the state (for host-side interop). */
 int qfvm_sv_device_ptr(qfvm_sv* sv, void** dev_ptr, uint64_t* nbytes);
 /* Stream the engine issues this state's work on (cudaStream_t as void*). */

@@ -21,7 +21,7 @@ LIB = os.path.join(LIBDIR, "libqfvm_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["kernels.cu", "pass_c128.cu", "pass_c64.cu", "pass_ds.cu", "adjoint.cu", "batch.cu", "shots.cu",
-              "noise.cu", "capi.cu", "batch_capi.cu", "shots_capi.cu", "noise_capi.cu", "noalloc.cu", "jit.cu"]
+              "noise.cu", "sample.cu", "capi.cu", "batch_capi.cu", "shots_capi.cu", "noise_capi.cu", "noalloc.cu", "jit.cu"]
 CPP_SOURCES = ["plan.cpp", "jit_ptx.cpp"]
 
 

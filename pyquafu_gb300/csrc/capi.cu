@@ -357,41 +357,49 @@ int sv_sample(qfvm_sv* sv, const double* uni, int64_t shots, uint64_t* out) {
     if (shots < 0) return fail(QFVM_ERR_INVALID, "negative shot count");
     if (shots == 0) return QFVM_OK;
     if (!uni || !out) return fail(QFVM_ERR_INVALID, "null sample buffer");
+    // the approximate total (parallel FP64 block sums) fixes the candidate binades
     const uint64_t bs = std::min<uint64_t>(4096, sv->N);
-    const uint64_t nb = sv->N / bs;
-    QSV_TRY(sv->sample_blk.ensure(align256(nb * 8) + align256((nb + 1) * 8)));
-    double* dbsum = sv->sample_blk.as<double>();
-    double* dpre = reinterpret_cast<double*>(reinterpret_cast<char*>(sv->sample_blk.p) + align256(nb * 8));
-    const size_t s = static_cast<size_t>(shots);
-    QSV_TRY(sv->sample_shots.ensure(align256(s * 8) * 3 + align256(s)));
+    const uint64_t nbs = sv->N / bs;
+    const uint64_t nb = (sv->N + SAMPLE_BS - 1) / SAMPLE_BS;
+    const size_t b_bsum = align256(nbs * 8), b_pre = align256((nbs + 1) * 8);
+    const size_t b_cnt = align256(static_cast<size_t>(SAMPLE_BINADES) * nb * 8);
+    const size_t b_ties = align256(static_cast<size_t>(SAMPLE_BINADES) * nb);
+    const size_t b_start = align256((nb + 1) * 8);
+    QSV_TRY(sv->sample_blk.ensure(b_bsum + b_pre + b_cnt + b_ties + b_start + 256));
+    char* blk = static_cast<char*>(sv->sample_blk.p);
+    double* dbsum = reinterpret_cast<double*>(blk);
+    double* dpre = reinterpret_cast<double*>(blk + b_bsum);
+    uint64_t* dcnt = reinterpret_cast<uint64_t*>(blk + b_bsum + b_pre);
+    uint8_t* dties = reinterpret_cast<uint8_t*>(blk + b_bsum + b_pre + b_cnt);
+    double* dstart = reinterpret_cast<double*>(blk + b_bsum + b_pre + b_cnt + b_ties);
+    int64_t* dseq = reinterpret_cast<int64_t*>(blk + b_bsum + b_pre + b_cnt + b_ties + b_start);
+    const size_t sz = static_cast<size_t>(shots);
+    QSV_TRY(sv->sample_shots.ensure(align256(sz * 8) * 2));
     char* sb = static_cast<char*>(sv->sample_shots.p);
     double* duni = reinterpret_cast<double*>(sb);
-    uint64_t* didx = reinterpret_cast<uint64_t*>(sb + align256(s * 8));
-    int64_t* dord = reinterpret_cast<int64_t*>(sb + 2 * align256(s * 8));
-    uint8_t* dunsure = reinterpret_cast<uint8_t*>(sb + 3 * align256(s * 8));
-    QSV_CUDA(cudaMemcpyAsync(duni, uni, s * 8, cudaMemcpyHostToDevice, sv->stream), "uniform upload");
-    QSV_CUDA(launch_sample(sv->precision, sv->d, sv->N, bs, dbsum, dpre, duni, shots, didx, dunsure, sv->stream),
-             "sampling");
-    g_launches.fetch_add(3, std::memory_order_relaxed);
-    std::vector<uint8_t> unsure(s);
-    QSV_CUDA(cudaMemcpyAsync(out, didx, s * 8, cudaMemcpyDeviceToHost, sv->stream), "sample download");
-    QSV_CUDA(cudaMemcpyAsync(unsure.data(), dunsure, s, cudaMemcpyDeviceToHost, sv->stream), "sample download");
+    uint64_t* didx = reinterpret_cast<uint64_t*>(sb + align256(sz * 8));
+    QSV_CUDA(cudaMemcpyAsync(duni, uni, sz * 8, cudaMemcpyHostToDevice, sv->stream), "uniform upload");
+    QSV_CUDA(launch_block_prefix(sv->precision, sv->d, sv->N, bs, dbsum, dpre, sv->stream), "block sums");
+    double total = 0.0;
+    QSV_CUDA(cudaMemcpyAsync(&total, dpre + nbs, 8, cudaMemcpyDeviceToHost, sv->stream), "total download");
     QSV_CUDA(cudaStreamSynchronize(sv->stream), "sampling sync");
-    std::vector<int64_t> ord;
-    for (size_t i = 0; i < s; ++i)
-        if (unsure[i]) ord.push_back(static_cast<int64_t>(i));
-    sv->last_exact = static_cast<int64_t>(ord.size());
-    if (!ord.empty()) {
-        std::stable_sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return uni[a] < uni[b]; });
-        QSV_CUDA(cudaMemcpyAsync(dord, ord.data(), ord.size() * 8, cudaMemcpyHostToDevice, sv->stream),
-                 "order upload");
-        QSV_CUDA(launch_sample_exact(sv->precision, sv->d, sv->N, duni, dord, static_cast<int64_t>(ord.size()), didx,
-                                     sv->stream),
-                 "exact sampling");
-        g_launches.fetch_add(1, std::memory_order_relaxed);
-        QSV_CUDA(cudaMemcpyAsync(out, didx, s * 8, cudaMemcpyDeviceToHost, sv->stream), "sample download");
-        QSV_CUDA(cudaStreamSynchronize(sv->stream), "sampling sync");
+    // binade of a value a little above the total (so a sequential total just
+    // past a power of two is still covered)
+    int e_top = 0;
+    const double tb = total * (1.0 + 1.0 / (1 << 20));
+    if (tb > 0.0 && std::isfinite(tb)) {
+        std::frexp(tb, &e_top);  // tb = f * 2^e_top, f in [0.5, 1)
+        e_top -= 1;
     }
+    QSV_CUDA(launch_sample_binade(sv->precision, sv->d, sv->N, e_top, dcnt, dties, dstart, dseq, duni, shots, didx,
+                                  sv->stream),
+             "exact sampling");
+    g_launches.fetch_add(5, std::memory_order_relaxed);
+    int64_t seq = 0;
+    QSV_CUDA(cudaMemcpyAsync(out, didx, sz * 8, cudaMemcpyDeviceToHost, sv->stream), "sample download");
+    QSV_CUDA(cudaMemcpyAsync(&seq, dseq, 8, cudaMemcpyDeviceToHost, sv->stream), "sample download");
+    QSV_CUDA(cudaStreamSynchronize(sv->stream), "sampling sync");
+    sv->last_seq_blocks = seq;
     return QFVM_OK;
 }
 
@@ -538,9 +546,9 @@ int qfvm_sv_sample(qfvm_sv* sv, const double* uniforms, int64_t shots, uint64_t*
     if (!sv) return fail(QFVM_ERR_INVALID, "null state");
     return sv_sample(sv, uniforms, shots, out_indices);
 }
-int qfvm_sv_sample_stats(qfvm_sv* sv, int64_t* exact_shots) {
-    if (!sv || !exact_shots) return fail(QFVM_ERR_INVALID, "null argument");
-    *exact_shots = sv->last_exact;
+int qfvm_sv_sample_stats(qfvm_sv* sv, int64_t* sequential_blocks) {
+    if (!sv || !sequential_blocks) return fail(QFVM_ERR_INVALID, "null argument");
+    *sequential_blocks = sv->last_seq_blocks;
     return QFVM_OK;
 }
 int qfvm_sv_norm2(qfvm_sv* sv, double* out) {

@@ -81,7 +81,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255);
 struct qfvm_sv {
     int n = 0, precision = QFVM_C128;  // storage: QFVM_C128 or QFVM_C64
     int arith = QFVM_C128;             // arithmetic of qfvm_sv_apply: QFVM_C128, QFVM_C128_DS or QFVM_C64
-    int64_t last_exact = 0;            // shots the last qfvm_sv_sample resolved by the exact sequential scan
+    int64_t last_seq_blocks = 0;       // blocks the last qfvm_sv_sample summed element by element
     uint64_t N = 0;
     void* d = nullptr;
     cudaStream_t stream = nullptr;

@@ -240,96 +240,6 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(const double* __restrict__
     if (threadIdx.x == 0) pre[nb] = carry_s;
 }
 
-// One warp per shot: find the block whose prefix range holds r, scan it with
-// per-lane sequential sums, and certify the answer against the error bound
-// of both summation orders; uncertain shots are resolved by k_sample_exact.
-template <class P>
-__global__ void __launch_bounds__(256) k_sample_locate(const typename P::G* __restrict__ state, uint64_t N,
-                                                       uint64_t bs, uint64_t nb, const double* __restrict__ pre,
-                                                       const double* __restrict__ uni, int64_t shots,
-                                                       uint64_t* __restrict__ out, uint8_t* __restrict__ unsure) {
-    const int lane = threadIdx.x & 31;
-    const int64_t s = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (s >= shots) return;
-    const double r = uni[s];
-    const double total = pre[nb];
-    const double u = 1.1102230246251565e-16;  // 2^-53
-    const double scale = (total > 1.0 ? total : 1.0) * 1.01 * u;
-    const double gerr = (2.0 * static_cast<double>(bs) + static_cast<double>(nb) + 8.0) * scale;
-    if (r >= total) {
-        // the reference loop ends with sample = N
-        const double d = static_cast<double>(N + 1) * scale + gerr;
-        if (lane == 0) {
-            out[s] = N;
-            unsure[s] = (r < total + d) ? 1 : 0;
-        }
-        return;
-    }
-    // largest b with pre[b] <= r
-    uint64_t lo = 0, hi = nb - 1;
-    while (lo < hi) {
-        const uint64_t mid = (lo + hi + 1) >> 1;
-        if (pre[mid] <= r) lo = mid;
-        else hi = mid - 1;
-    }
-    const uint64_t b = lo;
-    const uint64_t per = (bs + 31) / 32;
-    const uint64_t i0 = b * bs + lane * per;
-    const uint64_t i1 = (i0 + per < (b + 1) * bs) ? i0 + per : (b + 1) * bs;
-    double ls = 0.0;
-    for (uint64_t i = i0; i < i1; ++i) ls += prob_of<P>(state[i]);
-    double incl = ls;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const double y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-    }
-    const double start = pre[b] + (incl - ls);
-    // find the first index k in this lane's range with r < running sum
-    double run = start, prev = start;
-    uint64_t found = ~0ULL;
-    for (uint64_t i = i0; i < i1; ++i) {
-        prev = run;
-        run += prob_of<P>(state[i]);
-        if (r < run) {
-            found = i;
-            break;
-        }
-    }
-    const unsigned ball = __ballot_sync(0xffffffffu, found != ~0ULL);
-    if (ball == 0) {
-        if (lane == 0) {
-            out[s] = N;
-            unsure[s] = 1;
-        }
-        return;
-    }
-    const int first = __ffs(ball) - 1;
-    if (lane == first) {
-        const double d = static_cast<double>(found + 2) * scale * (run > 1.0 ? run : 1.0) + gerr;
-        out[s] = found;
-        unsure[s] = (r < run - d && r >= prev + d) ? 0 : 1;
-    }
-}
-
-// Exact sequential scan (one thread) for the shots flagged as uncertain;
-// `ord` lists them by increasing uniform.  The loop is bounded by N.
-template <class P>
-__global__ void k_sample_exact(const typename P::G* __restrict__ state, uint64_t N, const double* __restrict__ uni,
-                               const int64_t* __restrict__ ord, int64_t m, uint64_t* __restrict__ out) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    double p = 0.0;
-    int64_t k = 0;
-    for (uint64_t i = 0; i < N && k < m; ++i) {
-        p = __dadd_rn(p, prob_of<P>(state[i]));
-        while (k < m && uni[ord[k]] < p) {
-            out[ord[k]] = i;
-            ++k;
-        }
-    }
-    for (; k < m; ++k) out[ord[k]] = N;
-}
-
 // ---------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------
@@ -485,8 +395,8 @@ cudaError_t launch_reduce_partials(const double* dpartial, int nblocks, int nter
     return cudaGetLastError();
 }
 
-cudaError_t launch_sample(int precision, const void* state, uint64_t N, uint64_t bs, double* dbsum, double* dpre,
-                          const double* duni, int64_t shots, uint64_t* dout, uint8_t* dunsure, cudaStream_t st) {
+cudaError_t launch_block_prefix(int precision, const void* state, uint64_t N, uint64_t bs, double* dbsum,
+                                double* dpre, cudaStream_t st) {
     const uint64_t nb = N / bs;
     if (precision == QFVM_C64)
         k_block_sums<P32><<<static_cast<unsigned>(nb), 256, 0, st>>>(static_cast<const float2*>(state), bs, dbsum);
@@ -495,27 +405,8 @@ cudaError_t launch_sample(int precision, const void* state, uint64_t N, uint64_t
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_scan_blocks<<<1, 1024, 0, st>>>(dbsum, nb, dpre);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    if (shots > 0) {
-        const unsigned blocks = static_cast<unsigned>((shots * 32 + 255) / 256);
-        if (precision == QFVM_C64)
-            k_sample_locate<P32><<<blocks, 256, 0, st>>>(static_cast<const float2*>(state), N, bs, nb, dpre, duni,
-                                                         shots, dout, dunsure);
-        else
-            k_sample_locate<P64><<<blocks, 256, 0, st>>>(static_cast<const double2*>(state), N, bs, nb, dpre, duni,
-                                                         shots, dout, dunsure);
-    }
     return cudaGetLastError();
 }
 
-cudaError_t launch_sample_exact(int precision, const void* state, uint64_t N, const double* duni,
-                                const int64_t* dord, int64_t m, uint64_t* dout, cudaStream_t st) {
-    if (precision == QFVM_C64)
-        k_sample_exact<P32><<<1, 32, 0, st>>>(static_cast<const float2*>(state), N, duni, dord, m, dout);
-    else
-        k_sample_exact<P64><<<1, 32, 0, st>>>(static_cast<const double2*>(state), N, duni, dord, m, dout);
-    return cudaGetLastError();
-}
 
 }  // namespace qsv

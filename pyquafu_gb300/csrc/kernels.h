@@ -44,10 +44,19 @@ cudaError_t launch_expect_x(int precision, const void* state, uint64_t N, uint64
                             const uint64_t* dzm, const int32_t* dny, int nterms, double* dpartial, int nblocks,
                             cudaStream_t st);
 cudaError_t launch_reduce_partials(const double* dpartial, int nblocks, int nterms, double* dout, cudaStream_t st);
-cudaError_t launch_sample(int precision, const void* state, uint64_t N, uint64_t bs, double* dbsum, double* dpre,
-                          const double* duni, int64_t shots, uint64_t* dout, uint8_t* dunsure, cudaStream_t st);
-cudaError_t launch_sample_exact(int precision, const void* state, uint64_t N, const double* duni,
-                                const int64_t* dord, int64_t m, uint64_t* dout, cudaStream_t st);
+// Exact parallel sampling (sample.cu): blocks of SAMPLE_BS amplitudes, grid
+// counts for SAMPLE_BINADES binades below 2^e_top.  cnt: SAMPLE_BINADES * nb
+// uint64, ties: SAMPLE_BINADES * nb bytes, start: nb + 1 doubles (the exact
+// running sum at every block start), seq: blocks summed element by element.
+constexpr int SAMPLE_BS = 4096;
+constexpr int SAMPLE_BINADES = 16;
+cudaError_t launch_sample_binade(int precision, const void* state, uint64_t N, int e_top, uint64_t* cnt,
+                                 uint8_t* ties, double* start, int64_t* seq, const double* uni, int64_t shots,
+                                 uint64_t* out, cudaStream_t st);
+// FP64 sums of |a|^2 over blocks of bs amplitudes and their exclusive prefix
+// (dpre[N / bs] = the parallel total)
+cudaError_t launch_block_prefix(int precision, const void* state, uint64_t N, uint64_t bs, double* dbsum,
+                                double* dpre, cudaStream_t st);
 
 }  // namespace qsv
 

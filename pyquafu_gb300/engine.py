@@ -122,9 +122,10 @@ class DeviceState:
         nat.check(self._lib.qfvm_sv_sample(self._h, nat.dptr(u), u.size, nat.u64ptr(out)), "sample")
         return out
 
-    def exact_sampled_shots(self) -> int:
-        """Shots of the last sample() that needed the exact sequential scan
-        (the parallel scan could not certify them)."""
+    def sequential_blocks(self) -> int:
+        """Blocks of 4096 amplitudes the last sample() summed element by
+        element (the rest advanced the exact running sum by one integer
+        addition each)."""
         v = ctypes.c_int64()
         nat.check(self._lib.qfvm_sv_sample_stats(self._h, ctypes.byref(v)), "sample stats")
         return v.value
