@@ -917,10 +917,13 @@ def run_gpu(args):
         adj, adj_data = measure_adjoint(args.adjoint_qubits, peak=peak, cpu=cpu_here)
     batched = None
     if not args.skip_batch:
-        batched = {"uneven_2048": measure_uneven_batch(cpu=cpu_here, tune=not args.no_autotune, peak=peak),
-                   "qnn_training_step": measure_qnn(tune=not args.no_autotune, peak=peak, cpu=cpu_here),
-                   "trajectories": measure_trajectories(cpu=cpu_here),
-                   "noise": measure_noise(cpu=cpu_here)}
+        batched = {}
+        if not args.skip_uneven:
+            batched["uneven_2048"] = measure_uneven_batch(cpu=cpu_here, tune=not args.no_autotune, peak=peak)
+        batched["qnn_training_step"] = measure_qnn(tune=not args.no_autotune, peak=peak, cpu=cpu_here)
+        if not args.skip_trajectories:
+            batched["trajectories"] = measure_trajectories(cpu=cpu_here)
+            batched["noise"] = measure_noise(cpu=cpu_here)
 
     cpu = None
     if cpu_here:
@@ -1040,6 +1043,8 @@ def main():
     ap.add_argument("--precision", default=DEFAULT_PRECISION, choices=["c128", "c128_ds", "c64"])
     ap.add_argument("--variants", default="c128,c64")
     ap.add_argument("--skip-c1", action="store_true")
+    ap.add_argument("--skip-uneven", action="store_true")
+    ap.add_argument("--skip-trajectories", action="store_true")
     ap.add_argument("--skip-oracle-check", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
