@@ -785,12 +785,24 @@ def oracle_check_c2(n, ops, precisions):
     zz_ref = oracle.expect_pauli(ref, "ZZ", [0, 1])
     out = {"oracle_full_circuit_s": round(oracle_s, 1), "oracle_cores": os.cpu_count()}
     buf = np.empty(1 << n, dtype=np.complex128)
+    u = np.random.Generator(np.random.MT19937(0)).random(4096)
     for prec in precisions:
         plan = engine.Plan(n, ops, prec)
         st = engine.DeviceState(n, prec).set_zero()
         plan.run(st)
         torch.cuda.synchronize()
         zz = float(st.expect([("ZZ", [0, 1])])[0])
+        if prec == precisions[0]:
+            # 4096 shots on the final state, exact against the oracle's sequential scan
+            st.sample(u)
+            t0 = time.perf_counter()
+            idx = st.sample(u)
+            sample_ms = (time.perf_counter() - t0) * 1e3
+            t1 = time.perf_counter()
+            ref_idx = oracle.sample_indices(ref, u)
+            out["sampling_4096_shots"] = {"gpu_ms": round(sample_ms, 2), "sequential_blocks": st.sequential_blocks(),
+                                          "oracle_scan_s": round(time.perf_counter() - t1, 2),
+                                          "mismatches_vs_oracle": int(np.sum(idx != ref_idx))}
         st.download(buf)
         st.close()
         plan.close()
@@ -1005,6 +1017,8 @@ def summary_rows(line):
                                         "err": chk.get(line["engine"]["precision"], {}).get("max_abs_err")}}
     for v, r in (line.get("variants") or {}).items():
         c2[v] = {"ms": r["ms_per_step"], "frac": r["tile_pass_frac_hbm"], "err": chk.get(v, {}).get("max_abs_err")}
+    if "sampling_4096_shots" in chk:
+        c2["sampling_4096_shots"] = chk["sampling_4096_shots"]
     rows["C2_30q"] = c2
     c1 = line.get("c1_sampling")
     if c1:
