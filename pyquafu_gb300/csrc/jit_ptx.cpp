@@ -154,7 +154,12 @@ class Gen {
         I(fmt("neg.f32 %s, %s", d.c_str(), a.c_str()));
         return d;
     }
-    // double-single: a + b (TwoSum on the high parts), c * x unnormalised
+    // Double-single values inside a pass are float pairs (h, l) that need not
+    // be renormalised: h + l is the value, and |l| stays below a few units in
+    // the last place of the operands that made it, so every operation's
+    // absolute error stays near 2^-46 of its operands' magnitudes.  Pairs are
+    // renormalised (TwoSum) only where the FP64 conversion needs |l| <= |h|.
+    // a + b: TwoSum of the high parts, low parts and error summed
     std::string ds_add(const std::string& a, const std::string& b) {
         auto [ah, al] = hl(a);
         auto [bh, bl] = hl(b);
@@ -162,8 +167,15 @@ class Gen {
         const std::string v = f32op("sub", sh, ah);
         std::string e = f32op("add", f32op("sub", ah, f32op("sub", sh, v)), f32op("sub", bh, v));
         e = f32op("add", e, f32op("add", al, bl));
-        const std::string h = f32op("add", sh, e);
-        return h + "|" + f32op("sub", e, f32op("sub", h, sh));
+        return sh + "|" + e;
+    }
+    // (h, l) -> the same value with |l| <= ulp(h) / 2 (TwoSum: exact for any pair)
+    std::string ds_norm(const std::string& a) {
+        auto [h, l] = hl(a);
+        const std::string s = f32op("add", h, l);
+        const std::string v = f32op("sub", s, h);
+        const std::string e = f32op("add", f32op("sub", h, f32op("sub", s, v)), f32op("sub", l, v));
+        return s + "|" + e;
     }
     std::string ds_mul_raw(const std::string& c, const std::string& x) {
         auto [ch, cl] = hl(c);
@@ -175,11 +187,7 @@ class Gen {
         return p + "|" + e;
     }
     std::string mul(const std::string& c, const std::string& x) {
-        if (ds_) {
-            auto [ph, pl] = hl(ds_mul_raw(c, x));
-            const std::string h = f32op("add", ph, pl);
-            return h + "|" + f32op("sub", pl, f32op("sub", h, ph));
-        }
+        if (ds_) return ds_mul_raw(c, x);
         std::string d = A();
         I(fmt("mul.rn.%s %s, %s, %s", ft_, d.c_str(), c.c_str(), x.c_str()));
         return d;
@@ -209,8 +217,7 @@ class Gen {
             err = f32op("add", f32op("add", err, e), r);
             s = sn;
         }
-        const std::string h = f32op("add", s, err);
-        return h + "|" + f32op("sub", err, f32op("sub", h, s));
+        return s + "|" + err;
     }
     std::string add(const std::string& x, const std::string& y) {
         if (ds_) return ds_add(x, y);
@@ -335,7 +342,8 @@ class Gen {
         I(fmt("mov.b32 %s, %s", l.c_str(), lz.c_str()));
         return h + "|" + l;
     }
-    std::string ds_to(const std::string& v) {
+    std::string ds_to(const std::string& vin) {
+        const std::string v = ds_norm(vin);
         auto [h, l] = hl(v);
         std::string H = R32(), Lb = R32(), sh = R32(), eh = R32(), el = R32(), mh = R32(), ml = R32(), x = R32(),
                     d = R32(), z = R32(), ex = R32(), hi = R32(), lo = R32(), hw = R32(), hw2 = R32(), lw2 = R32();
