@@ -106,8 +106,6 @@ int upload_plan(qfvm_plan* p) {
     return QFVM_OK;
 }
 
-int make_plan_gops(int n, int precision, const std::vector<GOp>& gops, int T, int R, qfvm_plan** out);
-
 int make_plan(int n, int precision, const qfvm_op* ops, int64_t n_ops, const double* matpool, int64_t matpool_len,
               int T, int R, qfvm_plan** out) {
     if (n < 1 || n > QFVM_MAX_QUBITS) return fail(QFVM_ERR_INVALID, "qubit count out of range");
@@ -125,10 +123,11 @@ int make_plan(int n, int precision, const qfvm_op* ops, int64_t n_ops, const dou
         if (!pass_shape_supported(precision == QFVM_C128_DS ? QFVM_C128_DS : sp, tt, rr))
             return fail(QFVM_ERR_INVALID, "tile shape not compiled in");
     }
-    return make_plan_gops(n, precision, gops, T, R, out);
+    return make_plan_gops(n, precision, gops, T, R, out, true);
 }
 
-int make_plan_gops(int n, int precision, const std::vector<GOp>& gops, int T, int R, qfvm_plan** out) {
+int make_plan_gops(int n, int precision, const std::vector<GOp>& gops, int T, int R, qfvm_plan** out,
+                   bool merge_diagonals) {
     std::string err;
     const int sp = store_precision(precision);
     if (T <= 0 && R <= 0) resolve_shape(precision, 0, n, &T, &R);
@@ -137,6 +136,7 @@ int make_plan_gops(int n, int precision, const std::vector<GOp>& gops, int T, in
         delete p;
         return fail(QFVM_ERR_INVALID, err);
     }
+    if (merge_diagonals) merge_round_diagonals(&p->hp);
     p->hp.arith = (precision == QFVM_C128_DS) ? QFVM_C128_DS : sp;
     int rc = upload_plan(p);
     if (rc != QFVM_OK) {
@@ -635,6 +635,7 @@ int qfvm_plan_host_build(int32_t num_qubits, int32_t precision, const qfvm_op* o
         delete p;
         return fail(QFVM_ERR_INVALID, err);
     }
+    merge_round_diagonals(&p->hp);
     *out = p;
     return QFVM_OK;
 }

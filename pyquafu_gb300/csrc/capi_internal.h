@@ -105,7 +105,9 @@ struct qfvm_plan {
 namespace qsv_capi {
 int make_plan(int n, int precision, const qfvm_op* ops, int64_t n_ops, const double* matpool, int64_t matpool_len,
               int T, int R, qfvm_plan** out);
-int make_plan_gops(int n, int precision, const std::vector<qsv::GOp>& gops, int T, int R, qfvm_plan** out);
+// merge_diagonals: plain simulation plans only (merge_round_diagonals)
+int make_plan_gops(int n, int precision, const std::vector<qsv::GOp>& gops, int T, int R, qfvm_plan** out,
+                   bool merge_diagonals = false);
 void free_plan(qfvm_plan* p);
 // Every pass of a plan over `items` states back to back (shared coefficients;
 // active = optional per-item write-back mask).

@@ -285,6 +285,23 @@ __device__ __forceinline__ void reg_apply(RegState<P, R, NS>& a, const KOp& op, 
     if ((op.flags & F_TCTRL) && (gthr & op.cthr) != op.cthr) return;  // a control outside the registers is 0
     switch (op.kind) {
         case K_DIAG: reg_diag<P, R, NS>(a, op, gthr, coef, ph); break;
+        case K_DIAGR:
+#pragma unroll
+            for (int j = 0; j < (1 << R); ++j) {
+                const int code = diagr_code(op.tk, j);
+                if (code == DIAGR_ONE) continue;
+                if (code != DIAGR_GENERAL) {
+                    const int sp = code == DIAGR_NEG1 ? SP_NEG1 : (code == DIAGR_I ? SP_I : SP_NEGI);
+#pragma unroll
+                    for (int s = 0; s < NS; ++s) amp_special<P>(a[s][j], sp);
+                    continue;
+                }
+                const typename P::C dr = P::coef(coef, op.coef + 2 * j), di = P::coef(coef, op.coef + 2 * j + 1);
+                const typename P::C ndi = P::cneg(di);
+#pragma unroll
+                for (int s = 0; s < NS; ++s) amp_phase<P>(a[s][j], dr, di, ndi);
+            }
+            break;
         case K_SWAP:
             if (op.creg) reg_swap<P, R, NS, true>(a, op);
             else reg_swap<P, R, NS, false>(a, op);

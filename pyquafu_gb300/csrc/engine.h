@@ -25,8 +25,22 @@ enum GKind : uint8_t {
     K_DENSE2 = 8, // 4x4 complex on (t0 = bit 0, t1 = bit 1), 32 coefs
     K_DENSEK = 9, // 2^k x 2^k complex on tk[0..k-1] (bit j = tk[j]), 2*4^k coefs
     K_PROBE = 10, // adjoint sweep: accumulate Im<lam| Q |psi> (reads both states, changes neither)
-    K_HAD = 11    // sqrt(2) H = [[1, 1], [1, -1]] on t0, no coefficients (see unnormalize_hadamards)
+    K_HAD = 11,   // sqrt(2) H = [[1, 1], [1, -1]] on t0, no coefficients (see unnormalize_hadamards)
+    K_DIAGR = 12  // register round only: amp j of the thread's 2^k registers *= d[j] (2 * 2^k coefs);
+                  // tk[0..5] hold a 3-bit code per entry (DIAGR_* below), k <= 4
 };
+enum : uint8_t { DIAGR_GENERAL = 0, DIAGR_ONE = 1, DIAGR_NEG1 = 2, DIAGR_I = 3, DIAGR_NEGI = 4 };
+#if defined(__CUDACC__)
+#define QSV_HD __host__ __device__
+#else
+#define QSV_HD
+#endif
+// code of register entry j of a K_DIAGR op
+QSV_HD inline int diagr_code(const uint8_t* tk, int j) {
+    uint64_t c = 0;
+    for (int b = 0; b < 6; ++b) c |= static_cast<uint64_t>(tk[b]) << (8 * b);
+    return static_cast<int>((c >> (3 * j)) & 7);
+}
 
 // DIAG flags
 enum : uint8_t {
@@ -185,6 +199,14 @@ void unnormalize_hadamards(std::vector<GOp>* gops);
 // the qubit only as a control; X-type gates pass X / RX on the same target):
 // d.d' -> one diagonal, rx(a) rx(b) -> rx(a + b), X X -> nothing.
 void fuse_single_qubit(std::vector<GOp>* gops);
+// Plain simulation plans: inside every register round of at most 4 register
+// qubits, diagonal ops whose parity and controls are all register bits are
+// multiplied into one per-register-entry phase table (K_DIAGR), applied
+// where the first op that acts non-diagonally on one of the table's bits
+// comes (or at the round's end).  The merged ops commute with everything
+// between their places and that point.  Entries that come out exactly 1,
+// -1, i or -i are coded so the kernels apply them without arithmetic.
+void merge_round_diagonals(HostPlan* plan);
 // Coefficients of a bindable gate kind at angle th (2 or 4 doubles).
 int bind_coef(int kind, double th, double* c);
 // Gate-equivalent bytes of one gop: 2 * bytes per amplitude * amplitudes it

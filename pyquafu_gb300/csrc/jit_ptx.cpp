@@ -83,6 +83,9 @@ class Gen {
                 switch (o.kind) {
                     case K_DENSE: case K_REAL: case K_RX: case K_DIAG: case K_X: case K_Y: case K_SWAP: case K_HAD:
                         break;
+                    case K_DIAGR:
+                        if (o.k != R_) return no(why, "merged diagonal of another register count");
+                        break;
                     case K_PROBE:
                         if (NS_ != 2) return no(why, "probe in a one-state pass");
                         break;
@@ -893,6 +896,24 @@ class Gen {
         guard(old, ctl);
     }
 
+    // merged register-round diagonal: entry j multiplies register j (exact
+    // entries 1, -1, i, -i without arithmetic)
+    void op_diagr(const KOp& o) {
+        std::vector<std::string> c;
+        for (int j = 0; j < NA_; ++j) {
+            const int code = diagr_code(o.tk, j);
+            if (code == DIAGR_ONE) continue;
+            if (code != DIAGR_GENERAL) {
+                const int sp = code == DIAGR_NEG1 ? SP_NEG1 : (code == DIAGR_I ? SP_I : SP_NEGI);
+                for (int s = 0; s < NS_; ++s) A_[s][j] = special(A_[s][j], sp);
+                continue;
+            }
+            if (c.empty()) c = coefs(o.coef, 2 * NA_);
+            const std::string dr = c[2 * j], di = c[2 * j + 1], ndi = neg(di);
+            for (int s = 0; s < NS_; ++s) A_[s][j] = phase(A_[s][j], dr, di, ndi);
+        }
+    }
+
     // round phase *= f (only where ctl holds, when given)
     void phase_mul(const Cx& f, const std::string& ctl) {
         Cx n;
@@ -1294,10 +1315,12 @@ class Gen {
             if (o.kind == K_Y || o.kind == K_HAD) need |= 1u << o.t0;
             if (o.kind == K_SWAP && o.creg) need |= (1u << o.t0) | (1u << o.t1);
             if (o.kind == K_PROBE) need |= o.xreg | o.preg;
+            if (o.kind == K_DIAGR) need |= (1u << R_) - 1;  // its entries are per register index
             for (int t = 0; t < R_; ++t)
                 if ((need >> t) & 1) materialize(t);
             if (o.kind == K_PROBE) op_probe(o, gthr, ctl);
             else if (o.kind == K_DIAG) op_diag(o, gthr, ctl);
+            else if (o.kind == K_DIAGR) op_diagr(o);
             else op_gate(o, ctl);
         }
         flush_probes();
@@ -1439,6 +1462,8 @@ bool jit_pass_key(const HostPlan& hp, int pi, const JitShape& sh, std::string* k
             put(&k, o.pthr);
             put(&k, o.coef);
             put(&k, o.xreg);
+            put(&k, o.k);
+            k.append(reinterpret_cast<const char*>(o.tk), sizeof o.tk);
         }
     }
     return true;

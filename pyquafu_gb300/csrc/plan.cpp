@@ -1012,4 +1012,118 @@ void unnormalize_hadamards(std::vector<GOp>* gops) {
     }
 }
 
+namespace {
+
+// bits of the register index an op of a round acts on non-diagonally
+uint32_t nondiag_reg_bits(const KOp& o) {
+    switch (o.kind) {
+        case K_X: case K_Y: case K_REAL: case K_RX: case K_DENSE: case K_HAD:
+            return 1u << o.t0;
+        case K_SWAP:
+            return (1u << o.t0) | (1u << o.t1);
+        case K_DIAG: case K_DIAGR:
+            return 0;
+        default:
+            return ~0u;  // anything else: flush
+    }
+}
+
+bool mergeable_diag(const KOp& o) {
+    return o.kind == K_DIAG && !(o.flags & (F_TCTRL | F_TPAR | F_UNIFORM));
+}
+
+int entry_code(cd z) {
+    if (z == cd(1.0, 0.0)) return DIAGR_ONE;
+    if (z == cd(-1.0, 0.0)) return DIAGR_NEG1;
+    if (z == cd(0.0, 1.0)) return DIAGR_I;
+    if (z == cd(0.0, -1.0)) return DIAGR_NEGI;
+    return DIAGR_GENERAL;
+}
+
+}  // namespace
+
+void merge_round_diagonals(HostPlan* plan) {
+    if (plan->R < 1 || plan->R > 4 || !plan->binds.empty() || !plan->probe_slot.empty()) return;
+    const int R = plan->R;
+    const int NA = 1 << R;
+    std::vector<KOp> out;
+    out.reserve(plan->ops.size());
+    // whole-state passes keep their ops (re-indexed); rounds are rewritten
+    std::vector<int32_t> step_begin(plan->steps.size()), step_count(plan->steps.size());
+    std::vector<int32_t> pass_begin(plan->passes.size());
+    std::vector<bool> step_done(plan->steps.size(), false);
+    for (size_t pi = 0; pi < plan->passes.size(); ++pi) {
+        PassDesc& pd = plan->passes[pi];
+        if (pd.type != PASS_TILE) {
+            pass_begin[pi] = static_cast<int32_t>(out.size());
+            out.insert(out.end(), plan->ops.begin() + pd.op_begin, plan->ops.begin() + pd.op_begin + pd.op_count);
+            continue;
+        }
+        for (int si = pd.step_begin; si < pd.step_begin + pd.step_count; ++si) {
+            const StepDesc& sd = plan->steps[si];
+            step_begin[si] = static_cast<int32_t>(out.size());
+            step_done[si] = true;
+            if (sd.type != STEP_ROUND) {
+                out.insert(out.end(), plan->ops.begin() + sd.op_begin, plan->ops.begin() + sd.op_begin + sd.op_count);
+                step_count[si] = static_cast<int32_t>(out.size()) - step_begin[si];
+                continue;
+            }
+            std::vector<cd> table(NA, cd(1.0, 0.0));
+            std::vector<KOp> merged;
+            uint32_t support = 0;
+            auto flush = [&]() {
+                if (merged.empty()) return;
+                if (merged.size() == 1) {
+                    out.push_back(merged[0]);
+                } else {
+                    while (plan->coef.size() % 4) plan->coef.push_back(0.0);
+                    KOp k;
+                    std::memset(&k, 0, sizeof(k));
+                    k.kind = K_DIAGR;
+                    k.k = static_cast<uint8_t>(R);
+                    k.coef = static_cast<uint32_t>(plan->coef.size());
+                    uint64_t codes = 0;
+                    for (int j = 0; j < NA; ++j) {
+                        plan->coef.push_back(table[j].real());
+                        plan->coef.push_back(table[j].imag());
+                        codes |= static_cast<uint64_t>(entry_code(table[j])) << (3 * j);
+                    }
+                    for (int b = 0; b < 6; ++b) k.tk[b] = static_cast<uint8_t>(codes >> (8 * b));
+                    out.push_back(k);
+                }
+                merged.clear();
+                std::fill(table.begin(), table.end(), cd(1.0, 0.0));
+                support = 0;
+            };
+            for (int oi = sd.op_begin; oi < sd.op_begin + sd.op_count; ++oi) {
+                const KOp& o = plan->ops[oi];
+                if (mergeable_diag(o)) {
+                    const double* c = plan->coef.data() + o.coef;
+                    const cd d0(c[0], c[1]), d1(c[2], c[3]);
+                    for (int j = 0; j < NA; ++j) {
+                        if ((static_cast<uint32_t>(j) & o.creg) != o.creg) continue;
+                        table[j] *= (__builtin_popcount(static_cast<uint32_t>(j) & o.preg) & 1) ? d1 : d0;
+                    }
+                    support |= o.creg | o.preg;
+                    merged.push_back(o);
+                    continue;
+                }
+                if (nondiag_reg_bits(o) & support) flush();
+                out.push_back(o);
+            }
+            flush();
+            step_count[si] = static_cast<int32_t>(out.size()) - step_begin[si];
+        }
+    }
+    for (size_t si = 0; si < plan->steps.size(); ++si) {
+        if (!step_done[si]) continue;
+        plan->steps[si].op_begin = step_begin[si];
+        plan->steps[si].op_count = step_count[si];
+    }
+    for (size_t pi = 0; pi < plan->passes.size(); ++pi)
+        if (plan->passes[pi].type != PASS_TILE) plan->passes[pi].op_begin = pass_begin[pi];
+    plan->ops.swap(out);
+    while (plan->coef.size() % 4) plan->coef.push_back(0.0);
+}
+
 }  // namespace qsv

@@ -129,8 +129,10 @@ def _assemble(para_grads, gate_grads):
     return out
 
 
-def grad_adjoint(qc, hamiltonian, psi_in=np.array([], dtype=complex), precision="c128"):
-    """Drop-in for quafu.algorithms.gradients.grad_adjoint on the GPU."""
+def grad_adjoint(qc, hamiltonian, psi_in=np.array([], dtype=complex), precision="c128_ds"):
+    """Drop-in for quafu.algorithms.gradients.grad_adjoint on the GPU
+    (complex128 with float-pair arithmetic by default, as the engine's other
+    complex128 work; "c128" for IEEE FP64)."""
     para_grads = qc._calc_parameter_grads()
     n, gates, ngates = _slotted_ops(qc)
     psi = None if psi_in is None or np.size(psi_in) == 0 else np.asarray(psi_in, dtype=np.complex128)
@@ -138,8 +140,9 @@ def grad_adjoint(qc, hamiltonian, psi_in=np.array([], dtype=complex), precision=
     return _assemble(para_grads, gate_grads)
 
 
-def grad_para_shift(qc, hamiltonian, precision="c128"):
-    """Drop-in for quafu.algorithms.gradients.grad_para_shift on the GPU."""
+def grad_para_shift(qc, hamiltonian, precision="c128_ds"):
+    """Drop-in for quafu.algorithms.gradients.grad_para_shift on the GPU
+    (float-pair complex128 by default)."""
     para_grads = qc._calc_parameter_grads()
     n, gates, _ = _slotted_ops(qc)
     return _assemble(para_grads, param_shift(n, gates, _circuit_terms(hamiltonian), precision))

@@ -44,7 +44,7 @@ KOP_DT = np.dtype([("kind", "u1"), ("flags", "u1"), ("special", "u1"), ("k", "u1
                   align=True)
 assert PASS_DT.itemsize == 56 and STEP_DT.itemsize == 100 and KOP_DT.itemsize == 48
 
-K_DENSE, K_REAL, K_RX, K_DIAG, K_X, K_Y, K_SWAP, K_DENSE2, K_DENSEK, K_PROBE, K_HAD = range(1, 12)
+K_DENSE, K_REAL, K_RX, K_DIAG, K_X, K_Y, K_SWAP, K_DENSE2, K_DENSEK, K_PROBE, K_HAD, K_DIAGR = range(1, 13)
 PASS_TILE, PASS_SMALL, PASS_GLOBALOP = 0, 1, 2
 STEP_ROUND, STEP_SMEM = 0, 1
 
@@ -197,6 +197,25 @@ def kop_targets(o):
     return [int(x) for x in o["tk"][: o["k"]]], int(o["pthr"])
 
 
+def apply_diagr(psi, g_of_reg, coef, off, tk):
+    """A merged register-round diagonal: amplitude i *= d[j], j the register
+    index of i (bit b of j = bit g_of_reg[b] of i); entries coded exactly
+    1, -1, i, -i (3-bit codes in tk) must equal their coefficients."""
+    idx = np.arange(psi.size, dtype=np.int64)
+    j = np.zeros(psi.size, dtype=np.int64)
+    for b, q in enumerate(g_of_reg):
+        j |= ((idx >> q) & 1) << b
+    n = 1 << len(g_of_reg)
+    d = coef[off:off + 2 * n:2] + 1j * coef[off + 1:off + 2 * n:2]
+    codes = int.from_bytes(tk[:6], "little")
+    want = {1: 1.0, 2: -1.0, 3: 1j, 4: -1j}
+    for e in range(n):
+        c = (codes >> (3 * e)) & 7
+        if c:
+            assert d[e] == want[c], (e, c, d[e])
+    psi *= d[j]
+
+
 def interpret2(plan, psi, lam):
     """Execute an adjoint sweep plan on (psi, lam); returns the probe values."""
     states = [psi.copy(), lam.copy()]
@@ -301,6 +320,9 @@ def interpret(plan, psi):
                 for b in _bits(o["preg"]):
                     pm |= 1 << g_of_reg[b]
                 kind = int(o["kind"])
+                if kind == K_DIAGR:
+                    apply_diagr(psi, g_of_reg, coef, int(o["coef"]), bytes(o["tk"]))
+                    continue
                 if kind in (K_SWAP,):
                     t = (g_of_reg[o["t0"]], g_of_reg[o["t1"]])
                 elif kind == K_DIAG:
