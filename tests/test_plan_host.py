@@ -132,6 +132,31 @@ def test_wide_dense_gate_in_adjoint_sweep():
     np.testing.assert_allclose(grads, ref, atol=1e-12)
 
 
+@pytest.mark.parametrize("R", [3, 4])
+def test_round_diagonals_merge(R):
+    """Plain plans merge the register-only diagonals of a round into one
+    phase table (K_DIAGR, exact quarter turns coded), applied before the
+    first op that acts non-diagonally on its bits; the interpreter checks the
+    codes against the coefficients and the state against the oracle."""
+    n = 14
+    rng = np.random.default_rng(R)
+    ops = []
+    for layer in range(6):
+        for q in range(n):
+            g = ["s", "t", "z", "rz", "h", "rx", "sdg", "tdg"][int(rng.integers(8))]
+            ops.append(workloads.named(g, (q,), (float(rng.uniform(0, 6.3)),) if g in ("rz", "rx") else ()))
+        for _ in range(3):
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            ops.append(workloads.named(["cz", "rzz", "cp"][layer % 3], (a, b),
+                                       (0.7,) if layer % 3 else (), ncontrols=0 if layer % 3 == 1 else 1))
+    plan = helpers.host_plan(n, ops, 0, 12, R)
+    assert int(np.sum(plan["ops"]["kind"] == helpers.K_DIAGR)) > 0
+    got = helpers.interpret(plan, oracle.zero_state(n))
+    assert np.abs(got - oracle.simulate(n, ops)).max() < 1e-13
+    # batched and adjoint plans keep every gate
+    assert int(np.sum(helpers.host_plan(n, ops, 0, adjoint=True)["ops"]["kind"] == helpers.K_DIAGR)) == 0
+
+
 def test_invalid_ops_rejected():
     from pyquafu_gb300 import _native as nat
 
