@@ -10,6 +10,8 @@ records, for seeded circuits built with pyquafu's QuantumCircuit API:
   * single-gate applications (qfvm.applyop_statevec) on random states
   * counts of deterministic circuits (bitstring / cbit conventions)
   * gradients from quafu.algorithms.gradients (adjoint and parameter shift)
+  * the calls quafu's own front end (quafu.simulate) makes into qfvm, with
+    their arguments and the reference module's return values
 
 Usage (build container only; the reference tree is not on GPU machines):
     ./oracle/build_ref.sh && python tests/golden/make_golden.py
@@ -111,14 +113,64 @@ PAULI_SETS = [
 ]
 
 
+class RecordingQfvm:
+    """Stands in for quafu.simulators.qfvm while quafu's own front end runs:
+    forwards every call to the reference module and, while `calls` is a
+    list, records what the front end passed and what it got back."""
+
+    def __init__(self, ref):
+        self.ref = ref
+        self.calls = None
+        self.states = {}
+
+    def _circuit(self, qc):
+        circ = ir.read_circuit(qc)
+        return {"n": qc.num, "cbits_num": qc.cbits_num, "ops": [op_to_json(o) for o in circ.ops],
+                "measures": [list(m) for m in circ.measure_vec]}
+
+    def _state(self, key, psi):
+        tag = f"frontend_{len(self.states)}_{key}"
+        self.states[tag] = np.array(psi, dtype=np.complex128, copy=True)
+        return tag
+
+    def simulate_circuit(self, qc, inputstate=np.array(0, dtype=np.complex128), shots=0):
+        rec = None
+        if self.calls is not None:
+            rec = {"fn": "simulate_circuit", "circuit": self._circuit(qc), "shots": int(shots),
+                   "input": self._state("in", inputstate) if np.size(inputstate) else None}
+        counts, psi = self.ref.simulate_circuit(qc, inputstate, shots)
+        if rec is not None:
+            rec["counts"] = {str(k): int(v) for k, v in dict(counts).items()}
+            rec["output"] = self._state("out", psi)
+            self.calls.append(rec)
+        return counts, psi
+
+    def expect_statevec(self, inputstate, paulis):
+        res = self.ref.expect_statevec(inputstate, paulis)
+        if self.calls is not None:
+            self.calls.append({"fn": "expect_statevec", "input": self._state("in", inputstate),
+                               "paulis": [[p.paulistr, [int(x) for x in p.pos]] for p in paulis],
+                               "result": [float(x) for x in res]})
+        return res
+
+    def applyop_statevec(self, op, inputstate):
+        return self.ref.applyop_statevec(op, inputstate)
+
+    def sampling_statevec(self, measures, inputstate, shots):
+        return self.ref.sampling_statevec(measures, inputstate, shots)
+
+    def simulate_circuit_clifford(self, qc, shots):
+        return self.ref.simulate_circuit_clifford(qc, shots)
+
+
 def main():
-    refload.load()
+    ref = refload.load_ref_qfvm()
+    recorder = RecordingQfvm(ref)
+    refload.load(recorder)  # quafu imports its qfvm functions from the recorder
     from quafu import QuantumCircuit
     import quafu.elements.element_gates as eg
     from quafu.algorithms.hamiltonian import Hamiltonian, PauliOp
     from quafu.elements import Parameter
-
-    ref = refload.load_ref_qfvm()
     out_cases = []
     states = {}
 
@@ -417,8 +469,32 @@ def main():
     terms = [(f"Z{i} Z{i+1}", float(rng.normal())) for i in range(n - 1)] + [(f"X{i}", float(rng.normal())) for i in range(n)]
     grad_case("hea6_l3", n, hea(n, 3, 21), terms)
 
+    # quafu's own front end (quafu.simulate -> SVSimulator.run,
+    # simulator.py:90-145) over the recording module: the calls it makes into
+    # qfvm and what the reference module returned for them
+    import quafu
+
+    recorder.calls = []
+    qc = QuantumCircuit(4, 4)
+    qc.x(0)
+    qc.x(2)
+    qc.cx(2, 3)
+    qc.measure([0, 1, 2, 3], [3, 2, 1, 0])
+    quafu.simulate(qc, shots=64)
+    qc = random_layer_circuit(QuantumCircuit, 10, 12, 4, extras=True)
+    ham = Hamiltonian.from_pauli_list([("Z0 Z1", 0.7), ("X3 Y4", -0.4), ("Z9", 1.1)])
+    quafu.simulate(qc, hamiltonian=ham)
+    rng = np.random.default_rng(41)
+    psi0 = rng.normal(size=1 << 6) + 1j * rng.normal(size=1 << 6)
+    psi0 = (psi0 / np.linalg.norm(psi0)).astype(np.complex128)
+    qc = build_all_gates_circuit(QuantumCircuit, eg, 6, 2, 42)
+    quafu.simulate(qc, psi=psi0.copy(), hamiltonian=Hamiltonian.from_pauli_list([("X0 Z5", 1.0), ("Y2", 0.5)]))
+    frontend_calls = recorder.calls
+    recorder.calls = None
+    states.update(recorder.states)
+
     meta = {"cases": out_cases, "apply": apply_cases, "counts": count_cases, "sampling": sampling_cases,
-            "gradients": grad_cases, "mid_circuit": mid_cases, "noise": noise_cases,
+            "gradients": grad_cases, "mid_circuit": mid_cases, "noise": noise_cases, "frontend": frontend_calls,
             "generator": "tests/golden/make_golden.py (reference qfvm.cpp via oracle/build_ref.sh)"}
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(meta, f)

@@ -102,3 +102,34 @@ def test_errors_are_raised_not_crashes():
     pc.instructions = [R()] + pc.instructions
     with pytest.raises(qfvm.QfvmError):
         qfvm.simulate_circuit(pc, None, 10)
+
+
+class _Pauli:
+    def __init__(self, paulistr, pos):
+        self.paulistr, self.pos = paulistr, pos
+
+
+def test_reference_frontend_calls_replayed(golden):
+    """The calls quafu's own front end (quafu.simulate -> SVSimulator.run,
+    quafu/simulators/simulator.py:90-145) made into the reference qfvm module
+    when tests/golden/make_golden.py ran it, replayed on this module with the
+    same arguments: same counts, same statevector (in place when an input
+    state is given), same expectation values."""
+    meta, states = golden
+    calls = meta["frontend"]
+    assert [c["fn"] for c in calls].count("simulate_circuit") == 3
+    for c in calls:
+        if c["fn"] == "simulate_circuit":
+            ci = c["circuit"]
+            ops = [helpers.op_from_json(d) for d in ci["ops"] if d["kind"] < 40]
+            circ = workloads.ProtoCircuit(ci["n"], ops, [tuple(m) for m in ci["measures"]] or None, ci["cbits_num"])
+            psi_in = states[c["input"]].copy() if c["input"] else np.array([], dtype=np.complex128)
+            counts, psi = qfvm.simulate_circuit(circ, psi_in, c["shots"])
+            if c["input"]:
+                assert psi is psi_in
+            assert {str(k): v for k, v in counts.items()} == c["counts"]
+            assert np.abs(psi - states[c["output"]]).max() <= 1e-12
+        else:
+            paulis = [_Pauli(p, pos) for p, pos in c["paulis"]]
+            got = qfvm.expect_statevec(states[c["input"]].copy(), paulis)
+            np.testing.assert_allclose(got, c["result"], atol=1e-12, rtol=0)

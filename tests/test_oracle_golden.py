@@ -140,3 +140,20 @@ def test_noise_golden(golden):
             for st in strings:
                 counts[st] = counts.get(st, 0) + 1
             assert counts == case["counts"], case["tag"]
+
+
+def test_frontend_calls_match_oracle(golden):
+    """The recorded calls of quafu's front end into qfvm, replayed on the
+    oracle: the recorded circuits (as read by pyquafu_gb300.ir) give the
+    recorded states, and the recorded Pauli terms the recorded values."""
+    meta, states = golden
+    for c in meta["frontend"]:
+        if c["fn"] == "simulate_circuit":
+            ops = [helpers.op_from_json(d) for d in c["circuit"]["ops"] if d["kind"] < 40]
+            psi_in = states[c["input"]] if c["input"] else None
+            got = oracle.simulate(c["circuit"]["n"], ops, psi_in)
+            assert np.abs(got - states[c["output"]]).max() < 1e-13
+        else:
+            psi = states[c["input"]]
+            got = [oracle.expect_pauli(psi, p, pos) for p, pos in c["paulis"]]
+            np.testing.assert_allclose(got, c["result"], atol=1e-13, rtol=0)
