@@ -357,7 +357,7 @@ def plain_passes(n, ops, precision):
     return out[0], out[1]
 
 
-def measure_adjoint(n=24, layers=20, ps_params=6, peak=FALLBACK_HBM, cpu=True, cpu_seconds=10.0):
+def measure_adjoint(n=24, layers=20, ps_params=6, peak=FALLBACK_HBM, cpu=True, cpu_seconds=10.0, defer=None):
     """Adjoint gradients of a hardware-efficient ansatz (ry, rz on every qubit
     then a cx ladder, 2 * n * layers parameters; observable sum a_i Z_i Z_i+1 +
     sum b_i X_i): time per full gradient for each precision, its HBM rate
@@ -365,8 +365,8 @@ def measure_adjoint(n=24, layers=20, ps_params=6, peak=FALLBACK_HBM, cpu=True, c
     same GPU's parameter-shift rate (timed on `ps_params` parameters, 2
     forward runs each, extrapolated), and the CPU baseline (the oracle's
     restatement of grad_adjoint, gradiant.py:144-173, its reverse sweep timed
-    for `cpu_seconds` and extrapolated).  Gradients are returned for the
-    oracle comparison."""
+    for `cpu_seconds` and extrapolated; appended to `defer` when given).
+    Gradients are returned for the oracle comparison."""
     import torch
 
     from pyquafu_gb300 import batch as bmod
@@ -405,7 +405,7 @@ def measure_adjoint(n=24, layers=20, ps_params=6, peak=FALLBACK_HBM, cpu=True, c
                                "max_abs_diff_vs_adjoint": float(np.abs(ps[: len(keep)] - grads["c128"][: len(keep)]).max())}
     out["adjoint_speedup_vs_param_shift"] = {
         p: round(per_param * nparam / out[p]["s_per_gradient"], 1) for p in ("c128_ds", "c128", "c64")}
-    if cpu:
+    def host_part():
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle
 
@@ -416,6 +416,12 @@ def measure_adjoint(n=24, layers=20, ps_params=6, peak=FALLBACK_HBM, cpu=True, c
                                "kind": "port", "s_per_gradient": round(total, 2),
                                "sample": f"oracle grad_adjoint: forward {fwd_s:.1f} s and lam {lam_s:.1f} s in full, "
                                          f"reverse sweep {done} of {len(ops)} gates in {rev_s:.1f} s, extrapolated"}
+
+    if cpu:
+        if defer is None:
+            host_part()
+        else:
+            defer.append(host_part)
     return out, (ops, terms, grads)
 
 
@@ -698,7 +704,7 @@ def measure_qnn(steps=5, warmup=3, ps_forwards=20, tune=True, peak=FALLBACK_HBM,
             "speedup_vs_param_shift": round(ps_step / dt, 1), "autotuned": tuned}
 
 
-def measure_c1(steps=20, shots=4096, cpu=True, peak=FALLBACK_HBM):
+def measure_c1(steps=20, shots=4096, cpu=True, peak=FALLBACK_HBM, defer=None):
     """The 20-qubit random circuit (depth 20, seed 0, complex128) with 4096
     shots: gate time on the device (the 16 MiB state stays in L2 between
     steps, so its GB/s are L2-resident figures), sampling time (one call:
@@ -706,7 +712,8 @@ def measure_c1(steps=20, shots=4096, cpu=True, peak=FALLBACK_HBM):
     indices down), shots the exact scan resolved, and the oracle's gate and
     sequential-scan times on the host cores (statevector.hpp:1380-1412 is
     serial).  Errors: final state against the oracle per amplitude, sampled
-    indices against the oracle's scan with the same seeded uniforms."""
+    indices against the oracle's scan with the same seeded uniforms.  With
+    `defer` (a list) the host part is appended to it instead of run."""
     import torch
 
     from pyquafu_gb300 import engine, workloads
@@ -748,7 +755,9 @@ def measure_c1(steps=20, shots=4096, cpu=True, peak=FALLBACK_HBM):
         st.close()
         plan.close()
         out[prec] = row
-    if cpu:
+    indices = out.pop("indices")
+
+    def host_part():
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle
 
@@ -763,29 +772,97 @@ def measure_c1(steps=20, shots=4096, cpu=True, peak=FALLBACK_HBM):
                                "sample": "the full circuit and all 4096 shots (sequential scan, one core)"}
         for prec in ("c128_ds", "c128"):
             out[prec]["max_abs_err_vs_oracle"] = max_abs_diff(states[prec], ref)
-        out["sample_mismatches_vs_oracle"] = int(np.sum(out["indices"] != ref_idx))
-    del out["indices"]
+        out["sample_mismatches_vs_oracle"] = int(np.sum(indices != ref_idx))
+
+    if cpu:
+        if defer is None:
+            host_part()
+        else:
+            defer.append(host_part)
     return out
 
 
-def oracle_check_c2(n, ops, precisions):
-    """Final state of every arithmetic against the oracle (its full run on
-    the host cores, timed), per amplitude, and <Z0 Z1>."""
+SHOT_SEED = 0
+SHOTS = 4096
+
+
+class OracleRun:
+    """The oracle's full run of the benchmark circuit on the host cores, in a
+    child process forked before the first GPU call, so it runs while the
+    device-timed rows do (rows whose figures include host time wait for it).
+    The final state lands in an anonymous shared mapping; the child also
+    computes <Z0 Z1> and the indices of the 4096 seeded shots (the oracle's
+    single-walk scan, equal to its per-shot scan)."""
+
+    def __init__(self, n, ops):
+        import mmap
+
+        self.n = n
+        self.u = np.random.Generator(np.random.MT19937(SHOT_SEED)).random(SHOTS)
+        self._map = mmap.mmap(-1, (16 << n) + 8 * (4 + SHOTS))
+        self.pid = os.fork()
+        if self.pid == 0:  # child: no GPU, no torch
+            code = 1
+            try:
+                sys.path.insert(0, os.path.join(ROOT, "oracle"))
+                import oracle
+
+                oracle.build()
+                psi = self._state()
+                hdr = self._header()
+                t0 = time.perf_counter()
+                psi[:] = 0
+                psi[0] = 1.0
+                for op in ops:
+                    oracle.apply_op(psi, op)
+                hdr[0] = time.perf_counter() - t0
+                hdr[1] = oracle.expect_pauli(psi, "ZZ", [0, 1])
+                t1 = time.perf_counter()
+                self._indices()[:] = oracle.sample_indices_sorted(psi, self.u)
+                hdr[2] = time.perf_counter() - t1
+                hdr[3] = 1.0
+                code = 0
+            except BaseException as e:  # reported by the parent as a failed check
+                print(f"[bench] oracle run failed: {e!r}", file=sys.stderr, flush=True)
+            finally:
+                os._exit(code)
+
+    def _state(self):
+        return np.frombuffer(self._map, dtype=np.complex128, count=1 << self.n)
+
+    def _header(self):
+        return np.frombuffer(self._map, dtype=np.float64, count=4, offset=16 << self.n)
+
+    def _indices(self):
+        return np.frombuffer(self._map, dtype=np.uint64, count=SHOTS, offset=(16 << self.n) + 32)
+
+    def result(self):
+        """Waits for the child; (state, <Z0Z1>, shot indices, seconds of the
+        circuit, seconds of the scan), or None when it failed."""
+        if self.pid:
+            _, status = os.waitpid(self.pid, 0)
+            self.pid = 0
+            self.status = status
+        hdr = self._header()
+        if hdr[3] != 1.0:
+            return None
+        return self._state(), float(hdr[1]), self._indices(), float(hdr[0]), float(hdr[2])
+
+
+def oracle_check_c2(n, ops, precisions, run):
+    """Final state of every arithmetic against the oracle's full run (`run`,
+    an OracleRun), per amplitude, and <Z0 Z1>; the first arithmetic's 4096
+    shots against the oracle's scan with the same seeded uniforms."""
     import torch
 
     from pyquafu_gb300 import engine
 
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-
-    oracle.build()
-    t0 = time.perf_counter()
-    ref = oracle.simulate(n, ops)
-    oracle_s = time.perf_counter() - t0
-    zz_ref = oracle.expect_pauli(ref, "ZZ", [0, 1])
+    res = run.result()
+    if res is None:
+        return {"error": "the oracle run failed (see stderr)"}
+    ref, zz_ref, ref_idx, oracle_s, scan_s = res
     out = {"oracle_full_circuit_s": round(oracle_s, 1), "oracle_cores": os.cpu_count()}
     buf = np.empty(1 << n, dtype=np.complex128)
-    u = np.random.Generator(np.random.MT19937(0)).random(4096)
     for prec in precisions:
         plan = engine.Plan(n, ops, prec)
         st = engine.DeviceState(n, prec).set_zero()
@@ -793,21 +870,35 @@ def oracle_check_c2(n, ops, precisions):
         torch.cuda.synchronize()
         zz = float(st.expect([("ZZ", [0, 1])])[0])
         if prec == precisions[0]:
-            # 4096 shots on the final state, exact against the oracle's sequential scan
-            st.sample(u)
+            # 4096 shots on the final state, exact against the oracle's scan
+            st.sample(run.u)
             t0 = time.perf_counter()
-            idx = st.sample(u)
+            idx = st.sample(run.u)
             sample_ms = (time.perf_counter() - t0) * 1e3
-            t1 = time.perf_counter()
-            ref_idx = oracle.sample_indices(ref, u)
             out["sampling_4096_shots"] = {"gpu_ms": round(sample_ms, 2), "sequential_blocks": st.sequential_blocks(),
-                                          "oracle_scan_s": round(time.perf_counter() - t1, 2),
+                                          "oracle_scan_s": round(scan_s, 2),
+                                          "oracle_scan": "one walk of the FP64 running sum, shots by ascending "
+                                                         "uniform (equal to the per-shot scan)",
                                           "mismatches_vs_oracle": int(np.sum(idx != ref_idx))}
         st.download(buf)
         st.close()
         plan.close()
         out[prec] = {"max_abs_err": max_abs_diff(buf, ref), "zz_abs_err": abs(zz - zz_ref)}
     return out
+
+
+class Sections:
+    """Wall time of each part of the run, on stderr as it goes."""
+
+    def __init__(self):
+        self.t = {}
+
+    def __call__(self, name, fn, *a, **k):
+        t0 = time.perf_counter()
+        r = fn(*a, **k)
+        self.t[name] = round(time.perf_counter() - t0, 1)
+        print(f"[bench] {name}: {self.t[name]} s", file=sys.stderr, flush=True)
+        return r
 
 
 def max_over_ranks(value: float, world: int, device: str = "cuda") -> float:
@@ -848,15 +939,21 @@ def autotune_all(args, n, ops):
 
 
 def run_gpu(args):
+    world = env_int("WORLD_SIZE", 1)
+    rank = env_int("RANK", 0)
+    local = env_int("LOCAL_RANK", 0)
+    n = N_QUBITS
+    ops = workload()
+    # the oracle's full run starts first, in a child forked before any GPU call
+    oracle_run = OracleRun(n, ops) if rank == 0 and not args.skip_oracle_check else None
+    sec = Sections()
+
     import torch
 
     from pyquafu_gb300 import _native as nat
     from pyquafu_gb300 import qfvm, workloads
     from pyquafu_gb300.builder import build
 
-    world = env_int("WORLD_SIZE", 1)
-    rank = env_int("RANK", 0)
-    local = env_int("LOCAL_RANK", 0)
     if world > 1:
         import torch.distributed as dist
 
@@ -864,8 +961,6 @@ def run_gpu(args):
         dist.init_process_group("nccl")
     build()
     nat.load()
-    n = N_QUBITS
-    ops = workload()
     peak, peak_kind = hbm_peak()
     cpu_here = rank == 0 and not args.skip_cpu
 
@@ -876,11 +971,11 @@ def run_gpu(args):
 
             dist.barrier()
 
-    tuning = None if args.no_autotune else autotune_all(args, n, ops)
+    tuning = None if args.no_autotune else sec("autotune", autotune_all, args, n, ops)
     barrier()
     clocks = ClockSampler()
     clocks.start()
-    main = measure(args.precision, ops, n, args.steps, args.warmup)
+    main = sec("headline", measure, args.precision, ops, n, args.steps, args.warmup)
     clk = clocks.stop()
     barrier()
     total_ms = max_over_ranks(main["ms_per_step"] * args.steps, world, "cuda")
@@ -892,12 +987,22 @@ def run_gpu(args):
 
     variants = {}
     for v in [x for x in args.variants.split(",") if x and x != args.precision]:
-        r = measure(v, ops, n, min(args.steps, 3), max(1, min(args.warmup, 3)))
+        r = sec(f"variant {v}", measure, v, ops, n, min(args.steps, 3), max(1, min(args.warmup, 3)))
         variants[v] = {"value": round(r["gbps"], 2), "unit": "GB/s", "ms_per_step": round(r["ms_per_step"], 3),
                        "passes": r["passes"], "tile_kernel": kernel_name(v, n, r["specialised_passes"] > 0),
                        "specialised_passes": r["specialised_passes"], "tile_pass_gbps": round(r["tile_gbps"], 1),
                        "tile_pass_frac_hbm": round(r["tile_gbps"] / peak, 4),
                        "hbm_gbps": round(r["pass_bytes"] / (r["ms_per_step"] * 1e-3) / 1e9, 1)}
+
+    # device-timed rows whose host parts wait for the oracle run
+    deferred = []
+    c1 = None if args.skip_c1 else sec("C1", measure_c1, cpu=cpu_here, peak=peak, defer=deferred)
+    adj = adj_data = None
+    if not args.skip_adjoint:
+        adj, adj_data = sec("C3 adjoint", measure_adjoint, args.adjoint_qubits, peak=peak, cpu=cpu_here,
+                            defer=deferred)
+    if oracle_run is not None:
+        sec("oracle run (wait)", oracle_run.result)
 
     # --- end to end through the reference-shaped API (host buffers) ---
     e2e = None
@@ -910,6 +1015,7 @@ def run_gpu(args):
         circuit = workloads.as_protocol(n, ops)
         qfvm.simulate_circuit(circuit, psi, 0)
         torch.cuda.synchronize()
+        t_e2e = time.perf_counter()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             qfvm.simulate_circuit(circuit, psi, 0)
@@ -922,24 +1028,24 @@ def run_gpu(args):
                "api": "pyquafu_gb300.qfvm.simulate_circuit(circuit, pinned complex128 state, shots=0)"}
         del psi, host
         qfvm.set_arithmetic("ds")
+        print(f"[bench] e2e: {time.perf_counter() - t_e2e:.1f} s", file=sys.stderr, flush=True)
 
-    c1 = None if args.skip_c1 else measure_c1(cpu=cpu_here, peak=peak)
-    adj = adj_data = None
-    if not args.skip_adjoint:
-        adj, adj_data = measure_adjoint(args.adjoint_qubits, peak=peak, cpu=cpu_here)
     batched = None
     if not args.skip_batch:
         batched = {}
         if not args.skip_uneven:
-            batched["uneven_2048"] = measure_uneven_batch(cpu=cpu_here, tune=not args.no_autotune, peak=peak)
-        batched["qnn_training_step"] = measure_qnn(tune=not args.no_autotune, peak=peak, cpu=cpu_here)
+            batched["uneven_2048"] = sec("C4 batch", measure_uneven_batch, cpu=cpu_here, tune=not args.no_autotune,
+                                         peak=peak)
+        batched["qnn_training_step"] = sec("C5 qnn", measure_qnn, tune=not args.no_autotune, peak=peak, cpu=cpu_here)
         if not args.skip_trajectories:
-            batched["trajectories"] = measure_trajectories(cpu=cpu_here)
-            batched["noise"] = measure_noise(cpu=cpu_here)
+            batched["trajectories"] = sec("trajectories", measure_trajectories, cpu=cpu_here)
+            batched["noise"] = sec("noise", measure_noise, cpu=cpu_here)
+    for i, part in enumerate(deferred):
+        sec(f"host part {i}", part)
 
     cpu = None
     if cpu_here:
-        cgbps, gates_done, cdt = cpu_sample(ops, n, seconds=args.cpu_seconds)
+        cgbps, gates_done, cdt = sec("cpu baseline", cpu_sample, ops, n, seconds=args.cpu_seconds)
         info = cpu_info()
         cpu = {"value": round(cgbps, 3), "unit": "GB/s", "cores": info["cores"], "kind": "port",
                "sample": f"{gates_done} gates of the circuit in strided order on the {n}-qubit complex128 state "
@@ -947,9 +1053,9 @@ def run_gpu(args):
 
     # --- the error of every result against the oracle (after all timing) ---
     check = None
-    if rank == 0 and not args.skip_oracle_check:
+    if oracle_run is not None:
         precs = [args.precision] + [v for v in args.variants.split(",") if v and v != args.precision]
-        check = oracle_check_c2(n, ops, precs)
+        check = sec("oracle check", oracle_check_c2, n, ops, precs, oracle_run)
         if adj_data is not None:
             sys.path.insert(0, os.path.join(ROOT, "oracle"))
             import oracle

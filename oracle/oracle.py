@@ -64,6 +64,8 @@ def lib():
         L.qor_expect_pauli.restype = ctypes.c_double
         L.qor_sample_indices.argtypes = [dp, u64, dp, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64)]
         L.qor_sequential_cdf.argtypes = [dp, u64, dp]
+        L.qor_sample_indices_sorted.argtypes = [dp, u64, dp, ctypes.POINTER(ctypes.c_int64), ctypes.c_int64,
+                                                ctypes.POINTER(ctypes.c_uint64)]
         _lib = L
     return _lib
 
@@ -326,6 +328,20 @@ def sample_indices(psi: np.ndarray, uniforms: np.ndarray) -> np.ndarray:
     out = np.zeros(u.size, dtype=np.uint64)
     lib().qor_sample_indices(_dptr(psi.view(np.float64)), psi.size, _dptr(u), u.size,
                              out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+    return out
+
+
+def sample_indices_sorted(psi: np.ndarray, uniforms: np.ndarray) -> np.ndarray:
+    """The indices of sample_indices from one walk of the FP64 running sum
+    (shots visited by ascending uniform): O(size + shots) instead of
+    O(size * shots), the same sums and comparisons."""
+    psi = np.ascontiguousarray(psi, dtype=np.complex128)
+    u = np.ascontiguousarray(uniforms, dtype=np.float64)
+    order = np.ascontiguousarray(np.argsort(u, kind="stable"), dtype=np.int64)
+    out = np.zeros(u.size, dtype=np.uint64)
+    lib().qor_sample_indices_sorted(_dptr(psi.view(np.float64)), psi.size, _dptr(u),
+                                    order.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), u.size,
+                                    out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
     return out
 
 

@@ -420,6 +420,25 @@ void qor_sample_indices(const double* data_, uint64_t size, const double* unifor
     }
 }
 
+/* The scan above for every shot in one walk of the running sum: `order`
+ * lists the shots by ascending uniform, so each shot's first index whose
+ * running sum exceeds its uniform is found in turn.  The sums and the
+ * comparisons are those of the per-shot loop, so the indices are equal. */
+void qor_sample_indices_sorted(const double* data_, uint64_t size, const double* uniforms, const int64_t* order,
+                               int64_t shots, uint64_t* out) {
+    const cplx* data = (const cplx*)data_;
+    double p = 0.0;
+    int64_t k = 0;
+    for (uint64_t i = 0; i < size && k < shots; ++i) {
+        double re = data[i].re, im = data[i].im;
+        double pr = re * re;
+        double pi = im * im;
+        p += pr + pi;
+        while (k < shots && uniforms[order[k]] < p) out[order[k++]] = i;
+    }
+    for (; k < shots; ++k) out[order[k]] = size;
+}
+
 /* Inclusive FP64 CDF in index order (the running sum of the scan above). */
 void qor_sequential_cdf(const double* data_, uint64_t size, double* cdf) {
     const cplx* data = (const cplx*)data_;

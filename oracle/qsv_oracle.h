@@ -27,6 +27,8 @@ int qor_apply_named(double* data, uint64_t size, int kind, const int32_t* qubits
 int qor_apply_matrix(double* data, uint64_t size, const int32_t* posv, int npos, int control_num, const double* mat);
 double qor_expect_pauli(const double* data, uint64_t size, uint64_t x_mask, uint64_t z_mask, int y_count);
 void qor_sample_indices(const double* data, uint64_t size, const double* uniforms, int64_t shots, uint64_t* out);
+void qor_sample_indices_sorted(const double* data, uint64_t size, const double* uniforms, const int64_t* order,
+                               int64_t shots, uint64_t* out);
 void qor_sequential_cdf(const double* data, uint64_t size, double* cdf);
 
 #ifdef __cplusplus

@@ -85,6 +85,12 @@ def test_sampling_scan_semantics():
     expect = [int(np.searchsorted(cdf, r, side="right")) for r in u]  # first k with r < cdf[k]
     assert [int(i) for i in idx] == expect
     assert int(idx[-1]) == psi.size  # r >= total -> index 2^n (loop end)
+    # the single-walk variant (shots by ascending uniform) gives the same indices
+    assert np.array_equal(oracle.sample_indices_sorted(psi, u), idx)
+    big = rng.normal(size=1 << 12) + 1j * rng.normal(size=1 << 12)
+    big /= np.linalg.norm(big)
+    ub = np.concatenate([rng.random(3000), oracle.sequential_cdf(big)[::97], [1.0, 0.0, 0.5, 0.5]])
+    assert np.array_equal(oracle.sample_indices_sorted(big, ub), oracle.sample_indices(big, ub))
 
 
 def test_known_answers_bell():
