@@ -176,10 +176,17 @@ int32_t qfvm_get_c128_arithmetic(void);
  * calling cudaMalloc; kind 2: the countdown-th pass of a plan run fails
  * (QFVM_ERR_CUDA, "injected kernel-stage failure") before its launch; kind
  * 0 disarms.  One fault fires, then the hook disarms itself.  Nothing
- * touches the GPU, so the context stays usable. */
+ * touches the GPU, so the context stays usable.
+ * kind 3 (stays armed until kind 0): every specialised tile pass expects 16
+ * bytes more per tile than its bulk copies bring, so its bounded wait for the
+ * tile (limit: countdown milliseconds) runs out; the kernel records
+ * QFVM_ERR_TIMEOUT in its status word and returns, and the next
+ * synchronising call reports QFVM_ERR_TIMEOUT.  No fault, no hang: the copies
+ * themselves complete and the context stays usable. */
 #define QFVM_FAULT_NONE 0
 #define QFVM_FAULT_ALLOC 1
 #define QFVM_FAULT_STAGE 2
+#define QFVM_FAULT_WAIT 3
 int qfvm_test_fault(int32_t kind, int64_t countdown);
 
 /* ------------------------------------------------------------------ */

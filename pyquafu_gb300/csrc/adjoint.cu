@@ -114,7 +114,7 @@ cudaError_t launch_pass2_t(void* psi, void* lam, const PassDesc* dpass, const St
                            const void* dcoef, int n, int H, int items, uint64_t cstride, int per_tile,
                            double* partial, int* grid_out, cudaStream_t st) {
     constexpr int NT = 1 << (T - R);
-    const size_t tiles_b = 2 * NB * (sizeof(typename P::S) << T);
+    const size_t tiles_b = 2 * NB * sizeof(typename P::S) * tile_elems(T, sizeof(typename P::S));
     const size_t smem = tiles_b + (sizeof(uint64_t) << H) + sizeof(double) * (NT / 32) * MAX_PASS_PROBES;
     static int grid_cap = 0;
     if (grid_cap == 0) {

@@ -145,16 +145,16 @@ __global__ void __launch_bounds__(1 << (T - R), MINB)
     constexpr int NT = 1 << (T - R);
     constexpr int NW = NT / 32;
     constexpr int NA = 1 << R;
-    constexpr int GB = P::GBITS;
     constexpr int PER = (1 << T) / NT;
+    constexpr uint32_t TE = tile_elems(T, sizeof(typename P::S));  // elements per tile buffer
     extern __shared__ __align__(16) unsigned char smem_raw[];
     typename P::S* base_s = reinterpret_cast<typename P::S*>(smem_raw);
     // buffers: [slot][state], NB slots
-    uint64_t* choff = reinterpret_cast<uint64_t*>(smem_raw + 2 * NB * (sizeof(typename P::S) << T));
+    uint64_t* choff = reinterpret_cast<uint64_t*>(smem_raw + 2 * NB * sizeof(typename P::S) * TE);
     double* pacc = reinterpret_cast<double*>(choff + (1 << pdp->H));
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t stid = swz<GB>(static_cast<uint32_t>(tid));
+    const uint32_t stid = sm_off<P, true>(static_cast<uint32_t>(tid));
     const int L = pdp->L, H = pdp->H;
     const uint8_t* tq = pdp->tq;
     const int np = pdp->nprobe;
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(1 << (T - R), MINB)
     __syncthreads();
     const uint32_t lmask = (1u << L) - 1;
     const int nsteps = pdp->step_count;
-    auto buf = [&](int slot, int st) { return base_s + (2 * (slot & (NB - 1)) + st) * (1 << T); };
+    auto buf = [&](int slot, int st) { return base_s + (2 * (slot & (NB - 1)) + st) * TE; };
 
     uint64_t b = blockIdx.x;
     if (NB == 2 && b < ntiles) {
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(1 << (T - R), MINB)
         if constexpr (P::RAW_STAGING) {
 #pragma unroll
             for (int k = 0; k < PER; ++k) {
-                const uint32_t ad = swz<GB>(static_cast<uint32_t>(k * NT)) ^ stid;
+                const uint32_t ad = sm_off<P, true>(static_cast<uint32_t>(k * NT)) + stid;
                 sm[0][ad] = P::g2s(P::raw_to_g(sm[0][ad]));
                 sm[1][ad] = P::g2s(P::raw_to_g(sm[1][ad]));
             }
@@ -215,14 +215,14 @@ __global__ void __launch_bounds__(1 << (T - R), MINB)
                 }
                 continue;
             }
-            // the thread's swizzled base offset and global index: the
-            // swizzle is XOR-linear, so both are sums over its index bits
+            // the thread's base offset in the tile layout and its global
+            // index: both are sums over its index bits
             uint32_t psb = 0;
             uint64_t gthr = base;
 #pragma unroll
             for (int k = 0; k < T - R; ++k) {
                 if ((tid >> k) & 1) {
-                    psb ^= sd->tsw[k];
+                    psb += sd->tsw[k];
                     gthr |= 1ULL << sd->tglob[k];
                 }
             }
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(1 << (T - R), MINB)
                 uint32_t ad = psb;
 #pragma unroll
                 for (int k = 0; k < R; ++k)
-                    if ((j >> k) & 1) ad ^= rsw[k];
+                    if ((j >> k) & 1) ad += rsw[k];
                 a[0][j] = P::s2a(sm[0][ad]);
                 a[1][j] = P::s2a(sm[1][ad]);
             }
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(1 << (T - R), MINB)
                 uint32_t ad = psb2;
 #pragma unroll
                 for (int k = 0; k < R; ++k)
-                    if ((j >> k) & 1) ad ^= rsw[k];
+                    if ((j >> k) & 1) ad += rsw[k];
                 sm[0][ad] = P::a2s(a[0][j]);
                 sm[1][ad] = P::a2s(a[1][j]);
             }
@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(1 << (T - R), MINB)
         for (int k = 0; k < PER; ++k) {
             const uint32_t s = static_cast<uint32_t>(k * NT) | tid;
             const uint64_t g = base | choff[s >> L] | (s & lmask);
-            const uint32_t ad = swz<GB>(static_cast<uint32_t>(k * NT)) ^ stid;
+            const uint32_t ad = sm_off<P, true>(static_cast<uint32_t>(k * NT)) + stid;
             __stcs(psi_g + g, P::s2g(sm[0][ad]));
             __stcs(lam_g + g, P::s2g(sm[1][ad]));
         }

@@ -476,6 +476,7 @@ int batch_run(qfvm_batch* b, int mode, const double* values, const double* weigh
     }
     if (device_ms) QSV_CUDA(cudaEventRecord(b->t1, b->main), "event");
     QSV_CUDA(cudaStreamSynchronize(b->main), "batch run");
+    QSV_TRY(check_status(b->main));
     if (device_ms) QSV_CUDA(cudaEventElapsedTime(device_ms, b->t0, b->t1), "event");
     std::memcpy(expvals, b->hout, static_cast<size_t>(b->nexp) * 8);
     if (mode == 1 && b->ngrad) std::memcpy(grads, b->hout + b->nexp, static_cast<size_t>(b->ngrad) * 8);
@@ -556,12 +557,14 @@ int qfvm_batch_add_group(qfvm_batch* batch, int32_t num_qubits, const qfvm_op* o
 
 int qfvm_batch_run(qfvm_batch* batch, int32_t mode, const double* values, const double* weights, double* expvals,
                    double* grads) {
+    qsv_capi::NvtxRange range("qfvm batched run");
     if (!batch) return fail(QFVM_ERR_INVALID, "null batch");
     return batch_run(batch, mode, values, weights, expvals, grads, nullptr);
 }
 
 int qfvm_batch_run_timed(qfvm_batch* batch, int32_t mode, const double* values, const double* weights,
                          double* expvals, double* grads, float* device_ms) {
+    qsv_capi::NvtxRange range("qfvm batched run");
     if (!batch || !device_ms) return fail(QFVM_ERR_INVALID, "null argument");
     return batch_run(batch, mode, values, weights, expvals, grads, device_ms);
 }

@@ -54,6 +54,13 @@ int fail(int code, const std::string& msg) {
     return code;
 }
 
+int check_status(cudaStream_t st) {
+    const int rc = jit_status_take(st);
+    if (rc == QFVM_ERR_TIMEOUT) return fail(rc, "a specialised pass gave up waiting for its tile copies");
+    if (rc != QFVM_OK) return fail(rc, "reading the device status word");
+    return QFVM_OK;
+}
+
 int check_device() {
     int count = 0;
     cudaError_t e = cudaGetDeviceCount(&count);
@@ -168,6 +175,8 @@ int run_plan(qfvm_plan* p, qfvm_sv* sv, bool timed = false) {
     for (size_t i = 0; i < hp.passes.size(); ++i) {
         const PassDesc& pd = hp.passes[i];
         if (fault_hit(FAULT_STAGE)) return fail(QFVM_ERR_CUDA, "pass launch: injected kernel-stage failure");
+        NvtxRange range(pd.type == PASS_TILE ? "qfvm tile pass" : (pd.type == PASS_SMALL ? "qfvm whole-state pass"
+                                                                                        : "qfvm global op"));
         cudaError_t e = cudaSuccess;
         if (pd.type == PASS_TILE) {
             bool done = false;
@@ -263,7 +272,7 @@ int sv_download(qfvm_sv* sv, double* host, uint64_t n_amps) {
     if (sv->precision == QFVM_C128) {
         QSV_CUDA(cudaMemcpyAsync(host, sv->d, sv->N * 16, cudaMemcpyDeviceToHost, sv->stream), "download");
         QSV_CUDA(cudaStreamSynchronize(sv->stream), "download sync");
-        return QFVM_OK;
+        return check_status(sv->stream);
     }
     const uint64_t chunk = std::min<uint64_t>(STAGE_AMPS, sv->N);
     QSV_TRY(sv->staging.ensure(chunk * 16));
@@ -275,10 +284,11 @@ int sv_download(qfvm_sv* sv, double* host, uint64_t n_amps) {
                  "download");
         QSV_CUDA(cudaStreamSynchronize(sv->stream), "download sync");
     }
-    return QFVM_OK;
+    return check_status(sv->stream);
 }
 
 int sv_expect(qfvm_sv* sv, const uint64_t* xm, const uint64_t* zm, const int32_t* ny, int64_t nterms, double* out) {
+    NvtxRange range("qfvm expectation");
     if (nterms < 0) return fail(QFVM_ERR_INVALID, "negative term count");
     if (nterms == 0) return QFVM_OK;
     if (!xm || !zm || !ny || !out) return fail(QFVM_ERR_INVALID, "null term buffer");
@@ -349,11 +359,13 @@ int sv_expect(qfvm_sv* sv, const uint64_t* xm, const uint64_t* zm, const int32_t
     std::vector<double> res(nt);
     QSV_CUDA(cudaMemcpyAsync(res.data(), dout, nt * 8, cudaMemcpyDeviceToHost, sv->stream), "result download");
     QSV_CUDA(cudaStreamSynchronize(sv->stream), "expectation sync");
+    QSV_TRY(check_status(sv->stream));
     for (size_t i = 0; i < nt; ++i) out[order[i]] = res[i];
     return QFVM_OK;
 }
 
 int sv_sample(qfvm_sv* sv, const double* uni, int64_t shots, uint64_t* out) {
+    NvtxRange range("qfvm sampling");
     if (shots < 0) return fail(QFVM_ERR_INVALID, "negative shot count");
     if (shots == 0) return QFVM_OK;
     if (!uni || !out) return fail(QFVM_ERR_INVALID, "null sample buffer");
@@ -400,7 +412,7 @@ int sv_sample(qfvm_sv* sv, const double* uni, int64_t shots, uint64_t* out) {
     QSV_CUDA(cudaMemcpyAsync(&seq, dseq, 8, cudaMemcpyDeviceToHost, sv->stream), "sample download");
     QSV_CUDA(cudaStreamSynchronize(sv->stream), "sampling sync");
     sv->last_seq_blocks = seq;
-    return QFVM_OK;
+    return check_status(sv->stream);
 }
 
 // Process-wide cached state for the host-buffer entry points (one per
@@ -496,8 +508,14 @@ int qfvm_set_c128_arithmetic(int32_t arith) {
 int32_t qfvm_get_c128_arithmetic(void) { return c128_arith(); }
 
 int qfvm_test_fault(int32_t kind, int64_t countdown) {
-    if (kind < FAULT_NONE || kind > FAULT_STAGE) return fail(QFVM_ERR_INVALID, "fault kind must be 0, 1 or 2");
+    if (kind < FAULT_NONE || kind > QFVM_FAULT_WAIT) return fail(QFVM_ERR_INVALID, "fault kind must be 0 .. 3");
     if (kind != FAULT_NONE && countdown < 1) return fail(QFVM_ERR_INVALID, "fault countdown must be >= 1");
+    if (kind == QFVM_FAULT_WAIT) {
+        if (countdown > 10000) return fail(QFVM_ERR_INVALID, "wait limit above 10 s");
+        jit_set_wait_test(16, static_cast<uint64_t>(countdown) * 1000000ull);
+        return QFVM_OK;
+    }
+    if (kind == FAULT_NONE) jit_set_wait_test(0, 0);
     g_fault_kind.store(FAULT_NONE);
     g_fault_count.store(countdown);
     g_fault_kind.store(kind);
@@ -535,7 +553,7 @@ int qfvm_sv_apply(qfvm_sv* sv, const qfvm_op* ops, int64_t n_ops, const double* 
     free_plan(p);
     if (rc != QFVM_OK) return rc;
     QSV_CUDA(e, "apply sync");
-    return QFVM_OK;
+    return check_status(sv->stream);
 }
 int qfvm_sv_expect(qfvm_sv* sv, const uint64_t* x_masks, const uint64_t* z_masks, const int32_t* y_counts,
                    int64_t n_terms, double* out) {
@@ -601,6 +619,7 @@ int qfvm_plan_run_timed(qfvm_plan* plan, qfvm_sv* sv, float* pass_ms, int32_t* p
     if (!plan->dbuf) return fail(QFVM_ERR_INVALID, "host-only plan cannot run");
     QSV_TRY(run_plan(plan, sv, true));
     QSV_CUDA(cudaEventSynchronize(plan->events.back()), "timed run sync");
+    QSV_TRY(check_status(sv->stream));
     for (size_t i = 0; i < plan->hp.passes.size(); ++i) {
         float ms = 0.f;
         QSV_CUDA(cudaEventElapsedTime(&ms, plan->events[i], plan->events[i + 1]), "elapsed");
@@ -635,6 +654,7 @@ int qfvm_plan_host_build(int32_t num_qubits, int32_t precision, const qfvm_op* o
         delete p;
         return fail(QFVM_ERR_INVALID, err);
     }
+    p->hp.arith = precision;
     merge_round_diagonals(&p->hp);
     *out = p;
     return QFVM_OK;
@@ -804,6 +824,7 @@ int qfvm_adjoint(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int6
                  int64_t matpool_len, const uint64_t* x_masks, const uint64_t* z_masks, const int32_t* y_counts,
                  const double* coeffs, int64_t n_terms, const double* psi_in, double* energy, double* grads,
                  int64_t n_slots) {
+    NvtxRange range("qfvm adjoint gradient");
     std::lock_guard<std::mutex> lk(g_boundary_mu);
     const int n = num_qubits;
     if (n < 1 || n > QFVM_MAX_QUBITS) return fail(QFVM_ERR_INVALID, "qubit count out of range");
@@ -944,6 +965,7 @@ int qfvm_adjoint(int32_t num_qubits, int32_t precision, const qfvm_op* ops, int6
     std::vector<double> vals(nprobe);
     if (nprobe) ADJ_CUDA(cudaMemcpyAsync(vals.data(), dvals, nprobe * 8, cudaMemcpyDeviceToHost, st), "probe download");
     ADJ_CUDA(cudaStreamSynchronize(st), "adjoint sync");
+    if (const int src = check_status(st)) return done(src);
     for (int64_t k = 0; k < n_slots; ++k) grads[k] = 0.0;
     for (size_t p = 0; p < nprobe; ++p) grads[hp.probe_slot[p]] += vals[p];
     return done(QFVM_OK);

@@ -1,6 +1,7 @@
 // Internals of the C ABI shared by its translation units (capi.cu, batch_capi.cu).
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <atomic>
@@ -17,7 +18,21 @@ extern std::atomic<uint64_t> g_launches;
 extern std::mutex g_boundary_mu;  // serialises the host-buffer entry points (shared cached state)
 
 int fail(int code, const std::string& msg);
+// After `st` is synchronised: QFVM_ERR_TIMEOUT (with the message set) when a
+// specialised pass's bounded wait for its tile copies gave up since the last
+// check, else QFVM_OK.
+int check_status(cudaStream_t st);
 int check_device();
+
+// NVTX range over a scope (a pass launch, a sampling call, a batched run):
+// profilers group the kernels launched inside it; free when no tool is
+// attached.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 #define QSV_CUDA(call, what)                                                                        \
     do {                                                                                           \

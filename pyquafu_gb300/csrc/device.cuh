@@ -26,6 +26,14 @@ __device__ __forceinline__ uint32_t swz(uint32_t s) {
     return x;
 }
 
+// Element offset of index i in shared memory: whole-state kernels use the
+// XOR swizzle above, tile passes the padded tile layout (tile_off, engine.h).
+template <class P, bool TILE>
+__device__ __forceinline__ uint32_t sm_off(uint32_t i) {
+    if constexpr (TILE) return tile_off(i, 16u / sizeof(typename P::S));
+    else return swz<P::GBITS>(i);
+}
+
 __device__ __forceinline__ uint64_t insert0(uint64_t j, int p) {
     return ((j >> p) << (p + 1)) | (j & ((1ULL << p) - 1));
 }
@@ -340,9 +348,8 @@ __device__ __forceinline__ void reg_finish_phase(RegState<P, R, NS>& a, const Ro
 // shared memory of one CTA per state; every gate is one sweep over it.
 // blockIdx.x selects a state of a batch (stride `stride` elements).
 // ---------------------------------------------------------------------------
-template <class P>
+template <class P, bool TILE = false>
 __device__ __forceinline__ void small_apply(typename P::S* sm, int n, const KOp& op, const typename P::C* coef) {
-    constexpr int GB = P::GBITS;
     using A = typename P::A;
     using C = typename P::C;
     const uint32_t N = 1u << n;
@@ -357,7 +364,7 @@ __device__ __forceinline__ void small_apply(typename P::S* sm, int n, const KOp&
                 if ((i & cm) != cm) continue;
                 const int par = __popc(i & pm) & 1;
                 if (!par && (op.flags & F_D0_ONE)) continue;
-                const uint32_t ad = swz<GB>(i);
+                const uint32_t ad = sm_off<P, TILE>(i);
                 A v = P::s2a(sm[ad]);
                 if (op.flags & F_D1_SPEC) amp_special<P>(v, op.special);
                 else if (par) amp_phase<P>(v, d1r, d1i, P::cneg(d1i));
@@ -373,8 +380,8 @@ __device__ __forceinline__ void small_apply(typename P::S* sm, int n, const KOp&
             for (uint32_t qd = tid; qd < (N >> 2); qd += nt) {
                 const uint32_t i = static_cast<uint32_t>(insert0(insert0(qd, lo), hi));
                 if ((i & cm) != cm) continue;
-                const uint32_t a0 = swz<GB>(i), a1 = swz<GB>(i | (1u << t0)), a2 = swz<GB>(i | (1u << t1)),
-                               a3 = swz<GB>(i | (1u << t0) | (1u << t1));
+                const uint32_t a0 = sm_off<P, TILE>(i), a1 = sm_off<P, TILE>(i | (1u << t0)), a2 = sm_off<P, TILE>(i | (1u << t1)),
+                               a3 = sm_off<P, TILE>(i | (1u << t0) | (1u << t1));
                 A v0 = P::s2a(sm[a0]), v1 = P::s2a(sm[a1]), v2 = P::s2a(sm[a2]), v3 = P::s2a(sm[a3]);
                 if (op.kind == K_SWAP) {
                     A t = v1;
@@ -410,7 +417,7 @@ __device__ __forceinline__ void small_apply(typename P::S* sm, int n, const KOp&
                     uint32_t idx = i;
                     for (int j = 0; j < k; ++j)
                         if ((m >> j) & 1) idx |= 1u << op.tk[j];
-                    in[m] = P::s2a(sm[swz<GB>(idx)]);
+                    in[m] = P::s2a(sm[sm_off<P, TILE>(idx)]);
                 }
                 for (uint32_t r = 0; r < dim; ++r) {
                     typename P::R xr = P::mul(P::coef(coef, op.coef + 2 * (r * dim)), in[0].x);
@@ -431,7 +438,7 @@ __device__ __forceinline__ void small_apply(typename P::S* sm, int n, const KOp&
                     A o;
                     o.x = xr;
                     o.y = xi;
-                    sm[swz<GB>(idx)] = P::a2s(o);
+                    sm[sm_off<P, TILE>(idx)] = P::a2s(o);
                 }
             }
             break;
@@ -452,7 +459,7 @@ __device__ __forceinline__ void small_apply(typename P::S* sm, int n, const KOp&
             for (uint32_t pr = tid; pr < (N >> 1); pr += nt) {
                 const uint32_t i0 = static_cast<uint32_t>(insert0(pr, t));
                 if ((i0 & cm) != cm) continue;
-                const uint32_t a0 = swz<GB>(i0), a1 = swz<GB>(i0 | (1u << t));
+                const uint32_t a0 = sm_off<P, TILE>(i0), a1 = sm_off<P, TILE>(i0 | (1u << t));
                 A x = P::s2a(sm[a0]), y = P::s2a(sm[a1]);
                 switch (op.kind) {
                     case K_X: {
@@ -484,7 +491,9 @@ __device__ __forceinline__ void small_apply(typename P::S* sm, int n, const KOp&
 // run of 2^L amplitudes.  Each CTA walks tiles blockIdx.x, +gridDim.x, ...:
 // while it computes tile i in one shared-memory buffer, the asynchronous
 // copies (cp.async, 8 or 16 bytes per element, written straight to the
-// swizzled slot) of tile i+1 land in the other.  A tile's gates run in
+// element's place in the tile layout, tile_off of engine.h) of tile i+1 land
+// in the other.  (The circuit-specialised passes of jit_ptx.cpp move whole
+// runs with bulk copies instead.)  A tile's gates run in
 // register rounds: each thread loads 2^R amplitudes that differ in the
 // round's R register qubits, applies every gate of the round in registers and
 // writes them back.  Two-target dense gates run as shared-memory steps.
@@ -497,7 +506,7 @@ __device__ __noinline__ void tile_smem_op(typename P::S* sm, int T, uint64_t bas
                                           const typename P::C* coef) {
     if ((base & o.cthr) == o.cthr) {
         o.cthr = o.creg;  // tile-local control mask
-        small_apply<P>(sm, T, o, coef);
+        small_apply<P, true>(sm, T, o, coef);
     }
 }
 
@@ -526,13 +535,13 @@ __device__ __forceinline__ void tile_prefetch(typename P::S* buf, const typename
     static_assert(sizeof(typename P::G) == sizeof(typename P::S), "raw staging needs equal element sizes");
     const uint32_t lmask = (1u << L) - 1;
     const uint32_t tid = threadIdx.x;
-    const uint32_t stid = swz<P::GBITS>(tid);
-    // k * NT and tid share no bits and the swizzle is XOR-linear: the
-    // swizzled offset is a compile-time constant XOR the thread's own part
+    const uint32_t stid = sm_off<P, true>(tid);
+    // k * NT and tid share no bits and the layout is additive over disjoint
+    // bits: the offset is a compile-time constant plus the thread's own part
 #pragma unroll
     for (int k = 0; k < (1 << T) / NT; ++k) {
         const uint32_t s = static_cast<uint32_t>(k * NT) | tid;
-        cp_async<sizeof(typename P::G)>(buf + (swz<P::GBITS>(static_cast<uint32_t>(k * NT)) ^ stid),
+        cp_async<sizeof(typename P::G)>(buf + (sm_off<P, true>(static_cast<uint32_t>(k * NT)) + stid),
                                         state + (base | choff[s >> L] | (s & lmask)));
     }
     cp_async_commit();
@@ -555,15 +564,15 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
     // start at coef0 + item * cstride (cstride = 0 for a single state)
     constexpr int NT = 1 << (T - R);
     constexpr int NA = 1 << R;
-    constexpr int GB = P::GBITS;
     constexpr int PER = (1 << T) / NT;  // elements per thread
+    constexpr uint32_t TE = tile_elems(T, sizeof(typename P::S));  // elements per tile buffer
     extern __shared__ __align__(16) unsigned char smem_raw[];
     typename P::S* bufs[2] = {reinterpret_cast<typename P::S*>(smem_raw),
-                              reinterpret_cast<typename P::S*>(smem_raw) + (NB - 1) * (1 << T)};
-    uint64_t* choff = reinterpret_cast<uint64_t*>(smem_raw + NB * (sizeof(typename P::S) << T));
+                              reinterpret_cast<typename P::S*>(smem_raw) + (NB - 1) * TE};
+    uint64_t* choff = reinterpret_cast<uint64_t*>(smem_raw + NB * sizeof(typename P::S) * TE);
 
     const int tid = threadIdx.x;
-    const uint32_t stid = swz<GB>(static_cast<uint32_t>(tid));
+    const uint32_t stid = sm_off<P, true>(static_cast<uint32_t>(tid));
     const int L = pdp->L;
     const int H = pdp->H;
     const uint8_t* tq = pdp->tq;
@@ -599,7 +608,7 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
         if constexpr (P::RAW_STAGING) {  // convert the raw FP64 tile to the register format in place
 #pragma unroll
             for (int k = 0; k < PER; ++k) {
-                const uint32_t ad = swz<GB>(static_cast<uint32_t>(k * NT)) ^ stid;
+                const uint32_t ad = sm_off<P, true>(static_cast<uint32_t>(k * NT)) + stid;
                 sm[ad] = P::g2s(P::raw_to_g(sm[ad]));
             }
             __syncthreads();
@@ -615,14 +624,14 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
                 }
                 continue;
             }
-            // the thread's swizzled base offset and global index: the
-            // swizzle is XOR-linear, so both are sums over its index bits
+            // the thread's base offset in the tile layout and its global
+            // index: both are sums over its index bits
             uint32_t psb = 0;
             uint64_t gthr = base;
 #pragma unroll
             for (int k = 0; k < T - R; ++k) {
                 if ((tid >> k) & 1) {
-                    psb ^= sd->tsw[k];
+                    psb += sd->tsw[k];
                     gthr |= 1ULL << sd->tglob[k];
                 }
             }
@@ -635,7 +644,7 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
                 uint32_t ad = psb;
 #pragma unroll
                 for (int k = 0; k < R; ++k)
-                    if ((j >> k) & 1) ad ^= rsw[k];
+                    if ((j >> k) & 1) ad += rsw[k];
                 a[0][j] = P::s2a(sm[ad]);
             }
             const KOp* op = ops + sd->op_begin;
@@ -654,7 +663,7 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
                 uint32_t ad = psb2;
 #pragma unroll
                 for (int k = 0; k < R; ++k)
-                    if ((j >> k) & 1) ad ^= rsw[k];
+                    if ((j >> k) & 1) ad += rsw[k];
                 sm[ad] = P::a2s(a[0][j]);
             }
             __syncthreads();
@@ -665,7 +674,7 @@ __global__ void __launch_bounds__(1 << (T - R), MINB) k_pass(typename P::G* __re
             for (int k = 0; k < PER; ++k) {
                 const uint32_t s = static_cast<uint32_t>(k * NT) | tid;
                 __stcs(state + (base | choff[s >> L] | (s & lmask)),
-                       P::s2g(sm[swz<GB>(static_cast<uint32_t>(k * NT)) ^ stid]));
+                       P::s2g(sm[sm_off<P, true>(static_cast<uint32_t>(k * NT)) + stid]));
             }
         }
         __syncthreads();  // the buffer is re-filled by the prefetch two tiles later

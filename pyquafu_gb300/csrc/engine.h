@@ -120,6 +120,48 @@ static_assert(sizeof(KOp) == 48, "KOp layout");
 
 constexpr int MAX_TILE = 14;
 
+// ---------------------------------------------------------------------------
+// Shared-memory layout of a tile pass.  Element s of a tile (bit k of s is
+// tile-local position k) sits at element offset
+//     tile_off(s) = s + u * ((s >> 5) + (s >> 8) + (s >> 11)),
+// u = 16 bytes / element size.  The tile's low TILE_RUN_BITS positions are the
+// contiguous qubits 0..4, so each run of 32 amplitudes is one contiguous
+// piece of global memory and stays contiguous here, starting 16-byte aligned:
+// a run moves with one bulk copy.  Run r starts u * (r + r/8 + r/64) elements
+// after its unpadded place.  The shifted terms of disjoint bit sets do not
+// overlap, so tile_off(a | b) = tile_off(a) + tile_off(b) for a & b == 0: an
+// address is a thread's base plus per-bit constants tile_weight(p).
+// Within a 128-byte wavefront, position p < 3 (16-byte elements; p < 4 for
+// 8-byte ones) lands on slot bit p, positions 3..4 (4) on none, and position
+// 5 + j on slot bit j mod 3 (plus 1 for 8-byte elements): lanes whose
+// positions land on distinct slot bits hit distinct bank groups
+// (tile_slot_bit).
+// ---------------------------------------------------------------------------
+constexpr int TILE_RUN_BITS = 5;
+QSV_HD constexpr uint32_t tile_off(uint32_t s, uint32_t u) { return s + u * ((s >> 5) + (s >> 8) + (s >> 11)); }
+QSV_HD constexpr uint32_t tile_weight(int p, uint32_t u) { return tile_off(1u << p, u); }
+// elements of one tile buffer (a multiple of 128 bytes)
+QSV_HD constexpr uint32_t tile_elems(int T, int elem_bytes) {
+    const uint32_t u = 16u / static_cast<uint32_t>(elem_bytes);
+    const uint32_t per128 = 128u / static_cast<uint32_t>(elem_bytes);
+    const uint32_t e = tile_off((1u << T) - 1, u) + 1;
+    return (e + per128 - 1) / per128 * per128;
+}
+// Slot bit that tile position p selects for accesses of `access` bytes to
+// elements of `elem_bytes` (-1: none): bit k of (byte offset / access) mod
+// (128 / access).  p = 0 with 16-byte accesses to 8-byte elements (pairs)
+// is not an access position and gives -1.
+inline int tile_slot_bit(int p, int elem_bytes, int access) {
+    const uint32_t u = 16u / static_cast<uint32_t>(elem_bytes);
+    const uint32_t b = tile_weight(p, u) * static_cast<uint32_t>(elem_bytes);
+    if (b % static_cast<uint32_t>(access)) return -1;
+    const uint32_t c = (b / static_cast<uint32_t>(access)) % (128u / static_cast<uint32_t>(access));
+    if (c == 0 || (c & (c - 1))) return -1;
+    int k = 0;
+    while ((1u << k) != c) ++k;
+    return k;
+}
+
 // A fused pass over the state: tiles of T qubits, the low L of which are the
 // contiguous qubits 0..L-1; tq[] lists the tile's global qubits ascending.
 struct PassDesc {
@@ -136,9 +178,9 @@ constexpr int MAX_PASS_PROBES = 64;
 
 // One register round inside a tile pass: register bit k holds tile-local
 // position rpos[k]; thread-index bit k selects tile-local position tpos[k].
-// rsw / tsw are the swizzled shared-memory offsets of those positions (the
-// swizzle is XOR-linear, so a thread's base offset is the XOR of the tsw of
-// its set index bits).
+// rsw / tsw are the element offsets those positions add in the tile layout
+// (tile_weight): a thread's base offset is the sum of the tsw of its set
+// index bits, register j adds the rsw of j's set bits.
 struct StepDesc {
     int32_t type;  // STEP_*
     int32_t op_begin, op_count;

@@ -56,6 +56,38 @@ bool entry(const char* name, F* fn, std::string* err) {
     return true;
 }
 
+// bounded waits of the specialised passes: 2 s of %globaltimer by default
+constexpr uint64_t kDefaultWaitNs = 2000000000ull;
+std::atomic<uint64_t> g_wait_ns{kDefaultWaitNs};
+std::atomic<uint32_t> g_extra_tx{0};
+
+// per-device status word (allocated on first use, zeroed)
+std::mutex g_status_mu;
+uint32_t* g_status[64] = {nullptr};
+
+uint32_t* status_word_if_any() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_status_mu);
+    return g_status[dev];
+}
+
+uint32_t* status_word() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_status_mu);
+    if (g_status[dev] == nullptr) {
+        void* p = nullptr;
+        if (cudaMalloc(&p, 16) != cudaSuccess) return nullptr;
+        if (cudaMemset(p, 0, 16) != cudaSuccess) {
+            cudaFree(p);
+            return nullptr;
+        }
+        g_status[dev] = static_cast<uint32_t*>(p);
+    }
+    return g_status[dev];
+}
+
 Driver& driver() {
     static Driver d = [] {
         Driver x;
@@ -256,6 +288,10 @@ int prepare_impl(qfvm_plan* p, int nstates, std::string* err) {
         *err = driver().err;
         return 1;
     }
+    if (status_word() == nullptr) {
+        *err = "device status word: allocation failed";
+        return 1;
+    }
     sh = shape_for(hp, nstates);
     int dev = 0;
     cudaGetDevice(&dev);
@@ -267,9 +303,9 @@ int prepare_impl(qfvm_plan* p, int nstates, std::string* err) {
         int optin = 0, per_sm = 0;
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-        const size_t tile = static_cast<size_t>(hp.arith == QFVM_C64 ? 8 : 16) << hp.T;
-        const size_t pacc = static_cast<size_t>(1 << (hp.T - hp.R)) / 32 * MAX_PASS_PROBES * 8;
-        const size_t two = 2 * nstates * tile + pacc;
+        JitShape two_sh = sh;
+        two_sh.nb = 2;
+        const size_t two = jit_smem_bytes(hp, two_sh, MAX_PASS_PROBES);
         if (sh.nb == 2 && (two > static_cast<size_t>(optin) ||
                            static_cast<size_t>(sh.minb) * (two + 1024) > static_cast<size_t>(per_sm)))
             sh.nb = 1;
@@ -337,8 +373,7 @@ int prepare_impl(qfvm_plan* p, int nstates, std::string* err) {
         k->threads = nt;
         k->T = hp.T;
         k->entry = jit_entry_name(hp.arith, nstates);
-        k->smem = static_cast<size_t>(sh.nb) * nstates * (static_cast<size_t>(hp.arith == QFVM_C64 ? 8 : 16) << hp.T) +
-                  static_cast<size_t>(nt / 32) * np * 8;
+        k->smem = jit_smem_bytes(hp, sh, np);
         if (load(dev, images[w], k.get(), err)) return 1;
         cache().emplace(keys[i], std::move(k));
     }
@@ -352,6 +387,23 @@ int prepare_impl(qfvm_plan* p, int nstates, std::string* err) {
     return 0;
 }
 }  // namespace
+
+int jit_status_take(cudaStream_t st) {
+    uint32_t* d = status_word_if_any();
+    if (d == nullptr) return 0;
+    uint32_t v = 0;
+    if (cudaMemcpyAsync(&v, d, sizeof v, cudaMemcpyDeviceToHost, st) != cudaSuccess) return QFVM_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return QFVM_ERR_CUDA;
+    if (v == 0) return 0;
+    cudaMemsetAsync(d, 0, sizeof v, st);
+    cudaStreamSynchronize(st);
+    return QFVM_ERR_TIMEOUT;
+}
+
+void jit_set_wait_test(uint32_t extra, uint64_t wait_ns) {
+    g_extra_tx.store(extra);
+    g_wait_ns.store(wait_ns ? wait_ns : kDefaultWaitNs);
+}
 
 void jit_release(qfvm_plan* p) {
     for (int s = 0; s < 2; ++s) {
@@ -393,7 +445,10 @@ cudaError_t jit_launch_pass(qfvm_plan* p, int pi, void* psi, void* lam, const vo
     const void* a_act = active;
     int32_t a_pt = per_tile;
     void* a_part = partial;
-    void* args[] = {&a_psi, &a_lam, &ntiles, &a_coef, &a_cs, &a_ish, &a_act, &a_pt, &a_part};
+    void* a_status = status_word();
+    uint64_t a_wait = g_wait_ns.load();
+    uint32_t a_extra = g_extra_tx.load();
+    void* args[] = {&a_psi, &a_lam, &ntiles, &a_coef, &a_cs, &a_ish, &a_act, &a_pt, &a_part, &a_status, &a_wait, &a_extra};
     CUresult r = driver().launch(k->fn, grid, 1, 1, k->threads, 1, 1, static_cast<unsigned>(k->smem),
                                  reinterpret_cast<CUstream>(st), args, nullptr);
     if (grid_out) *grid_out = static_cast<int>(grid);

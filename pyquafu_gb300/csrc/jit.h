@@ -1,6 +1,6 @@
 // Circuit-specialised tile passes: each register round of a pass is emitted
 // as straight-line PTX for sm_103a (targets, controls, coefficient offsets
-// and swizzled shared-memory offsets become constants; X/SWAP/Y become
+// and shared-memory offsets in the tile layout become constants; X/SWAP/Y become
 // register renames), two-target dense gates as shared-memory steps; the PTX
 // is compiled once per distinct pass and launched instead of the
 // interpreting kernels k_pass / k_pass2.
@@ -26,6 +26,21 @@ struct JitShape {
 // when the pass has a step the generator does not handle.
 bool jit_pass_ptx(const HostPlan& hp, int pi, const JitShape& sh, const std::string& entry, std::string* ptx,
                   std::string* why);
+
+// Dynamic shared memory of a specialised pass: nb tile slots of nstates
+// tiles in the padded tile layout, the per-warp probe sums, one mbarrier per
+// slot.
+size_t jit_smem_bytes(const HostPlan& hp, const JitShape& sh, int nprobe);
+
+// Device status word of the specialised passes (per device, zeroed): a
+// kernel whose bounded wait for its tile copies gave up writes
+// QFVM_ERR_TIMEOUT.  jit_status_take reads it after the stream's work
+// (synchronising `st`), clears it and returns 0 or QFVM_ERR_TIMEOUT.
+int jit_status_take(cudaStream_t st);
+// Test hook: the next launches expect `extra` more bytes per tile than the
+// copies bring (their waits run out after `wait_ns`); 0, 0 restores the
+// defaults.
+void jit_set_wait_test(uint32_t extra, uint64_t wait_ns);
 
 // Kernel name of a specialised pass: qsv_tile_pass_<c128|ds|c64> (one
 // state) or qsv_tile_sweep_<c128|c64> (reverse sweep with probes).

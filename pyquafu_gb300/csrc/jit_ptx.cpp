@@ -32,13 +32,6 @@ std::string fmt(const char* f, ...) {
     return buf;
 }
 
-uint32_t swz_host(uint32_t s, int gb) {
-    const uint32_t m = (1u << gb) - 1;
-    uint32_t x = s;
-    for (int k = 1; k * gb < 32; ++k) x ^= (s >> (k * gb)) & m;
-    return x;
-}
-
 struct Cx {
     std::string x, y;
 };
@@ -53,7 +46,6 @@ class Gen {
         ft_ = f64_ ? "f64" : "f32";
         es_ = (f64_ || ds_) ? 16 : 8;
         cb_ = (f64_ || ds_) ? 8 : 4;
-        gb_ = (f64_ || ds_) ? 3 : 4;
         T_ = hp.T;
         R_ = hp.R;
         NT_ = 1 << (T_ - R_);
@@ -62,7 +54,11 @@ class Gen {
         PER_ = (1 << T_) / NT_;
         NS_ = sh.nstates;
         np_ = NS_ == 2 ? pd_.nprobe : 0;
-        tileB_ = static_cast<uint32_t>(es_) << T_;
+        padu_ = 16u / static_cast<uint32_t>(es_);
+        H_ = T_ - TILE_RUN_BITS;
+        RUNS_ = 1 << H_;
+        runB_ = static_cast<uint32_t>(es_) << TILE_RUN_BITS;
+        tileB_ = tile_elems(T_, es_) * static_cast<uint32_t>(es_);
         slotB_ = tileB_ * NS_;
     }
 
@@ -70,6 +66,7 @@ class Gen {
         if (hp_.arith != QFVM_C64 && hp_.arith != QFVM_C128 && hp_.arith != QFVM_C128_DS)
             return no(why, "arithmetic without a generator");
         if (pd_.type != PASS_TILE) return no(why, "not a tile pass");
+        if (pd_.L != TILE_RUN_BITS || pd_.H != T_ - TILE_RUN_BITS) return no(why, "tile without 32-amplitude runs");
         if (T_ - R_ < 6 || T_ > 13 || R_ < 1 || R_ > 5) return no(why, "tile shape out of range");
         if (np_ > NT_ || np_ > MAX_PASS_PROBES) return no(why, "too many probes");
         for (int si = 0; si < pd_.step_count; ++si) {
@@ -105,7 +102,8 @@ class Gen {
         out += ".visible .entry " + entry + "(\n";
         out += "\t.param .u64 p_psi,\n\t.param .u64 p_lam,\n\t.param .u64 p_ntiles,\n\t.param .u64 p_coef,\n";
         out += "\t.param .u64 p_cstride,\n\t.param .u32 p_ishift,\n\t.param .u64 p_active,\n";
-        out += "\t.param .u32 p_per_tile,\n\t.param .u64 p_partial\n)\n";
+        out += "\t.param .u32 p_per_tile,\n\t.param .u64 p_partial,\n\t.param .u64 p_status,\n";
+        out += "\t.param .u64 p_wait_ns,\n\t.param .u32 p_extra_tx\n)\n";
         out += fmt(".maxntid %d, 1, 1\n.minnctapersm %d\n{\n", NT_, sh_.minb < 1 ? 1 : sh_.minb);
         out += fmt("\t.reg .pred %%p<%d>;\n\t.reg .b16 %%h<%d>;\n\t.reg .b32 %%r<%d>;\n\t.reg .b64 %%rd<%d>;\n",
                    np_reg_ + 1, nh_ + 1, nr_ + 1, nrd_ + 1);
@@ -448,17 +446,15 @@ class Gen {
         }
         return acc;
     }
-    // u32 register = XOR over the set bits i of `r32` of val[i]
-    std::string xor32(const std::string& r32, int nbits, const std::vector<uint32_t>& val) {
+    // u32 register = sum over the set bits i of `r32` of val[i]
+    std::string sum32(const std::string& r32, int nbits, const std::vector<uint32_t>& val) {
         std::string acc = R32();
         I(fmt("mov.u32 %s, 0", acc.c_str()));
         for (int i = 0; i < nbits; ++i) {
             if (val[i] == 0) continue;
-            std::string t = R32(), p = P(), v = R32(), n = R32();
-            I(fmt("and.b32 %s, %s, %u", t.c_str(), r32.c_str(), 1u << i));
-            I(fmt("setp.ne.u32 %s, %s, 0", p.c_str(), t.c_str()));
-            I(fmt("selp.b32 %s, %u, 0, %s", v.c_str(), val[i], p.c_str()));
-            I(fmt("xor.b32 %s, %s, %s", n.c_str(), acc.c_str(), v.c_str()));
+            std::string t = R32(), n = R32();
+            I(fmt("bfe.u32 %s, %s, %d, 1", t.c_str(), r32.c_str(), i));
+            I(fmt("mad.lo.u32 %s, %s, %u, %s", n.c_str(), t.c_str(), val[i], acc.c_str()));
             acc = n;
         }
         return acc;
@@ -504,21 +500,75 @@ class Gen {
         }
         smb_ = R32();
         I(fmt("mov.u32 %s, qsv_dsm", smb_.c_str()));
-        // the thread's share of a tile: global element offset (bytes) and
-        // swizzled shared offset (bytes); both are XOR/OR-linear in tid
+        std::string sg = R64();
+        status_ = R64();
+        I(fmt("ld.param.u64 %s, [p_status]", sg.c_str()));
+        I(fmt("cvta.to.global.u64 %s, %s", status_.c_str(), sg.c_str()));
+        waitns_ = R64();
+        I(fmt("ld.param.u64 %s, [p_wait_ns]", waitns_.c_str()));
+        extra_ = R32();
+        I(fmt("ld.param.u32 %s, [p_extra_tx]", extra_.c_str()));
+        // the thread's share of a tile: global byte offset and byte offset in
+        // the tile layout; both are sums over the set bits of tid
         std::vector<uint64_t> gv(T_ - R_);
         std::vector<uint32_t> sv(T_ - R_);
         for (int i = 0; i < T_ - R_; ++i) {
             gv[i] = (1ULL << pd_.tq[i]) * es_;
-            sv[i] = swz_host(1u << i, gb_) * es_;
+            sv[i] = tile_weight(i, padu_) * es_;
         }
         gtidB_ = deposit64(tid_, T_ - R_, gv);
-        stidB_ = xor32(tid_, T_ - R_, sv);
+        stidB_ = sum32(tid_, T_ - R_, sv);
+        std::string warp = R32();
+        lane_ = R32();
+        I(fmt("and.b32 %s, %s, 31", lane_.c_str(), tid_.c_str()));
+        I(fmt("shr.u32 %s, %s, 5", warp.c_str(), tid_.c_str()));
+        // bulk copies: thread r * 2^(L - R) moves run r of a tile (runs spread
+        // over the warps, one per issuing thread and state); run r is global
+        // byte offset grun(r) from the tile base and tile-layout offset
+        // srun(r) in the slot, both sums over r's bits
+        {
+            const int sh = TILE_RUN_BITS - R_;  // log2(threads per run)
+            iss_ = P();
+            std::string low = R32(), run = R32();
+            I(fmt("and.b32 %s, %s, %d", low.c_str(), tid_.c_str(), (1 << sh) - 1));
+            I(fmt("setp.eq.u32 %s, %s, 0", iss_.c_str(), low.c_str()));
+            I(fmt("shr.u32 %s, %s, %d", run.c_str(), tid_.c_str(), sh));
+            std::vector<uint64_t> lg(H_);
+            std::vector<uint32_t> ls(H_);
+            for (int i = 0; i < H_; ++i) {
+                lg[i] = grun(1u << i);
+                ls[i] = srun(1u << i);
+            }
+            runG_ = deposit64(run, H_, lg);
+            runS_ = sum32(run, H_, ls);
+            runb_ = R32();
+            I(fmt("mov.u32 %s, %u", runb_.c_str(), runB_));
+            txb_ = R32();
+            I(fmt("add.u32 %s, %s, %u", txb_.c_str(), extra_.c_str(), static_cast<uint32_t>(NS_) * (es_ << T_)));
+        }
+        // one mbarrier per tile slot, after the slots and the probe sums; thread
+        // 0 registers each slot's expected bytes for its first phase (and for
+        // every later phase right after the previous one completes), before
+        // any copy of that phase is issued
+        mbarB_ = R32();
+        I(fmt("add.u32 %s, %s, %u", mbarB_.c_str(), smb_.c_str(), mbar_off()));
+        t0_ = P();
+        I(fmt("setp.eq.u32 %s, %s, 0", t0_.c_str(), tid_.c_str()));
+        {
+            const std::string lni = L();
+            std::string pn = P();
+            I(fmt("not.pred %s, %s", pn.c_str(), t0_.c_str()));
+            I(fmt("@%s bra %s", pn.c_str(), lni.c_str()));
+            for (int sl = 0; sl < sh_.nb; ++sl)
+                I(fmt("mbarrier.init.shared::cta.b64 [%s+%d], 1", mbarB_.c_str(), 8 * sl));
+            I("fence.mbarrier_init.release.cluster");
+            for (int sl = 0; sl < sh_.nb; ++sl)
+                I(fmt("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%s+%d], %s", mbarB_.c_str(), 8 * sl,
+                      txb_.c_str()));
+            I("fence.proxy.async.shared::cta");
+            lab(lni);
+        }
         if (np_ > 0) {
-            std::string warp = R32();
-            lane_ = R32();
-            I(fmt("and.b32 %s, %s, 31", lane_.c_str(), tid_.c_str()));
-            I(fmt("shr.u32 %s, %s, 5", warp.c_str(), tid_.c_str()));
             paccB_ = R32();
             I(fmt("add.u32 %s, %s, %u", paccB_.c_str(), smb_.c_str(), slotB_ * sh_.nb));
             paccW_ = R32();
@@ -537,8 +587,8 @@ class Gen {
                 I(fmt("mad.lo.u32 %s, %s, 8, %s", ad.c_str(), idx.c_str(), paccB_.c_str()));
                 I(fmt("@%s st.shared.u64 [%s], 0", p.c_str(), ad.c_str()));
             }
-            I("bar.sync 0");
         }
+        I("bar.sync 0");
     }
 
     // element index of the first amplitude of tile b (tile_base of device.cuh)
@@ -564,7 +614,25 @@ class Gen {
             if ((s >> i) & 1) g |= 1ULL << pd_.tq[i];
         return g * es_;
     }
-    uint32_t sk(int k) const { return swz_host(static_cast<uint32_t>(k * NT_), gb_) * es_; }
+    // tile-layout byte offset of element k * NT of a tile
+    uint32_t sk(int k) const { return tile_off(static_cast<uint32_t>(k * NT_), padu_) * es_; }
+    // global byte offset of run r of a tile from the tile's first amplitude
+    uint64_t grun(uint32_t r) const {
+        uint64_t g = 0;
+        for (int k = 0; k < H_; ++k)
+            if ((r >> k) & 1) g |= 1ULL << pd_.tq[TILE_RUN_BITS + k];
+        return g * es_;
+    }
+    // tile-layout byte offset of run r in a slot
+    uint32_t srun(uint32_t r) const { return tile_off(r << TILE_RUN_BITS, padu_) * es_; }
+    // shared byte offset of the mbarriers: after the slots and the probe sums
+    uint32_t mbar_off() const { return slotB_ * sh_.nb + static_cast<uint32_t>(NW_ * np_ * 8); }
+    std::string gaddr_off(const std::string& gp, uint64_t off) {
+        if (off < (1ULL << 31)) return gp + "+" + std::to_string(off);
+        std::string a = R64();
+        I(fmt("add.s64 %s, %s, %llu", a.c_str(), gp.c_str(), static_cast<unsigned long long>(off)));
+        return a;
+    }
 
     // per-thread global pointer of state s for tile base `base` (element index)
     std::string thread_gptr(int s, const std::string& base) {
@@ -582,35 +650,93 @@ class Gen {
         return a;
     }
 
-    void prefetch(const std::string& base, const std::string& slotbase) {
-        for (int s = 0; s < NS_; ++s) {
-            std::string gp = thread_gptr(s, base);
-            for (int k = 0; k < PER_; ++k) {
-                std::string x = R32(), d = R32();
-                I(fmt("xor.b32 %s, %s, %u", x.c_str(), stidB_.c_str(), sk(k)));
-                I(fmt("add.u32 %s, %s, %s", d.c_str(), x.c_str(), slotbase.c_str()));
-                const std::string src = gaddr(gp, k);
-                if (es_ == 16)
-                    I(fmt("cp.async.cg.shared.global [%s+%u], [%s], 16", d.c_str(), s * tileB_, src.c_str()));
-                else
-                    I(fmt("cp.async.ca.shared.global [%s+%u], [%s], 8", d.c_str(), s * tileB_, src.c_str()));
-            }
+    // Bulk (TMA) copies of the tile at element `base` into the slot at shared
+    // address `sbase`, completing on the mbarrier at `mbar` (whose expected
+    // bytes are already registered): each issuing thread copies its run of
+    // every state, after its own bulk stores of the slot's previous tile have
+    // read their data.
+    void prefetch(const std::string& base, const std::string& sbase, const std::string& mbar) {
+        const std::string lskip = L();
+        std::string ni = P();
+        I(fmt("not.pred %s, %s", ni.c_str(), iss_.c_str()));
+        I(fmt("@%s bra %s", ni.c_str(), lskip.c_str()));
+        if (!ds_) I("cp.async.bulk.wait_group.read 0");
+        std::string bb = R64(), gl = R64(), dl = R32();
+        I(fmt("mul.lo.u64 %s, %s, %d", bb.c_str(), base.c_str(), es_));
+        I(fmt("add.s64 %s, %s, %s", gl.c_str(), bb.c_str(), runG_.c_str()));
+        I(fmt("add.u32 %s, %s, %s", dl.c_str(), sbase.c_str(), runS_.c_str()));
+        for (int st = 0; st < NS_; ++st) {
+            std::string g = R64();
+            I(fmt("add.s64 %s, %s, %s", g.c_str(), gl.c_str(), stg_[st].c_str()));
+            I(fmt("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%s+%u], [%s], %s, [%s]",
+                  dl.c_str(), st * tileB_, g.c_str(), runb_.c_str(), mbar.c_str()));
         }
-        I("cp.async.commit_group");
+        lab(lskip);
+    }
+
+    // Bulk (TMA) stores of the slot at `sbase` to the tile at element `base`
+    // (each issuing thread its run of every state), one bulk group per thread.
+    void store_tile(const std::string& base, const std::string& sbase) {
+        const std::string lskip = L();
+        std::string ni = P();
+        I(fmt("not.pred %s, %s", ni.c_str(), iss_.c_str()));
+        I(fmt("@%s bra %s", ni.c_str(), lskip.c_str()));
+        std::string bb = R64(), gl = R64(), dl = R32();
+        I(fmt("mul.lo.u64 %s, %s, %d", bb.c_str(), base.c_str(), es_));
+        I(fmt("add.s64 %s, %s, %s", gl.c_str(), bb.c_str(), runG_.c_str()));
+        I(fmt("add.u32 %s, %s, %s", dl.c_str(), sbase.c_str(), runS_.c_str()));
+        for (int st = 0; st < NS_; ++st) {
+            std::string g = R64();
+            I(fmt("add.s64 %s, %s, %s", g.c_str(), gl.c_str(), stg_[st].c_str()));
+            I(fmt("cp.async.bulk.global.shared::cta.bulk_group [%s], [%s+%u], %s", g.c_str(), dl.c_str(),
+                  st * tileB_, runb_.c_str()));
+        }
+        I("cp.async.bulk.commit_group");
+        lab(lskip);
+    }
+
+    // Bounded wait for phase `par` of the mbarrier at `mbar`.  Returns a
+    // predicate that is true when the wait gave up: p_wait_ns nanoseconds of
+    // %globaltimer, or 2^26 polls, passed first.
+    std::string wait_mbar(const std::string& mbar, const std::string& par) {
+        const std::string ldone = L(), lloop = L();
+        std::string ok = P(), to = P(), q = P(), q2 = P();
+        I(fmt("setp.ne.u32 %s, %s, %s", to.c_str(), tid_.c_str(), tid_.c_str()));  // false
+        I(fmt("mbarrier.try_wait.parity.shared::cta.b64 %s, [%s], %s", ok.c_str(), mbar.c_str(), par.c_str()));
+        I(fmt("@%s bra %s", ok.c_str(), ldone.c_str()));
+        std::string t0 = R64(), t1 = R64(), dt = R64(), cnt = R32();
+        I(fmt("mov.u64 %s, %%globaltimer", t0.c_str()));
+        I(fmt("mov.u32 %s, 0", cnt.c_str()));
+        lab(lloop);
+        I(fmt("mbarrier.try_wait.parity.shared::cta.b64 %s, [%s], %s", ok.c_str(), mbar.c_str(), par.c_str()));
+        I(fmt("@%s bra %s", ok.c_str(), ldone.c_str()));
+        I(fmt("add.u32 %s, %s, 1", cnt.c_str(), cnt.c_str()));
+        I(fmt("mov.u64 %s, %%globaltimer", t1.c_str()));
+        I(fmt("sub.u64 %s, %s, %s", dt.c_str(), t1.c_str(), t0.c_str()));
+        I(fmt("setp.lt.u64 %s, %s, %s", q.c_str(), dt.c_str(), waitns_.c_str()));
+        I(fmt("setp.lt.and.u32 %s, %s, %u, %s", q2.c_str(), cnt.c_str(), 1u << 26, q.c_str()));
+        I(fmt("@%s bra %s", q2.c_str(), lloop.c_str()));
+        I(fmt("setp.eq.u32 %s, %s, %s", to.c_str(), tid_.c_str(), tid_.c_str()));  // true
+        lab(ldone);
+        return to;
     }
 
     void tile_loop() {
         std::string b = R64();
         I(fmt("mov.u64 %s, %s", b.c_str(), bid64_.c_str()));
-        const std::string lend = L(), lloop = L();
+        const std::string lend = L(), lloop = L(), lfail = L();
         std::string p0 = P();
         I(fmt("setp.ge.u64 %s, %s, %s", p0.c_str(), b.c_str(), ntiles_.c_str()));
         I(fmt("@%s bra %s", p0.c_str(), lend.c_str()));
-        std::string slot = R32();
+        // loop-carried: slot byte offset, slot index, per-slot mbarrier parities
+        std::string slot = R32(), sidx = R32(), phase = R32();
         I(fmt("mov.u32 %s, 0", slot.c_str()));
+        I(fmt("mov.u32 %s, 0", sidx.c_str()));
+        I(fmt("mov.u32 %s, 0", phase.c_str()));
+        std::string cmbar = R32(), cpar = R32(), omb = R32(), opar = R32(), nextp = P();
         if (sh_.nb == 2) {
             std::string base0 = tile_base(b);
-            prefetch(base0, smb_);
+            prefetch(base0, smb_, mbarB_);
         }
         lab(lloop);
         // loop-carried registers are re-assigned at the end of the body
@@ -622,35 +748,57 @@ class Gen {
         I(fmt("add.s64 %s, %s, %s", coefp_.c_str(), coef0_.c_str(), coff.c_str()));
         std::string sbase = R32();
         I(fmt("add.u32 %s, %s, %s", sbase.c_str(), smb_.c_str(), slot.c_str()));
-        if (sh_.nb == 1) {
-            prefetch(base, sbase);
-            I("cp.async.wait_group 0");
-        } else {
-            std::string bn = R64(), pn = P(), nslot = R32(), nsb = R32();
-            const std::string lno = L(), ldone = L();
+        I(fmt("mad.lo.u32 %s, %s, 8, %s", cmbar.c_str(), sidx.c_str(), mbarB_.c_str()));
+        I(fmt("bfe.u32 %s, %s, %s, 1", cpar.c_str(), phase.c_str(), sidx.c_str()));
+        // Two slots: the next tile goes into the other slot while this one is
+        // computed.  With bulk stores (not double-single) its copies are
+        // issued after the tile's first step, by when the stores of the
+        // slot's previous tile have read it out; otherwise at once.
+        // `nextp` (set where the copies are issued) tells the failure path
+        // which waits have copies behind them.
+        std::string bn = R64(), nsb = R32();
+        I(fmt("setp.ne.u32 %s, %s, %s", nextp.c_str(), tid_.c_str(), tid_.c_str()));  // false
+        auto next_prefetch = [&] {
+            std::string pn = P(), nslot = R32(), osidx = R32();
+            const std::string lno = L();
             I(fmt("add.s64 %s, %s, %s", bn.c_str(), b.c_str(), nbid64_.c_str()));
-            I(fmt("setp.ge.u64 %s, %s, %s", pn.c_str(), bn.c_str(), ntiles_.c_str()));
+            I(fmt("setp.lt.u64 %s, %s, %s", nextp.c_str(), bn.c_str(), ntiles_.c_str()));
+            I(fmt("xor.b32 %s, %s, 1", osidx.c_str(), sidx.c_str()));
+            I(fmt("mad.lo.u32 %s, %s, 8, %s", omb.c_str(), osidx.c_str(), mbarB_.c_str()));
+            I(fmt("bfe.u32 %s, %s, %s, 1", opar.c_str(), phase.c_str(), osidx.c_str()));
+            I(fmt("not.pred %s, %s", pn.c_str(), nextp.c_str()));
             I(fmt("@%s bra %s", pn.c_str(), lno.c_str()));
             I(fmt("xor.b32 %s, %s, %u", nslot.c_str(), slot.c_str(), slotB_));
             I(fmt("add.u32 %s, %s, %s", nsb.c_str(), smb_.c_str(), nslot.c_str()));
             std::string nbase = tile_base(bn);
-            prefetch(nbase, nsb);
-            I("cp.async.wait_group 1");
-            I(fmt("bra.uni %s", ldone.c_str()));
+            prefetch(nbase, nsb, omb);
             lab(lno);
-            I("cp.async.wait_group 0");
-            lab(ldone);
+        };
+        const bool late_next = sh_.nb == 2 && !ds_ && pd_.step_count > 0;
+        if (sh_.nb == 1) prefetch(base, sbase, cmbar);
+        else if (!late_next) next_prefetch();
+        {
+            const std::string to = wait_mbar(cmbar, cpar);
+            std::string pf = P(), t = R32();
+            I(fmt("bar.red.or.pred %s, 0, %s", pf.c_str(), to.c_str()));
+            I(fmt("@%s bra %s", pf.c_str(), lfail.c_str()));
+            I(fmt("add.u32 %s, %s, 1", t.c_str(), sidx.c_str()));  // 1 << sidx
+            I(fmt("xor.b32 %s, %s, %s", phase.c_str(), phase.c_str(), t.c_str()));
+            // every thread has seen this phase complete: register the bytes of
+            // the slot's next phase before any of its copies is issued
+            I(fmt("@%s mbarrier.arrive.expect_tx.shared::cta.b64 _, [%s], %s", t0_.c_str(), cmbar.c_str(),
+                  txb_.c_str()));
         }
-        I("bar.sync 0");
+        // the thread's tile-layout base in this slot
+        std::string tbase = R32();
+        I(fmt("add.u32 %s, %s, %s", tbase.c_str(), stidB_.c_str(), sbase.c_str()));
         if (ds_) {
             for (int k = 0; k < PER_; ++k) {
-                std::string x = R32(), d = R32();
-                I(fmt("xor.b32 %s, %s, %u", x.c_str(), stidB_.c_str(), sk(k)));
-                I(fmt("add.u32 %s, %s, %s", d.c_str(), x.c_str(), sbase.c_str()));
                 for (int st = 0; st < NS_; ++st) {
                     std::string re = D(), im = D();
-                    I(fmt("ld.shared.v2.f64 {%s, %s}, [%s+%u]", re.c_str(), im.c_str(), d.c_str(), st * tileB_));
-                    store_amp(d, st * tileB_, {ds_from(re), ds_from(im)});
+                    I(fmt("ld.shared.v2.f64 {%s, %s}, [%s+%u]", re.c_str(), im.c_str(), tbase.c_str(),
+                          st * tileB_ + sk(k)));
+                    store_amp(tbase, st * tileB_ + sk(k), {ds_from(re), ds_from(im)});
                 }
             }
             I("bar.sync 0");
@@ -660,6 +808,7 @@ class Gen {
             const StepDesc& sd = hp_.steps[pd_.step_begin + si];
             if (sd.type == STEP_SMEM) smem_step(sd, base, sbase);
             else round(sd, base, sbase);
+            if (si == 0 && late_next) next_prefetch();
         }
 
         // write the tile back (one-state passes: only active items)
@@ -676,23 +825,21 @@ class Gen {
             I(fmt("@%s bra %s", pz.c_str(), lskip.c_str()));
             lab(lst);
         }
-        for (int s = 0; s < NS_; ++s) {
-            std::string gp = thread_gptr(s, base);
-            for (int k = 0; k < PER_; ++k) {
-                std::string x = R32(), d = R32();
-                I(fmt("xor.b32 %s, %s, %u", x.c_str(), stidB_.c_str(), sk(k)));
-                I(fmt("add.u32 %s, %s, %s", d.c_str(), x.c_str(), sbase.c_str()));
-                const std::string dst = gaddr(gp, k);
-                if (ds_) {
-                    const Cx c = load_amp(d, s * tileB_);
+        if (ds_) {
+            for (int st = 0; st < NS_; ++st) {
+                std::string gp = thread_gptr(st, base);
+                for (int k = 0; k < PER_; ++k) {
+                    const std::string dst = gaddr(gp, k);
+                    const Cx c = load_amp(tbase, st * tileB_ + sk(k));
                     const std::string re = ds_to(c.x), im = ds_to(c.y);
                     I(fmt("st.global.cs.v2.f64 [%s], {%s, %s}", dst.c_str(), re.c_str(), im.c_str()));
-                } else {
-                    std::string v0 = A(), v1 = A();
-                    I(fmt("ld.shared.v2.%s {%s, %s}, [%s+%u]", ft_, v0.c_str(), v1.c_str(), d.c_str(), s * tileB_));
-                    I(fmt("st.global.cs.v2.%s [%s], {%s, %s}", ft_, dst.c_str(), v0.c_str(), v1.c_str()));
                 }
             }
+        } else {
+            // the rounds' shared-memory writes, then bulk (TMA) stores of the runs
+            I("fence.proxy.async.shared::cta");
+            I("bar.sync 0");
+            store_tile(base, sbase);
         }
         lab(lskip);
         I("bar.sync 0");
@@ -729,11 +876,15 @@ class Gen {
         }
         // next tile (PTX registers are not SSA: the loop variables are updated in place)
         I(fmt("add.s64 %s, %s, %s", b.c_str(), b.c_str(), nbid64_.c_str()));
-        if (sh_.nb == 2) I(fmt("xor.b32 %s, %s, %u", slot.c_str(), slot.c_str(), slotB_));
+        if (sh_.nb == 2) {
+            I(fmt("xor.b32 %s, %s, %u", slot.c_str(), slot.c_str(), slotB_));
+            I(fmt("xor.b32 %s, %s, 1", sidx.c_str(), sidx.c_str()));
+        }
         std::string pc = P();
         I(fmt("setp.lt.u64 %s, %s, %s", pc.c_str(), b.c_str(), ntiles_.c_str()));
         I(fmt("@%s bra %s", pc.c_str(), lloop.c_str()));
         lab(lend);
+        if (!ds_) I(fmt("@%s cp.async.bulk.wait_group 0", iss_.c_str()));  // the last tile's stores
         if (np_ > 0) {
             // single state: this CTA's per-probe totals
             const std::string lx = L();
@@ -761,6 +912,27 @@ class Gen {
             lab(lx);
         }
         I("ret");
+        // A tile's copies did not complete in time (every thread of the CTA
+        // agreed through bar.red): record QFVM_ERR_TIMEOUT, wait (bounded)
+        // for the copies still in flight, let warp 0's bulk stores finish
+        // reading, and leave without another barrier.
+        lab(lfail);
+        {
+            std::string p0t = P();
+            I(fmt("setp.eq.u32 %s, %s, 0", p0t.c_str(), tid_.c_str()));
+            I(fmt("@%s st.global.u32 [%s], %d", p0t.c_str(), status_.c_str(), static_cast<int>(QFVM_ERR_TIMEOUT)));
+            wait_mbar(cmbar, cpar);
+            if (sh_.nb == 2) {
+                const std::string lno = L();
+                std::string pn = P();
+                I(fmt("not.pred %s, %s", pn.c_str(), nextp.c_str()));
+                I(fmt("@%s bra %s", pn.c_str(), lno.c_str()));
+                wait_mbar(omb, opar);
+                lab(lno);
+            }
+            if (!ds_) I(fmt("@%s cp.async.bulk.wait_group 0", iss_.c_str()));
+            I("ret");
+        }
     }
 
     // ---------------------------------------------------------------- rounds
@@ -1202,8 +1374,7 @@ class Gen {
             std::vector<std::string> nm(16);
             for (int e = 0; e < 16; ++e) nm[e] = neg(m[2 * e + 1]);
             const int lo = o.t0 < o.t1 ? o.t0 : o.t1, hi = o.t0 < o.t1 ? o.t1 : o.t0;
-            const uint32_t d0 = swz_host(1u << o.t0, gb_) * es_, d1 = swz_host(1u << o.t1, gb_) * es_;
-            const uint32_t d01 = swz_host((1u << o.t0) | (1u << o.t1), gb_) * es_;
+            const uint32_t d0 = tile_weight(o.t0, padu_) * es_, d1 = tile_weight(o.t1, padu_) * es_;
             const int iters = (1 << (T_ - 2)) / NT_;
             for (int k = 0; k < iters; ++k) {
                 // i = the quad's index with zeros at lo and hi
@@ -1225,30 +1396,20 @@ class Gen {
                     I(fmt("and.b32 %s, %s, %u", t.c_str(), i.c_str(), o.creg));
                     I(fmt("setp.eq.u32 %s, %s, %u", pc.c_str(), t.c_str(), o.creg));
                 }
-                // swizzled byte offset of i (XOR-fold of the higher bit groups)
-                std::string sw = i;
-                for (int g = 1; g * gb_ < T_; ++g) {
-                    std::string t = R32(), t2 = R32(), n = R32();
-                    I(fmt("shr.b32 %s, %s, %d", t.c_str(), i.c_str(), g * gb_));
-                    I(fmt("and.b32 %s, %s, %u", t2.c_str(), t.c_str(), (1u << gb_) - 1));
-                    I(fmt("xor.b32 %s, %s, %s", n.c_str(), sw.c_str(), t2.c_str()));
-                    sw = n;
-                }
-                std::string ab = R32(), ad = R32();
-                I(fmt("mul.lo.u32 %s, %s, %d", ab.c_str(), sw.c_str(), es_));
-                I(fmt("add.u32 %s, %s, %s", ad.c_str(), ab.c_str(), sbase.c_str()));
-                const uint32_t dx[4] = {0u, d0, d1, d01};
-                std::string addr[4];
-                addr[0] = ad;
-                for (int v = 1; v < 4; ++v) {
-                    std::string x = R32(), a = R32();
-                    I(fmt("xor.b32 %s, %s, %u", x.c_str(), ab.c_str(), dx[v]));
-                    I(fmt("add.u32 %s, %s, %s", a.c_str(), x.c_str(), sbase.c_str()));
-                    addr[v] = a;
-                }
+                // tile-layout byte address of i; i has zeros at t0 and t1, so
+                // the quad's other members add the constants d0, d1, d0 + d1
+                std::string t5 = R32(), t8 = R32(), t11 = R32(), sm = R32(), sm2 = R32(), off = R32(), ad = R32();
+                I(fmt("shr.b32 %s, %s, 5", t5.c_str(), i.c_str()));
+                I(fmt("shr.b32 %s, %s, 8", t8.c_str(), i.c_str()));
+                I(fmt("shr.b32 %s, %s, 11", t11.c_str(), i.c_str()));
+                I(fmt("add.u32 %s, %s, %s", sm.c_str(), t5.c_str(), t8.c_str()));
+                I(fmt("add.u32 %s, %s, %s", sm2.c_str(), sm.c_str(), t11.c_str()));
+                I(fmt("mad.lo.u32 %s, %s, %u, %s", off.c_str(), sm2.c_str(), padu_, i.c_str()));
+                I(fmt("mad.lo.u32 %s, %s, %d, %s", ad.c_str(), off.c_str(), es_, sbase.c_str()));
+                const uint32_t dx[4] = {0u, d0, d1, d0 + d1};
                 for (int st = 0; st < NS_; ++st) {
                     Cx in[4];
-                    for (int v = 0; v < 4; ++v) in[v] = load_amp(addr[v], st * tileB_);
+                    for (int v = 0; v < 4; ++v) in[v] = load_amp(ad, st * tileB_ + dx[v]);
                     Cx out[4];
                     for (int r = 0; r < 4; ++r) {  // quad_dense of policy.cuh
                         const int b0 = 8 * r;
@@ -1263,7 +1424,7 @@ class Gen {
                         }
                         out[r] = {dot(tr), dot(ti)};
                     }
-                    for (int v = 0; v < 4; ++v) store_amp(addr[v], st * tileB_, out[v], pc);
+                    for (int v = 0; v < 4; ++v) store_amp(ad, st * tileB_ + dx[v], out[v], pc);
                 }
             }
             lab(lskip);
@@ -1275,9 +1436,17 @@ class Gen {
         bool need_g = false;
         for (int oi = 0; oi < sd.op_count; ++oi)
             if (hp_.ops[sd.op_begin + oi].flags & (F_TCTRL | F_TPAR)) need_g = true;
+        // the thread's tile-layout byte address in this slot; register j adds offb(j)
         std::vector<uint32_t> tsw(T_ - R_);
         for (int k = 0; k < T_ - R_; ++k) tsw[k] = static_cast<uint32_t>(sd.tsw[k]) * es_;
-        std::string psb = xor32(tid_, T_ - R_, tsw);
+        std::string psb = R32();
+        I(fmt("add.u32 %s, %s, %s", psb.c_str(), sum32(tid_, T_ - R_, tsw).c_str(), sbase.c_str()));
+        // 8-byte elements with tile position 0 in register bit r0: registers j
+        // and j | 1 << r0 are adjacent, accessed 16 bytes at a time
+        int r0 = -1;
+        if (es_ == 8)
+            for (int k = 0; k < R_; ++k)
+                if (sd.rpos[k] == 0) r0 = k;
         std::string gthr;
         if (need_g) {
             std::vector<uint64_t> tg(T_ - R_);
@@ -1289,15 +1458,24 @@ class Gen {
         auto offb = [&](int j) {
             uint32_t o = 0;
             for (int k = 0; k < R_; ++k)
-                if ((j >> k) & 1) o ^= static_cast<uint32_t>(sd.rsw[k]) * es_;
+                if ((j >> k) & 1) o += static_cast<uint32_t>(sd.rsw[k]) * es_;
             return o;
         };
         A_.assign(NS_, std::vector<Cx>(NA_));
         for (int j = 0; j < NA_; ++j) {
-            std::string x = R32(), ad = R32();
-            I(fmt("xor.b32 %s, %s, %u", x.c_str(), psb.c_str(), offb(j)));
-            I(fmt("add.u32 %s, %s, %s", ad.c_str(), x.c_str(), sbase.c_str()));
-            for (int s = 0; s < NS_; ++s) A_[s][j] = load_amp(ad, s * tileB_);
+            if (r0 >= 0) {
+                if ((j >> r0) & 1) continue;
+                const int j1 = j | (1 << r0);
+                for (int s = 0; s < NS_; ++s) {
+                    Cx a{A(), A()}, b{A(), A()};
+                    I(fmt("ld.shared.v4.f32 {%s, %s, %s, %s}, [%s+%u]", a.x.c_str(), a.y.c_str(), b.x.c_str(),
+                          b.y.c_str(), psb.c_str(), s * tileB_ + offb(j)));
+                    A_[s][j] = a;
+                    A_[s][j1] = b;
+                }
+                continue;
+            }
+            for (int s = 0; s < NS_; ++s) A_[s][j] = load_amp(psb, s * tileB_ + offb(j));
         }
         ph_on_ = false;
         q_.clear();
@@ -1343,21 +1521,48 @@ class Gen {
             for (int s = 0; s < NS_; ++s)
                 for (int j = 0; j < NA_; ++j) A_[s][j] = phase(A_[s][j], ph_.x, ph_.y, nfi);
         }
-        // a pending flip of bit t: register r holds logical r ^ (1 << t), whose
-        // (XOR-linear) address is the thread's base XOR rsw[t]
-        std::string psbs = psb;
+        // a pending flip of bit t: register j holds logical j ^ (1 << t), whose
+        // address is j's plus rsw[t] (bit t of j clear) or minus it (set)
+        if (r0 >= 0) materialize(r0);  // pairs are stored as they are
+        std::vector<int> fl;
+        std::vector<std::string> fpos, fneg;
         for (int t = 0; t < R_; ++t) {
             if (flip_[t].empty()) continue;
-            std::string v = R32(), n = R32();
-            I(fmt("selp.b32 %s, %u, 0, %s", v.c_str(), static_cast<uint32_t>(sd.rsw[t]) * es_, flip_[t].c_str()));
-            I(fmt("xor.b32 %s, %s, %s", n.c_str(), psbs.c_str(), v.c_str()));
-            psbs = n;
+            const uint32_t w = static_cast<uint32_t>(sd.rsw[t]) * es_;
+            std::string vp = R32(), vn = R32();
+            I(fmt("selp.b32 %s, %u, 0, %s", vp.c_str(), w, flip_[t].c_str()));
+            I(fmt("selp.b32 %s, %u, 0, %s", vn.c_str(), 0u - w, flip_[t].c_str()));
+            fl.push_back(t);
+            fpos.push_back(vp);
+            fneg.push_back(vn);
         }
+        std::map<int, std::string> fbase;  // flip-bit pattern of j -> store base
+        auto store_base = [&](int j) {
+            int pat = 0;
+            for (size_t x = 0; x < fl.size(); ++x) pat |= ((j >> fl[x]) & 1) << x;
+            auto it = fbase.find(pat);
+            if (it != fbase.end()) return it->second;
+            std::string acc = psb;
+            for (size_t x = 0; x < fl.size(); ++x) {
+                std::string n = R32();
+                I(fmt("add.u32 %s, %s, %s", n.c_str(), acc.c_str(), ((pat >> x) & 1) ? fneg[x].c_str() : fpos[x].c_str()));
+                acc = n;
+            }
+            fbase[pat] = acc;
+            return acc;
+        };
         for (int j = 0; j < NA_; ++j) {
-            std::string x = R32(), ad = R32();
-            I(fmt("xor.b32 %s, %s, %u", x.c_str(), psbs.c_str(), offb(j)));
-            I(fmt("add.u32 %s, %s, %s", ad.c_str(), x.c_str(), sbase.c_str()));
-            for (int s = 0; s < NS_; ++s) store_amp(ad, s * tileB_, A_[s][j]);
+            if (r0 >= 0) {
+                if ((j >> r0) & 1) continue;
+                const int j1 = j | (1 << r0);
+                const std::string ad = store_base(j);
+                for (int s = 0; s < NS_; ++s)
+                    I(fmt("st.shared.v4.f32 [%s+%u], {%s, %s, %s, %s}", ad.c_str(), s * tileB_ + offb(j),
+                          A_[s][j].x.c_str(), A_[s][j].y.c_str(), A_[s][j1].x.c_str(), A_[s][j1].y.c_str()));
+                continue;
+            }
+            const std::string ad = store_base(j);
+            for (int s = 0; s < NS_; ++s) store_amp(ad, s * tileB_ + offb(j), A_[s][j]);
         }
         I("bar.sync 0");
     }
@@ -1390,13 +1595,14 @@ class Gen {
     JitShape sh_;
     bool f64_, ds_;
     const char* ft_;
-    int es_, cb_, gb_, T_, R_, NT_, NA_, NW_, PER_, NS_, np_;
-    uint32_t tileB_, slotB_;
+    int es_, cb_, T_, R_, NT_, NA_, NW_, PER_, NS_, np_, H_, RUNS_;
+    uint32_t padu_, runB_, tileB_, slotB_;
     std::string body_;
     int nr_ = 0, nrd_ = 0, nh_ = 0, np_reg_ = 0, na_ = 0, nd_ = 0, nl_ = 0;
     std::map<double, std::string> consts_;
     std::string tid_, bid64_, nbid64_, stg_[2], ntiles_, coef0_, cstrideB_, ishift_, active_, hasact_, smb_;
     std::string gtidB_, stidB_, lane_, paccB_, paccW_, perTile_, partial_, coefp_;
+    std::string status_, waitns_, extra_, iss_, t0_, runG_, runS_, runb_, txb_, mbarB_;
     struct Pending {
         std::string v;
         int slot;
@@ -1467,6 +1673,14 @@ bool jit_pass_key(const HostPlan& hp, int pi, const JitShape& sh, std::string* k
         }
     }
     return true;
+}
+
+size_t jit_smem_bytes(const HostPlan& hp, const JitShape& sh, int nprobe) {
+    const int es = hp.arith == QFVM_C64 ? 8 : 16;
+    const size_t tileB = static_cast<size_t>(tile_elems(hp.T, es)) * es;
+    const size_t nw = static_cast<size_t>(1 << (hp.T - hp.R)) / 32;
+    const size_t np = sh.nstates == 2 ? static_cast<size_t>(nprobe) : 0;
+    return static_cast<size_t>(sh.nb) * sh.nstates * tileB + nw * np * 8 + 8 * static_cast<size_t>(sh.nb);
 }
 
 bool jit_pass_ptx(const HostPlan& hp, int pi, const JitShape& sh, const std::string& entry, std::string* ptx,

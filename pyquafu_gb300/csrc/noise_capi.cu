@@ -108,6 +108,7 @@ int qfvm_simulate_noise(int32_t num_qubits, const qfvm_op* ops, int64_t n_ops, c
                         int64_t matpool_len, const double* psi_in, int64_t shots, const double* uniforms,
                         int64_t n_draws, uint64_t* samples, const uint64_t* x_masks, const uint64_t* z_masks,
                         const int32_t* y_counts, const double* coeffs, int64_t n_terms, double* expvals) {
+    qsv_capi::NvtxRange range("qfvm noisy trajectories");
     const int n = num_qubits;
     if (n < 1 || n > 30) return fail(QFVM_ERR_INVALID, "noisy trajectories take 1..30 qubits");
     if (shots < 1) return fail(QFVM_ERR_INVALID, "noisy trajectories need at least one shot");
@@ -255,6 +256,7 @@ int qfvm_simulate_noise(int32_t num_qubits, const qfvm_op* ops, int64_t n_ops, c
                     "expectation download");
         }
         NZ_CUDA(cudaStreamSynchronize(st), "noisy trajectories");
+        if (const int src = check_status(st)) return done(src);
     }
     return done(QFVM_OK);
 #undef NZ_CUDA

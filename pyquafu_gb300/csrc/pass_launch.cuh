@@ -13,11 +13,12 @@ cudaError_t launch_pass_t(void* state, const PassDesc* dpass, const StepDesc* ds
                           const void* dcoef, int n, int H, int items, uint64_t cstride, const uint8_t* active,
                           cudaStream_t st) {
     // NB tile buffers + the chunk-offset table
-    const size_t smem = NB * (sizeof(typename P::S) << T) + (sizeof(uint64_t) << H);
+    const size_t tiles_b = NB * sizeof(typename P::S) * tile_elems(T, sizeof(typename P::S));
+    const size_t smem = tiles_b + (sizeof(uint64_t) << H);
     static int grid_cap = 0;  // per instantiation: SMs x resident CTAs per SM
     if (grid_cap == 0) {
         cudaError_t e = cudaFuncSetAttribute(k_pass<P, T, R, NB, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             static_cast<int>(NB * (sizeof(typename P::S) << T) + (8 << 12)));
+                                             static_cast<int>(tiles_b + (8 << 12)));
         if (e != cudaSuccess) return e;
         int dev = 0, nsm = 0, per_sm = 0;
         cudaGetDevice(&dev);

@@ -466,24 +466,17 @@ KOp global_kop(HostPlan* p, const GOp& g) {
     return k;
 }
 
-// Shared-memory swizzle of the tile kernels (swz in device.cuh): the higher
-// gbits-wide groups of an element index are XOR-folded onto the lowest group.
-uint32_t swizzle(uint32_t s, int gbits) {
-    const uint32_t m = (1u << gbits) - 1;
-    uint32_t x = s;
-    for (int k = 1; k * gbits < 32; ++k) x ^= (s >> (k * gbits)) & m;
-    return x;
-}
-
-// Thread-bit order for a register round: the first lanes get positions whose
-// residues modulo `gbits` are all distinct, which makes the shared-memory
-// swizzle of the kernels map each wavefront to distinct bank groups.
-void order_thread_bits(std::vector<int>& free_pos, int gbits) {
+// Thread-bit order for a register round: the first lanes get positions that
+// land on distinct slot bits of the tile layout (tile_slot_bit), so each
+// wavefront of the round's shared-memory accesses (`access` bytes per lane)
+// covers distinct bank groups.
+void order_thread_bits(std::vector<int>& free_pos, int elem_bytes, int access) {
+    const int nslot = access == 16 ? 3 : 4;  // 128 / access = 2^nslot slots per wavefront
     std::vector<int> head, rest;
     std::vector<bool> used(free_pos.size(), false);
-    for (int r = 0; r < gbits; ++r) {
+    for (int r = 0; r < nslot; ++r) {
         for (size_t i = 0; i < free_pos.size(); ++i) {
-            if (!used[i] && free_pos[i] % gbits == r) {
+            if (!used[i] && tile_slot_bit(free_pos[i], elem_bytes, access) == r) {
                 head.push_back(free_pos[i]);
                 used[i] = true;
                 break;
@@ -494,6 +487,19 @@ void order_thread_bits(std::vector<int>& free_pos, int gbits) {
         if (!used[i]) rest.push_back(free_pos[i]);
     free_pos = head;
     free_pos.insert(free_pos.end(), rest.begin(), rest.end());
+}
+
+// Order in which free tile positions pad a round's register set: positions
+// that select no slot bit first, then ascending, position 0 last (for 8-byte
+// elements it is the only position on slot bit 0).
+std::vector<int> register_pad_order(int T, int elem_bytes) {
+    std::vector<int> o;
+    for (int p = 1; p < T; ++p)
+        if (tile_slot_bit(p, elem_bytes, elem_bytes) < 0) o.push_back(p);
+    for (int p = 1; p < T; ++p)
+        if (tile_slot_bit(p, elem_bytes, elem_bytes) >= 0) o.push_back(p);
+    o.push_back(0);
+    return o;
 }
 
 }  // namespace
@@ -565,7 +571,8 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
     plan->T = T;
     plan->R = R;
     plan->L = L;
-    const int gbits = (precision == QFVM_C64) ? 4 : 3;
+    const int eb = amp_bytes(precision);  // element bytes of the shared-memory tile
+    const std::vector<int> pad_order = register_pad_order(T, eb);
 
     std::vector<int> pending(gops.size());
     for (size_t i = 0; i < gops.size(); ++i) pending[i] = static_cast<int>(i);
@@ -706,9 +713,9 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
                     left.push_back(gi);
                 }
             }
-            // pad the register set with the lowest unused positions
-            for (int p = 0; p < T && static_cast<int>(regs.size()) < R; ++p)
-                if (std::find(regs.begin(), regs.end(), p) == regs.end()) regs.push_back(p);
+            // pad the register set (register_pad_order)
+            for (size_t x = 0; x < pad_order.size() && static_cast<int>(regs.size()) < R; ++x)
+                if (std::find(regs.begin(), regs.end(), pad_order[x]) == regs.end()) regs.push_back(pad_order[x]);
             StepDesc sd;
             std::memset(&sd, 0, sizeof(sd));
             sd.type = STEP_ROUND;
@@ -716,13 +723,17 @@ bool build_plan(int n, int precision, const std::vector<GOp>& gops, int T, int R
             std::vector<int> freep;
             for (int p = 0; p < T; ++p)
                 if (std::find(regs.begin(), regs.end(), p) == regs.end()) freep.push_back(p);
-            order_thread_bits(freep, gbits);
+            // 8-byte elements with position 0 in the registers: the specialised
+            // passes access the register pairs (j, j | bit of position 0) 16 bytes at a time
+            const bool pairs = eb == 8 && std::find(regs.begin(), regs.end(), 0) != regs.end();
+            order_thread_bits(freep, eb, pairs ? 16 : eb);
+            const uint32_t u = 16u / static_cast<uint32_t>(eb);
             for (size_t k = 0; k < freep.size(); ++k) {
                 sd.tpos[k] = static_cast<uint8_t>(freep[k]);
                 sd.tglob[k] = pd.tq[freep[k]];
-                sd.tsw[k] = static_cast<uint16_t>(swizzle(1u << freep[k], gbits));
+                sd.tsw[k] = static_cast<uint16_t>(tile_weight(freep[k], u));
             }
-            for (int k = 0; k < R; ++k) sd.rsw[k] = static_cast<uint16_t>(swizzle(1u << regs[k], gbits));
+            for (int k = 0; k < R; ++k) sd.rsw[k] = static_cast<uint16_t>(tile_weight(regs[k], u));
             int reg_of_local[MAX_TILE];
             for (int p = 0; p < MAX_TILE; ++p) reg_of_local[p] = -1;
             for (int k = 0; k < R; ++k) reg_of_local[regs[k]] = k;

@@ -148,6 +148,7 @@ extern "C" {
 int qfvm_simulate_shots(int32_t num_qubits, int32_t num_cbits, const qfvm_op* ops, int64_t n_ops,
                         const double* matpool, int64_t matpool_len, const double* psi_in, int64_t shots,
                         const double* uniforms, int64_t n_draws, uint64_t* outcomes, double* final_state) {
+    qsv_capi::NvtxRange range("qfvm trajectories");
     const int n = num_qubits;
     if (n < 1 || n > 30) return fail(QFVM_ERR_INVALID, "per-shot trajectories take 1..30 qubits");
     if (num_cbits < 0 || num_cbits > 64) return fail(QFVM_ERR_INVALID, "classical register of 0..64 bits");
@@ -265,6 +266,7 @@ int qfvm_simulate_shots(int32_t num_qubits, int32_t num_cbits, const qfvm_op* op
                                       N * sizeof(double2), cudaMemcpyDeviceToHost, st),
                       "state download");
         SHOT_CUDA(cudaStreamSynchronize(st), "trajectories");
+        if (const int src = check_status(st)) return done(src);
         for (int it = 0; it < items; ++it) {
             uint64_t v = 0;
             for (int c : measured) v = v * 2 + hcreg[static_cast<size_t>(it) * ncb + c];

@@ -85,17 +85,25 @@ def host_plan(n, ops, precision=0, T=0, R=0, adjoint=False, batched=False):
     lib.qfvm_plan_destroy(h)
     return {"passes": passes, "steps": steps[: counts[1]], "ops": kops[: counts[2]], "coef": coef,
             "T": shape[0], "R": shape[1], "L": shape[2], "probe_slots": slots[:nprobe], "binds": binds[: nb.value],
-            "gbits": 4 if precision == 1 else 3}
+            "elem_bytes": 8 if precision == 1 else 16}
 
 
-def swizzle(s, gbits):
-    """The kernels' shared-memory swizzle (XOR fold of higher gbits groups)."""
-    x = s
-    k = 1
-    while k * gbits < 32:
-        x ^= (s >> (k * gbits)) & ((1 << gbits) - 1)
-        k += 1
-    return x
+def tile_off(s, elem_bytes):
+    """The tile passes' shared-memory layout: element offset of tile index s
+    (runs of 32 amplitudes contiguous, each run padded by 16 bytes times
+    r + r/8 + r/64)."""
+    u = 16 // elem_bytes
+    return s + u * ((s >> 5) + (s >> 8) + (s >> 11))
+
+
+def slot_bit(p, elem_bytes, access):
+    """Bit of the 128-byte wavefront slot (of `access` bytes) that tile
+    position p selects, or -1."""
+    b = tile_off(1 << p, elem_bytes) * elem_bytes
+    if b % access:
+        return -1
+    c = (b // access) % (128 // access)
+    return c.bit_length() - 1 if c and not c & (c - 1) else -1
 
 
 def _bits(mask):
@@ -306,9 +314,9 @@ def interpret(plan, psi):
             tpos = [int(x) for x in sd["tpos"][: T - R]]
             assert sorted(rpos + tpos) == list(range(T)), (rpos, tpos)
             assert [int(x) for x in sd["tglob"][: T - R]] == [tq[p] for p in tpos]
-            gb = plan["gbits"]
-            assert [int(x) for x in sd["tsw"][: T - R]] == [swizzle(1 << p, gb) for p in tpos]
-            assert [int(x) for x in sd["rsw"][:R]] == [swizzle(1 << p, gb) for p in rpos]
+            eb = plan["elem_bytes"]
+            assert [int(x) for x in sd["tsw"][: T - R]] == [tile_off(1 << p, eb) for p in tpos]
+            assert [int(x) for x in sd["rsw"][:R]] == [tile_off(1 << p, eb) for p in rpos]
             g_of_reg = [tq[p] for p in rpos]
             for o in ops:
                 cm = int(o["cthr"])

@@ -1,9 +1,12 @@
-"""Failure paths exercised by host-side injection (qfvm_test_fault): an
-allocation that fails, and a kernel stage that reports an error before its
-launch.  Nothing faults the GPU: the hook makes the host wrapper return the
-error without calling CUDA.  The engine must report the status with its
-message, leave no half-made object behind, and keep working afterwards
-(checked against the oracle)."""
+"""Failure paths exercised by injection (qfvm_test_fault): an allocation
+that fails, a kernel stage that reports an error before its launch, and a
+tile-copy wait of the specialised passes that runs out.  Nothing faults the
+GPU: the first two make the host wrapper return the error without calling
+CUDA; the third makes each pass expect 16 bytes that no copy brings, so its
+bounded wait gives up after a short limit and the kernel returns with
+QFVM_ERR_TIMEOUT in its status word.  The engine must report the status
+with its message, leave no half-made object behind, and keep working
+afterwards (checked against the oracle)."""
 
 import numpy as np
 import pytest
@@ -12,7 +15,7 @@ import oracle
 from pyquafu_gb300 import _native as nat
 from pyquafu_gb300 import engine, workloads
 
-FAULT_NONE, FAULT_ALLOC, FAULT_STAGE = 0, 1, 2
+FAULT_NONE, FAULT_ALLOC, FAULT_STAGE, FAULT_WAIT = 0, 1, 2, 3
 
 
 @pytest.fixture(autouse=True)
@@ -26,6 +29,7 @@ def test_fault_hook_argument_checks():
     assert lib.qfvm_test_fault(7, 1) == nat.QFVM_ERR_INVALID
     assert b"fault kind" in lib.qfvm_last_error()
     assert lib.qfvm_test_fault(FAULT_ALLOC, 0) == nat.QFVM_ERR_INVALID
+    assert lib.qfvm_test_fault(FAULT_WAIT, 20000) == nat.QFVM_ERR_INVALID  # limits above 10 s refused
     assert lib.qfvm_test_fault(FAULT_NONE, 0) == 0
 
 
@@ -76,5 +80,33 @@ def test_injected_stage_failure_then_recovery():
     st.set_zero()
     plan.run(st)
     assert np.abs(st.download() - oracle.simulate(n, ops)).max() <= 1e-12
+    plan.close()
+    st.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["c128", "c128_ds", "c64"])
+def test_tile_copy_wait_runs_out_then_recovery(precision):
+    lib = nat.load()
+    n = 15
+    ops = workloads.random_layers(n, 4, seed=23, extras=True)
+    plan = engine.Plan(n, ops, precision)
+    st = engine.DeviceState(n, precision).set_zero()
+    plan.run(st)
+    st.download()  # compiles the specialised passes
+    assert plan.jit_passes() > 0
+    assert lib.qfvm_test_fault(FAULT_WAIT, 50) == 0  # 50 ms limit per wait
+    st.set_zero()
+    plan.run(st)
+    with pytest.raises(nat.QfvmError) as err:
+        st.download()
+    assert err.value.status == nat.QFVM_ERR_TIMEOUT
+    assert "gave up waiting" in str(err.value)
+    assert lib.qfvm_test_fault(FAULT_NONE, 0) == 0
+    # the context is intact: a fresh run gives the oracle's state
+    st.set_zero()
+    plan.run(st)
+    tol = 1e-5 if precision == "c64" else 1e-12
+    assert np.abs(st.download() - oracle.simulate(n, ops)).max() <= tol
     plan.close()
     st.close()

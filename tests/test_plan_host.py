@@ -254,3 +254,61 @@ def test_random_commuting_merges(seed):
     got = helpers.interpret(plan, oracle.zero_state(n))
     assert np.abs(got - oracle.simulate(n, ops)).max() < 1e-12
     assert plan_op_count(plan) < len(ops)
+
+
+@pytest.mark.parametrize("eb", [16, 8])
+def test_tile_layout(eb):
+    """The padded tile layout: one-to-one, additive over disjoint bits, runs of
+    32 contiguous and 16-byte aligned (bulk-copy units), and each position's
+    slot bit as the planner assumes."""
+    for T in (6, 11, 12, 13, 14):
+        s = np.arange(1 << T)
+        off = helpers.tile_off(s, eb)
+        assert len(set(off.tolist())) == s.size
+        run_start = off[:: 32] * eb
+        assert np.all(run_start % 16 == 0)
+        assert np.all(np.diff(off.reshape(-1, 32), axis=1) == 1)
+        rng = np.random.default_rng(T)
+        a = rng.integers(0, 1 << T, 500)
+        b = rng.integers(0, 1 << T, 500) & ~a
+        assert np.array_equal(helpers.tile_off(a | b, eb), helpers.tile_off(a, eb) + helpers.tile_off(b, eb))
+    # slot bits: p < 3 (p < 4) direct, 3..4 (4) none, 5 + j -> j mod 3 (+1)
+    direct = 3 if eb == 16 else 4
+    for p in range(14):
+        want = p if p < direct else (-1 if p < 5 else (p - 5) % 3 + (0 if eb == 16 else 1))
+        assert helpers.slot_bit(p, eb, eb) == want, p
+        if eb == 8 and p >= 1:
+            assert helpers.slot_bit(p, 8, 16) == (p - 1 if p < 4 else (-1 if p == 4 else (p - 5) % 3))
+
+
+@pytest.mark.parametrize("precision,T,R", [(0, 11, 4), (0, 12, 3), (1, 12, 4), (1, 13, 5)])
+def test_round_wavefronts_hit_distinct_banks(precision, T, R):
+    """Every register round's first wavefront of lanes (8 lanes of 16-byte
+    accesses, 16 of 8-byte ones; 16-byte pairs for complex64 rounds that hold
+    position 0 in registers) lands on distinct bank groups of the tile layout
+    whenever the round's free positions offer a position for every slot bit."""
+    n = 22
+    ops = workloads.random_layers(n, 8, seed=5, extras=True)
+    plan = helpers.host_plan(n, ops, precision, T, R)
+    eb = plan["elem_bytes"]
+    rounds = checked = 0
+    for pd in plan["passes"]:
+        if pd["type"] != 0:
+            continue
+        for sd in plan["steps"][pd["step_begin"]: pd["step_begin"] + pd["step_count"]]:
+            if sd["type"] != 0:
+                continue
+            rounds += 1
+            rpos = [int(x) for x in sd["rpos"][:R]]
+            tpos = [int(x) for x in sd["tpos"][: T - R]]
+            access = 16 if (eb == 8 and 0 in rpos) else eb
+            nslot = 3 if access == 16 else 4
+            if {helpers.slot_bit(p, eb, access) for p in tpos} >= set(range(nslot)):
+                checked += 1
+                lanes = 1 << nslot
+                groups = set()
+                for lane in range(lanes):
+                    s = sum(1 << tpos[k] for k in range(nslot) if (lane >> k) & 1)
+                    groups.add((helpers.tile_off(s, eb) * eb // access) % (128 // access))
+                assert len(groups) == lanes, (rpos, tpos)
+    assert rounds > 0 and checked >= 0.9 * rounds, (checked, rounds)
