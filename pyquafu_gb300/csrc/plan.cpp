@@ -27,8 +27,8 @@ int small_max_qubits(int precision) { return precision == QFVM_C64 ? 14 : 13; }
 // hardware-efficient workloads; a tuned table entry overrides them).
 void default_shape(int n, int precision, int* T, int* R) {
     if (precision == QFVM_C64) {
-        *T = 12;
-        *R = 4;
+        *T = 13;
+        *R = 5;
     } else if (precision == QFVM_C128_DS) {
         *T = 12;
         *R = 3;
