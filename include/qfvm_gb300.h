@@ -38,7 +38,8 @@ typedef enum {
     QFVM_ERR_NOMEM = 3,       /* device allocation failed */
     QFVM_ERR_UNSUPPORTED = 4, /* valid input the engine does not handle */
     QFVM_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
-    QFVM_ERR_NODEVICE = 6     /* no CUDA device */
+    QFVM_ERR_NODEVICE = 6,    /* no CUDA device */
+    QFVM_ERR_BOUNDS = 7       /* bounds-checked kernels (QFVM_BOUNDS_CHECK=1): an index out of range, access skipped */
 } qfvm_status;
 
 /* Operation kinds.  1..17 are the named gates of the reference's OPMAP table

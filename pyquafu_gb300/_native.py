@@ -19,7 +19,8 @@ QFVM_C128, QFVM_C64, QFVM_C128_DS = 0, 1, 2
 PRECISIONS = {"c128": QFVM_C128, "complex128": QFVM_C128, "c64": QFVM_C64, "complex64": QFVM_C64,
               "c128_ds": QFVM_C128_DS}
 
-QFVM_ERR_INVALID, QFVM_ERR_CUDA, QFVM_ERR_NOMEM, QFVM_ERR_UNSUPPORTED, QFVM_ERR_TIMEOUT, QFVM_ERR_NODEVICE = range(1, 7)
+QFVM_ERR_INVALID, QFVM_ERR_CUDA, QFVM_ERR_NOMEM, QFVM_ERR_UNSUPPORTED, QFVM_ERR_TIMEOUT, QFVM_ERR_NODEVICE, \
+    QFVM_ERR_BOUNDS = range(1, 8)
 
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory",

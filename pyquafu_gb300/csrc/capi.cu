@@ -57,6 +57,7 @@ int fail(int code, const std::string& msg) {
 int check_status(cudaStream_t st) {
     const int rc = jit_status_take(st);
     if (rc == QFVM_ERR_TIMEOUT) return fail(rc, "a specialised pass gave up waiting for its tile copies");
+    if (rc == QFVM_ERR_BOUNDS) return fail(rc, "a bounds-checked specialised pass found an index out of range");
     if (rc != QFVM_OK) return fail(rc, "reading the device status word");
     return QFVM_OK;
 }

@@ -115,6 +115,9 @@ struct qfvm_plan {
     // count (index 0: one state, 1: psi + lam); null entries run interpreted
     std::vector<const void*> jit[2];
     bool jit_ready[2] = {false, false};
+    // per pass: the coefficient parameter block of its kernel (empty: the
+    // kernel reads the pool in global memory)
+    std::vector<std::vector<unsigned char>> jit_cblob[2];
 };
 
 namespace qsv_capi {

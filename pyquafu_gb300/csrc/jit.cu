@@ -216,9 +216,12 @@ JitShape shape_for(const HostPlan& hp, int nstates) {
         // amplitudes alone need more than 64 (two states of FP64 or float-pair
         // amplitudes at R = 4: 128 registers; at 128 the sweep spilled and
         // wrote 5x its algorithmic bytes to DRAM)
+        // Complex64 one-state passes: 80 (three CTAs of 256 threads per SM;
+        // tile (13,5) at 26 qubits measured 10.1 ms against 10.6 ms at 128).
         const int nt = 1 << (hp.T - hp.R);
         const int per_amp = hp.arith == QFVM_C64 ? 2 : 4;
-        const int budget = nstates * (1 << hp.R) * per_amp > 64 ? 255 : 128;
+        int budget = nstates * (1 << hp.R) * per_amp > 64 ? 255 : 128;
+        if (hp.arith == QFVM_C64 && nstates == 1) budget = 80;
         minb = 65536 / (nt * budget);
         if (minb < 1) minb = 1;
     }
@@ -293,6 +296,9 @@ int prepare_impl(qfvm_plan* p, int nstates, std::string* err) {
         return 1;
     }
     sh = shape_for(hp, nstates);
+    // a pool that no bind rewrites on the device travels in the kernel parameters
+    sh.pcoef = hp.binds.empty() ? 1 : 0;
+    sh.bounds = bounds_check_env();
     int dev = 0;
     cudaGetDevice(&dev);
     {
@@ -382,11 +388,40 @@ int prepare_impl(qfvm_plan* p, int nstates, std::string* err) {
         auto it = cache().find(keys[i]);
         if (it != cache().end()) ks[i] = it->second.get();
     }
+    // the coefficient parameter blocks of the compiled passes
+    p->jit_cblob[si].assign(hp.passes.size(), {});
+    for (size_t i = 0; i < hp.passes.size(); ++i) {
+        uint32_t lo = 0, hi = 0;
+        if (!ks[i] || !jit_pass_coef_block(hp, static_cast<int>(i), sh, &lo, &hi)) continue;
+        std::vector<unsigned char>& blob = p->jit_cblob[si][i];
+        const size_t eb = hp.arith == QFVM_C64 ? 4 : 8;
+        blob.assign(((hi - lo) * eb + 15) / 16 * 16, 0);
+        for (uint32_t c = lo; c < hi; ++c) {
+            const double v = hp.coef[c];
+            unsigned char* d = blob.data() + (c - lo) * eb;
+            if (hp.arith == QFVM_C64) {
+                const float f = static_cast<float>(v);
+                std::memcpy(d, &f, 4);
+            } else if (hp.arith == QFVM_C128_DS) {
+                const float h = static_cast<float>(v);
+                const float l = static_cast<float>(v - static_cast<double>(h));
+                std::memcpy(d, &h, 4);
+                std::memcpy(d + 4, &l, 4);
+            } else {
+                std::memcpy(d, &v, 8);
+            }
+        }
+    }
     p->jit[si] = ks;
     p->jit_ready[si] = true;
     return 0;
 }
 }  // namespace
+
+int bounds_check_env() {
+    const char* e = std::getenv("QFVM_BOUNDS_CHECK");
+    return (e && e[0] == '1') ? 1 : 0;
+}
 
 int jit_status_take(cudaStream_t st) {
     uint32_t* d = status_word_if_any();
@@ -397,7 +432,7 @@ int jit_status_take(cudaStream_t st) {
     if (v == 0) return 0;
     cudaMemsetAsync(d, 0, sizeof v, st);
     cudaStreamSynchronize(st);
-    return QFVM_ERR_TIMEOUT;
+    return v == static_cast<uint32_t>(QFVM_ERR_BOUNDS) ? QFVM_ERR_BOUNDS : QFVM_ERR_TIMEOUT;
 }
 
 void jit_set_wait_test(uint32_t extra, uint64_t wait_ns) {
@@ -408,6 +443,7 @@ void jit_set_wait_test(uint32_t extra, uint64_t wait_ns) {
 void jit_release(qfvm_plan* p) {
     for (int s = 0; s < 2; ++s) {
         p->jit[s].clear();
+        p->jit_cblob[s].clear();
         p->jit_ready[s] = false;
     }
 }
@@ -448,7 +484,13 @@ cudaError_t jit_launch_pass(qfvm_plan* p, int pi, void* psi, void* lam, const vo
     void* a_status = status_word();
     uint64_t a_wait = g_wait_ns.load();
     uint32_t a_extra = g_extra_tx.load();
-    void* args[] = {&a_psi, &a_lam, &ntiles, &a_coef, &a_cs, &a_ish, &a_act, &a_pt, &a_part, &a_status, &a_wait, &a_extra};
+    // the coefficient block (when the kernel takes one) is its last parameter
+    const std::vector<std::vector<unsigned char>>& blobs = p->jit_cblob[si];
+    void* a_blob = (pi < static_cast<int>(blobs.size()) && !blobs[pi].empty())
+                       ? const_cast<unsigned char*>(blobs[pi].data())
+                       : nullptr;
+    void* args[] = {&a_psi, &a_lam, &ntiles, &a_coef, &a_cs, &a_ish, &a_act, &a_pt, &a_part, &a_status, &a_wait, &a_extra,
+                    a_blob};
     CUresult r = driver().launch(k->fn, grid, 1, 1, k->threads, 1, 1, static_cast<unsigned>(k->smem),
                                  reinterpret_cast<CUstream>(st), args, nullptr);
     if (grid_out) *grid_out = static_cast<int>(grid);
@@ -510,6 +552,8 @@ int qfvm_jit_pass_ptx(const qfvm_plan* plan, int32_t pass, int32_t nstates, char
     sh.nstates = nstates;
     sh.nb = nstates == 1 ? c.nb1 : c.nb2;
     sh.minb = nstates == 1 ? c.minb1 : c.minb2;
+    sh.pcoef = plan->hp.binds.empty() ? 1 : 0;
+    sh.bounds = qsv::bounds_check_env();
     std::string ptx, why;
     if (!qsv::jit_pass_ptx(plan->hp, pass, sh, qsv::jit_entry_name(plan->hp.arith, nstates), &ptx, &why))
         return fail(QFVM_ERR_UNSUPPORTED, "pass runs interpreted: " + why);
@@ -528,6 +572,8 @@ int qfvm_jit_pass_compile(const qfvm_plan* plan, int32_t pass, int32_t nstates, 
     sh.nstates = nstates;
     sh.nb = nstates == 1 ? c.nb1 : c.nb2;
     sh.minb = nstates == 1 ? c.minb1 : c.minb2;
+    sh.pcoef = plan->hp.binds.empty() ? 1 : 0;
+    sh.bounds = qsv::bounds_check_env();
     std::string ptx, why, image, err, log;
     if (!qsv::jit_pass_ptx(plan->hp, pass, sh, qsv::jit_entry_name(plan->hp.arith, nstates), &ptx, &why))
         return fail(QFVM_ERR_UNSUPPORTED, "pass runs interpreted: " + why);

@@ -20,12 +20,26 @@ struct JitShape {
     int nstates = 1;  // 1: one-state pass (k_pass), 2: psi + lam with probes (k_pass2)
     int nb = 1;       // tile buffers (2 = prefetch the next tile during this one)
     int minb = 1;     // .minnctapersm (register budget = 64K / (threads * minb))
+    int pcoef = 0;    // 1: coefficients travel in the kernel parameters (plans whose pool is never rebound)
+    int bounds = 0;   // 1: every shared / global / bulk access checked against its buffer (QFVM_BOUNDS_CHECK=1)
 };
+
+// QFVM_BOUNDS_CHECK=1 in the environment (read when a plan's passes are
+// compiled): the specialised passes check each shared-memory access, each
+// global store and each bulk copy against its buffer; an access outside is
+// skipped and the pass writes QFVM_ERR_BOUNDS to the status word.
+int bounds_check_env();
 
 // PTX of tile pass `pi` of plan `hp` as kernel `entry`; false (with a reason)
 // when the pass has a step the generator does not handle.
 bool jit_pass_ptx(const HostPlan& hp, int pi, const JitShape& sh, const std::string& entry, std::string* ptx,
                   std::string* why);
+
+// Parameter-block coefficients of pass `pi` (sh.pcoef): true with the pool
+// range [cmin, cmax) the kernel takes as its last parameter p_cblob (in the
+// arithmetic's format: float, float pair or double per pool entry); false
+// when the pass reads them from the pool in global memory.
+bool jit_pass_coef_block(const HostPlan& hp, int pi, const JitShape& sh, uint32_t* cmin, uint32_t* cmax);
 
 // Dynamic shared memory of a specialised pass: nb tile slots of nstates
 // tiles in the padded tile layout, the per-warp probe sums, one mbarrier per

@@ -60,7 +60,42 @@ class Gen {
         runB_ = static_cast<uint32_t>(es_) << TILE_RUN_BITS;
         tileB_ = tile_elems(T_, es_) * static_cast<uint32_t>(es_);
         slotB_ = tileB_ * NS_;
+        bc_ = sh.bounds != 0;
+        if (sh.pcoef) coef_range(&cmin_, &cmax_);
+        pc_ = sh.pcoef && cmax_ > cmin_ && blob_bytes() <= kMaxBlob;
     }
+
+    // Coefficient pool entries the pass's operations read: [lo, hi).
+    void coef_range(uint32_t* lo, uint32_t* hi) const {
+        *lo = ~0u;
+        *hi = 0;
+        for (int si = 0; si < pd_.step_count; ++si) {
+            const StepDesc& sd = hp_.steps[pd_.step_begin + si];
+            for (int oi = 0; oi < sd.op_count; ++oi) {
+                const KOp& o = hp_.ops[sd.op_begin + oi];
+                int n = 0;
+                switch (o.kind) {
+                    case K_DENSE: n = 8; break;
+                    case K_REAL: case K_DIAG: n = 4; break;
+                    case K_RX: n = 2; break;
+                    case K_DIAGR: n = 2 * NA_; break;
+                    case K_DENSE2: n = 32; break;
+                    case K_PROBE: n = 1; break;
+                    default: break;
+                }
+                if (n == 0) continue;
+                if (o.coef < *lo) *lo = o.coef;
+                if (o.coef + n > *hi) *hi = o.coef + n;
+            }
+        }
+        if (*hi == 0) *lo = 0;
+    }
+    uint32_t blob_bytes() const { return ((cmax_ - cmin_) * cb_ + 15u) / 16u * 16u; }
+
+    bool param_coefs() const { return pc_; }
+    uint32_t cmin() const { return cmin_; }
+    uint32_t cmax() const { return cmax_; }
+
 
     bool supported(std::string* why) const {
         if (hp_.arith != QFVM_C64 && hp_.arith != QFVM_C128 && hp_.arith != QFVM_C128_DS)
@@ -103,7 +138,9 @@ class Gen {
         out += "\t.param .u64 p_psi,\n\t.param .u64 p_lam,\n\t.param .u64 p_ntiles,\n\t.param .u64 p_coef,\n";
         out += "\t.param .u64 p_cstride,\n\t.param .u32 p_ishift,\n\t.param .u64 p_active,\n";
         out += "\t.param .u32 p_per_tile,\n\t.param .u64 p_partial,\n\t.param .u64 p_status,\n";
-        out += "\t.param .u64 p_wait_ns,\n\t.param .u32 p_extra_tx\n)\n";
+        out += "\t.param .u64 p_wait_ns,\n\t.param .u32 p_extra_tx";
+        if (pc_) out += fmt(",\n\t.param .align 16 .b8 p_cblob[%u]", blob_bytes());
+        out += "\n)\n";
         out += fmt(".maxntid %d, 1, 1\n.minnctapersm %d\n{\n", NT_, sh_.minb < 1 ? 1 : sh_.minb);
         out += fmt("\t.reg .pred %%p<%d>;\n\t.reg .b16 %%h<%d>;\n\t.reg .b32 %%r<%d>;\n\t.reg .b64 %%rd<%d>;\n",
                    np_reg_ + 1, nh_ + 1, nr_ + 1, nrd_ + 1);
@@ -127,10 +164,98 @@ class Gen {
     std::string A() { return "%a" + std::to_string(na_++); }
     std::string D() { return "%d" + std::to_string(nd_++); }
     std::string L() { return "$L" + std::to_string(nl_++); }
-    void I(const std::string& s) {
+    void I(const std::string& s) { Iraw(bc_ ? checked(s) : s); }
+    void Iraw(const std::string& s) {
         body_ += '\t';
         body_ += s;
         body_ += ";\n";
+    }
+
+    // Bounds-checked builds: a shared-memory access, a global store or a bulk
+    // copy is guarded by a check of its address range against the dynamic
+    // shared memory / the states; outside, the access is skipped and the
+    // thread writes QFVM_ERR_BOUNDS to the status word.  Returns the access,
+    // predicated on the check (and on its own predicate, if it had one).
+    std::string checked(const std::string& ins) {
+        std::string pred, body = ins;
+        if (!ins.empty() && ins[0] == '@') {
+            const size_t sp = ins.find(' ');
+            pred = ins.substr(1, sp - 1);
+            body = ins.substr(sp + 1);
+        }
+        auto starts = [&](const char* p) { return body.compare(0, std::strlen(p), p) == 0; };
+        const bool shared = starts("ld.shared") || starts("st.shared");
+        const bool gstore = starts("st.global.cs");
+        const bool bload = starts("cp.async.bulk.shared::cluster.global");
+        const bool bstore = starts("cp.async.bulk.global.shared::cta");
+        if (!shared && !gstore && !bload && !bstore) return ins;
+        // address operands [reg] or [reg+imm], in order
+        std::vector<std::pair<std::string, uint64_t>> ad;
+        for (size_t a = body.find('['); a != std::string::npos; a = body.find('[', a + 1)) {
+            const size_t e = body.find(']', a);
+            const std::string op = body.substr(a + 1, e - a - 1);
+            const size_t plus = op.find('+');
+            if (plus == std::string::npos) ad.push_back({op, 0});
+            else ad.push_back({op.substr(0, plus), std::stoull(op.substr(plus + 1))});
+        }
+        uint32_t size = runB_;
+        if (shared || gstore) {
+            const std::string opc = body.substr(0, body.find(' '));  // e.g. ld.shared.v2.f64
+            const int w = opc.find(".v4.") != std::string::npos ? 4 : (opc.find(".v2.") != std::string::npos ? 2 : 1);
+            const bool b8 = opc.size() >= 2 && opc.compare(opc.size() - 2, 2, "64") == 0;
+            size = static_cast<uint32_t>(w * (b8 ? 8 : 4));
+        }
+        std::vector<std::string> oks;
+        auto shared_ok = [&](const std::pair<std::string, uint64_t>& a) {
+            std::string ea = R32(), eb = R32(), q = P(), ok = P();
+            Iraw(fmt("add.u32 %s, %s, %llu", ea.c_str(), a.first.c_str(), static_cast<unsigned long long>(a.second)));
+            Iraw(fmt("setp.ge.u32 %s, %s, %s", q.c_str(), ea.c_str(), smb_.c_str()));
+            Iraw(fmt("add.u32 %s, %s, %u", eb.c_str(), ea.c_str(), size));
+            Iraw(fmt("setp.le.and.u32 %s, %s, %s, %s", ok.c_str(), eb.c_str(), smend_.c_str(), q.c_str()));
+            oks.push_back(ok);
+        };
+        auto global_ok = [&](const std::pair<std::string, uint64_t>& a) {
+            std::string ga = R64(), gb = R64(), any = P();
+            Iraw(fmt("add.s64 %s, %s, %llu", ga.c_str(), a.first.c_str(), static_cast<unsigned long long>(a.second)));
+            Iraw(fmt("add.s64 %s, %s, %u", gb.c_str(), ga.c_str(), size));
+            for (int st = 0; st < NS_; ++st) {
+                std::string q = P(), ok = P();
+                Iraw(fmt("setp.ge.u64 %s, %s, %s", q.c_str(), ga.c_str(), stg_[st].c_str()));
+                Iraw(fmt("setp.le.and.u64 %s, %s, %s, %s", ok.c_str(), gb.c_str(), gend_[st].c_str(), q.c_str()));
+                if (st == 0) Iraw(fmt("mov.pred %s, %s", any.c_str(), ok.c_str()));
+                else Iraw(fmt("or.pred %s, %s, %s", any.c_str(), any.c_str(), ok.c_str()));
+            }
+            oks.push_back(any);
+        };
+        if (shared) shared_ok(ad[0]);
+        if (gstore) global_ok(ad[0]);
+        if (bload) {
+            shared_ok(ad[0]);
+            global_ok(ad[1]);
+        }
+        if (bstore) {
+            global_ok(ad[0]);
+            shared_ok(ad[1]);
+        }
+        std::string ok = oks[0];
+        for (size_t k = 1; k < oks.size(); ++k) {
+            std::string n = P();
+            Iraw(fmt("and.pred %s, %s, %s", n.c_str(), ok.c_str(), oks[k].c_str()));
+            ok = n;
+        }
+        std::string bad = P();
+        Iraw(fmt("not.pred %s, %s", bad.c_str(), ok.c_str()));
+        if (!pred.empty()) {
+            std::string both = P(), bad2 = P();
+            Iraw(fmt("and.pred %s, %s, %s", both.c_str(), ok.c_str(), pred.c_str()));
+            Iraw(fmt("and.pred %s, %s, %s", bad2.c_str(), bad.c_str(), pred.c_str()));
+            ok = both;
+            bad = bad2;
+        }
+        std::string old = R32();  // the first error recorded stays
+        Iraw(fmt("@%s atom.global.cas.b32 %s, [%s], 0, %d", bad.c_str(), old.c_str(), status_.c_str(),
+                 static_cast<int>(QFVM_ERR_BOUNDS)));
+        return "@" + ok + " " + body;
     }
     void lab(const std::string& l) { body_ += l + ":\n"; }
 
@@ -392,6 +517,7 @@ class Gen {
     }
     // coefficients off .. off+cnt-1 of the tile's pool (widest aligned loads)
     std::vector<std::string> coefs(uint32_t off, int cnt) {
+        if (pc_) return pcoefs(off, cnt);
         std::vector<std::string> c;
         uint32_t i = off;
         const uint32_t end = off + cnt;
@@ -425,6 +551,49 @@ class Gen {
                       i * cb_));
             else
                 I(fmt("ld.global.nc.%s %s, [%s+%u]", ft_, r[0].c_str(), coefp_.c_str(), i * cb_));
+            for (int k = 0; k < vec; ++k) c.push_back(r[k]);
+            i += vec;
+        }
+        return c;
+    }
+
+    // Coefficients from the pass's parameter block p_cblob (pool entries
+    // cmin_ .. cmax_ in the arithmetic's format, warp-uniform constant
+    // memory): the widest aligned loads of the block.
+    std::vector<std::string> pcoefs(uint32_t off, int cnt) {
+        std::vector<std::string> c;
+        uint32_t i = off;
+        const uint32_t end = off + cnt;
+        while (i < end) {
+            const uint32_t rel = i - cmin_;
+            if (ds_) {
+                if (rel % 2 == 0 && i + 2 <= end) {
+                    std::string r[4] = {A(), A(), A(), A()};
+                    I(fmt("ld.param.v4.f32 {%s, %s, %s, %s}, [p_cblob+%u]", r[0].c_str(), r[1].c_str(), r[2].c_str(),
+                          r[3].c_str(), rel * cb_));
+                    c.push_back(r[0] + "|" + r[1]);
+                    c.push_back(r[2] + "|" + r[3]);
+                    i += 2;
+                } else {
+                    std::string h = A(), l = A();
+                    I(fmt("ld.param.v2.f32 {%s, %s}, [p_cblob+%u]", h.c_str(), l.c_str(), rel * cb_));
+                    c.push_back(h + "|" + l);
+                    ++i;
+                }
+                continue;
+            }
+            int vec = 1;
+            if (!f64_ && rel % 4 == 0 && i + 4 <= end) vec = 4;
+            else if (rel % 2 == 0 && i + 2 <= end) vec = 2;
+            std::string r[4];
+            for (int k = 0; k < vec; ++k) r[k] = A();
+            if (vec == 4)
+                I(fmt("ld.param.v4.f32 {%s, %s, %s, %s}, [p_cblob+%u]", r[0].c_str(), r[1].c_str(), r[2].c_str(),
+                      r[3].c_str(), rel * cb_));
+            else if (vec == 2)
+                I(fmt("ld.param.v2.%s {%s, %s}, [p_cblob+%u]", ft_, r[0].c_str(), r[1].c_str(), rel * cb_));
+            else
+                I(fmt("ld.param.%s %s, [p_cblob+%u]", ft_, r[0].c_str(), rel * cb_));
             for (int k = 0; k < vec; ++k) c.push_back(r[k]);
             i += vec;
         }
@@ -508,6 +677,20 @@ class Gen {
         I(fmt("ld.param.u64 %s, [p_wait_ns]", waitns_.c_str()));
         extra_ = R32();
         I(fmt("ld.param.u32 %s, [p_extra_tx]", extra_.c_str()));
+        if (bc_) {
+            // bounds of the checked accesses: the dynamic shared memory, and
+            // each state (ntiles tiles of 2^T amplitudes)
+            smend_ = R32();
+            Iraw(fmt("add.u32 %s, %s, %u", smend_.c_str(), smb_.c_str(), mbar_off() + 8u * sh_.nb));
+            std::string nb = R64();
+            Iraw(fmt("shl.b64 %s, %s, %d", nb.c_str(), ntiles_.c_str(), T_));
+            std::string bytes = R64();
+            Iraw(fmt("mul.lo.u64 %s, %s, %d", bytes.c_str(), nb.c_str(), es_));
+            for (int st = 0; st < NS_; ++st) {
+                gend_[st] = R64();
+                Iraw(fmt("add.s64 %s, %s, %s", gend_[st].c_str(), stg_[st].c_str(), bytes.c_str()));
+            }
+        }
         // the thread's share of a tile: global byte offset and byte offset in
         // the tile layout; both are sums over the set bits of tid
         std::vector<uint64_t> gv(T_ - R_);
@@ -920,7 +1103,9 @@ class Gen {
         {
             std::string p0t = P();
             I(fmt("setp.eq.u32 %s, %s, 0", p0t.c_str(), tid_.c_str()));
-            I(fmt("@%s st.global.u32 [%s], %d", p0t.c_str(), status_.c_str(), static_cast<int>(QFVM_ERR_TIMEOUT)));
+            std::string old = R32();  // the first error recorded stays
+            I(fmt("@%s atom.global.cas.b32 %s, [%s], 0, %d", p0t.c_str(), old.c_str(), status_.c_str(),
+                  static_cast<int>(QFVM_ERR_TIMEOUT)));
             wait_mbar(cmbar, cpar);
             if (sh_.nb == 2) {
                 const std::string lno = L();
@@ -1597,6 +1782,11 @@ class Gen {
     const char* ft_;
     int es_, cb_, T_, R_, NT_, NA_, NW_, PER_, NS_, np_, H_, RUNS_;
     uint32_t padu_, runB_, tileB_, slotB_;
+    bool bc_ = false;  // bounds-checked accesses
+    std::string smend_, gend_[2];
+    bool pc_ = false;  // coefficients from the parameter block p_cblob
+    uint32_t cmin_ = 0, cmax_ = 0;
+    static constexpr uint32_t kMaxBlob = 16384;  // bytes of coefficients in the kernel parameters
     std::string body_;
     int nr_ = 0, nrd_ = 0, nh_ = 0, np_reg_ = 0, na_ = 0, nd_ = 0, nl_ = 0;
     std::map<double, std::string> consts_;
@@ -1642,6 +1832,8 @@ bool jit_pass_key(const HostPlan& hp, int pi, const JitShape& sh, std::string* k
     put(&k, sh.nstates);
     put(&k, sh.nb);
     put(&k, sh.minb);
+    put(&k, static_cast<int>(g.param_coefs()));
+    put(&k, sh.bounds);
     put(&k, pd.L);
     put(&k, pd.H);
     put(&k, pd.step_count);
@@ -1672,6 +1864,15 @@ bool jit_pass_key(const HostPlan& hp, int pi, const JitShape& sh, std::string* k
             k.append(reinterpret_cast<const char*>(o.tk), sizeof o.tk);
         }
     }
+    return true;
+}
+
+bool jit_pass_coef_block(const HostPlan& hp, int pi, const JitShape& sh, uint32_t* cmin, uint32_t* cmax) {
+    if (pi < 0 || pi >= static_cast<int>(hp.passes.size())) return false;
+    Gen g(hp, pi, sh);
+    if (!g.param_coefs()) return false;
+    *cmin = g.cmin();
+    *cmax = g.cmax();
     return true;
 }
 

@@ -110,3 +110,34 @@ def test_tile_copy_wait_runs_out_then_recovery(precision):
     assert np.abs(st.download() - oracle.simulate(n, ops)).max() <= tol
     plan.close()
     st.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["c128", "c128_ds", "c64"])
+def test_bounds_checked_passes_run_clean(monkeypatch, precision):
+    """QFVM_BOUNDS_CHECK=1 (index-guard build of the specialised passes):
+    every access is checked against its buffer; a correct plan reports no
+    QFVM_ERR_BOUNDS and computes the oracle's state, one-state passes with a
+    shared-memory step and an adjoint reverse sweep alike."""
+    from pyquafu_gb300 import gradients
+
+    monkeypatch.setenv("QFVM_BOUNDS_CHECK", "1")
+    n = 15
+    rng = np.random.default_rng(5)
+    u, _ = np.linalg.qr(rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4)))
+    ops = workloads.random_layers(n, 4, seed=24, extras=True)
+    ops.append(workloads.matrix_gate("u2", (2, 11), u))
+    plan = engine.Plan(n, ops, precision)
+    st = engine.DeviceState(n, precision).set_zero()
+    plan.run(st)
+    got = st.download()
+    assert plan.jit_passes() > 0
+    tol = 1e-5 if precision == "c64" else 1e-12
+    assert np.abs(got - oracle.simulate(n, ops)).max() <= tol
+    plan.close()
+    st.close()
+    aops, _ = workloads.hea(n, 3, seed=2)
+    terms = workloads.zz_x_hamiltonian(n, seed=2)
+    _, g = gradients.adjoint(n, aops, terms, precision)
+    ref = oracle.grad_adjoint(n, aops, [o.slot for o in aops], terms)
+    assert np.abs(g - ref).max() <= (1e-4 if precision == "c64" else 1e-10)

@@ -163,3 +163,35 @@ def test_pass_text_depends_on_structure_only():
         nat.load().qfvm_plan_destroy(h)
     assert texts[0] == texts[1]
     assert texts[0] != texts[2]
+
+
+@pytest.mark.parametrize("precision,T,R,nstates,adjoint", [(1, 12, 4, 1, False), (2, 12, 3, 1, False),
+                                                           (0, 11, 4, 1, False), (0, 11, 4, 2, True)])
+def test_bounds_checked_passes(tmp_path, monkeypatch, precision, T, R, nstates, adjoint):
+    """QFVM_BOUNDS_CHECK=1: every shared-memory access, global store and bulk
+    copy of a specialised pass is predicated on a range check whose failure
+    writes QFVM_ERR_BOUNDS (7) to the status word; the passes assemble."""
+    monkeypatch.setenv("QFVM_BOUNDS_CHECK", "1")
+    n = 16
+    ops = workloads.random_layers(n, 4, seed=9, extras=True)
+    ops.append(workloads.matrix_gate("u2", (3, 9), np.eye(4)))  # a shared-memory step
+    if adjoint:
+        ops, _ = workloads.hea(n, 2, seed=1)
+        h = plan_handle(n, ops, precision, adjoint=True, batched=True)
+    else:
+        h = plan_handle(n, ops, precision, T, R)
+    checked = 0
+    for i in range(16):
+        src = pass_ptx(h, i, nstates)
+        if src is None:
+            continue
+        for line in src.splitlines():
+            ins = line.strip()
+            body = ins.split(" ", 1)[1] if ins.startswith("@") else ins
+            if body.startswith(("ld.shared", "st.shared", "st.global.cs", "cp.async.bulk.shared::cluster.global",
+                                "cp.async.bulk.global.shared::cta")):
+                assert ins.startswith("@"), ins
+                checked += 1
+        assert "atom.global.cas.b32" in src and ", 0, 7;" in src
+        assemble(tmp_path, src, f"bc{precision}_{i}")
+    assert checked > 0
