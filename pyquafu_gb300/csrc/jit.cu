@@ -299,6 +299,7 @@ int prepare_impl(qfvm_plan* p, int nstates, std::string* err) {
     // a pool that no bind rewrites on the device travels in the kernel parameters
     sh.pcoef = hp.binds.empty() ? 1 : 0;
     sh.bounds = bounds_check_env();
+    sh.chain = p->chain_ok ? chain_for(hp, sh) : 0;
     int dev = 0;
     cudaGetDevice(&dev);
     {
@@ -413,10 +414,24 @@ int prepare_impl(qfvm_plan* p, int nstates, std::string* err) {
         }
     }
     p->jit[si] = ks;
+    p->jit_chain[si] = sh.chain != 0;
     p->jit_ready[si] = true;
     return 0;
 }
 }  // namespace
+
+int chain_for(const HostPlan& hp, const JitShape& sh) {
+    // float pairs between the passes of a double-single one-state plan whose
+    // passes are all specialised tile passes (an interpreted pass reads FP64)
+    if (sh.nstates != 1 || hp.arith != QFVM_C128_DS || hp.passes.size() < 2) return 0;
+    JitShape s0 = sh;
+    s0.chain = 0;
+    for (size_t i = 0; i < hp.passes.size(); ++i) {
+        std::string k, why;
+        if (hp.passes[i].type != PASS_TILE || !jit_pass_key(hp, static_cast<int>(i), s0, &k, &why)) return 0;
+    }
+    return 1;
+}
 
 int bounds_check_env() {
     const char* e = std::getenv("QFVM_BOUNDS_CHECK");
@@ -444,6 +459,7 @@ void jit_release(qfvm_plan* p) {
     for (int s = 0; s < 2; ++s) {
         p->jit[s].clear();
         p->jit_cblob[s].clear();
+        p->jit_chain[s] = false;
         p->jit_ready[s] = false;
     }
 }
@@ -498,7 +514,8 @@ cudaError_t jit_launch_pass(qfvm_plan* p, int pi, void* psi, void* lam, const vo
         *launched = true;
         return cudaSuccess;
     }
-    if (r == CUDA_ERROR_INVALID_VALUE || r == CUDA_ERROR_LAUNCH_OUT_OF_RESOURCES || r == CUDA_ERROR_INVALID_HANDLE) {
+    if (!p->jit_chain[si] &&
+        (r == CUDA_ERROR_INVALID_VALUE || r == CUDA_ERROR_LAUNCH_OUT_OF_RESOURCES || r == CUDA_ERROR_INVALID_HANDLE)) {
         // a launch-configuration error leaves the context usable: the caller
         // runs the interpreting kernel for this pass instead
         static std::atomic<int> reported{0};
@@ -508,7 +525,8 @@ cudaError_t jit_launch_pass(qfvm_plan* p, int pi, void* psi, void* lam, const vo
         return cudaSuccess;
     }
     // anything else is reported with the driver's own code (the runtime and
-    // driver APIs share the numbering of these errors)
+    // driver APIs share the numbering of these errors); so is a refused
+    // launch inside a float-pair chain, whose neighbours expect float pairs
     *launched = true;
     return static_cast<cudaError_t>(r);
 }
@@ -554,6 +572,7 @@ int qfvm_jit_pass_ptx(const qfvm_plan* plan, int32_t pass, int32_t nstates, char
     sh.minb = nstates == 1 ? c.minb1 : c.minb2;
     sh.pcoef = plan->hp.binds.empty() ? 1 : 0;
     sh.bounds = qsv::bounds_check_env();
+    sh.chain = plan->chain_ok ? qsv::chain_for(plan->hp, sh) : 0;
     std::string ptx, why;
     if (!qsv::jit_pass_ptx(plan->hp, pass, sh, qsv::jit_entry_name(plan->hp.arith, nstates), &ptx, &why))
         return fail(QFVM_ERR_UNSUPPORTED, "pass runs interpreted: " + why);
@@ -574,6 +593,7 @@ int qfvm_jit_pass_compile(const qfvm_plan* plan, int32_t pass, int32_t nstates, 
     sh.minb = nstates == 1 ? c.minb1 : c.minb2;
     sh.pcoef = plan->hp.binds.empty() ? 1 : 0;
     sh.bounds = qsv::bounds_check_env();
+    sh.chain = plan->chain_ok ? qsv::chain_for(plan->hp, sh) : 0;
     std::string ptx, why, image, err, log;
     if (!qsv::jit_pass_ptx(plan->hp, pass, sh, qsv::jit_entry_name(plan->hp.arith, nstates), &ptx, &why))
         return fail(QFVM_ERR_UNSUPPORTED, "pass runs interpreted: " + why);

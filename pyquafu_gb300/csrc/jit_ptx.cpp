@@ -61,6 +61,11 @@ class Gen {
         tileB_ = tile_elems(T_, es_) * static_cast<uint32_t>(es_);
         slotB_ = tileB_ * NS_;
         bc_ = sh.bounds != 0;
+        // double-single plans chained in float-pair format: every pass but
+        // the first reads float pairs, every pass but the last writes them
+        in_pair_ = ds_ && sh.chain && pi > 0;
+        out_pair_ = ds_ && sh.chain && pi + 1 < static_cast<int>(hp.passes.size());
+        bulk_out_ = !ds_ || out_pair_;
         if (sh.pcoef) coef_range(&cmin_, &cmax_);
         pc_ = sh.pcoef && cmax_ > cmin_ && blob_bytes() <= kMaxBlob;
     }
@@ -93,6 +98,8 @@ class Gen {
     uint32_t blob_bytes() const { return ((cmax_ - cmin_) * cb_ + 15u) / 16u * 16u; }
 
     bool param_coefs() const { return pc_; }
+    bool in_pairs() const { return in_pair_; }
+    bool out_pairs() const { return out_pair_; }
     uint32_t cmin() const { return cmin_; }
     uint32_t cmax() const { return cmax_; }
 
@@ -843,7 +850,7 @@ class Gen {
         std::string ni = P();
         I(fmt("not.pred %s, %s", ni.c_str(), iss_.c_str()));
         I(fmt("@%s bra %s", ni.c_str(), lskip.c_str()));
-        if (!ds_) I("cp.async.bulk.wait_group.read 0");
+        if (bulk_out_) I("cp.async.bulk.wait_group.read 0");
         std::string bb = R64(), gl = R64(), dl = R32();
         I(fmt("mul.lo.u64 %s, %s, %d", bb.c_str(), base.c_str(), es_));
         I(fmt("add.s64 %s, %s, %s", gl.c_str(), bb.c_str(), runG_.c_str()));
@@ -957,7 +964,7 @@ class Gen {
             prefetch(nbase, nsb, omb);
             lab(lno);
         };
-        const bool late_next = sh_.nb == 2 && !ds_ && pd_.step_count > 0;
+        const bool late_next = sh_.nb == 2 && bulk_out_ && pd_.step_count > 0;
         if (sh_.nb == 1) prefetch(base, sbase, cmbar);
         else if (!late_next) next_prefetch();
         {
@@ -975,7 +982,7 @@ class Gen {
         // the thread's tile-layout base in this slot
         std::string tbase = R32();
         I(fmt("add.u32 %s, %s, %s", tbase.c_str(), stidB_.c_str(), sbase.c_str()));
-        if (ds_) {
+        if (ds_ && !in_pair_) {
             for (int k = 0; k < PER_; ++k) {
                 for (int st = 0; st < NS_; ++st) {
                     std::string re = D(), im = D();
@@ -1008,7 +1015,15 @@ class Gen {
             I(fmt("@%s bra %s", pz.c_str(), lskip.c_str()));
             lab(lst);
         }
-        if (ds_) {
+        if (out_pair_) {
+            // float pairs for the next pass: renormalised (TwoSum) once here,
+            // so |low| stays within half an ulp of high from pass to pass
+            for (int k = 0; k < PER_; ++k) {
+                const Cx c = load_amp(tbase, sk(k));
+                store_amp(tbase, sk(k), {ds_norm(c.x), ds_norm(c.y)});
+            }
+        }
+        if (ds_ && !out_pair_) {
             for (int st = 0; st < NS_; ++st) {
                 std::string gp = thread_gptr(st, base);
                 for (int k = 0; k < PER_; ++k) {
@@ -1067,7 +1082,7 @@ class Gen {
         I(fmt("setp.lt.u64 %s, %s, %s", pc.c_str(), b.c_str(), ntiles_.c_str()));
         I(fmt("@%s bra %s", pc.c_str(), lloop.c_str()));
         lab(lend);
-        if (!ds_) I(fmt("@%s cp.async.bulk.wait_group 0", iss_.c_str()));  // the last tile's stores
+        if (bulk_out_) I(fmt("@%s cp.async.bulk.wait_group 0", iss_.c_str()));  // the last tile's stores
         if (np_ > 0) {
             // single state: this CTA's per-probe totals
             const std::string lx = L();
@@ -1115,7 +1130,7 @@ class Gen {
                 wait_mbar(omb, opar);
                 lab(lno);
             }
-            if (!ds_) I(fmt("@%s cp.async.bulk.wait_group 0", iss_.c_str()));
+            if (bulk_out_) I(fmt("@%s cp.async.bulk.wait_group 0", iss_.c_str()));
             I("ret");
         }
     }
@@ -1783,6 +1798,8 @@ class Gen {
     int es_, cb_, T_, R_, NT_, NA_, NW_, PER_, NS_, np_, H_, RUNS_;
     uint32_t padu_, runB_, tileB_, slotB_;
     bool bc_ = false;  // bounds-checked accesses
+    bool in_pair_ = false, out_pair_ = false;  // float pairs in global memory before / after the pass
+    bool bulk_out_ = true;                     // write-back by bulk stores of the slot
     std::string smend_, gend_[2];
     bool pc_ = false;  // coefficients from the parameter block p_cblob
     uint32_t cmin_ = 0, cmax_ = 0;
@@ -1834,6 +1851,8 @@ bool jit_pass_key(const HostPlan& hp, int pi, const JitShape& sh, std::string* k
     put(&k, sh.minb);
     put(&k, static_cast<int>(g.param_coefs()));
     put(&k, sh.bounds);
+    put(&k, static_cast<int>(g.in_pairs()));
+    put(&k, static_cast<int>(g.out_pairs()));
     put(&k, pd.L);
     put(&k, pd.H);
     put(&k, pd.step_count);

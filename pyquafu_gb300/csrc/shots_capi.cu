@@ -119,6 +119,7 @@ namespace qsv_capi {
 
 // Every pass of a plan over `items` states (shared coefficient pool).
 int run_plan_items(qfvm_plan* p, void* state, int items, const uint8_t* active, cudaStream_t st) {
+    p->chain_ok = false;  // inactive items keep their FP64 state: no float pairs between passes
     const HostPlan& hp = p->hp;
     for (size_t i = 0; i < hp.passes.size(); ++i) {
         const PassDesc& pd = hp.passes[i];

@@ -13,6 +13,7 @@ import numpy as np
 import pytest
 
 import oracle
+from pyquafu_gb300 import _native as nat
 from pyquafu_gb300 import engine, gradients, ir, qfvm, workloads
 from pyquafu_gb300.batch import BatchSession
 
@@ -198,3 +199,39 @@ def test_trajectories_with_classical_control():
         res.append(qfvm._shots(n, ncb, ops, np.zeros(0, dtype=np.complex128), shots))
     assert res[0][0].tolist() == res[1][0].tolist()
     assert np.abs(res[0][1] - res[1][1]).max() < 1e-12
+
+
+def test_double_single_passes_chained_as_float_pairs():
+    """A double-single plan whose passes are all specialised hands the state
+    from pass to pass as float pairs: the first pass converts FP64 to pairs,
+    the middle ones move pairs by bulk copies both ways, the last converts
+    back.  The final state matches the oracle to 1e-12, and so do runs that
+    start from a given state and repeat."""
+    import ctypes
+
+    n = 20
+    ops = workloads.random_layers(n, 16, seed=31, extras=True)
+    plan = engine.Plan(n, ops, "c128_ds")
+    assert plan.stats()["passes"] >= 3
+    st = engine.DeviceState(n, "c128_ds").set_zero()
+    plan.run(st)
+    got = st.download()
+    assert plan.jit_passes() == plan.stats()["passes"]
+    ref = oracle.simulate(n, ops)
+    assert np.abs(got - ref).max() <= 1e-12
+    # the middle passes neither convert nor store per thread: their PTX reads
+    # and writes float pairs through bulk copies only
+    lib = nat.load()
+    ln = ctypes.c_int64()
+    assert lib.qfvm_jit_pass_ptx(plan._h, 1, 1, None, 0, ctypes.byref(ln)) == 0
+    buf = ctypes.create_string_buffer(ln.value + 1)
+    assert lib.qfvm_jit_pass_ptx(plan._h, 1, 1, buf, ln.value + 1, ctypes.byref(ln)) == 0
+    mid = buf.value.decode()
+    assert "ld.shared.v2.f64" not in mid and "st.global.cs" not in mid and "cp.async.bulk.global.shared" in mid
+    # a second run from the result (state given as FP64 again)
+    plan.run(st)
+    again = st.download()
+    ref2 = oracle.simulate(n, ops, ref)
+    assert np.abs(again - ref2).max() <= 1e-12
+    plan.close()
+    st.close()
