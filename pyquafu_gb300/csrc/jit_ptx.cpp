@@ -566,43 +566,21 @@ class Gen {
 
     // Coefficients from the pass's parameter block p_cblob (pool entries
     // cmin_ .. cmax_ in the arithmetic's format, warp-uniform constant
-    // memory): the widest aligned loads of the block.
+    // memory), one scalar load each, so each can become a constant operand.
     std::vector<std::string> pcoefs(uint32_t off, int cnt) {
         std::vector<std::string> c;
-        uint32_t i = off;
-        const uint32_t end = off + cnt;
-        while (i < end) {
+        for (uint32_t i = off; i < off + static_cast<uint32_t>(cnt); ++i) {
             const uint32_t rel = i - cmin_;
             if (ds_) {
-                if (rel % 2 == 0 && i + 2 <= end) {
-                    std::string r[4] = {A(), A(), A(), A()};
-                    I(fmt("ld.param.v4.f32 {%s, %s, %s, %s}, [p_cblob+%u]", r[0].c_str(), r[1].c_str(), r[2].c_str(),
-                          r[3].c_str(), rel * cb_));
-                    c.push_back(r[0] + "|" + r[1]);
-                    c.push_back(r[2] + "|" + r[3]);
-                    i += 2;
-                } else {
-                    std::string h = A(), l = A();
-                    I(fmt("ld.param.v2.f32 {%s, %s}, [p_cblob+%u]", h.c_str(), l.c_str(), rel * cb_));
-                    c.push_back(h + "|" + l);
-                    ++i;
-                }
-                continue;
+                std::string h = A(), l = A();
+                I(fmt("ld.param.f32 %s, [p_cblob+%u]", h.c_str(), rel * cb_));
+                I(fmt("ld.param.f32 %s, [p_cblob+%u]", l.c_str(), rel * cb_ + 4));
+                c.push_back(h + "|" + l);
+            } else {
+                std::string r = A();
+                I(fmt("ld.param.%s %s, [p_cblob+%u]", ft_, r.c_str(), rel * cb_));
+                c.push_back(r);
             }
-            int vec = 1;
-            if (!f64_ && rel % 4 == 0 && i + 4 <= end) vec = 4;
-            else if (rel % 2 == 0 && i + 2 <= end) vec = 2;
-            std::string r[4];
-            for (int k = 0; k < vec; ++k) r[k] = A();
-            if (vec == 4)
-                I(fmt("ld.param.v4.f32 {%s, %s, %s, %s}, [p_cblob+%u]", r[0].c_str(), r[1].c_str(), r[2].c_str(),
-                      r[3].c_str(), rel * cb_));
-            else if (vec == 2)
-                I(fmt("ld.param.v2.%s {%s, %s}, [p_cblob+%u]", ft_, r[0].c_str(), r[1].c_str(), rel * cb_));
-            else
-                I(fmt("ld.param.%s %s, [p_cblob+%u]", ft_, r[0].c_str(), rel * cb_));
-            for (int k = 0; k < vec; ++k) c.push_back(r[k]);
-            i += vec;
         }
         return c;
     }
