@@ -118,9 +118,10 @@ struct qfvm_plan {
     // per pass: the coefficient parameter block of its kernel (empty: the
     // kernel reads the pool in global memory)
     std::vector<std::vector<unsigned char>> jit_cblob[2];
-    // double-single one-state plans whose passes are all specialised hand the
-    // state from pass to pass as float pairs (jit_chain); runs that write
-    // back only some items (active masks) clear chain_ok before the first run
+    // double-single plans whose passes are all specialised hand the states
+    // from pass to pass as float pairs (jit_chain, per state count); runs
+    // that write back only some items (active masks) clear chain_ok before
+    // the first run
     bool chain_ok = true;
     bool jit_chain[2] = {false, false};
 };

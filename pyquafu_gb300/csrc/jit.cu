@@ -421,9 +421,10 @@ int prepare_impl(qfvm_plan* p, int nstates, std::string* err) {
 }  // namespace
 
 int chain_for(const HostPlan& hp, const JitShape& sh) {
-    // float pairs between the passes of a double-single one-state plan whose
-    // passes are all specialised tile passes (an interpreted pass reads FP64)
-    if (sh.nstates != 1 || hp.arith != QFVM_C128_DS || hp.passes.size() < 2) return 0;
+    // float pairs between the passes of a double-single plan whose passes
+    // are all specialised tile passes (an interpreted pass reads FP64); the
+    // kernels between the passes of a reverse sweep read only probe partials
+    if (hp.arith != QFVM_C128_DS || hp.passes.size() < 2) return 0;
     JitShape s0 = sh;
     s0.chain = 0;
     for (size_t i = 0; i < hp.passes.size(); ++i) {

@@ -22,11 +22,11 @@ struct JitShape {
     int minb = 1;     // .minnctapersm (register budget = 64K / (threads * minb))
     int pcoef = 0;    // 1: coefficients travel in the kernel parameters (plans whose pool is never rebound)
     int bounds = 0;   // 1: every shared / global / bulk access checked against its buffer (QFVM_BOUNDS_CHECK=1)
-    int chain = 0;    // 1: double-single passes hand the state on as float pairs (first reads FP64, last writes it)
+    int chain = 0;    // 1: double-single passes hand the states on as float pairs (first reads FP64, last writes it)
 };
 
-// 1 when the passes of `hp` run with shape `sh` hand the state on as float
-// pairs (double-single, one state, every pass a specialised tile pass).
+// 1 when the passes of `hp` run with shape `sh` hand the states on as float
+// pairs (double-single, every pass a specialised tile pass).
 int chain_for(const HostPlan& hp, const JitShape& sh);
 
 // QFVM_BOUNDS_CHECK=1 in the environment (read when a plan's passes are

@@ -996,10 +996,11 @@ class Gen {
         if (out_pair_) {
             // float pairs for the next pass: renormalised (TwoSum) once here,
             // so |low| stays within half an ulp of high from pass to pass
-            for (int k = 0; k < PER_; ++k) {
-                const Cx c = load_amp(tbase, sk(k));
-                store_amp(tbase, sk(k), {ds_norm(c.x), ds_norm(c.y)});
-            }
+            for (int k = 0; k < PER_; ++k)
+                for (int st = 0; st < NS_; ++st) {
+                    const Cx c = load_amp(tbase, st * tileB_ + sk(k));
+                    store_amp(tbase, st * tileB_ + sk(k), {ds_norm(c.x), ds_norm(c.y)});
+                }
         }
         if (ds_ && !out_pair_) {
             for (int st = 0; st < NS_; ++st) {
