@@ -195,3 +195,28 @@ def test_bounds_checked_passes(tmp_path, monkeypatch, precision, T, R, nstates, 
         assert "atom.global.cas.b32" in src and ", 0, 7;" in src
         assemble(tmp_path, src, f"bc{precision}_{i}")
     assert checked > 0
+
+
+def test_double_single_chain_pattern(tmp_path):
+    """A double-single plan of several specialised passes hands the state on
+    as float pairs: the first pass converts FP64 at staging and writes pairs
+    with bulk stores, the middle passes neither convert nor store per thread,
+    the last converts back and stores FP64 per thread.  Every pass assembles."""
+    n = 18
+    ops = workloads.random_layers(n, 6, seed=3, extras=True)
+    h = plan_handle(n, ops, 2, 12, 3)
+    counts = (ctypes.c_int64 * 4)()
+    shape = (ctypes.c_int32 * 3)()
+    nat.check(nat.load().qfvm_plan_host_counts(h, counts, shape))
+    npass = int(counts[0])
+    assert npass >= 3
+    srcs = [pass_ptx(h, i, 1) for i in range(npass)]
+    assert all(s is not None for s in srcs)
+    for i, src in enumerate(srcs):
+        converts_in = "ld.shared.v2.f64" in src
+        stores_fp64 = "st.global.cs.v2.f64" in src
+        bulk_out = "cp.async.bulk.global.shared" in src
+        assert converts_in == (i == 0), i
+        assert stores_fp64 == (i == npass - 1), i
+        assert bulk_out == (i < npass - 1), i
+        assemble(tmp_path, src, f"chain{i}")
