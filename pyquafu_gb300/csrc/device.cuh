@@ -296,7 +296,7 @@ __device__ __forceinline__ void reg_apply(RegState<P, R, NS>& a, const KOp& op, 
         case K_DIAGR:
 #pragma unroll
             for (int j = 0; j < (1 << R); ++j) {
-                const int code = diagr_code(op.tk, j);
+                const int code = diagr_code(op, j);
                 if (code == DIAGR_ONE) continue;
                 if (code != DIAGR_GENERAL) {
                     const int sp = code == DIAGR_NEG1 ? SP_NEG1 : (code == DIAGR_I ? SP_I : SP_NEGI);

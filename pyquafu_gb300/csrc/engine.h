@@ -27,7 +27,7 @@ enum GKind : uint8_t {
     K_PROBE = 10, // adjoint sweep: accumulate Im<lam| Q |psi> (reads both states, changes neither)
     K_HAD = 11,   // sqrt(2) H = [[1, 1], [1, -1]] on t0, no coefficients (see unnormalize_hadamards)
     K_DIAGR = 12  // register round only: amp j of the thread's 2^k registers *= d[j] (2 * 2^k coefs);
-                  // tk[0..5] hold a 3-bit code per entry (DIAGR_* below), k <= 4
+                  // a 3-bit code per entry (DIAGR_* below) in cthr / pthr (diagr_code), k <= 5
 };
 enum : uint8_t { DIAGR_GENERAL = 0, DIAGR_ONE = 1, DIAGR_NEG1 = 2, DIAGR_I = 3, DIAGR_NEGI = 4 };
 #if defined(__CUDACC__)
@@ -35,12 +35,6 @@ enum : uint8_t { DIAGR_GENERAL = 0, DIAGR_ONE = 1, DIAGR_NEG1 = 2, DIAGR_I = 3, 
 #else
 #define QSV_HD
 #endif
-// code of register entry j of a K_DIAGR op
-QSV_HD inline int diagr_code(const uint8_t* tk, int j) {
-    uint64_t c = 0;
-    for (int b = 0; b < 6; ++b) c |= static_cast<uint64_t>(tk[b]) << (8 * b);
-    return static_cast<int>((c >> (3 * j)) & 7);
-}
 
 // DIAG flags
 enum : uint8_t {
@@ -117,6 +111,14 @@ struct KOp {
     uint32_t xreg;  // K_PROBE: flip mask over register bits (or over global bits in whole-state passes)
 };
 static_assert(sizeof(KOp) == 48, "KOp layout");
+
+// Code of register entry j of a K_DIAGR op: entries 0..20 in cthr, 21..31
+// in pthr, 3 bits each (a K_DIAGR op has no controls or parities).
+constexpr int DIAGR_LOW = 21;
+QSV_HD inline int diagr_code(const KOp& o, int j) {
+    return j < DIAGR_LOW ? static_cast<int>((o.cthr >> (3 * j)) & 7)
+                         : static_cast<int>((o.pthr >> (3 * (j - DIAGR_LOW))) & 7);
+}
 
 constexpr int MAX_TILE = 14;
 

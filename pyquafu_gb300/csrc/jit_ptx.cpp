@@ -172,6 +172,13 @@ class Gen {
     std::string D() { return "%d" + std::to_string(nd_++); }
     std::string L() { return "$L" + std::to_string(nl_++); }
     void I(const std::string& s) { Iraw(bc_ ? checked(s) : s); }
+    // a comment line in the emitted PTX (marks what the following
+    // instructions do, for readers of the generated code)
+    void note(const std::string& s) {
+        body_ += "\t// ";
+        body_ += s;
+        body_ += '\n';
+    }
     void Iraw(const std::string& s) {
         body_ += '\t';
         body_ += s;
@@ -957,6 +964,7 @@ class Gen {
             I(fmt("@%s mbarrier.arrive.expect_tx.shared::cta.b64 _, [%s], %s", t0_.c_str(), cmbar.c_str(),
                   txb_.c_str()));
         }
+        note("tile staged: conversions");
         // the thread's tile-layout base in this slot
         std::string tbase = R32();
         I(fmt("add.u32 %s, %s, %s", tbase.c_str(), stidB_.c_str(), sbase.c_str()));
@@ -979,6 +987,7 @@ class Gen {
             if (si == 0 && late_next) next_prefetch();
         }
 
+        note("write-back");
         // write the tile back (one-state passes: only active items)
         const std::string lskip = L();
         if (NS_ == 1) {
@@ -1252,7 +1261,7 @@ class Gen {
     void op_diagr(const KOp& o) {
         std::vector<std::string> c;
         for (int j = 0; j < NA_; ++j) {
-            const int code = diagr_code(o.tk, j);
+            const int code = diagr_code(o, j);
             if (code == DIAGR_ONE) continue;
             if (code != DIAGR_GENERAL) {
                 const int sp = code == DIAGR_NEG1 ? SP_NEG1 : (code == DIAGR_I ? SP_I : SP_NEGI);
@@ -1542,6 +1551,7 @@ class Gen {
     void smem_step(const StepDesc& sd, const std::string& base, const std::string& sbase) {
         for (int oi = 0; oi < sd.op_count; ++oi) {
             const KOp& o = hp_.ops[sd.op_begin + oi];
+            note("shared-memory step: two-target dense gate");
             const std::string lskip = L();
             if (o.cthr) {
                 std::string t = R64(), p = P();
@@ -1640,6 +1650,7 @@ class Gen {
                 if ((j >> k) & 1) o += static_cast<uint32_t>(sd.rsw[k]) * es_;
             return o;
         };
+        note("round: loads");
         A_.assign(NS_, std::vector<Cx>(NA_));
         for (int j = 0; j < NA_; ++j) {
             if (r0 >= 0) {
@@ -1674,13 +1685,18 @@ class Gen {
             if (o.kind == K_PROBE) need |= o.xreg | o.preg;
             if (o.kind == K_DIAGR) need |= (1u << R_) - 1;  // its entries are per register index
             for (int t = 0; t < R_; ++t)
-                if ((need >> t) & 1) materialize(t);
+                if ((need >> t) & 1) {
+                    if (!flip_[t].empty()) note(fmt("materialize flip %d for kind %d", t, o.kind));
+                    materialize(t);
+                }
+            note(fmt("op kind %d t0 %d%s", o.kind, o.t0, ctl.empty() ? "" : " thread-controlled"));
             if (o.kind == K_PROBE) op_probe(o, gthr, ctl);
             else if (o.kind == K_DIAG) op_diag(o, gthr, ctl);
             else if (o.kind == K_DIAGR) op_diagr(o);
             else op_gate(o, ctl);
         }
         flush_probes();
+        note("round end: uniform phase, stores");
         // the round's uniform phase (reg_finish_phase)
         if (!q_.empty()) {
             std::string q1 = R32(), q2 = R32(), s1 = P(), s2 = P();

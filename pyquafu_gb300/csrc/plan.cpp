@@ -1054,7 +1054,7 @@ int entry_code(cd z) {
 }  // namespace
 
 void merge_round_diagonals(HostPlan* plan) {
-    if (plan->R < 1 || plan->R > 4 || !plan->binds.empty() || !plan->probe_slot.empty()) return;
+    if (plan->R < 1 || plan->R > 5 || !plan->binds.empty() || !plan->probe_slot.empty()) return;
     const int R = plan->R;
     const int NA = 1 << R;
     std::vector<KOp> out;
@@ -1093,13 +1093,13 @@ void merge_round_diagonals(HostPlan* plan) {
                     k.kind = K_DIAGR;
                     k.k = static_cast<uint8_t>(R);
                     k.coef = static_cast<uint32_t>(plan->coef.size());
-                    uint64_t codes = 0;
                     for (int j = 0; j < NA; ++j) {
                         plan->coef.push_back(table[j].real());
                         plan->coef.push_back(table[j].imag());
-                        codes |= static_cast<uint64_t>(entry_code(table[j])) << (3 * j);
+                        const uint64_t c = static_cast<uint64_t>(entry_code(table[j]));
+                        if (j < DIAGR_LOW) k.cthr |= c << (3 * j);
+                        else k.pthr |= c << (3 * (j - DIAGR_LOW));
                     }
-                    for (int b = 0; b < 6; ++b) k.tk[b] = static_cast<uint8_t>(codes >> (8 * b));
                     out.push_back(k);
                 }
                 merged.clear();

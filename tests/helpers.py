@@ -205,17 +205,21 @@ def kop_targets(o):
     return [int(x) for x in o["tk"][: o["k"]]], int(o["pthr"])
 
 
-def apply_diagr(psi, g_of_reg, coef, off, tk):
+def diagr_codes(o):
+    """3-bit entry codes of a K_DIAGR op: entries 0..20 in cthr, 21..31 in pthr."""
+    return int(o["cthr"]) | (int(o["pthr"]) << 63)
+
+
+def apply_diagr(psi, g_of_reg, coef, off, codes):
     """A merged register-round diagonal: amplitude i *= d[j], j the register
     index of i (bit b of j = bit g_of_reg[b] of i); entries coded exactly
-    1, -1, i, -i (3-bit codes in tk) must equal their coefficients."""
+    1, -1, i, -i (3-bit codes) must equal their coefficients."""
     idx = np.arange(psi.size, dtype=np.int64)
     j = np.zeros(psi.size, dtype=np.int64)
     for b, q in enumerate(g_of_reg):
         j |= ((idx >> q) & 1) << b
     n = 1 << len(g_of_reg)
     d = coef[off:off + 2 * n:2] + 1j * coef[off + 1:off + 2 * n:2]
-    codes = int.from_bytes(tk[:6], "little")
     want = {1: 1.0, 2: -1.0, 3: 1j, 4: -1j}
     for e in range(n):
         c = (codes >> (3 * e)) & 7
@@ -319,6 +323,9 @@ def interpret(plan, psi):
             assert [int(x) for x in sd["rsw"][:R]] == [tile_off(1 << p, eb) for p in rpos]
             g_of_reg = [tq[p] for p in rpos]
             for o in ops:
+                if int(o["kind"]) == K_DIAGR:
+                    apply_diagr(psi, g_of_reg, coef, int(o["coef"]), diagr_codes(o))
+                    continue
                 cm = int(o["cthr"])
                 pm = int(o["pthr"])
                 assert bool(int(o["flags"]) & 16) == (cm != 0) and bool(int(o["flags"]) & 32) == (pm != 0)
@@ -328,9 +335,6 @@ def interpret(plan, psi):
                 for b in _bits(o["preg"]):
                     pm |= 1 << g_of_reg[b]
                 kind = int(o["kind"])
-                if kind == K_DIAGR:
-                    apply_diagr(psi, g_of_reg, coef, int(o["coef"]), bytes(o["tk"]))
-                    continue
                 if kind in (K_SWAP,):
                     t = (g_of_reg[o["t0"]], g_of_reg[o["t1"]])
                 elif kind == K_DIAG:
