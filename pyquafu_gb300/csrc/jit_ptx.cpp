@@ -1259,7 +1259,6 @@ class Gen {
     // merged register-round diagonal: entry j multiplies register j (exact
     // entries 1, -1, i, -i without arithmetic)
     void op_diagr(const KOp& o) {
-        std::vector<std::string> c;
         for (int j = 0; j < NA_; ++j) {
             const int code = diagr_code(o, j);
             if (code == DIAGR_ONE) continue;
@@ -1268,8 +1267,10 @@ class Gen {
                 for (int s = 0; s < NS_; ++s) A_[s][j] = special(A_[s][j], sp);
                 continue;
             }
-            if (c.empty()) c = coefs(o.coef, 2 * NA_);
-            const std::string dr = c[2 * j], di = c[2 * j + 1], ndi = neg(di);
+            // each entry's coefficients just before their use (a table of 2^R
+            // entries loaded at once would hold 2^(R+1) registers)
+            const std::vector<std::string> c = coefs(o.coef + 2 * j, 2);
+            const std::string dr = c[0], di = c[1], ndi = neg(di);
             for (int s = 0; s < NS_; ++s) A_[s][j] = phase(A_[s][j], dr, di, ndi);
         }
     }

@@ -1054,7 +1054,10 @@ int entry_code(cd z) {
 }  // namespace
 
 void merge_round_diagonals(HostPlan* plan) {
-    if (plan->R < 1 || plan->R > 5 || !plan->binds.empty() || !plan->probe_slot.empty()) return;
+    // rounds of five register qubits are left alone: their 32-entry tables,
+    // and the flips they resolve, measured slower at the complex64 register
+    // budget (spills)
+    if (plan->R < 1 || plan->R > 4 || !plan->binds.empty() || !plan->probe_slot.empty()) return;
     const int R = plan->R;
     const int NA = 1 << R;
     std::vector<KOp> out;

@@ -25,7 +25,7 @@ def test_random_layers_plans(T, R):
         # register-round diagonals fold some)
         applied = sum(int(s["op_count"]) for s in plan["steps"])
         applied += sum(int(p["op_count"]) for p in plan["passes"] if p["type"] != 0)
-        assert 0.6 * len(ops) <= applied <= len(ops)
+        assert 0.7 * len(ops) <= applied <= len(ops)
 
 
 def plan_op_count(plan):
@@ -133,7 +133,7 @@ def test_wide_dense_gate_in_adjoint_sweep():
     np.testing.assert_allclose(grads, ref, atol=1e-12)
 
 
-@pytest.mark.parametrize("R", [3, 4, 5])
+@pytest.mark.parametrize("R", [3, 4])
 def test_round_diagonals_merge(R):
     """Plain plans merge the register-only diagonals of a round into one
     phase table (K_DIAGR, exact quarter turns coded), applied before the
