@@ -220,3 +220,31 @@ def test_double_single_chain_pattern(tmp_path):
         assert stores_fp64 == (i == npass - 1), i
         assert bulk_out == (i < npass - 1), i
         assemble(tmp_path, src, f"chain{i}")
+
+
+def test_no_chain_across_a_global_pass():
+    """A double-single plan with a pass that is not a tile pass (a dense gate
+    on eight targets runs as its own global pass, which reads FP64) keeps
+    FP64 between all passes: every tile pass converts at staging and stores
+    FP64, none writes float pairs."""
+    n = 18
+    rng = np.random.default_rng(2)
+    u, _ = np.linalg.qr(rng.normal(size=(256, 256)) + 1j * rng.normal(size=(256, 256)))
+    ops = workloads.random_layers(n, 3, seed=4) + [workloads.matrix_gate("u8", tuple(range(2, 10)), u)]
+    ops += workloads.random_layers(n, 3, seed=5)
+    h = plan_handle(n, ops, 2, 12, 3)
+    counts = (ctypes.c_int64 * 4)()
+    shape = (ctypes.c_int32 * 3)()
+    nat.check(nat.load().qfvm_plan_host_counts(h, counts, shape))
+    passes = np.zeros(counts[0], helpers.PASS_DT)
+    nat.check(nat.load().qfvm_plan_host_copy(h, nat.vptr(passes), None, None, None))
+    assert any(int(p["type"]) != 0 for p in passes)
+    tiles = 0
+    for i, p in enumerate(passes):
+        if int(p["type"]) != 0:
+            continue
+        src = pass_ptx(h, i, 1)
+        assert "ld.shared.v2.f64" in src and "st.global.cs.v2.f64" in src
+        assert "cp.async.bulk.global.shared" not in src
+        tiles += 1
+    assert tiles >= 2
