@@ -159,13 +159,19 @@ cudaError_t launch_small2_p(void* psi, void* lam, int n, const KOp* dops, int no
 
 // shapes of the two-state pass: X(T, R, NB, MINB) as for the one-state pass
 #define QSV_SHAPES_P64(X) X(11, 4, 2, 1) X(11, 3, 1, 2)
-#define QSV_SHAPES_PDS(X) X(11, 4, 2, 1)
+#define QSV_SHAPES_PDS(X) X(11, 4, 2, 1) X(12, 3, 1, 1) X(11, 3, 1, 2)
 #define QSV_SHAPES_P32(X) X(12, 4, 1, 2) X(11, 4, 1, 4) X(13, 4, 1, 1)
 
 void adjoint_shape(int arith, int* T, int* R) {
     if (arith == QFVM_C64) {
         *T = 12;
         *R = 4;
+    } else if (arith == QFVM_C128_DS) {
+        // three register qubits: the specialised float-pair sweep of two
+        // states at R = 4 outgrew the instruction cache (ncu: no_instruction
+        // the top stall); 24-qubit gradient 132.9 ms against 191.5 ms
+        *T = 11;
+        *R = 3;
     } else {
         *T = 11;
         *R = 4;
