@@ -55,3 +55,26 @@ def test_engine_arm_line():
     assert rows["C2_30q"][d["engine"]["precision"]]["err"] <= 1e-12
     c1 = rows["C1_20q_4096shots"]
     assert c1["sample_mismatches"] == 0 and c1["err"] <= 1e-12
+
+
+def test_forked_oracle_run():
+    """The bench's oracle run in a child forked before any GPU call: the
+    final state in the shared mapping, <Z0 Z1> and the indices of the seeded
+    shots equal the oracle's own (a 14-qubit instance of the benchmark
+    circuit)."""
+    import numpy as np
+
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import bench
+    import oracle
+
+    n = 14
+    ops = bench.workload(n)
+    run = bench.OracleRun(n, ops)
+    psi, zz, idx, secs, scan_s = run.result()
+    ref = oracle.simulate(n, ops)
+    assert np.array_equal(psi, ref)
+    assert abs(zz - oracle.expect_pauli(ref, "ZZ", [0, 1])) <= 1e-15
+    assert np.array_equal(idx, oracle.sample_indices(ref, run.u))
+    assert secs >= 0 and scan_s >= 0
