@@ -792,7 +792,10 @@ class OracleRun:
     device-timed rows do (rows whose figures include host time wait for it).
     The final state lands in an anonymous shared mapping; the child also
     computes <Z0 Z1> and the indices of the 4096 seeded shots (the oracle's
-    single-walk scan, equal to its per-shot scan)."""
+    single-walk scan, equal to its per-shot scan).  The fork also comes
+    before this process's first oracle call: the oracle's OpenMP runtime
+    does not carry its thread pool across a fork, and a child forked after
+    a parallel region waits in its first one."""
 
     def __init__(self, n, ops):
         import mmap

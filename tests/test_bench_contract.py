@@ -57,24 +57,34 @@ def test_engine_arm_line():
     assert c1["sample_mismatches"] == 0 and c1["err"] <= 1e-12
 
 
+FORKED_ORACLE_CHECK = """
+import os, sys
+import numpy as np
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, ROOT)
+import bench
+import oracle
+n = 14
+ops = bench.workload(n)
+run = bench.OracleRun(n, ops)
+psi, zz, idx, secs, scan_s = run.result()
+ref = oracle.simulate(n, ops)
+assert np.array_equal(psi, ref)
+assert abs(zz - oracle.expect_pauli(ref, "ZZ", [0, 1])) <= 1e-15
+assert np.array_equal(idx, oracle.sample_indices(ref, run.u))
+assert secs >= 0 and scan_s >= 0
+print("ok")
+"""
+
+
 def test_forked_oracle_run():
     """The bench's oracle run in a child forked before any GPU call: the
     final state in the shared mapping, <Z0 Z1> and the indices of the seeded
     shots equal the oracle's own (a 14-qubit instance of the benchmark
-    circuit)."""
-    import numpy as np
-
-    sys.path.insert(0, ROOT)
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import bench
-    import oracle
-
-    n = 14
-    ops = bench.workload(n)
-    run = bench.OracleRun(n, ops)
-    psi, zz, idx, secs, scan_s = run.result()
-    ref = oracle.simulate(n, ops)
-    assert np.array_equal(psi, ref)
-    assert abs(zz - oracle.expect_pauli(ref, "ZZ", [0, 1])) <= 1e-15
-    assert np.array_equal(idx, oracle.sample_indices(ref, run.u))
-    assert secs >= 0 and scan_s >= 0
+    circuit).  It runs in a fresh interpreter, as in the bench: the fork must
+    come before the process's first OpenMP region, since the oracle's OpenMP
+    runtime does not carry its thread pool across a fork, and this test
+    process has run the oracle already."""
+    code = "ROOT = %r\n" % ROOT + FORKED_ORACLE_CHECK
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=ROOT, timeout=300)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stderr[-2000:]

@@ -35,7 +35,7 @@ def _worker(rank, world, port, out):
 
 def test_max_over_ranks_two_gloo_ranks():
     world = 2
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()  # no fork of this multi-threaded process
     mp.spawn(_worker, args=(world, _free_port(), out), nprocs=world, join=True)
     assert dict(out) == {0: 20.0, 1: 20.0}
 
