@@ -20,9 +20,13 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(LIBDIR, "libqfvm_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["kernels.cu", "pass_c128.cu", "pass_c64.cu", "pass_ds.cu", "adjoint.cu", "batch.cu", "shots.cu",
-              "noise.cu", "sample.cu", "capi.cu", "batch_capi.cu", "shots_capi.cu", "noise_capi.cu", "noalloc.cu", "jit.cu"]
-CPP_SOURCES = ["plan.cpp", "jit_ptx.cpp"]
+# CUDA and host translation units, longest compiles first (the float-pair and
+# two-state instantiations, then the PTX generator), so that the parallel
+# build is not left waiting on one of them at the end
+SOURCES = ["adjoint_ds_r4.cu", "pass_ds_r5.cu", "adjoint_ds.cu", "pass_ds.cu", "adjoint_c64.cu", "pass_c128.cu",
+           "pass_c64.cu", "adjoint_c128.cu", "jit_ptx.cpp", "kernels.cu", "plan.cpp", "adjoint.cu", "batch.cu",
+           "shots.cu", "noise.cu", "sample.cu", "capi.cu", "batch_capi.cu", "shots_capi.cu", "noise_capi.cu",
+           "noalloc.cu", "jit.cu"]
 
 
 def nvcc() -> str:
@@ -44,7 +48,7 @@ def ptx_compiler_lib():
 
 
 def _sources():
-    return [os.path.join(CSRC, s) for s in CU_SOURCES + CPP_SOURCES]
+    return [os.path.join(CSRC, s) for s in SOURCES]
 
 
 def _deps():
@@ -85,7 +89,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             sys.stderr.write(r.stderr)
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 8))) as ex:
         objs = list(ex.map(run, jobs))
     tmp = LIB + ".tmp"
     link = [cc] + ARCH + ["-shared", "-o", tmp] + objs + ([ptxc, "-lpthread", "-lm"] if ptxc else []) + ["-lcudart"]

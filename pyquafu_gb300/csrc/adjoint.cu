@@ -1,5 +1,7 @@
-// Adjoint-method kernels and launchers (two-state passes, lam = H psi, probe
-// reductions).  The reverse sweep itself is planned by build_adjoint_sweep.
+// Adjoint-method kernels and launchers (whole-state two-state passes for small
+// states, lam = H psi, probe reductions, and the dispatch of the tiled
+// two-state passes, which adjoint_c128.cu, adjoint_ds.cu and adjoint_c64.cu
+// instantiate).  The reverse sweep itself is planned by build_adjoint_sweep.
 #include "adjoint.cuh"
 #include "kernels.h"
 
@@ -109,36 +111,6 @@ __global__ void k_probe_reduce(const double* __restrict__ partial, int grid, int
 
 namespace {
 
-template <class P, int T, int R, int NB, int MINB>
-cudaError_t launch_pass2_t(void* psi, void* lam, const PassDesc* dpass, const StepDesc* dsteps, const KOp* dops,
-                           const void* dcoef, int n, int H, int items, uint64_t cstride, int per_tile,
-                           double* partial, int* grid_out, cudaStream_t st) {
-    constexpr int NT = 1 << (T - R);
-    const size_t tiles_b = 2 * NB * sizeof(typename P::S) * tile_elems(T, sizeof(typename P::S));
-    const size_t smem = tiles_b + (sizeof(uint64_t) << H) + sizeof(double) * (NT / 32) * MAX_PASS_PROBES;
-    static int grid_cap = 0;
-    if (grid_cap == 0) {
-        const size_t most = tiles_b + (8 << 12) + sizeof(double) * (NT / 32) * MAX_PASS_PROBES;
-        cudaError_t e = cudaFuncSetAttribute(k_pass2<P, T, R, NB, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             static_cast<int>(most));
-        if (e != cudaSuccess) return e;
-        int dev = 0, nsm = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pass2<P, T, R, NB, MINB>, NT, smem);
-        if (e != cudaSuccess) return e;
-        grid_cap = (nsm > 0 ? nsm : 1) * (per_sm > 0 ? per_sm : 1);
-        if (grid_cap > pass2_grid_cap()) grid_cap = pass2_grid_cap();  // partial[] is sized for this many CTAs
-    }
-    const uint64_t tiles = static_cast<uint64_t>(items) << (n - T);
-    const unsigned grid = static_cast<unsigned>(tiles < static_cast<uint64_t>(grid_cap) ? tiles : grid_cap);
-    *grid_out = static_cast<int>(grid);
-    k_pass2<P, T, R, NB, MINB><<<grid, NT, smem, st>>>(
-        static_cast<typename P::G*>(psi), static_cast<typename P::G*>(lam), tiles, dpass, dsteps, dops,
-        static_cast<const typename P::C*>(dcoef), cstride, n - T, per_tile, partial);
-    return cudaGetLastError();
-}
-
 template <class P>
 cudaError_t launch_small2_p(void* psi, void* lam, int n, const KOp* dops, int nops, const void* dcoef, int items,
                             uint64_t cstride, double* probe_out, uint64_t pstride, cudaStream_t st) {
@@ -157,11 +129,6 @@ cudaError_t launch_small2_p(void* psi, void* lam, int n, const KOp* dops, int no
 
 }  // namespace
 
-// shapes of the two-state pass: X(T, R, NB, MINB) as for the one-state pass
-#define QSV_SHAPES_P64(X) X(11, 4, 2, 1) X(11, 3, 1, 2)
-#define QSV_SHAPES_PDS(X) X(11, 4, 2, 1) X(12, 3, 1, 1) X(11, 3, 1, 2)
-#define QSV_SHAPES_P32(X) X(12, 4, 1, 2) X(11, 4, 1, 4) X(13, 4, 1, 1)
-
 void adjoint_shape(int arith, int* T, int* R) {
     if (arith == QFVM_C64) {
         *T = 12;
@@ -179,17 +146,9 @@ void adjoint_shape(int arith, int* T, int* R) {
 }
 
 bool pass2_shape_supported(int arith, int T, int R) {
-#define QSV_HAS2(TT, RR, NBB, MB) \
-    if (T == TT && R == RR) return true;
-    if (arith == QFVM_C64) {
-        QSV_SHAPES_P32(QSV_HAS2)
-    } else if (arith == QFVM_C128_DS) {
-        QSV_SHAPES_PDS(QSV_HAS2)
-    } else {
-        QSV_SHAPES_P64(QSV_HAS2)
-    }
-    return false;
-#undef QSV_HAS2
+    if (arith == QFVM_C64) return pass2_shape_c64(T, R);
+    if (arith == QFVM_C128_DS) return pass2_shape_ds(T, R);
+    return pass2_shape_c128(T, R);
 }
 
 int adjoint_small_max(int arith) { return arith == QFVM_C64 ? 11 : 10; }
@@ -197,22 +156,14 @@ int adjoint_small_max(int arith) { return arith == QFVM_C64 ? 11 : 10; }
 cudaError_t launch_pass2(int arith, int T, int R, void* psi, void* lam, const PassDesc* dpass, const StepDesc* dsteps,
                          const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride, int per_tile,
                          double* partial, int* grid_out, cudaStream_t st) {
-#define QSV_LAUNCH2(TT, RR, NBB, MB)                                                                              \
-    if (T == TT && R == RR)                                                                                       \
-        return launch_pass2_t<P, TT, RR, NBB, MB>(psi, lam, dpass, dsteps, dops, dcoef, n, H, items, cstride,     \
-                                                  per_tile, partial, grid_out, st);
-    if (arith == QFVM_C64) {
-        using P = P32;
-        QSV_SHAPES_P32(QSV_LAUNCH2)
-    } else if (arith == QFVM_C128_DS) {
-        using P = PDS;
-        QSV_SHAPES_PDS(QSV_LAUNCH2)
-    } else {
-        using P = P64;
-        QSV_SHAPES_P64(QSV_LAUNCH2)
-    }
-    return cudaErrorInvalidValue;
-#undef QSV_LAUNCH2
+    if (arith == QFVM_C64)
+        return launch_pass2_c64(T, R, psi, lam, dpass, dsteps, dops, dcoef, n, H, items, cstride, per_tile, partial,
+                                grid_out, st);
+    if (arith == QFVM_C128_DS)
+        return launch_pass2_ds(T, R, psi, lam, dpass, dsteps, dops, dcoef, n, H, items, cstride, per_tile, partial,
+                               grid_out, st);
+    return launch_pass2_c128(T, R, psi, lam, dpass, dsteps, dops, dcoef, n, H, items, cstride, per_tile, partial,
+                             grid_out, st);
 }
 
 int pass2_grid_cap() { return 152 * 4; }

@@ -1,0 +1,23 @@
+// Fused two-state pass of the adjoint reverse sweep, complex128 storage with
+// double-single (FP32 pair) arithmetic: the four-register shape.
+#include "pass2_launch.cuh"
+
+// shapes: (tile qubits, register qubits, tile buffers per state, min CTAs per SM)
+#define QSV_SHAPES2(X) X(11, 4, 2, 1)
+
+namespace qsv {
+
+cudaError_t launch_pass2_ds_r4(int T, int R, void* psi, void* lam, const PassDesc* dpass, const StepDesc* dsteps,
+                               const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride,
+                               int per_tile, double* partial, int* grid_out, cudaStream_t st) {
+    using P = PDS;
+    QSV_SHAPES2(QSV_LAUNCH2_SHAPE)
+    return cudaErrorInvalidValue;
+}
+
+bool pass2_shape_ds_r4(int T, int R) {
+    QSV_SHAPES2(QSV_HAS2_SHAPE)
+    return false;
+}
+
+}  // namespace qsv

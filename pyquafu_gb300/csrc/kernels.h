@@ -18,9 +18,13 @@ bool set_tuned_shape(int arith, int kind, int n, int T, int R);
 bool pass_shape_c128(int T, int R);
 bool pass_shape_c64(int T, int R);
 bool pass_shape_ds(int T, int R);
+bool pass_shape_ds_r5(int T, int R);  // pass_ds_r5.cu
 cudaError_t launch_pass_ds(int T, int R, void* state, const PassDesc* dpass, const StepDesc* dsteps,
                            const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride,
                             const uint8_t* active, cudaStream_t st);
+cudaError_t launch_pass_ds_r5(int T, int R, void* state, const PassDesc* dpass, const StepDesc* dsteps,
+                              const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride,
+                              const uint8_t* active, cudaStream_t st);
 cudaError_t launch_pass_c128(int T, int R, void* state, const PassDesc* dpass, const StepDesc* dsteps,
                              const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride,
                             const uint8_t* active, cudaStream_t st);
@@ -69,6 +73,24 @@ cudaError_t launch_pass2(int arith, int T, int R, void* psi, void* lam, const Pa
                          const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride, int per_tile,
                          double* partial, int* grid_out, cudaStream_t st);
 int pass2_grid_cap();
+// adjoint_c128.cu, adjoint_ds.cu (+ adjoint_ds_r4.cu), adjoint_c64.cu: the tiled two-state
+// pass per arithmetic
+bool pass2_shape_c128(int T, int R);
+bool pass2_shape_ds(int T, int R);
+bool pass2_shape_ds_r4(int T, int R);  // adjoint_ds_r4.cu
+bool pass2_shape_c64(int T, int R);
+cudaError_t launch_pass2_c128(int T, int R, void* psi, void* lam, const PassDesc* dpass, const StepDesc* dsteps,
+                              const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride,
+                              int per_tile, double* partial, int* grid_out, cudaStream_t st);
+cudaError_t launch_pass2_ds(int T, int R, void* psi, void* lam, const PassDesc* dpass, const StepDesc* dsteps,
+                            const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride,
+                            int per_tile, double* partial, int* grid_out, cudaStream_t st);
+cudaError_t launch_pass2_ds_r4(int T, int R, void* psi, void* lam, const PassDesc* dpass, const StepDesc* dsteps,
+                               const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride,
+                               int per_tile, double* partial, int* grid_out, cudaStream_t st);
+cudaError_t launch_pass2_c64(int T, int R, void* psi, void* lam, const PassDesc* dpass, const StepDesc* dsteps,
+                             const KOp* dops, const void* dcoef, int n, int H, int items, uint64_t cstride,
+                             int per_tile, double* partial, int* grid_out, cudaStream_t st);
 cudaError_t launch_small2(int arith, void* psi, void* lam, int n, const KOp* dops, int nops, const void* dcoef,
                           int items, uint64_t cstride, double* probe_out, uint64_t pstride, cudaStream_t st);
 cudaError_t launch_hamiltonian(int storage, const void* psi, void* lam, uint64_t N, const uint64_t* dx,

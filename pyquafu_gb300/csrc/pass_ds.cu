@@ -3,7 +3,9 @@
 #include "pass_launch.cuh"
 
 // shapes: (tile qubits, register qubits, tile buffers, min CTAs per SM)
-#define QSV_SHAPES(X) X(11, 4, 2, 1) X(12, 4, 2, 1) X(12, 5, 2, 1) X(12, 3, 1, 1)
+// (the five-register shape is in pass_ds_r5.cu: its unrolled rounds compile as long
+// as the rest of this unit)
+#define QSV_SHAPES(X) X(11, 4, 2, 1) X(12, 4, 2, 1) X(12, 3, 1, 1)
 
 namespace qsv {
 
@@ -12,12 +14,12 @@ cudaError_t launch_pass_ds(int T, int R, void* state, const PassDesc* dpass, con
                             const uint8_t* active, cudaStream_t st) {
     using P = PDS;
     QSV_SHAPES(QSV_LAUNCH_SHAPE)
-    return cudaErrorInvalidValue;
+    return launch_pass_ds_r5(T, R, state, dpass, dsteps, dops, dcoef, n, H, items, cstride, active, st);
 }
 
 bool pass_shape_ds(int T, int R) {
     QSV_SHAPES(QSV_HAS_SHAPE)
-    return false;
+    return pass_shape_ds_r5(T, R);
 }
 
 }  // namespace qsv

@@ -54,3 +54,32 @@ def test_no_device_is_an_error_not_a_crash(lib):
     rc = lib.qfvm_sv_create(4, 0, ctypes.byref(h))
     assert rc == 6
     assert b"CUDA" in lib.qfvm_last_error()
+
+
+COMPILED_SHAPES = {  # (arithmetic, pass kind): the (tile qubits, register qubits) the library instantiates
+    (nat.QFVM_C128, 0): {(11, 4), (12, 4), (12, 5), (12, 3), (11, 3)},
+    (nat.QFVM_C64, 0): {(12, 5), (13, 5), (12, 4), (13, 4)},
+    (nat.QFVM_C128_DS, 0): {(11, 4), (12, 4), (12, 5), (12, 3)},
+    (nat.QFVM_C128, 1): {(11, 4), (11, 3)},
+    (nat.QFVM_C64, 1): {(12, 4), (11, 4), (13, 4)},
+    (nat.QFVM_C128_DS, 1): {(11, 4), (12, 3), (11, 3)},
+}
+DEFAULT_SHAPES = {  # one-state passes, then the adjoint's two-state reverse sweep
+    (nat.QFVM_C128, 0): (11, 4), (nat.QFVM_C64, 0): (13, 5), (nat.QFVM_C128_DS, 0): (12, 3),
+    (nat.QFVM_C128, 1): (11, 4), (nat.QFVM_C64, 1): (12, 4), (nat.QFVM_C128_DS, 1): (11, 3),
+}
+
+
+def test_compiled_shape_table(lib):
+    """The shapes each arithmetic's translation units instantiate (host
+    queries only), and the built-in defaults are among them."""
+    for (prec, kind), want in COMPILED_SHAPES.items():
+        got = {(t, r) for t in range(6, 16) for r in range(1, 8) if lib.qfvm_shape_supported(prec, kind, t, r)}
+        assert got == want, (prec, kind)
+    assert lib.qfvm_shape_supported(7, 0, 11, 4) == 0 and lib.qfvm_shape_supported(nat.QFVM_C128, 2, 11, 4) == 0
+    t, r = ctypes.c_int32(), ctypes.c_int32()
+    for (prec, kind), want in DEFAULT_SHAPES.items():
+        for n in (20, 24, 30):
+            assert lib.qfvm_set_tuned_shape(prec, kind, n, 0, 0) == 0  # the built-in default, not a tuned one
+            assert lib.qfvm_get_shape(prec, kind, n, ctypes.byref(t), ctypes.byref(r)) == 0
+            assert (t.value, r.value) == want, (prec, kind, n)
