@@ -68,7 +68,7 @@ def test_every_adjoint_shape_matches():
     ops, _ = workloads.hea(n, 3, seed=4)
     terms = workloads.zz_x_hamiltonian(n, seed=4)
     e0, g0 = gradients.adjoint(n, ops, terms, "c128")
-    for prec, tol in (("c128", 1e-10), ("c64", 1e-5)):
+    for prec, tol in (("c128", 1e-10), ("c128_ds", 1e-10), ("c64", 1e-5)):
         for shape in autotune.candidates(prec, 1):
             autotune.set_shape(prec, 1, n, shape)
             e, g = gradients.adjoint(n, ops, terms, prec)
