@@ -256,9 +256,8 @@ int jit_prepare(qfvm_plan* p, int nstates, std::string* err) {
     const int si = nstates == 2 ? 1 : 0;
     if (p->jit_ready[si]) return 0;
     if (prepare_impl(p, nstates, err) == 0) return 0;
-    static bool warned = false;
-    if (!warned) {
-        warned = true;
+    static std::atomic<bool> warned{false};
+    if (!warned.exchange(true)) {
         std::fprintf(stderr, "qfvm: specialised passes unavailable, interpreting kernels used: %s\n", err->c_str());
     }
     p->jit[si].assign(p->hp.passes.size(), nullptr);
@@ -486,6 +485,15 @@ cudaError_t jit_launch_pass(qfvm_plan* p, int pi, void* psi, void* lam, const vo
         jit_prepare(p, nstates, &err);
     }
     if (pi < 0 || pi >= static_cast<int>(p->jit[si].size()) || !p->jit[si][pi]) return cudaSuccess;
+    // the kernels record a failed wait or bound in this device's status word;
+    // without one (its allocation failed on this device) the pass is not
+    // launched: the interpreting kernel runs it, or, inside a float-pair
+    // chain, the run reports the failure
+    void* a_status = status_word();
+    if (a_status == nullptr) {
+        *launched = p->jit_chain[si];
+        return p->jit_chain[si] ? cudaErrorMemoryAllocation : cudaSuccess;
+    }
     const Kernel* k = static_cast<const Kernel*>(p->jit[si][pi]);
     const HostPlan& hp = p->hp;
     uint64_t ntiles = static_cast<uint64_t>(items) << (hp.n - hp.T);
@@ -498,7 +506,6 @@ cudaError_t jit_launch_pass(qfvm_plan* p, int pi, void* psi, void* lam, const vo
     const void* a_act = active;
     int32_t a_pt = per_tile;
     void* a_part = partial;
-    void* a_status = status_word();
     uint64_t a_wait = g_wait_ns.load();
     uint32_t a_extra = g_extra_tx.load();
     // the coefficient block (when the kernel takes one) is its last parameter
