@@ -22,9 +22,12 @@ PRECISIONS = {"c128": QFVM_C128, "complex128": QFVM_C128, "c64": QFVM_C64, "comp
 QFVM_ERR_INVALID, QFVM_ERR_CUDA, QFVM_ERR_NOMEM, QFVM_ERR_UNSUPPORTED, QFVM_ERR_TIMEOUT, QFVM_ERR_NODEVICE, \
     QFVM_ERR_BOUNDS = range(1, 8)
 
+QFVM_MAX_QUBITS = 34     # largest state the engine plans (2^34 amplitudes)
+QFVM_MAX_OP_QUBITS = 16  # most qubits (targets and controls) of one operation
+
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory",
-    4: "unsupported", 5: "device wait timed out", 6: "no CUDA device",
+    4: "unsupported", 5: "device wait timed out", 6: "no CUDA device", 7: "index out of bounds",
 }
 
 

@@ -83,3 +83,20 @@ def test_compiled_shape_table(lib):
             assert lib.qfvm_set_tuned_shape(prec, kind, n, 0, 0) == 0  # the built-in default, not a tuned one
             assert lib.qfvm_get_shape(prec, kind, n, ctypes.byref(t), ctypes.byref(r)) == 0
             assert (t.value, r.value) == want, (prec, kind, n)
+
+
+def test_python_constants_match_header():
+    """The ctypes layer's status codes, arithmetic kinds and limits are the
+    header's, and every status code the header declares has a name."""
+    text = open(os.path.join(ROOT, "include", "qfvm_gb300.h")).read()
+    defined = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+(QFVM_[A-Z0-9_]+)\s+(\d+)", text)}
+    enums = {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(QFVM_[A-Z0-9_]+)\s*=\s*(\d+)", text)}
+    header = {**defined, **enums}
+    names = [n for n in dir(nat) if n.startswith("QFVM_") and isinstance(getattr(nat, n), int)]
+    assert len(names) >= 12
+    for n in names:
+        assert n in header, n
+        assert getattr(nat, n) == header[n], n
+    for n, v in header.items():
+        if n.startswith("QFVM_ERR_"):
+            assert v in nat.STATUS, n

@@ -313,3 +313,26 @@ def test_round_wavefronts_hit_distinct_banks(precision, T, R):
                     groups.add((helpers.tile_off(s, eb) * eb // access) % (128 // access))
                 assert len(groups) == lanes, (rpos, tpos)
     assert rounds > 0 and checked >= 0.9 * rounds, (checked, rounds)
+
+
+@pytest.mark.parametrize("precision", [0, 1, 2])
+def test_edge_sizes(precision):
+    """Smallest states (one and two qubits, a whole-state pass), an empty
+    circuit (no passes), the largest supported qubit count (planned only)
+    and counts outside the supported range (refused)."""
+    from pyquafu_gb300 import _native as nat
+
+    cases = [(1, [workloads.named("h", (0,)), workloads.named("rz", (0,), [0.3])]),
+             (2, [workloads.named("h", (0,)), workloads.named("cx", (0, 1), ncontrols=1)]),
+             (3, [])]
+    for n, ops in cases:
+        plan = helpers.host_plan(n, ops, precision)
+        assert len(plan["passes"]) == (1 if ops else 0)
+        got = helpers.interpret(plan, oracle.zero_state(n))
+        assert np.abs(got - oracle.simulate(n, ops)).max() < 1e-15
+    plan = helpers.host_plan(nat.QFVM_MAX_QUBITS, [workloads.named("h", (nat.QFVM_MAX_QUBITS - 1,))], precision)
+    assert len(plan["passes"]) == 1
+    for n in (0, nat.QFVM_MAX_QUBITS + 1):
+        with pytest.raises(nat.QfvmError) as err:
+            helpers.host_plan(n, [workloads.named("h", (0,))], precision)
+        assert "qubit count out of range" in str(err.value)
