@@ -829,6 +829,22 @@ class OracleRun:
                 print(f"[bench] oracle run failed: {e!r}", file=sys.stderr, flush=True)
             finally:
                 os._exit(code)
+        import atexit
+
+        atexit.register(self.abandon)  # registered in the parent only, after the fork
+
+    def abandon(self):
+        """Ends the child (its exact pid) when the bench stops without
+        waiting for it, e.g. after an exception in the GPU rows."""
+        if self.pid:
+            import signal
+
+            try:
+                os.kill(self.pid, signal.SIGKILL)
+                os.waitpid(self.pid, 0)
+            except OSError:
+                pass
+            self.pid = 0
 
     def _state(self):
         return np.frombuffer(self._map, dtype=np.complex128, count=1 << self.n)

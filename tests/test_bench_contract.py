@@ -88,3 +88,27 @@ def test_forked_oracle_run():
     code = "ROOT = %r\n" % ROOT + FORKED_ORACLE_CHECK
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=ROOT, timeout=300)
     assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stderr[-2000:]
+
+
+ABANDONED_ORACLE = """
+import os, sys, time
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, ROOT)
+import bench
+n = 24
+run = bench.OracleRun(n, bench.workload(n))
+print(run.pid, flush=True)
+time.sleep(0.5)
+raise SystemExit(3)
+"""
+
+
+def test_bench_exit_ends_the_oracle_child():
+    """A bench that stops before waiting for the oracle run (an exception in
+    the GPU rows) ends its child instead of leaving it computing."""
+    code = "ROOT = %r\n" % ROOT + ABANDONED_ORACLE
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=ROOT, timeout=300)
+    assert r.returncode == 3, r.stderr[-2000:]
+    pid = int(r.stdout.split()[0])
+    with pytest.raises(ProcessLookupError):
+        os.kill(pid, 0)
