@@ -248,3 +248,47 @@ def test_no_chain_across_a_global_pass():
         assert "cp.async.bulk.global.shared" not in src
         tiles += 1
     assert tiles >= 2
+
+
+def ptx_instructions(src):
+    """Instruction statements of a PTX text (no directives, labels or comments)."""
+    k = 0
+    for ln in src.split("\n"):
+        t = ln.strip()
+        if t and not t.startswith(("//", ".")) and not t.endswith(":") and t not in ("{", "}") and t.endswith(";"):
+            k += 1
+    return k
+
+
+@pytest.mark.parametrize("precision,adjoint,median_max,max_max", [
+    (2, True, 18000, 60000),   # float-pair reverse sweep at (11, 3): 14.3 K / 50.2 K
+    (0, True, 8000, 24000),    # FP64 reverse sweep at (11, 4): 4.7 K / 15.2 K
+    (1, True, 8000, 24000),    # complex64 reverse sweep at (12, 4): 4.5 K / 16.3 K
+    (2, False, 6000, 9000),    # float-pair pass at (12, 3): 3.8 K / 6.0 K
+    (1, False, 5000, 7000),    # complex64 pass at (13, 5): 3.0 K / 4.5 K
+])
+def test_specialised_pass_code_size(precision, adjoint, median_max, max_max):
+    """Code size of the default specialised passes on the benchmark circuits
+    (24-qubit HEA gradient, 30-qubit random layers): the float-pair reverse
+    sweep at four register qubits emitted a median of 27 K instructions per
+    pass and stalled on instruction fetch on the GPU; the bounds keep the
+    defaults well below that."""
+    lib = nat.load()
+    if adjoint:
+        n = 24
+        ops, _ = workloads.hea(n, 20, seed=0)
+        arr, pool = ir.pack(ops)
+        h = ctypes.c_void_p()
+        nat.check(lib.qfvm_plan_host_build_adjoint(n, precision, nat.vptr(arr), arr.size,
+                                                   nat.dptr(pool.view(np.float64)), pool.size, ctypes.byref(h)))
+    else:
+        n = 30
+        h = plan_handle(n, workloads.random_layers(n, 40, seed=0, extras=True), precision)
+    counts = (ctypes.c_int64 * 4)()
+    shape = (ctypes.c_int32 * 3)()
+    nat.check(lib.qfvm_plan_host_counts(h, counts, shape))
+    nstates = 2 if adjoint else 1
+    sizes = [ptx_instructions(s) for s in (pass_ptx(h, i, nstates) for i in range(counts[0])) if s]
+    lib.qfvm_plan_destroy(h)
+    assert len(sizes) >= 40
+    assert np.median(sizes) <= median_max and max(sizes) <= max_max, (tuple(shape), np.median(sizes), max(sizes))
