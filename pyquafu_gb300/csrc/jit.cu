@@ -245,6 +245,42 @@ void jit_set_config(const JitConfig& c) {
     config() = c;
 }
 
+// The shape a plan's passes are compiled with: the configured or automatic
+// register budget (shape_for), coefficients in the kernel parameters when no
+// bind rewrites the pool on the device, the bounds mode, the float-pair
+// chain, and double buffering only where the register budget's resident
+// CTAs (minb) still fit in the SM's shared memory with two tiles each
+// (otherwise the second buffer costs a resident CTA: measured 1.5x slower
+// for double-single (12,4)).  optin / per_sm: the device's shared memory per
+// block (opt-in) and per SM.
+JitShape plan_shape(const qfvm_plan* p, int nstates, size_t optin, size_t per_sm) {
+    const HostPlan& hp = p->hp;
+    JitShape sh = shape_for(hp, nstates);
+    sh.pcoef = hp.binds.empty() ? 1 : 0;
+    sh.bounds = bounds_check_env();
+    sh.chain = p->chain_ok ? chain_for(hp, sh) : 0;
+    JitShape two_sh = sh;
+    two_sh.nb = 2;
+    const size_t two = jit_smem_bytes(hp, two_sh, MAX_PASS_PROBES);
+    if (sh.nb == 2 && (two > optin || static_cast<size_t>(sh.minb) * (two + 1024) > per_sm)) sh.nb = 1;
+    return sh;
+}
+
+// plan_shape with the current device's shared memory, or sm_103a's (227 KiB
+// per block, 228 KiB per SM) on a machine without a device: the shape the
+// host-side PTX queries report is the one the device path compiles
+JitShape host_query_shape(const qfvm_plan* p, int nstates) {
+    int dev = 0, optin = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess) {
+        cudaGetLastError();
+        optin = 227 * 1024;
+        per_sm = 228 * 1024;
+    }
+    return plan_shape(p, nstates, static_cast<size_t>(optin), static_cast<size_t>(per_sm));
+}
+
 namespace {
 int prepare_impl(qfvm_plan* p, int nstates, std::string* err);
 }
@@ -294,27 +330,13 @@ int prepare_impl(qfvm_plan* p, int nstates, std::string* err) {
         *err = "device status word: allocation failed";
         return 1;
     }
-    sh = shape_for(hp, nstates);
-    // a pool that no bind rewrites on the device travels in the kernel parameters
-    sh.pcoef = hp.binds.empty() ? 1 : 0;
-    sh.bounds = bounds_check_env();
-    sh.chain = p->chain_ok ? chain_for(hp, sh) : 0;
     int dev = 0;
     cudaGetDevice(&dev);
     {
-        // double buffering only where the register budget's resident CTAs
-        // (minb) still fit in the SM's shared memory with two tiles each:
-        // otherwise the second buffer costs a resident CTA (measured 1.5x
-        // slower for double-single (12,4))
         int optin = 0, per_sm = 0;
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-        JitShape two_sh = sh;
-        two_sh.nb = 2;
-        const size_t two = jit_smem_bytes(hp, two_sh, MAX_PASS_PROBES);
-        if (sh.nb == 2 && (two > static_cast<size_t>(optin) ||
-                           static_cast<size_t>(sh.minb) * (two + 1024) > static_cast<size_t>(per_sm)))
-            sh.nb = 1;
+        sh = plan_shape(p, nstates, static_cast<size_t>(optin), static_cast<size_t>(per_sm));
     }
     // look the passes up by structure; generate and compile the missing ones
     std::vector<std::string> keys(hp.passes.size());
@@ -573,14 +595,7 @@ int qfvm_jit_get_config(int32_t config[5]) {
 int qfvm_jit_pass_ptx(const qfvm_plan* plan, int32_t pass, int32_t nstates, char* text, int64_t capacity,
                       int64_t* len) {
     if (!plan || !len || (nstates != 1 && nstates != 2)) return fail(QFVM_ERR_INVALID, "bad argument");
-    const qsv::JitConfig c = qsv::jit_config();
-    qsv::JitShape sh;
-    sh.nstates = nstates;
-    sh.nb = nstates == 1 ? c.nb1 : c.nb2;
-    sh.minb = nstates == 1 ? c.minb1 : c.minb2;
-    sh.pcoef = plan->hp.binds.empty() ? 1 : 0;
-    sh.bounds = qsv::bounds_check_env();
-    sh.chain = plan->chain_ok ? qsv::chain_for(plan->hp, sh) : 0;
+    const qsv::JitShape sh = qsv::host_query_shape(plan, nstates);
     std::string ptx, why;
     if (!qsv::jit_pass_ptx(plan->hp, pass, sh, qsv::jit_entry_name(plan->hp.arith, nstates), &ptx, &why))
         return fail(QFVM_ERR_UNSUPPORTED, "pass runs interpreted: " + why);
@@ -594,14 +609,7 @@ int qfvm_jit_pass_ptx(const qfvm_plan* plan, int32_t pass, int32_t nstates, char
 
 int qfvm_jit_pass_compile(const qfvm_plan* plan, int32_t pass, int32_t nstates, char* info, int64_t capacity) {
     if (!plan || (nstates != 1 && nstates != 2)) return fail(QFVM_ERR_INVALID, "bad argument");
-    const qsv::JitConfig c = qsv::jit_config();
-    qsv::JitShape sh;
-    sh.nstates = nstates;
-    sh.nb = nstates == 1 ? c.nb1 : c.nb2;
-    sh.minb = nstates == 1 ? c.minb1 : c.minb2;
-    sh.pcoef = plan->hp.binds.empty() ? 1 : 0;
-    sh.bounds = qsv::bounds_check_env();
-    sh.chain = plan->chain_ok ? qsv::chain_for(plan->hp, sh) : 0;
+    const qsv::JitShape sh = qsv::host_query_shape(plan, nstates);
     std::string ptx, why, image, err, log;
     if (!qsv::jit_pass_ptx(plan->hp, pass, sh, qsv::jit_entry_name(plan->hp.arith, nstates), &ptx, &why))
         return fail(QFVM_ERR_UNSUPPORTED, "pass runs interpreted: " + why);

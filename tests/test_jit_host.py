@@ -292,3 +292,70 @@ def test_specialised_pass_code_size(precision, adjoint, median_max, max_max):
     lib.qfvm_plan_destroy(h)
     assert len(sizes) >= 40
     assert np.median(sizes) <= median_max and max(sizes) <= max_max, (tuple(shape), np.median(sizes), max(sizes))
+
+
+def default_plan(precision, adjoint):
+    """Host plan of a benchmark circuit at the default shape: the 24-qubit
+    HEA gradient's reverse sweep, or the 30-qubit random-layer circuit."""
+    lib = nat.load()
+    if adjoint:
+        ops, _ = workloads.hea(24, 20, seed=0)
+        arr, pool = ir.pack(ops)
+        h = ctypes.c_void_p()
+        nat.check(lib.qfvm_plan_host_build_adjoint(24, precision, nat.vptr(arr), arr.size,
+                                                   nat.dptr(pool.view(np.float64)), pool.size, ctypes.byref(h)))
+        return h
+    return plan_handle(30, workloads.random_layers(30, 40, seed=0, extras=True), precision)
+
+
+# (arithmetic, reverse sweep): threads per CTA and resident CTAs per SM of the
+# automatic register budget (128 registers; 80 for complex64 one-state passes;
+# 255 when a round's amplitudes alone need more than 64)
+RESIDENCY = {(0, False): (128, 4), (1, False): (256, 3), (2, False): (512, 1),
+             (0, True): (128, 2), (1, True): (256, 2), (2, True): (256, 2)}
+
+
+@pytest.mark.parametrize("precision,adjoint", sorted(RESIDENCY))
+def test_host_ptx_carries_device_residency(precision, adjoint):
+    """The host-side PTX query reports the pass the device path compiles:
+    its launch bounds are the automatic register budget's."""
+    h = default_plan(precision, adjoint)
+    src = pass_ptx(h, 0, 2 if adjoint else 1)
+    nat.load().qfvm_plan_destroy(h)
+    nt, minb = RESIDENCY[(precision, adjoint)]
+    assert f".maxntid {nt}, 1, 1" in src and f".minnctapersm {minb}\n" in src
+
+
+@pytest.mark.parametrize("precision,adjoint,spill_max", [
+    (2, False, 0),     # the float-pair pass of the headline: no local memory
+    (0, False, 64), (1, False, 64),
+    (0, True, 128), (1, True, 192), (2, True, 384),
+])
+def test_largest_passes_fit_their_register_budget(precision, adjoint, spill_max):
+    """The two largest default passes of each benchmark circuit compiled for
+    sm_103a on the host: registers within the launch bounds' budget and
+    spill traffic bounded (bytes of spill loads per thread)."""
+    import re
+
+    lib = nat.load()
+    h = default_plan(precision, adjoint)
+    nstates = 2 if adjoint else 1
+    counts = (ctypes.c_int64 * 4)()
+    shape = (ctypes.c_int32 * 3)()
+    nat.check(lib.qfvm_plan_host_counts(h, counts, shape))
+    sizes = sorted(((ptx_instructions(pass_ptx(h, i, nstates) or ""), i) for i in range(counts[0])), reverse=True)
+    nt, minb = RESIDENCY[(precision, adjoint)]
+    budget = min(255, 65536 // (nt * minb))
+    try:
+        for _, i in sizes[:2]:
+            info = ctypes.create_string_buffer(8192)
+            nat.check(lib.qfvm_jit_pass_compile(h, i, nstates, info, 8192))
+            log = info.value.decode()
+            regs = re.findall(r"Used (\d+) registers", log)
+            if not regs:
+                pytest.skip("the PTX compiler library is not linked in: no compile log on the host")
+            assert int(regs[0]) <= budget, (i, log)
+            spill = re.findall(r"(\d+) bytes spill loads", log)
+            assert spill and int(spill[0]) <= spill_max, (i, log)
+    finally:
+        lib.qfvm_plan_destroy(h)
